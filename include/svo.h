@@ -1,0 +1,276 @@
+/*
+ * svo.h -- C ABI of the GB300 sparse-voxel-octree cone tracer (libsvo.so).
+ *
+ * Every entry point returns an svo_status (0 = success) and never lets a C++
+ * exception cross the boundary. A non-zero status leaves a message that
+ * svo_last_error_string() returns; the C# facade turns it into an exception
+ * the way the reference's ComputeManager.HandleResultCode does
+ * (SvoTracer.Kernel/ComputeManager.cs:283-287).
+ *
+ * Structs use the OpenCL layouts the reference kernels declare
+ * (SvoTracer.Kernel/wavefront.cl:1-84), naturally aligned, with the sizes
+ * checked by static_assert below. Several of the reference's C# serialisers
+ * write shorter records than these OpenCL layouts; this ABI follows the
+ * kernel side.
+ *
+ * Threading: a context is used from one host thread at a time. All device
+ * work of a context runs on one CUDA stream (svo_set_stream may replace it).
+ * Host buffers belong to the caller; device buffers made by the library
+ * belong to the context and are released by svo_destroy.
+ */
+#ifndef SVO_H
+#define SVO_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define SVO_API __attribute__((visibility("default")))
+#else
+#define SVO_API
+#endif
+
+typedef int32_t svo_status;
+
+enum {
+  SVO_OK = 0,
+  SVO_ERR_INVALID_ARGUMENT = 1,
+  SVO_ERR_CUDA = 2,
+  SVO_ERR_OUT_OF_MEMORY = 3,
+  SVO_ERR_QUEUE_FULL = 4,  /* a capped device queue overflowed (child requests) */
+  SVO_ERR_TIMEOUT = 5,     /* a bounded device wait ran out */
+  SVO_ERR_NO_TREE = 6,     /* trace/prune/graft before svo_upload_octree */
+  SVO_ERR_STEP_LIMIT = 7,  /* a ray exceeded the per-ray step limit */
+  SVO_ERR_BUDGET = 8,      /* block budget exhausted (builder, graft) */
+  SVO_ERR_NO_DEVICE = 9,   /* no usable CUDA device / kernel image */
+  SVO_ERR_INTERNAL = 10
+};
+
+/* Sentinels of the reference format. */
+#define SVO_NO_CHILD 0xFFFFFFFFu      /* Block.Child with no children      */
+#define SVO_TICK_MULTI_PARENT 65534u  /* Usage.Tick: multi-parent group    */
+#define SVO_TICK_INVIOLATE 65535u     /* Usage.Tick: never collected       */
+#define SVO_MISS 0xFFFFFFFFu          /* hit_index of a ray that hit nothing */
+#define SVO_MAX_TREE_DEPTH 24         /* deepest node level a trace walks   */
+
+/* 16-byte node: wavefront.cl:1-12, SvoTracer.Domain/Models/Block.cs:7-21.
+ * chunk holds 2 bits per child octant k = x + 2y + 4z:
+ * bit 2k = child contains air, bit 2k+1 = child contains geometry. */
+typedef struct svo_block {
+  uint32_t child;  /* first of 8 consecutive children, SVO_NO_CHILD = none */
+  uint16_t chunk;
+  int16_t normal_pitch;
+  int16_t normal_yaw;
+  uint8_t colour_r;
+  uint8_t colour_g;
+  uint8_t colour_b;
+  uint8_t opacity;
+  uint8_t specularity; /* "Spare" in wavefront.cl */
+  uint8_t gloss;
+} svo_block;
+
+/* One per 8-node block group: wavefront.cl:14-17. Tick 0 = free. */
+typedef struct svo_usage {
+  uint16_t tick;
+  uint16_t _pad;
+  uint32_t parent; /* node address whose Child points at this group */
+} svo_usage;
+
+/* Camera/frame parameters, wavefront.cl:53-75 (104 bytes).
+ * facing is column-major 3x3: columns forward, left, up. */
+typedef struct svo_trace_input {
+  float origin[3];
+  float facing[9];
+  float fov[2];  /* horizontal, vertical FoV in radians */
+  float dof[2];  /* depth of field (angle, focal distance) */
+  uint32_t screen_size[2];
+  uint8_t max_opacity;
+  uint8_t base_depth;
+  uint16_t tick;
+  uint32_t max_child_request_id;
+  float fov_multiplier;
+  float fov_constant;
+  float weighting_multiplier;
+  float weighting_constant;
+  uint8_t ambient_light_level;
+  uint8_t _pad[7];
+} svo_trace_input;
+
+/* Tree-update parameters, wavefront.cl:77-84 (20 bytes). */
+typedef struct svo_update_input {
+  uint8_t base_depth;
+  uint8_t _pad;
+  uint16_t tick;
+  uint32_t max_child_request_id;
+  uint32_t memory_size; /* block count */
+  uint32_t offset;      /* stale threshold in ticks */
+  uint32_t graft_size;  /* block groups to claim */
+} svo_update_input;
+
+/* Host-issued tree edit, wavefront.cl:24-36 (20 bytes).
+ * properties: bit0 cull child subtree and set child_address; bits1-2 = 11
+ * make inviolate, 01 stamp the tick; bit3 overwrite the node (colour from
+ * the record's surface block) and its chunk; bit4 write a base chunk. */
+typedef struct svo_pruning {
+  uint8_t properties;
+  uint8_t depth;   /* 255: address is a node index, else a Location index */
+  uint8_t _pad0[2];
+  uint32_t address;
+  uint16_t chunk;
+  uint8_t _pad1[2];
+  uint32_t colour_address;
+  uint32_t child_address;
+} svo_pruning;
+
+/* Subtree graft, wavefront.cl:38-43 (16 bytes). */
+typedef struct svo_grafting {
+  uint32_t graft_data_address; /* first group of this subtree in the payload */
+  uint32_t graft_total_size;   /* groups in this subtree */
+  uint8_t depth;               /* 255: graft_address is a node index */
+  uint8_t _pad[3];
+  uint32_t graft_address;
+} svo_grafting;
+
+/* Missing-child request raised by a trace, wavefront.cl:45-51 (40 bytes). */
+typedef struct svo_child_request {
+  uint32_t address;
+  uint16_t tick;
+  uint8_t depth;
+  uint8_t _pad0;
+  uint64_t location[3];
+  uint8_t tree_size;
+  uint8_t _pad1[7];
+} svo_child_request;
+
+/* Per-pixel results of a trace. Pointers are host memory unless on_device is
+ * non-zero, then they are device pointers the caller owns. Any pointer may be
+ * NULL to skip that output. */
+typedef struct svo_trace_output {
+  uint32_t *hit_index; /* node index of the hit, SVO_MISS for background */
+  uint8_t *hit_depth;  /* level of the hit node, 0 for background */
+  float *t;            /* distance origin->hit location, +inf for background */
+  float *rgba;         /* 4 floats per pixel, drawTrace's colour */
+  int32_t on_device;
+  int32_t _pad;
+} svo_trace_output;
+
+/* Counters of the last trace (or batch). */
+typedef struct svo_trace_stats {
+  uint64_t rays;
+  uint64_t hits;
+  uint64_t base_steps;       /* V_base summed over rays */
+  uint64_t block_node_reads; /* V_block summed over rays (reference walk) */
+  uint64_t block_steps;
+  uint64_t child_requests;   /* raised, may exceed the cap */
+  uint64_t step_limited;     /* rays stopped by the step limit */
+} svo_trace_stats;
+
+/* Tuning of the persistent trace kernel (0 = library default). */
+typedef struct svo_trace_config {
+  int32_t block_size;   /* threads per CTA */
+  int32_t ctas_per_sm;  /* resident CTAs per SM for the persistent grid */
+  int32_t refill_lanes; /* idle lanes of a warp that trigger a ray-queue refill (1..32) */
+  int32_t cadence;      /* steps between lane refills */
+  int32_t max_steps;    /* per-ray step limit */
+  int32_t collect_stats; /* 0 none, 1 totals (svo_last_trace_stats), 2 totals and per-ray counts */
+  int32_t _pad[2];
+} svo_trace_config;
+
+/* ---- context ------------------------------------------------------------ */
+
+SVO_API const char *svo_last_error_string(void);
+SVO_API const char *svo_version(void);
+
+/* Replaces ComputeManagerFactory.Build (SvoTracer.Kernel/ComputeManagerFactory.cs:12-89). */
+SVO_API svo_status svo_create(int32_t device, void **ctx);
+/* Replaces ComputeManager.Dispose (ComputeManager.cs:357-367). */
+SVO_API svo_status svo_destroy(void *ctx);
+/* Runs the context's work on a caller stream (cudaStream_t); NULL = own stream. */
+SVO_API svo_status svo_set_stream(void *ctx, void *stream);
+SVO_API svo_status svo_synchronize(void *ctx);
+SVO_API svo_status svo_set_trace_config(void *ctx, const svo_trace_config *cfg);
+SVO_API svo_status svo_get_trace_config(void *ctx, svo_trace_config *cfg);
+
+/* ---- octree residency ---------------------------------------------------- */
+
+/* Replaces InitReadBuffer(Bases/Blocks) of MainWindow.SetupWavefrontKernels
+ * (SvoTracer.Window/MainWindow.cs:143-147). block_budget is the number of
+ * nodes the device arrays can hold (>= n_blocks, rounded up to whole groups);
+ * 0 = n_blocks. */
+SVO_API svo_status svo_upload_octree(void *ctx, uint8_t base_depth, const uint16_t *bases, size_t n_bases,
+                                     const svo_block *blocks, size_t n_blocks, uint32_t block_budget);
+/* Usage initialisation of MainWindow.cs:129-145. */
+SVO_API svo_status svo_init_usage(void *ctx);
+SVO_API svo_status svo_read_usage(void *ctx, svo_usage *out, size_t n_groups);
+SVO_API svo_status svo_write_usage(void *ctx, const svo_usage *in, size_t n_groups);
+SVO_API svo_status svo_read_blocks(void *ctx, svo_block *out, size_t first, size_t n);
+SVO_API svo_status svo_read_bases(void *ctx, uint16_t *out, size_t n);
+SVO_API svo_status svo_tree_size(void *ctx, uint8_t *base_depth, size_t *n_bases, size_t *n_blocks, size_t *block_budget);
+
+/* ---- trace ----------------------------------------------------------------- */
+
+/* One view: init -> runBaseTrace/runBlockTrace passes -> evaluateBackground ->
+ * resolveRemainders -> drawTrace (wavefront.cl:1352-1850, driven by
+ * MainWindow.RunWavefront, MainWindow.cs:356-426). Stamps usage ticks and
+ * queues child requests (capped at max_child_request_id). */
+SVO_API svo_status svo_trace(void *ctx, const svo_trace_input *input, const svo_trace_output *out);
+/* n_views views in one persistent launch. out[i] receives view i. */
+SVO_API svo_status svo_trace_batch(void *ctx, const svo_trace_input *inputs, int32_t n_views, const svo_trace_output *out);
+/* Same, replayed from a CUDA graph captured on first use for this view set. */
+SVO_API svo_status svo_trace_batch_graph(void *ctx, const svo_trace_input *inputs, int32_t n_views,
+                                         const svo_trace_output *out);
+SVO_API svo_status svo_last_trace_stats(void *ctx, svo_trace_stats *stats);
+/* Per-ray V_block / V_base of the last trace run with collect_stats = 2,
+ * in batch ray order (view 0's pixels first). */
+SVO_API svo_status svo_read_ray_counts(void *ctx, uint32_t *v_block, uint32_t *v_base, size_t n);
+/* Child requests of the last trace. *n = requests raised (may exceed cap). */
+SVO_API svo_status svo_read_child_requests(void *ctx, svo_child_request *out, uint32_t cap, uint32_t *n);
+
+/* ---- procedural scenes and the tree builder (host) ----------------------- */
+
+enum { SVO_SCENE_SPHERE = 0, SVO_SCENE_TERRAIN = 1 };
+
+typedef struct svo_scene_params {
+  int32_t kind;
+  uint32_t seed;
+  uint8_t base_depth;
+  uint8_t max_depth;  /* deepest node level */
+  uint8_t _pad[2];
+  int32_t threads;    /* 0 = all cores */
+  uint64_t max_size;  /* node capacity (TreeBuilder maxSize); 0 = UINT32_MAX/64 */
+} svo_scene_params;
+
+/* Replaces ITreeBuilder.BuildTree (SvoTracer.Domain/TreeBuilder.cs:102-150). */
+SVO_API svo_status svo_tree_build(const svo_scene_params *params, void **tree);
+SVO_API svo_status svo_tree_info(void *tree, uint8_t *base_depth, size_t *n_bases, size_t *n_blocks,
+                                 uint32_t *block_count);
+SVO_API svo_status svo_tree_data(void *tree, const uint16_t **bases, const svo_block **blocks);
+SVO_API svo_status svo_tree_free(void *tree);
+
+#ifdef __cplusplus
+} /* extern "C" */
+#endif
+
+#ifdef __cplusplus
+static_assert(sizeof(svo_block) == 16, "Block is 16 bytes");
+static_assert(sizeof(svo_usage) == 8, "Usage is 8 bytes");
+static_assert(sizeof(svo_trace_input) == 104, "TraceInput is 104 bytes");
+static_assert(sizeof(svo_update_input) == 20, "UpdateInputData is 20 bytes");
+static_assert(sizeof(svo_pruning) == 20, "Pruning is 20 bytes");
+static_assert(sizeof(svo_grafting) == 16, "Grafting is 16 bytes");
+static_assert(sizeof(svo_child_request) == 40, "ChildRequest is 40 bytes");
+#else
+_Static_assert(sizeof(svo_block) == 16, "Block is 16 bytes");
+_Static_assert(sizeof(svo_usage) == 8, "Usage is 8 bytes");
+_Static_assert(sizeof(svo_trace_input) == 104, "TraceInput is 104 bytes");
+_Static_assert(sizeof(svo_update_input) == 20, "UpdateInputData is 20 bytes");
+_Static_assert(sizeof(svo_pruning) == 20, "Pruning is 20 bytes");
+_Static_assert(sizeof(svo_grafting) == 16, "Grafting is 16 bytes");
+_Static_assert(sizeof(svo_child_request) == 40, "ChildRequest is 40 bytes");
+#endif
+
+#endif /* SVO_H */

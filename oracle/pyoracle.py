@@ -1,0 +1,144 @@
+"""ctypes bindings of the oracle libraries (TEST INFRASTRUCTURE ONLY).
+
+``trace_view`` runs the C restatement (libsvo_oracle.so); ``ref_trace_view`` runs the
+reference's own wavefront.cl kernels compiled for the CPU (oracle/_ref/libsvo_ref.so).
+Both take the same inputs as the CUDA path and return per-pixel results.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+import build_oracle  # noqa: E402
+import build_ref  # noqa: E402
+
+sys.path.insert(0, os.path.join(os.path.dirname(HERE), "svo-tracer_gb300"))
+from svo_tracer import BLOCK_DTYPE, CHILD_REQUEST_DTYPE, USAGE_DTYPE, TraceInput  # noqa: E402
+
+_vp = C.c_void_p
+_oracle = None
+_ref = None
+
+
+class _ViewOut(C.Structure):
+    _fields_ = [(n, _vp) for n in ("hit_index", "hit_depth", "t", "rgba", "acc", "v_block", "v_base", "steps")]
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(_vp)
+
+
+def oracle_lib() -> C.CDLL:
+    global _oracle
+    if _oracle is None:
+        lib = C.CDLL(build_oracle.build_oracle())
+        lib.oracle_trace_view.argtypes = [_vp, C.c_uint8, _vp, C.c_size_t, _vp, C.c_size_t, C.c_char_p, C.c_int32,
+                                          C.POINTER(_ViewOut), _vp, C.c_uint32, C.POINTER(C.c_uint32), C.c_int32]
+        lib.oracle_trace_view.restype = C.c_int64
+        lib.oracle_float_to_ulong.argtypes = [C.c_float]
+        lib.oracle_float_to_ulong.restype = C.c_uint64
+        lib.oracle_ulong_to_float.argtypes = [C.c_uint64]
+        lib.oracle_ulong_to_float.restype = C.c_float
+        lib.oracle_round_ulong.argtypes = [C.c_uint64, C.c_uint8, C.c_int]
+        lib.oracle_round_ulong.restype = C.c_uint64
+        lib.oracle_pow_sum.argtypes = [C.c_uint8]
+        lib.oracle_pow_sum.restype = C.c_uint32
+        lib.oracle_compare_positions.argtypes = [C.c_uint8, _vp, _vp, _vp]
+        lib.oracle_compare_positions.restype = C.c_uint8
+        lib.oracle_traverse_chunk.argtypes = [C.c_uint8, _vp, _vp, _vp, _vp]
+        lib.oracle_trace_into_volume.argtypes = [_vp, _vp, _vp, C.c_float, _vp, _vp]
+        lib.oracle_trace_into_volume.restype = C.c_int
+        lib.oracle_init_usage.argtypes = [_vp, C.c_uint8, _vp, C.c_size_t]
+        _oracle = lib
+    return _oracle
+
+
+def ref_available() -> bool:
+    try:
+        return build_ref.compile_ref() is not None
+    except Exception:
+        return False
+
+
+def ref_lib() -> C.CDLL:
+    global _ref
+    if _ref is None:
+        path = os.environ.get("SVO_REF_LIB") or build_ref.compile_ref()
+        if path is None:
+            raise RuntimeError("reference kernels unavailable (no wavefront.cl source)")
+        lib = C.CDLL(path)
+        lib.ref_trace_view.argtypes = [_vp, C.c_uint8, _vp, C.c_size_t, _vp, C.c_size_t, C.c_char_p, _vp, _vp, _vp,
+                                       _vp, _vp, _vp, C.c_uint32, C.POINTER(C.c_uint32), C.c_int, C.c_long]
+        lib.ref_trace_view.restype = C.c_long
+        _ref = lib
+    return _ref
+
+
+def _result(n, counts=True):
+    r = {
+        "hit_index": np.empty(n, np.uint32), "hit_depth": np.empty(n, np.uint8), "t": np.empty(n, np.float32),
+        "rgba": np.empty((n, 4), np.float32), "acc": np.empty((n, 4), np.uint32),
+    }
+    if counts:
+        r.update(v_block=np.empty(n, np.uint32), v_base=np.empty(n, np.uint32), steps=np.empty(n, np.uint32))
+    return r
+
+
+def trace_view(tree, inp: TraceInput, usage=None, max_steps: int = 1 << 16, threads: int = 0, req_cap: int = 1 << 20):
+    """Runs the oracle on one view. usage (USAGE_DTYPE array) is stamped in place."""
+    lib = oracle_lib()
+    w, h = inp.ScreenSize
+    n = w * h
+    r = _result(n)
+    vo = _ViewOut(*[_p(r[k]) for k in ("hit_index", "hit_depth", "t", "rgba", "acc", "v_block", "v_base", "steps")])
+    bases = np.ascontiguousarray(tree.BaseBlocks, np.uint16)
+    blocks = np.ascontiguousarray(tree.Blocks)
+    req = np.zeros(min(req_cap, n), CHILD_REQUEST_DTYPE)
+    nreq = C.c_uint32(0)
+    ng = 0 if usage is None else len(usage)
+    limited = lib.oracle_trace_view(_p(bases), tree.BaseDepth, _p(blocks), len(blocks), _p(usage), ng,
+                                    inp.to_bytes(), max_steps, C.byref(vo), _p(req), len(req), C.byref(nreq), threads)
+    r["step_limited"] = int(limited)
+    r["requests"] = req[: min(nreq.value, len(req))]
+    r["n_requests"] = nreq.value
+    return r
+
+
+def ref_trace_view(tree, inp: TraceInput, usage=None, threads: int = 0, max_passes: int = 1 << 20):
+    """Runs the reference's own kernels (CPU build) on one view."""
+    lib = ref_lib()
+    w, h = inp.ScreenSize
+    n = w * h
+    r = _result(n, counts=False)
+    bases = np.ascontiguousarray(tree.BaseBlocks, np.uint16)
+    blocks = np.ascontiguousarray(tree.Blocks)
+    req = np.zeros(n, CHILD_REQUEST_DTYPE)
+    nreq = C.c_uint32(0)
+    ng = 0 if usage is None else len(usage)
+    passes = lib.ref_trace_view(_p(bases), tree.BaseDepth, _p(blocks), len(blocks), _p(usage), ng, inp.to_bytes(),
+                                _p(r["hit_index"]), _p(r["hit_depth"]), _p(r["t"]), _p(r["rgba"]), _p(r["acc"]),
+                                _p(req), len(req), C.byref(nreq), threads, max_passes)
+    r["passes"] = int(passes)
+    r["requests"] = req[: min(nreq.value, len(req))]
+    r["n_requests"] = nreq.value
+    return r
+
+
+def init_usage(tree) -> np.ndarray:
+    u = np.zeros(len(tree.Blocks) // 8, USAGE_DTYPE)
+    oracle_lib().oracle_init_usage(_p(np.ascontiguousarray(tree.BaseBlocks, np.uint16)), tree.BaseDepth, _p(u), len(u))
+    return u
+
+
+def sort_requests(req: np.ndarray) -> np.ndarray:
+    """Child requests in a canonical order (queue order is not deterministic)."""
+    if len(req) == 0:
+        return req
+    keys = (req["tree_size"], req["location"][:, 2], req["location"][:, 1], req["location"][:, 0], req["depth"],
+            req["address"])
+    return req[np.lexsort(keys)]

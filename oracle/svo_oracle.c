@@ -1,0 +1,490 @@
+/*
+ * svo_oracle.c -- TEST INFRASTRUCTURE ONLY: the parity checker of the CUDA
+ * tracer. Not linked into, loaded by or called from the product.
+ *
+ * A plain-C restatement of the reference's wavefront cone tracer hot path
+ * (SvoTracer/SvoTracer.Kernel/wavefront.cl). The reference runs every ray as a
+ * sequence of queued kernel launches; each ray's state transitions depend only
+ * on that ray and the (read-only during a trace) octree, and the per-pixel
+ * accumulation is a commutative integer sum, so this file runs each ray's
+ * state machine to completion, one ray at a time. The results are the ones
+ * the queued passes produce in any order.
+ *
+ * Numerics (the parity contract for OpenCL's implementation-defined
+ * built-ins): every float operation is a single IEEE round-to-nearest
+ * operation in source order, built with -ffp-contract=off; native_divide is a
+ * correctly rounded division; native_sin/cos of the ray setup are the
+ * per-column/per-row tables (float)sin((double)angle); fast_length is
+ * sqrtf((x*x + y*y) + z*z); and every comparison of ConeDepth = -half_log2(c)
+ * with an integer k is evaluated exactly as a comparison of c with 2^-k, so no
+ * logarithm is evaluated. Float-to-integer conversions that the reference
+ * leaves undefined (out of range, NaN) saturate (NaN -> 0).
+ */
+#include "svo_oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#define ULMAX 0xFFFFFFFFFFFFFFFFull
+
+/* wavefront.cl:200-207 floatToUlong. 0.999999911f is the float 1 - 2^-24. */
+uint64_t oracle_float_to_ulong(float x) {
+  if (x >= 0.999999911f) return ULMAX;
+  float v = fabsf(x) * 18446744073709551616.0f; /* (float)ULONG_MAX == 2^64 */
+  if (v != v) return 0;
+  if (!(v < 18446744073709551616.0f)) return ULMAX;
+  return (uint64_t)v;
+}
+
+/* wavefront.cl:209 ulongToFloat: (float)x / 2^64, exact scaling. */
+float oracle_ulong_to_float(uint64_t x) { return (float)x / 18446744073709551616.0f; }
+
+/* wavefront.cl:211-221 roundUlong: distance to the next level-(depth+1)
+ * boundary in the travel direction. */
+uint64_t oracle_round_ulong(uint64_t value, uint8_t depth, int round_up) {
+  uint64_t mask = ULMAX - (ULMAX >> (depth + 1));
+  if (round_up) return ((value & mask) + ((ULMAX - (ULMAX >> 1)) >> depth)) - value;
+  uint64_t output = value - ((value & mask) - 1);
+  if (output >= value) return value;
+  return output;
+}
+
+/* wavefront.cl:224 powSum: sum of 8^i for i = 1..depth. */
+uint32_t oracle_pow_sum(uint8_t depth) {
+  uint32_t s = 0, p = 1;
+  for (int i = 1; i <= depth; i++) {
+    p *= 8;
+    s += p;
+  }
+  return s;
+}
+
+/* wavefront.cl:428-430 chunkPosition: child octant below level `depth`. */
+uint8_t oracle_chunk_position(uint8_t depth, const uint64_t loc[3]) {
+  int s = 64 - depth - 1;
+  return (uint8_t)(((loc[0] >> s) & 1) + (((loc[1] >> s) & 1) << 1) + (((loc[2] >> s) & 1) << 2));
+}
+
+/* wavefront.cl:405-411 baseLocation: dense index of the level-`depth` cell. */
+uint32_t oracle_base_location(uint8_t depth, const uint64_t loc[3]) {
+  uint32_t out = 0;
+  for (uint8_t i = 0; i < depth; i++) out = (out << 3) + oracle_chunk_position(i, loc);
+  return out;
+}
+
+/* wavefront.cl:440-497 traverseChunk (without the trailing setConeDepth,
+ * whose value is recomputed where it is read). */
+void oracle_traverse_chunk(uint8_t depth, const float dir[3], const float inv[3], const int sign[3], uint64_t loc[3]) {
+  uint64_t d[3];
+  float a[3];
+  for (int k = 0; k < 3; k++) {
+    d[k] = oracle_round_ulong(loc[k], depth, sign[k]);
+    a[k] = fabsf((float)d[k] * inv[k]);
+  }
+  if (a[0] <= a[1] && a[0] <= a[2]) {
+    float u = oracle_ulong_to_float(d[0]);
+    d[1] = oracle_float_to_ulong(dir[1] * inv[0] * u);
+    d[2] = oracle_float_to_ulong(dir[2] * inv[0] * u);
+  } else if (a[1] <= a[0] && a[1] <= a[2]) {
+    float u = oracle_ulong_to_float(d[1]);
+    d[0] = oracle_float_to_ulong(dir[0] * inv[1] * u);
+    d[2] = oracle_float_to_ulong(dir[2] * inv[1] * u);
+  } else {
+    float u = oracle_ulong_to_float(d[2]);
+    d[0] = oracle_float_to_ulong(dir[0] * inv[2] * u);
+    d[1] = oracle_float_to_ulong(dir[1] * inv[2] * u);
+  }
+  for (int k = 0; k < 3; k++) {
+    if (sign[k])
+      loc[k] += d[k];
+    else
+      loc[k] -= d[k];
+  }
+  for (int k = 0; k < 3; k++) {
+    if (sign[k] && loc[k] == 0)
+      loc[k] = ULMAX;
+    else if (!sign[k] && loc[k] == ULMAX)
+      loc[k] = 0;
+  }
+}
+
+/* wavefront.cl:413-426 comparePositions: pop while the step left the cell. */
+uint8_t oracle_compare_positions(uint8_t depth, const uint64_t prev[3], const uint64_t loc[3], const int sign[3]) {
+  for (;;) {
+    uint8_t np = oracle_chunk_position(depth, loc);
+    uint8_t pp = oracle_chunk_position(depth, prev);
+    int left = 0;
+    for (int k = 0; k < 3; k++) {
+      int pb = (pp >> k) & 1, nb = (np >> k) & 1;
+      if (pb == sign[k] && nb != sign[k]) left = 1;
+    }
+    if (!left) return depth;
+    if (depth == 1) return depth;
+    depth--;
+  }
+}
+
+/* wavefront.cl:433-437 leaving. */
+static int leaving(const uint64_t loc[3], const int sign[3]) {
+  for (int k = 0; k < 3; k++) {
+    if (!sign[k] && loc[k] == 0) return 1;
+    if (sign[k] && loc[k] == ULMAX) return 1;
+  }
+  return 0;
+}
+
+/* wavefront.cl:387-391 coneSize, max() as "y if x < y else x". */
+static float cone_size(float m, float fov, const float dof[2]) {
+  float eye = fov * m;
+  float f = fabsf(dof[0] * (dof[1] - m));
+  return eye < f ? f : eye;
+}
+
+/* wavefront.cl:394-399 setConeDepth's distance: fast_length(Origin - Location). */
+static float cone_distance(const float origin[3], const uint64_t loc[3]) {
+  float x = origin[0] - oracle_ulong_to_float(loc[0]);
+  float y = origin[1] - oracle_ulong_to_float(loc[1]);
+  float z = origin[2] - oracle_ulong_to_float(loc[2]);
+  return fabsf(sqrtf(x * x + y * y + z * z));
+}
+
+/* 2^-k as a float (k <= 126). */
+static float pow2_neg(int k) { return ldexpf(1.0f, -k); }
+
+/* wavefront.cl:639-1088 traceIntoVolume. The 27-way switch picks, among the
+ * axes whose slab the origin is outside of, the one with the largest entry
+ * distance (ties to x, then y), enters the cube on that face and rejects the
+ * ray when the entry point lies outside the cube grown by the cone size. */
+int oracle_trace_into_volume(const float o[3], const float dir[3], const float inv[3], float fov, const float dof[2],
+                             uint64_t loc[3]) {
+  int lo[3], hi[3];
+  int any = 0;
+  for (int k = 0; k < 3; k++) {
+    lo[k] = o[k] < 0;
+    hi[k] = o[k] > 1;
+    any |= lo[k] | hi[k];
+  }
+  if (!any) {
+    for (int k = 0; k < 3; k++) loc[k] = oracle_float_to_ulong(o[k]);
+    return 1;
+  }
+  for (int k = 0; k < 3; k++)
+    if ((lo[k] | hi[k]) && dir[k] == 0) return 0;
+  for (int k = 0; k < 3; k++) {
+    int pos = dir[k] >= 0;
+    if (lo[k] && !pos) return 0;
+    if (hi[k] && pos) return 0;
+  }
+  float mk[3] = {0, 0, 0};
+  int out[3], n = 0;
+  for (int k = 0; k < 3; k++) {
+    if (lo[k] | hi[k]) {
+      float bound = hi[k] ? 1.0f : 0.0f;
+      mk[k] = fabsf((bound - o[k]) * inv[k]);
+      out[n++] = k;
+    }
+  }
+  int axis;
+  if (n == 1) {
+    axis = out[0];
+  } else if (n == 2) {
+    axis = mk[out[0]] >= mk[out[1]] ? out[0] : out[1];
+  } else {
+    if (mk[0] >= mk[1] && mk[0] >= mk[2])
+      axis = 0;
+    else if (mk[1] >= mk[0] && mk[1] >= mk[2])
+      axis = 1;
+    else
+      axis = 2;
+  }
+  float m = mk[axis];
+  float p[3];
+  for (int k = 0; k < 3; k++) {
+    if (k == axis)
+      p[k] = hi[k] ? 1.0f : 0.0f;
+    else
+      p[k] = o[k] + (dir[k] * m);
+  }
+  for (int k = 0; k < 3; k++) loc[k] = oracle_float_to_ulong(p[k]);
+  float c = cone_size(m, fov, dof);
+  for (int k = 0; k < 3; k++)
+    if (p[k] < -c || p[k] > 1 + c) return 0;
+  return 1;
+}
+
+void oracle_view_tables(const svo_trace_input *in, float *sin_u, float *cos_u, float *sin_v, float *cos_v) {
+  float w = (float)in->screen_size[0], h = (float)in->screen_size[1];
+  /* wavefront.cl:566-572 */
+  for (uint32_t x = 0; x < in->screen_size[0]; x++) {
+    float u = in->fov[0] * ((w / 2.0f - (float)x) / w);
+    sin_u[x] = (float)sin((double)u);
+    cos_u[x] = (float)cos((double)u);
+  }
+  for (uint32_t y = 0; y < in->screen_size[1]; y++) {
+    float v = in->fov[1] * ((h / 2.0f - (float)y) / h);
+    sin_v[y] = (float)sin((double)v);
+    cos_v[y] = (float)cos((double)v);
+  }
+}
+
+static const svo_block zero_block;
+
+static const svo_block *node_at(const svo_block *blocks, size_t n_blocks, uint32_t addr) {
+  return addr < n_blocks ? &blocks[addr] : &zero_block;
+}
+
+/* wavefront.cl:296-304 getBlockAddress; *reads counts the node loads of the
+ * walk plus the load of the returned node. */
+static uint32_t block_address(const svo_block *blocks, size_t n_blocks, uint8_t base_depth, uint8_t depth,
+                              const uint64_t loc[3], uint32_t *reads) {
+  uint32_t addr = oracle_base_location((uint8_t)(base_depth + 2), loc);
+  for (uint8_t d = (uint8_t)(base_depth + 2); d < depth; d++) {
+    addr = node_at(blocks, n_blocks, addr)->child + oracle_chunk_position(d, loc);
+    (*reads)++;
+  }
+  (*reads)++;
+  return addr;
+}
+
+static uint8_t sat_u8(float v) {
+  if (v != v) return 0;
+  if (v <= 0.0f) return 0;
+  if (v >= 255.0f) return 255;
+  return (uint8_t)v;
+}
+
+void oracle_init_usage(const uint16_t *bases, uint8_t base_depth, svo_usage *usage, size_t n_groups) {
+  /* MainWindow.cs:129-141: entries [0, 8^B) look at the level-B base chunk of
+   * the same index and become inviolate when one of its low four octants is
+   * both air and geometry (j = 3, 12, 48, 192). */
+  memset(usage, 0, n_groups * sizeof(svo_usage));
+  uint32_t base_start = oracle_pow_sum((uint8_t)(base_depth - 1));
+  uint32_t range = oracle_pow_sum(base_depth);
+  for (uint32_t i = 0; i < range - base_start && i < n_groups; i++)
+    for (uint32_t j = 3; j <= 255; j <<= 2)
+      if ((bases[i + base_start] & j) == j) {
+        usage[i].tick = 65535;
+        usage[i].parent = 0xFFFFFFFFu;
+        break;
+      }
+}
+
+typedef struct ray_result {
+  uint32_t hit_index;
+  uint8_t hit_depth;
+  float t;
+  uint32_t acc[4];
+  uint32_t v_block, v_base, steps;
+  int step_limited;
+} ray_result;
+
+static void trace_ray(const uint16_t *bases, uint8_t B, const svo_block *blocks, size_t n_blocks, svo_usage *usage,
+                      size_t n_groups, const svo_trace_input *in, const float *su, const float *cu, const float *sv,
+                      const float *cv, uint32_t px, uint32_t py, int32_t max_steps, svo_child_request *req,
+                      uint32_t req_cap, uint32_t *n_req, ray_result *r) {
+  memset(r, 0, sizeof(*r));
+  r->hit_index = SVO_MISS;
+  r->t = INFINITY;
+  /* setupInitialTrace, wavefront.cl:563-595 */
+  float m0 = cu[px] * cv[py];
+  float m1 = (0.0f - su[px]) * cv[py];
+  float m2 = sv[py];
+  const float *F = in->facing;
+  float dir[3], inv[3], o[3];
+  int sign[3];
+  dir[0] = F[0] * m0 + F[3] * m1 + F[6] * m2;
+  dir[1] = F[1] * m0 + F[4] * m1 + F[7] * m2;
+  dir[2] = F[2] * m0 + F[5] * m1 + F[8] * m2;
+  for (int k = 0; k < 3; k++) {
+    inv[k] = 1.0f / dir[k];
+    sign[k] = dir[k] >= 0;
+    o[k] = in->origin[k];
+  }
+  float fov = in->fov[0] / (float)in->screen_size[0];
+  const float zero_dof[2] = {0.0f, 0.0f};
+  uint64_t loc[3];
+  int background = 1;
+  uint8_t depth = 1;
+  int hit = 0;
+  /* init, wavefront.cl:1376-1384: enter the cube or go to the background queue. */
+  if (oracle_trace_into_volume(o, dir, inv, fov, zero_dof, loc)) {
+    background = 0;
+    for (;;) {
+      if (max_steps > 0 && (int32_t)r->steps >= max_steps) {
+        r->step_limited = 1;
+        background = 1;
+        break;
+      }
+      r->steps++;
+      if (depth <= B) {
+        /* runBaseTrace, wavefront.cl:1400-1463 */
+        uint16_t chunk = bases[oracle_pow_sum((uint8_t)(depth - 1)) + oracle_base_location(depth, loc)];
+        r->v_base++;
+        if (((chunk >> (oracle_chunk_position(depth, loc) * 2)) & 2) != 2) {
+          uint64_t prev[3] = {loc[0], loc[1], loc[2]};
+          oracle_traverse_chunk(depth, dir, inv, sign, loc);
+          if (leaving(loc, sign)) {
+            background = 1;
+            break;
+          }
+          depth = oracle_compare_positions(depth, prev, loc, sign);
+        } else {
+          depth = depth < B ? (uint8_t)(depth + 1) : (uint8_t)(B + 2);
+          if (depth == B + 1) depth = B;
+        }
+        continue;
+      }
+      /* runBlockTrace, wavefront.cl:1465-1566 */
+      uint32_t addr = block_address(blocks, n_blocks, B, depth, loc, &r->v_block);
+      const svo_block *blk = node_at(blocks, n_blocks, addr);
+      if (usage && (addr >> 3) < n_groups) {
+        svo_usage *u = &usage[addr >> 3];
+        if (u->tick < 65534 && u->tick != in->tick) u->tick = in->tick;
+      }
+      int complete = 0;
+      if (((blk->chunk >> (oracle_chunk_position(depth, loc) * 2)) & 2) != 2) {
+        uint64_t prev[3] = {loc[0], loc[1], loc[2]};
+        oracle_traverse_chunk(depth, dir, inv, sign, loc);
+        if (leaving(loc, sign)) {
+          background = 1;
+          break;
+        }
+        depth = oracle_compare_positions(depth, prev, loc, sign);
+      } else {
+        /* ConeDepth = -half_log2(c): "ConeDepth < k" <=> c > 2^-k,
+         * "ConeDepth > k" <=> c < 2^-k. */
+        float c = cone_size(cone_distance(o, loc), fov, in->dof);
+        if (c > pow2_neg(B + 2)) {
+          depth = (uint8_t)(B + 2);
+          complete = 1;
+        } else if (c > pow2_neg(depth)) {
+          depth--;
+        } else if (blk->child == SVO_NO_CHILD) {
+          /* requestChild, wavefront.cl:362-375 with the call of :1539.
+           * TreeSize = min(1, (uchar)ConeDepth - Depth) is 1 exactly when
+           * ConeDepth >= Depth + 1; Tick is the unset TraceData.Tick (0). */
+          uint32_t slot;
+#ifdef _OPENMP
+#pragma omp atomic capture
+#endif
+          slot = (*n_req)++;
+          if (req && slot < req_cap) {
+            svo_child_request *q = &req[slot];
+            memset(q, 0, sizeof(*q));
+            q->address = addr;
+            q->tick = 0;
+            q->depth = depth;
+            q->location[0] = loc[0];
+            q->location[1] = loc[1];
+            q->location[2] = loc[2];
+            q->tree_size = c <= pow2_neg(depth + 1) ? 1 : 0;
+          }
+          complete = 1;
+        } else if (c < pow2_neg(depth + 1)) {
+          depth++;
+        } else {
+          complete = 1;
+        }
+      }
+      if (complete) {
+        hit = 1;
+        break;
+      }
+      if (depth == B + 1) depth = B;
+    }
+  }
+  if (hit) {
+    /* resolveRemainders, wavefront.cl:1799-1833 */
+    uint32_t addr = block_address(blocks, n_blocks, B, depth, loc, &r->v_block);
+    const svo_block *blk = node_at(blocks, n_blocks, addr);
+    r->hit_index = addr;
+    r->hit_depth = depth;
+    r->acc[0] = 255;
+    r->acc[1] = (uint32_t)blk->colour_r * 255u;
+    r->acc[2] = (uint32_t)blk->colour_g * 255u;
+    r->acc[3] = (uint32_t)blk->colour_b * 255u;
+    /* hit distance as kernel.cl's resolveRayData: length(Location - Origin) */
+    float x = oracle_ulong_to_float(loc[0]) - o[0];
+    float y = oracle_ulong_to_float(loc[1]) - o[1];
+    float z = oracle_ulong_to_float(loc[2]) - o[2];
+    r->t = sqrtf(x * x + y * y + z * z);
+  } else if (background) {
+    /* evaluateBackground, wavefront.cl:1741-1797, for a primary ray
+     * (Weighting 255, so the ambient blend does not apply). */
+    float dotp = dir[0] * 0.0f + dir[1] * 0.0f + dir[2] * -1.0f;
+    uint32_t cr, cg, cb;
+    uint8_t lum;
+    if (dotp > 0.8f) {
+      cr = cg = cb = 255;
+      lum = sat_u8(dotp * 200.0f);
+    } else {
+      cr = 135;
+      cg = 206;
+      cb = 235;
+      lum = 1;
+    }
+    r->acc[0] = 255;
+    if (lum > 0) {
+      r->acc[1] = cr * 255u;
+      r->acc[2] = cg * 255u;
+      r->acc[3] = cb * 255u;
+    }
+  }
+}
+
+int64_t oracle_trace_view(const uint16_t *bases, uint8_t base_depth, const svo_block *blocks, size_t n_blocks,
+                          svo_usage *usage, size_t n_groups, const svo_trace_input *in, int32_t max_steps,
+                          const oracle_view_out *out, svo_child_request *req, uint32_t req_cap, uint32_t *n_req,
+                          int32_t threads) {
+  uint32_t W = in->screen_size[0], H = in->screen_size[1];
+  float *su = (float *)malloc(sizeof(float) * (W + 1));
+  float *cu = (float *)malloc(sizeof(float) * (W + 1));
+  float *sv = (float *)malloc(sizeof(float) * (H + 1));
+  float *cv = (float *)malloc(sizeof(float) * (H + 1));
+  oracle_view_tables(in, su, cu, sv, cv);
+  int64_t limited = 0;
+  int64_t n = (int64_t)W * H;
+#ifdef _OPENMP
+  int nt = threads > 0 ? threads : omp_get_max_threads();
+#pragma omp parallel for schedule(dynamic, 256) num_threads(nt) reduction(+ : limited)
+#endif
+  for (int64_t id = 0; id < n; id++) {
+    ray_result r;
+    trace_ray(bases, base_depth, blocks, n_blocks, usage, n_groups, in, su, cu, sv, cv, (uint32_t)(id % W),
+              (uint32_t)(id / W), max_steps, req, req_cap, n_req, &r);
+    limited += r.step_limited;
+    if (out->hit_index) out->hit_index[id] = r.hit_index;
+    if (out->hit_depth) out->hit_depth[id] = r.hit_depth;
+    if (out->t) out->t[id] = r.t;
+    if (out->acc)
+      for (int k = 0; k < 4; k++) out->acc[4 * id + k] = r.acc[k];
+    if (out->v_block) out->v_block[id] = r.v_block;
+    if (out->v_base) out->v_base[id] = r.v_base;
+    if (out->steps) out->steps[id] = r.steps;
+    if (out->rgba) {
+      /* drawTrace, wavefront.cl:1835-1850 */
+      float *px = &out->rgba[4 * id];
+      if (r.acc[0] == 0) {
+        px[0] = 0.75f;
+        px[1] = 0.0f;
+        px[2] = 0.0f;
+        px[3] = 1.0f;
+      } else {
+        float fw = (float)r.acc[0] * 255.0f;
+        px[0] = fminf((float)r.acc[1] / fw, 1.0f);
+        px[1] = fminf((float)r.acc[2] / fw, 1.0f);
+        px[2] = fminf((float)r.acc[3] / fw, 1.0f);
+        px[3] = 1.0f;
+      }
+    }
+  }
+  free(su);
+  free(cu);
+  free(sv);
+  free(cv);
+  return limited;
+}

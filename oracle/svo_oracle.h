@@ -1,0 +1,67 @@
+/*
+ * svo_oracle.h -- TEST INFRASTRUCTURE ONLY.
+ *
+ * CPU restatement of the reference's wavefront cone tracer
+ * (SvoTracer/SvoTracer.Kernel/wavefront.cl) used as the parity checker of the
+ * CUDA path. Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline
+ * leg may load it. Nothing in the product links or calls it.
+ */
+#ifndef SVO_ORACLE_H
+#define SVO_ORACLE_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#include "../include/svo.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Per-pixel stats of one view (any pointer may be NULL). */
+typedef struct oracle_view_out {
+  uint32_t *hit_index;
+  uint8_t *hit_depth;
+  float *t;
+  float *rgba;    /* 4 per pixel */
+  uint32_t *acc;  /* 4 per pixel: FinalWeightings, FinalColourR, G, B */
+  uint32_t *v_block; /* node reads of the reference's getBlockAddress walks */
+  uint32_t *v_base;  /* base chunk reads */
+  uint32_t *steps;   /* traversal steps (base + block) */
+} oracle_view_out;
+
+/* Traces one view. usage (n_groups entries) is stamped like runBlockTrace;
+ * child requests are appended at *n_req (slots >= req_cap are counted, not
+ * written). Returns the number of rays stopped by max_steps. threads <= 0
+ * uses all OpenMP threads. */
+int64_t oracle_trace_view(const uint16_t *bases, uint8_t base_depth, const svo_block *blocks, size_t n_blocks,
+                          svo_usage *usage, size_t n_groups, const svo_trace_input *in, int32_t max_steps,
+                          const oracle_view_out *out, svo_child_request *req, uint32_t req_cap, uint32_t *n_req,
+                          int32_t threads);
+
+/* Ray-setup tables of the parity contract: sinU/cosU per column, sinV/cosV
+ * per row, each (float)sin((double)angle). */
+void oracle_view_tables(const svo_trace_input *in, float *sin_u, float *cos_u, float *sin_v, float *cos_v);
+
+/* Fixed-point helpers, exported for unit tests. */
+uint64_t oracle_float_to_ulong(float x);
+float oracle_ulong_to_float(uint64_t x);
+uint64_t oracle_round_ulong(uint64_t value, uint8_t depth, int round_up);
+uint32_t oracle_pow_sum(uint8_t depth);
+uint8_t oracle_chunk_position(uint8_t depth, const uint64_t loc[3]);
+uint32_t oracle_base_location(uint8_t depth, const uint64_t loc[3]);
+/* traverseChunk on a bare state; loc is updated in place. */
+void oracle_traverse_chunk(uint8_t depth, const float dir[3], const float inv[3], const int sign[3], uint64_t loc[3]);
+uint8_t oracle_compare_positions(uint8_t depth, const uint64_t prev[3], const uint64_t loc[3], const int sign[3]);
+/* traceIntoVolume: returns 1 and the entry location when the ray enters. */
+int oracle_trace_into_volume(const float origin[3], const float dir[3], const float inv[3], float fov,
+                             const float dof[2], uint64_t loc[3]);
+
+/* Usage initialisation rule of MainWindow.cs:129-141. */
+void oracle_init_usage(const uint16_t *bases, uint8_t base_depth, svo_usage *usage, size_t n_groups);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

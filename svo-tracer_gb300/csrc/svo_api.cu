@@ -1,0 +1,670 @@
+// C ABI of libsvo: context, octree residency and the trace entry points.
+//
+// This layer replaces the reference's OpenCL host wrapper
+// (SvoTracer.Kernel/ComputeManager.cs, ComputeManagerFactory.cs) and the frame
+// driver MainWindow.RunWavefront (SvoTracer.Window/MainWindow.cs:356-622):
+// buffers are owned by a context, the kernels read the same OpenCL struct
+// layouts, and every failure comes back as a status code with a message (the
+// reference throws "{method}: {code}", ComputeManager.cs:283-287).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <new>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "svo_internal.h"
+
+namespace svo {
+
+static thread_local std::string g_last_error;
+
+svo_status fail(svo_status status, const std::string &message) {
+  g_last_error = message;
+  return status;
+}
+
+#define SVO_CUDA(call, what)                                                                  \
+  do {                                                                                        \
+    cudaError_t e_ = (call);                                                                  \
+    if (e_ != cudaSuccess) return fail(SVO_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+template <class T>
+struct DevBuf {
+  T *p = nullptr;
+  size_t n = 0;
+  cudaError_t reserve(size_t want) {
+    if (want <= n && p) return cudaSuccess;
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+    cudaError_t e = cudaMalloc(&p, std::max<size_t>(want, 1) * sizeof(T));
+    if (e == cudaSuccess) n = want;
+    return e;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+};
+
+template <class T>
+struct PinBuf {
+  T *p = nullptr;
+  size_t n = 0;
+  cudaError_t reserve(size_t want) {
+    if (want <= n && p) return cudaSuccess;
+    if (p) cudaFreeHost(p);
+    p = nullptr;
+    n = 0;
+    cudaError_t e = cudaMallocHost(&p, std::max<size_t>(want, 1) * sizeof(T));
+    if (e == cudaSuccess) n = want;
+    return e;
+  }
+  void release() {
+    if (p) cudaFreeHost(p);
+    p = nullptr;
+    n = 0;
+  }
+};
+
+struct Context {
+  int device = 0;
+  int sm_count = 0;
+  cudaStream_t own_stream = nullptr;
+  cudaStream_t stream = nullptr;
+  // resident tree
+  bool has_tree = false;
+  uint8_t base_depth = 0;
+  size_t n_bases = 0, n_blocks = 0, budget = 0, n_groups = 0;
+  int tree_depth = 0;
+  DevBuf<uint16_t> bases;
+  DevBuf<svo_block> blocks;
+  DevBuf<svo_usage> usage;
+  // trace scratch
+  DevBuf<uint32_t> counters;  // [0] ray queue head, [1] child requests raised
+  DevBuf<unsigned long long> stats;
+  DevBuf<svo_child_request> requests;
+  DevBuf<ViewParams> views;
+  DevBuf<float> tables;
+  DevBuf<uint32_t> ray_v_block, ray_v_base;
+  PinBuf<ViewParams> h_views;
+  PinBuf<float> h_tables;
+  PinBuf<uint32_t> h_counters;
+  // library-owned outputs for host-memory results
+  DevBuf<uint32_t> o_index;
+  DevBuf<uint8_t> o_depth;
+  DevBuf<float> o_t;
+  DevBuf<float> o_rgba;
+  uint32_t request_cap = 0;
+  uint64_t last_rays = 0;
+  bool last_stats_valid = false;
+  svo_trace_config cfg{};
+  // graph cache for svo_trace_batch_graph
+  cudaGraphExec_t graph_exec = nullptr;
+  std::vector<uint32_t> graph_key;
+
+  ~Context() {
+    if (device >= 0) cudaSetDevice(device);
+    if (graph_exec) cudaGraphExecDestroy(graph_exec);
+    bases.release();
+    blocks.release();
+    usage.release();
+    counters.release();
+    stats.release();
+    requests.release();
+    views.release();
+    tables.release();
+    ray_v_block.release();
+    ray_v_base.release();
+    h_views.release();
+    h_tables.release();
+    h_counters.release();
+    o_index.release();
+    o_depth.release();
+    o_t.release();
+    o_rgba.release();
+    if (own_stream) cudaStreamDestroy(own_stream);
+  }
+};
+
+static svo_trace_config default_config() {
+  svo_trace_config c{};
+  c.block_size = 256;
+  c.ctas_per_sm = 0;  // occupancy-derived
+  c.refill_lanes = 16;
+  c.cadence = 4;
+  c.max_steps = 1 << 16;
+  c.collect_stats = 0;
+  return c;
+}
+
+static uint32_t pow_sum(int depth) {
+  uint32_t s = 0, p = 1;
+  for (int i = 1; i <= depth; i++) {
+    p *= 8;
+    s += p;
+  }
+  return s;
+}
+
+// Deepest node level reachable from the dense level B+2 (host scan).
+static int scan_tree_depth(const svo_block *blocks, size_t n_blocks, int B) {
+  size_t dense = (size_t)1 << (3 * (B + 2));
+  int threads = (int)std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+  std::vector<int> best(threads, B + 2);
+  std::vector<std::thread> pool;
+  for (int t = 0; t < threads; t++) {
+    pool.emplace_back([&, t]() {
+      std::vector<std::pair<uint32_t, int>> stack;
+      for (size_t a = t; a < std::min(dense, n_blocks); a += threads) {
+        stack.clear();
+        stack.push_back({(uint32_t)a, B + 2});
+        while (!stack.empty()) {
+          auto [addr, d] = stack.back();
+          stack.pop_back();
+          if (d > best[t]) best[t] = d;
+          if (d >= SVO_MAX_TREE_DEPTH + 1) continue;
+          uint32_t c = blocks[addr].child;
+          // only nodes the traversal can descend into: geometry octants
+          if (c == SVO_NO_CHILD || (size_t)c + 8 > n_blocks) continue;
+          for (uint32_t k = 0; k < 8; k++)
+            if ((blocks[addr].chunk >> (2 * k + 1)) & 1) stack.push_back({c + k, d + 1});
+        }
+      }
+    });
+  }
+  for (auto &th : pool) th.join();
+  return *std::max_element(best.begin(), best.end());
+}
+
+// Builds the view table and trig tables for `n` views in pinned staging.
+static svo_status stage_views(Context &c, const svo_trace_input *in, int32_t n, const svo_trace_output *out,
+                              bool outputs_on_device, uint32_t &total_rays, size_t &table_floats) {
+  total_rays = 0;
+  table_floats = 0;
+  for (int i = 0; i < n; i++) {
+    uint64_t w = in[i].screen_size[0], h = in[i].screen_size[1];
+    if (w == 0 || h == 0 || w > 65536 || h > 65536)
+      return fail(SVO_ERR_INVALID_ARGUMENT, "svo_trace: screen_size must be 1..65536 per axis");
+    if (in[i].base_depth != 0 && in[i].base_depth != c.base_depth)
+      return fail(SVO_ERR_INVALID_ARGUMENT, "svo_trace: input base_depth differs from the resident tree's");
+    if ((uint64_t)total_rays + w * h > 0xF0000000ull)
+      return fail(SVO_ERR_INVALID_ARGUMENT, "svo_trace: too many rays in one call");
+    total_rays += (uint32_t)(w * h);
+    table_floats += 2 * (w + h);
+  }
+  if (c.h_views.reserve(n) != cudaSuccess || c.h_tables.reserve(table_floats) != cudaSuccess)
+    return fail(SVO_ERR_OUT_OF_MEMORY, "svo_trace: pinned staging allocation failed");
+  uint32_t ray = 0;
+  size_t toff = 0;
+  size_t out_off = 0;
+  for (int i = 0; i < n; i++) {
+    const svo_trace_input &t = in[i];
+    ViewParams &v = c.h_views.p[i];
+    std::memset(&v, 0, sizeof(v));
+    for (int k = 0; k < 3; k++) v.origin[k] = t.origin[k];
+    for (int k = 0; k < 9; k++) v.facing[k] = t.facing[k];
+    uint32_t W = t.screen_size[0], H = t.screen_size[1];
+    v.fov_px = t.fov[0] / (float)W;  // native_divide(FoV[0], ScreenSize.x)
+    v.dof[0] = t.dof[0];
+    v.dof[1] = t.dof[1];
+    v.width = W;
+    v.height = H;
+    v.ray_begin = ray;
+    v.table_off = (uint32_t)toff;
+    v.tick = t.tick;
+    if (outputs_on_device) {
+      v.hit_index = out[i].hit_index;
+      v.hit_depth = out[i].hit_depth;
+      v.t = out[i].t;
+      v.rgba = out[i].rgba;
+    } else {
+      v.hit_index = out[i].hit_index ? c.o_index.p + out_off : nullptr;
+      v.hit_depth = out[i].hit_depth ? c.o_depth.p + out_off : nullptr;
+      v.t = out[i].t ? c.o_t.p + out_off : nullptr;
+      v.rgba = out[i].rgba ? c.o_rgba.p + 4 * out_off : nullptr;
+    }
+    // Ray-setup angles (wavefront.cl:566-572); sin/cos are (float)sin((double)a).
+    float *tb = c.h_tables.p + toff;
+    float fw = (float)W, fh = (float)H;
+    for (uint32_t x = 0; x < W; x++) {
+      float u = t.fov[0] * ((fw / 2.0f - (float)x) / fw);
+      tb[x] = (float)std::sin((double)u);
+      tb[W + x] = (float)std::cos((double)u);
+    }
+    for (uint32_t y = 0; y < H; y++) {
+      float vv = t.fov[1] * ((fh / 2.0f - (float)y) / fh);
+      tb[2 * W + y] = (float)std::sin((double)vv);
+      tb[2 * W + H + y] = (float)std::cos((double)vv);
+    }
+    toff += 2 * ((size_t)W + H);
+    out_off += (size_t)W * H;
+    ray += W * H;
+  }
+  return SVO_OK;
+}
+
+static svo_status prepare_launch(Context &c, int32_t n_views, uint32_t total_rays, TraceLaunch &a, bool stats) {
+  a = TraceLaunch{};
+  a.bases = c.bases.p;
+  a.blocks = c.blocks.p;
+  a.usage = c.usage.p;
+  a.requests = c.requests.p;
+  a.request_cap = c.request_cap;
+  a.ray_counter = c.counters.p;
+  a.request_count = c.counters.p + 1;
+  a.stats = stats ? c.stats.p : nullptr;
+  a.ray_v_block = (stats && c.cfg.collect_stats >= 2) ? c.ray_v_block.p : nullptr;
+  a.ray_v_base = (stats && c.cfg.collect_stats >= 2) ? c.ray_v_base.p : nullptr;
+  a.views = c.views.p;
+  a.tables = c.tables.p;
+  a.n_bases = (uint32_t)c.n_bases;
+  a.n_blocks = (uint32_t)c.budget;
+  a.n_groups = (uint32_t)c.n_groups;
+  a.total_rays = total_rays;
+  a.n_views = n_views;
+  a.base_depth = c.base_depth;
+  a.max_steps = c.cfg.max_steps;
+  a.cadence = std::max(1, c.cfg.cadence);
+  a.refill_lanes = std::min(32, std::max(1, c.cfg.refill_lanes));
+  a.block_size = c.cfg.block_size;
+  a.path_levels = std::max(1, c.tree_depth - (int)c.base_depth - 1);
+  int occ = c.cfg.ctas_per_sm > 0 ? c.cfg.ctas_per_sm : trace_occupancy(a, stats);
+  if (occ <= 0) return fail(SVO_ERR_NO_DEVICE, "svo_trace: the trace kernel cannot be resident (no sm_103a image?)");
+  long want = (long)occ * c.sm_count;
+  long need = ((long)total_rays + 31) / 32 * 32 / a.block_size + 1;
+  a.grid = (int)std::max(1L, std::min(want, need));
+  return SVO_OK;
+}
+
+static svo_status run_trace(Context &c, const svo_trace_input *in, int32_t n, const svo_trace_output *out,
+                            bool use_graph) {
+  if (!c.has_tree) return fail(SVO_ERR_NO_TREE, "svo_trace: no octree uploaded");
+  if (n <= 0 || !in || !out) return fail(SVO_ERR_INVALID_ARGUMENT, "svo_trace: bad view list");
+  SVO_CUDA(cudaSetDevice(c.device), "cudaSetDevice");
+  bool on_device = out[0].on_device != 0;
+  for (int i = 1; i < n; i++)
+    if ((out[i].on_device != 0) != on_device)
+      return fail(SVO_ERR_INVALID_ARGUMENT, "svo_trace: outputs of one call must all be host or all device");
+  size_t pixels = 0;
+  uint32_t cap = 0;
+  for (int i = 0; i < n; i++) {
+    pixels += (size_t)in[i].screen_size[0] * in[i].screen_size[1];
+    cap = std::max(cap, in[i].max_child_request_id);
+  }
+  if (!on_device) {
+    if (c.o_index.reserve(pixels) || c.o_depth.reserve(pixels) || c.o_t.reserve(pixels) ||
+        c.o_rgba.reserve(4 * pixels))
+      return fail(SVO_ERR_OUT_OF_MEMORY, "svo_trace: output buffer allocation failed");
+  }
+  if (c.requests.reserve(cap) != cudaSuccess) return fail(SVO_ERR_OUT_OF_MEMORY, "svo_trace: request queue allocation");
+  c.request_cap = cap;
+  uint32_t total_rays;
+  size_t table_floats;
+  svo_status st = stage_views(c, in, n, out, on_device, total_rays, table_floats);
+  if (st) return st;
+  bool stats = c.cfg.collect_stats > 0;
+  if (c.views.reserve(n) || c.tables.reserve(table_floats))
+    return fail(SVO_ERR_OUT_OF_MEMORY, "svo_trace: view table allocation failed");
+  if (stats && c.cfg.collect_stats >= 2 && (c.ray_v_block.reserve(total_rays) || c.ray_v_base.reserve(total_rays)))
+    return fail(SVO_ERR_OUT_OF_MEMORY, "svo_trace: per-ray counter allocation failed");
+  TraceLaunch a;
+  st = prepare_launch(c, n, total_rays, a, stats);
+  if (st) return st;
+
+  auto enqueue = [&]() -> svo_status {
+    SVO_CUDA(cudaMemcpyAsync(c.views.p, c.h_views.p, sizeof(ViewParams) * n, cudaMemcpyHostToDevice, c.stream),
+             "svo_trace: view upload");
+    SVO_CUDA(cudaMemcpyAsync(c.tables.p, c.h_tables.p, sizeof(float) * table_floats, cudaMemcpyHostToDevice, c.stream),
+             "svo_trace: table upload");
+    SVO_CUDA(cudaMemsetAsync(c.counters.p, 0, 2 * sizeof(uint32_t), c.stream), "svo_trace: counter reset");
+    if (stats) SVO_CUDA(cudaMemsetAsync(c.stats.p, 0, 8 * sizeof(unsigned long long), c.stream), "svo_trace: stats reset");
+    return launch_trace(a, stats, c.stream);
+  };
+
+  if (use_graph && !stats) {
+    std::vector<uint32_t> key;
+    key.push_back((uint32_t)n);
+    key.push_back(on_device ? 1u : 0u);
+    for (int i = 0; i < n; i++) {
+      key.push_back(in[i].screen_size[0]);
+      key.push_back(in[i].screen_size[1]);
+    }
+    key.push_back((uint32_t)(uintptr_t)c.h_views.p);
+    key.push_back((uint32_t)(uintptr_t)c.h_tables.p);
+    key.push_back((uint32_t)(uintptr_t)c.views.p);
+    key.push_back((uint32_t)(uintptr_t)c.tables.p);
+    key.push_back((uint32_t)a.grid);
+    if (!c.graph_exec || key != c.graph_key) {
+      if (c.graph_exec) cudaGraphExecDestroy(c.graph_exec);
+      c.graph_exec = nullptr;
+      cudaStream_t cap_stream = c.stream;
+      SVO_CUDA(cudaStreamBeginCapture(cap_stream, cudaStreamCaptureModeThreadLocal), "svo_trace_batch_graph: capture");
+      svo_status est = enqueue();
+      cudaGraph_t g = nullptr;
+      cudaError_t ce = cudaStreamEndCapture(cap_stream, &g);
+      if (est) {
+        if (g) cudaGraphDestroy(g);
+        return est;
+      }
+      if (ce != cudaSuccess) return fail(SVO_ERR_CUDA, std::string("svo_trace_batch_graph: end capture: ") + cudaGetErrorString(ce));
+      ce = cudaGraphInstantiate(&c.graph_exec, g, 0);
+      cudaGraphDestroy(g);
+      if (ce != cudaSuccess) {
+        c.graph_exec = nullptr;
+        return fail(SVO_ERR_CUDA, std::string("svo_trace_batch_graph: instantiate: ") + cudaGetErrorString(ce));
+      }
+      c.graph_key = key;
+    }
+    SVO_CUDA(cudaGraphLaunch(c.graph_exec, c.stream), "svo_trace_batch_graph: launch");
+  } else {
+    st = enqueue();
+    if (st) return st;
+  }
+  c.last_rays = total_rays;
+  c.last_stats_valid = stats;
+
+  if (!on_device) {
+    size_t off = 0;
+    for (int i = 0; i < n; i++) {
+      size_t np = (size_t)in[i].screen_size[0] * in[i].screen_size[1];
+      if (out[i].hit_index)
+        SVO_CUDA(cudaMemcpyAsync(out[i].hit_index, c.o_index.p + off, np * 4, cudaMemcpyDeviceToHost, c.stream), "svo_trace: read hit_index");
+      if (out[i].hit_depth)
+        SVO_CUDA(cudaMemcpyAsync(out[i].hit_depth, c.o_depth.p + off, np, cudaMemcpyDeviceToHost, c.stream), "svo_trace: read hit_depth");
+      if (out[i].t)
+        SVO_CUDA(cudaMemcpyAsync(out[i].t, c.o_t.p + off, np * 4, cudaMemcpyDeviceToHost, c.stream), "svo_trace: read t");
+      if (out[i].rgba)
+        SVO_CUDA(cudaMemcpyAsync(out[i].rgba, c.o_rgba.p + 4 * off, np * 16, cudaMemcpyDeviceToHost, c.stream), "svo_trace: read rgba");
+      off += np;
+    }
+    SVO_CUDA(cudaStreamSynchronize(c.stream), "svo_trace: synchronize");
+  }
+  return SVO_OK;
+}
+
+}  // namespace svo
+
+using svo::Context;
+using svo::fail;
+
+#define CTX_OR_FAIL(ptr, fn)                                                        \
+  if (!(ptr)) return fail(SVO_ERR_INVALID_ARGUMENT, std::string(fn) + ": null context"); \
+  Context &c = *static_cast<Context *>(ptr)
+
+#define GUARD_BEGIN try {
+#define GUARD_END(fn)                                                                  \
+  }                                                                                    \
+  catch (const std::bad_alloc &) {                                                     \
+    return fail(SVO_ERR_OUT_OF_MEMORY, std::string(fn) + ": out of host memory");      \
+  }                                                                                    \
+  catch (const std::exception &e) {                                                    \
+    return fail(SVO_ERR_INTERNAL, std::string(fn) + ": " + e.what());                  \
+  }
+
+extern "C" {
+
+SVO_API const char *svo_last_error_string(void) { return svo::g_last_error.c_str(); }
+
+SVO_API const char *svo_version(void) { return "svo-gb300 0.1 (sm_103a)"; }
+
+SVO_API svo_status svo_create(int32_t device, void **ctx) {
+  if (!ctx) return fail(SVO_ERR_INVALID_ARGUMENT, "svo_create: null output");
+  *ctx = nullptr;
+  GUARD_BEGIN
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (e != cudaSuccess || n == 0) return fail(SVO_ERR_NO_DEVICE, "svo_create: no CUDA device");
+  if (device < 0 || device >= n) return fail(SVO_ERR_INVALID_ARGUMENT, "svo_create: device index out of range");
+  SVO_CUDA(cudaSetDevice(device), "svo_create: cudaSetDevice");
+  std::unique_ptr<Context> c(new Context);
+  c->device = device;
+  SVO_CUDA(cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, device), "svo_create: SM count");
+  SVO_CUDA(cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking), "svo_create: stream");
+  c->stream = c->own_stream;
+  c->cfg = svo::default_config();
+  SVO_CUDA(c->counters.reserve(4), "svo_create: counters");
+  SVO_CUDA(c->stats.reserve(8), "svo_create: stats");
+  SVO_CUDA(c->h_counters.reserve(4), "svo_create: pinned counters");
+  *ctx = c.release();
+  return SVO_OK;
+  GUARD_END("svo_create")
+}
+
+SVO_API svo_status svo_destroy(void *ctx) {
+  if (!ctx) return SVO_OK;
+  delete static_cast<Context *>(ctx);
+  return SVO_OK;
+}
+
+SVO_API svo_status svo_set_stream(void *ctx, void *stream) {
+  CTX_OR_FAIL(ctx, "svo_set_stream");
+  c.stream = stream ? static_cast<cudaStream_t>(stream) : c.own_stream;
+  if (c.graph_exec) cudaGraphExecDestroy(c.graph_exec);
+  c.graph_exec = nullptr;
+  return SVO_OK;
+}
+
+SVO_API svo_status svo_synchronize(void *ctx) {
+  CTX_OR_FAIL(ctx, "svo_synchronize");
+  SVO_CUDA(cudaStreamSynchronize(c.stream), "svo_synchronize");
+  return SVO_OK;
+}
+
+SVO_API svo_status svo_set_trace_config(void *ctx, const svo_trace_config *cfg) {
+  CTX_OR_FAIL(ctx, "svo_set_trace_config");
+  if (!cfg) return fail(SVO_ERR_INVALID_ARGUMENT, "svo_set_trace_config: null config");
+  svo_trace_config d = svo::default_config(), n = *cfg;
+  if (n.block_size == 0) n.block_size = d.block_size;
+  if (n.refill_lanes == 0) n.refill_lanes = d.refill_lanes;
+  if (n.cadence == 0) n.cadence = d.cadence;
+  if (n.max_steps == 0) n.max_steps = d.max_steps;
+  if (n.block_size % 32 || n.block_size < 32 || n.block_size > 1024)
+    return fail(SVO_ERR_INVALID_ARGUMENT, "svo_set_trace_config: block_size must be a multiple of 32 in 32..1024");
+  if (n.refill_lanes < 1 || n.refill_lanes > 32 || n.cadence < 1 || n.max_steps < 1 || n.ctas_per_sm < 0 ||
+      n.collect_stats < 0 || n.collect_stats > 2)
+    return fail(SVO_ERR_INVALID_ARGUMENT, "svo_set_trace_config: value out of range");
+  c.cfg = n;
+  if (c.graph_exec) cudaGraphExecDestroy(c.graph_exec);
+  c.graph_exec = nullptr;
+  return SVO_OK;
+}
+
+SVO_API svo_status svo_get_trace_config(void *ctx, svo_trace_config *cfg) {
+  CTX_OR_FAIL(ctx, "svo_get_trace_config");
+  if (!cfg) return fail(SVO_ERR_INVALID_ARGUMENT, "svo_get_trace_config: null config");
+  *cfg = c.cfg;
+  return SVO_OK;
+}
+
+SVO_API svo_status svo_upload_octree(void *ctx, uint8_t base_depth, const uint16_t *bases, size_t n_bases,
+                                     const svo_block *blocks, size_t n_blocks, uint32_t block_budget) {
+  CTX_OR_FAIL(ctx, "svo_upload_octree");
+  GUARD_BEGIN
+  if (base_depth < 1 || base_depth > 8) return fail(SVO_ERR_INVALID_ARGUMENT, "svo_upload_octree: base_depth must be 1..8");
+  if (!bases || n_bases != svo::pow_sum(base_depth))
+    return fail(SVO_ERR_INVALID_ARGUMENT, "svo_upload_octree: need powSum(base_depth) base chunks");
+  if (!blocks && n_blocks) return fail(SVO_ERR_INVALID_ARGUMENT, "svo_upload_octree: null blocks");
+  if (n_blocks > 0xFFFFFFF8ull) return fail(SVO_ERR_INVALID_ARGUMENT, "svo_upload_octree: too many blocks");
+  size_t dense = (size_t)1 << (3 * (base_depth + 2));
+  size_t budget = std::max<size_t>({(size_t)block_budget, n_blocks, dense});
+  budget = (budget + 7) & ~(size_t)7;
+  if (budget > 0xFFFFFFF8ull) return fail(SVO_ERR_INVALID_ARGUMENT, "svo_upload_octree: block budget too large");
+  int depth = svo::scan_tree_depth(blocks, n_blocks, base_depth);
+  if (depth > SVO_MAX_TREE_DEPTH) return fail(SVO_ERR_INVALID_ARGUMENT, "svo_upload_octree: tree deeper than SVO_MAX_TREE_DEPTH");
+  SVO_CUDA(cudaSetDevice(c.device), "cudaSetDevice");
+  if (c.graph_exec) cudaGraphExecDestroy(c.graph_exec);
+  c.graph_exec = nullptr;
+  c.has_tree = false;
+  if (c.bases.reserve(n_bases) || c.blocks.reserve(budget) || c.usage.reserve(budget / 8))
+    return fail(SVO_ERR_OUT_OF_MEMORY, "svo_upload_octree: device allocation failed");
+  SVO_CUDA(cudaMemcpyAsync(c.bases.p, bases, n_bases * 2, cudaMemcpyHostToDevice, c.stream), "svo_upload_octree: bases");
+  if (n_blocks)
+    SVO_CUDA(cudaMemcpyAsync(c.blocks.p, blocks, n_blocks * sizeof(svo_block), cudaMemcpyHostToDevice, c.stream),
+             "svo_upload_octree: blocks");
+  if (budget > n_blocks)
+    SVO_CUDA(cudaMemsetAsync(c.blocks.p + n_blocks, 0, (budget - n_blocks) * sizeof(svo_block), c.stream),
+             "svo_upload_octree: block padding");
+  SVO_CUDA(cudaMemsetAsync(c.usage.p, 0, budget / 8 * sizeof(svo_usage), c.stream), "svo_upload_octree: usage");
+  SVO_CUDA(cudaStreamSynchronize(c.stream), "svo_upload_octree: synchronize");
+  c.base_depth = base_depth;
+  c.n_bases = n_bases;
+  c.n_blocks = n_blocks;
+  c.budget = budget;
+  c.n_groups = budget / 8;
+  c.tree_depth = std::max(depth, base_depth + 2);
+  c.has_tree = true;
+  return SVO_OK;
+  GUARD_END("svo_upload_octree")
+}
+
+SVO_API svo_status svo_init_usage(void *ctx) {
+  CTX_OR_FAIL(ctx, "svo_init_usage");
+  GUARD_BEGIN
+  if (!c.has_tree) return fail(SVO_ERR_NO_TREE, "svo_init_usage: no octree uploaded");
+  // MainWindow.cs:129-141: entries [0, 8^B) become inviolate when the level-B
+  // base chunk of the same index has air+geometry in one of its low 4 octants.
+  std::vector<uint16_t> hb(c.n_bases);
+  SVO_CUDA(cudaMemcpy(hb.data(), c.bases.p, c.n_bases * 2, cudaMemcpyDeviceToHost), "svo_init_usage: read bases");
+  uint32_t start = svo::pow_sum(c.base_depth - 1), range = svo::pow_sum(c.base_depth);
+  std::vector<svo_usage> u(std::min<size_t>(range - start, c.n_groups));
+  std::memset(u.data(), 0, u.size() * sizeof(svo_usage));
+  for (size_t i = 0; i < u.size(); i++)
+    for (uint32_t j = 3; j <= 255; j <<= 2)
+      if ((hb[start + i] & j) == j) {
+        u[i].tick = 65535;
+        u[i].parent = 0xFFFFFFFFu;
+        break;
+      }
+  SVO_CUDA(cudaMemsetAsync(c.usage.p, 0, c.n_groups * sizeof(svo_usage), c.stream), "svo_init_usage: clear");
+  SVO_CUDA(cudaMemcpyAsync(c.usage.p, u.data(), u.size() * sizeof(svo_usage), cudaMemcpyHostToDevice, c.stream),
+           "svo_init_usage: write");
+  SVO_CUDA(cudaStreamSynchronize(c.stream), "svo_init_usage: synchronize");
+  return SVO_OK;
+  GUARD_END("svo_init_usage")
+}
+
+SVO_API svo_status svo_read_usage(void *ctx, svo_usage *out, size_t n_groups) {
+  CTX_OR_FAIL(ctx, "svo_read_usage");
+  if (!c.has_tree) return fail(SVO_ERR_NO_TREE, "svo_read_usage: no octree uploaded");
+  if (!out || n_groups > c.n_groups) return fail(SVO_ERR_INVALID_ARGUMENT, "svo_read_usage: bad output");
+  SVO_CUDA(cudaStreamSynchronize(c.stream), "svo_read_usage: synchronize");
+  SVO_CUDA(cudaMemcpy(out, c.usage.p, n_groups * sizeof(svo_usage), cudaMemcpyDeviceToHost), "svo_read_usage");
+  return SVO_OK;
+}
+
+SVO_API svo_status svo_write_usage(void *ctx, const svo_usage *in, size_t n_groups) {
+  CTX_OR_FAIL(ctx, "svo_write_usage");
+  if (!c.has_tree) return fail(SVO_ERR_NO_TREE, "svo_write_usage: no octree uploaded");
+  if (!in || n_groups > c.n_groups) return fail(SVO_ERR_INVALID_ARGUMENT, "svo_write_usage: bad input");
+  SVO_CUDA(cudaStreamSynchronize(c.stream), "svo_write_usage: synchronize");
+  SVO_CUDA(cudaMemcpy(c.usage.p, in, n_groups * sizeof(svo_usage), cudaMemcpyHostToDevice), "svo_write_usage");
+  return SVO_OK;
+}
+
+SVO_API svo_status svo_read_blocks(void *ctx, svo_block *out, size_t first, size_t n) {
+  CTX_OR_FAIL(ctx, "svo_read_blocks");
+  if (!c.has_tree) return fail(SVO_ERR_NO_TREE, "svo_read_blocks: no octree uploaded");
+  if (!out || first > c.budget || n > c.budget - first) return fail(SVO_ERR_INVALID_ARGUMENT, "svo_read_blocks: range");
+  SVO_CUDA(cudaStreamSynchronize(c.stream), "svo_read_blocks: synchronize");
+  SVO_CUDA(cudaMemcpy(out, c.blocks.p + first, n * sizeof(svo_block), cudaMemcpyDeviceToHost), "svo_read_blocks");
+  return SVO_OK;
+}
+
+SVO_API svo_status svo_read_bases(void *ctx, uint16_t *out, size_t n) {
+  CTX_OR_FAIL(ctx, "svo_read_bases");
+  if (!c.has_tree) return fail(SVO_ERR_NO_TREE, "svo_read_bases: no octree uploaded");
+  if (!out || n > c.n_bases) return fail(SVO_ERR_INVALID_ARGUMENT, "svo_read_bases: range");
+  SVO_CUDA(cudaStreamSynchronize(c.stream), "svo_read_bases: synchronize");
+  SVO_CUDA(cudaMemcpy(out, c.bases.p, n * 2, cudaMemcpyDeviceToHost), "svo_read_bases");
+  return SVO_OK;
+}
+
+SVO_API svo_status svo_tree_size(void *ctx, uint8_t *base_depth, size_t *n_bases, size_t *n_blocks,
+                                 size_t *block_budget) {
+  CTX_OR_FAIL(ctx, "svo_tree_size");
+  if (!c.has_tree) return fail(SVO_ERR_NO_TREE, "svo_tree_size: no octree uploaded");
+  if (base_depth) *base_depth = c.base_depth;
+  if (n_bases) *n_bases = c.n_bases;
+  if (n_blocks) *n_blocks = c.n_blocks;
+  if (block_budget) *block_budget = c.budget;
+  return SVO_OK;
+}
+
+SVO_API svo_status svo_trace(void *ctx, const svo_trace_input *input, const svo_trace_output *out) {
+  CTX_OR_FAIL(ctx, "svo_trace");
+  GUARD_BEGIN
+  return svo::run_trace(c, input, 1, out, false);
+  GUARD_END("svo_trace")
+}
+
+SVO_API svo_status svo_trace_batch(void *ctx, const svo_trace_input *inputs, int32_t n_views,
+                                   const svo_trace_output *out) {
+  CTX_OR_FAIL(ctx, "svo_trace_batch");
+  GUARD_BEGIN
+  return svo::run_trace(c, inputs, n_views, out, false);
+  GUARD_END("svo_trace_batch")
+}
+
+SVO_API svo_status svo_trace_batch_graph(void *ctx, const svo_trace_input *inputs, int32_t n_views,
+                                         const svo_trace_output *out) {
+  CTX_OR_FAIL(ctx, "svo_trace_batch_graph");
+  GUARD_BEGIN
+  return svo::run_trace(c, inputs, n_views, out, true);
+  GUARD_END("svo_trace_batch_graph")
+}
+
+SVO_API svo_status svo_last_trace_stats(void *ctx, svo_trace_stats *stats) {
+  CTX_OR_FAIL(ctx, "svo_last_trace_stats");
+  if (!stats) return fail(SVO_ERR_INVALID_ARGUMENT, "svo_last_trace_stats: null output");
+  std::memset(stats, 0, sizeof(*stats));
+  SVO_CUDA(cudaStreamSynchronize(c.stream), "svo_last_trace_stats: synchronize");
+  uint32_t counters[2];
+  SVO_CUDA(cudaMemcpy(counters, c.counters.p, sizeof(counters), cudaMemcpyDeviceToHost), "svo_last_trace_stats: counters");
+  stats->rays = c.last_rays;
+  stats->child_requests = counters[1];
+  if (c.last_stats_valid) {
+    unsigned long long v[7];
+    SVO_CUDA(cudaMemcpy(v, c.stats.p, sizeof(v), cudaMemcpyDeviceToHost), "svo_last_trace_stats: stats");
+    stats->hits = v[1];
+    stats->base_steps = v[2];
+    stats->block_node_reads = v[3];
+    stats->block_steps = v[4];
+    stats->step_limited = v[6];
+  }
+  return SVO_OK;
+}
+
+SVO_API svo_status svo_read_ray_counts(void *ctx, uint32_t *v_block, uint32_t *v_base, size_t n) {
+  CTX_OR_FAIL(ctx, "svo_read_ray_counts");
+  if (!c.last_stats_valid || c.cfg.collect_stats < 2 || n > c.last_rays)
+    return fail(SVO_ERR_INVALID_ARGUMENT, "svo_read_ray_counts: last trace had no per-ray counts");
+  SVO_CUDA(cudaStreamSynchronize(c.stream), "svo_read_ray_counts: synchronize");
+  if (v_block) SVO_CUDA(cudaMemcpy(v_block, c.ray_v_block.p, n * 4, cudaMemcpyDeviceToHost), "svo_read_ray_counts");
+  if (v_base) SVO_CUDA(cudaMemcpy(v_base, c.ray_v_base.p, n * 4, cudaMemcpyDeviceToHost), "svo_read_ray_counts");
+  return SVO_OK;
+}
+
+SVO_API svo_status svo_read_child_requests(void *ctx, svo_child_request *out, uint32_t cap, uint32_t *n) {
+  CTX_OR_FAIL(ctx, "svo_read_child_requests");
+  if (!n) return fail(SVO_ERR_INVALID_ARGUMENT, "svo_read_child_requests: null count");
+  SVO_CUDA(cudaStreamSynchronize(c.stream), "svo_read_child_requests: synchronize");
+  uint32_t raised = 0;
+  SVO_CUDA(cudaMemcpy(&raised, c.counters.p + 1, 4, cudaMemcpyDeviceToHost), "svo_read_child_requests: count");
+  *n = raised;
+  uint32_t stored = std::min(raised, c.request_cap);
+  uint32_t copy = std::min(stored, cap);
+  if (copy && out)
+    SVO_CUDA(cudaMemcpy(out, c.requests.p, (size_t)copy * sizeof(svo_child_request), cudaMemcpyDeviceToHost),
+             "svo_read_child_requests: records");
+  return SVO_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,69 @@
+// Internal declarations shared by the libsvo translation units.
+#pragma once
+
+#include <cstdint>
+#include <string>
+
+#include "../../include/svo.h"
+
+namespace svo {
+
+// Records the message returned by svo_last_error_string and returns `status`.
+svo_status fail(svo_status status, const std::string &message);
+
+struct TreeHost;
+
+// Per-view constants of one trace, as the kernel reads them.
+struct ViewParams {
+  float origin[3];
+  float facing[9];
+  float fov_px;       // FoV[0] / ScreenSize.x (the pixel cone factor)
+  float dof[2];
+  uint32_t width;
+  uint32_t height;
+  uint32_t ray_begin;  // first ray of this view in the batch's ray index space
+  uint32_t table_off;  // sinU, cosU at [off, off+W); sinV, cosV at [off+2W, off+2W+2H)
+  uint16_t tick;
+  uint16_t _pad0;
+  uint32_t _pad1;
+  uint32_t *hit_index;
+  uint8_t *hit_depth;
+  float *t;
+  float *rgba;
+};
+static_assert(sizeof(ViewParams) % 8 == 0, "ViewParams alignment");
+
+struct TraceLaunch {
+  const uint16_t *bases;
+  const void *blocks;  // svo_block[n_blocks]
+  svo_usage *usage;
+  svo_child_request *requests;
+  uint32_t *request_count;
+  uint32_t *ray_counter;
+  unsigned long long *stats;  // 7 counters in svo_trace_stats order, or null
+  uint32_t *ray_v_block;      // per-ray V_block (stats launches only), or null
+  uint32_t *ray_v_base;
+  const ViewParams *views;    // device array
+  const float *tables;        // device trig tables
+  uint32_t n_bases;
+  uint32_t n_blocks;
+  uint32_t n_groups;
+  uint32_t request_cap;
+  uint32_t total_rays;
+  int32_t n_views;
+  int32_t base_depth;
+  int32_t max_steps;
+  int32_t cadence;
+  int32_t refill_lanes;
+  int32_t block_size;
+  int32_t grid;
+  int32_t path_levels;
+};
+
+// Launches the persistent trace kernel on `stream`.
+svo_status launch_trace(const TraceLaunch &a, bool with_stats, void *stream);
+// Dynamic shared memory the launch needs.
+size_t trace_smem_bytes(const TraceLaunch &a, bool bases_in_smem);
+int trace_occupancy(const TraceLaunch &a, bool with_stats);
+
+}  // namespace svo

@@ -1,0 +1,525 @@
+// Procedural scenes and the octree builder (host side of libsvo).
+//
+// The builder produces the reference's device format (SvoTracer.Domain/
+// TreeBuilder.cs:102-284): dense ushort base chunks for levels 1..B, a dense
+// level B+2 of 16-byte nodes at baseLocation, and deeper levels as 8-node
+// groups. Node addresses follow TreeBuilder's allocation order exactly:
+//   * level B+2 nodes sit at (level-(B+1) cell index << 3) + octant and exist
+//     only under level-(B+1) cells whose base chunk pair is air+geometry;
+//   * groups are taken from a queue that holds the sorted unused level-(B+1)
+//     slots first, then 8^(B+1), 8^(B+1)+1, ... (TreeBuilder.cs:113-118);
+//   * level B+2 nodes are visited x-major, then y, then z (TreeBuilder.cs:
+//     123-141), and each subtree is filled depth-first, a group being taken the
+//     moment a node turns out to need children (BuildBlocks, :237-256).
+// That order is sequential by nature; this builder gets the same addresses in
+// parallel by building each level-(B+2) subtree with local group numbers on
+// its own thread, prefix-summing the group counts in visiting order and then
+// mapping local group j of subtree k to queue entry offset_k + j.
+//
+// Geometry is the seeded scene of the workload, not the reference's analytic
+// spheres/cubes: a displaced SDF sphere or an fBm heightfield terrain. Cells
+// are classified exactly with respect to a leaf grid one level below the
+// deepest node level (a node's chunk describes its 8 children).
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <memory>
+#include <new>
+#include <stdexcept>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "../../include/svo.h"
+#include "svo_internal.h"
+
+namespace svo {
+namespace {
+
+inline uint32_t mix32(uint32_t h) {
+  h ^= h >> 16;
+  h *= 0x7feb352dU;
+  h ^= h >> 15;
+  h *= 0x846ca68bU;
+  h ^= h >> 16;
+  return h;
+}
+
+inline uint32_t hash4(uint32_t seed, uint32_t a, uint32_t b, uint32_t c, uint32_t d) {
+  uint32_t h = mix32(seed ^ 0x9e3779b9U);
+  h = mix32(h ^ a);
+  h = mix32(h + 0x632be5abU ^ b);
+  h = mix32(h + 0x85157af5U ^ c);
+  h = mix32(h + 0x2545f491U ^ d);
+  return h;
+}
+
+inline double unit_hash(uint32_t h) { return (h >> 8) * (1.0 / 16777216.0); }
+
+inline double quintic(double t) { return t * t * t * (t * (t * 6.0 - 15.0) + 10.0); }
+
+uint32_t morton3(uint32_t x, uint32_t y, uint32_t z) {
+  uint32_t out = 0;
+  for (int i = 0; i < 11; i++) {
+    out |= ((x >> i) & 1u) << (3 * i);
+    out |= ((y >> i) & 1u) << (3 * i + 1);
+    out |= ((z >> i) & 1u) << (3 * i + 2);
+  }
+  return out;
+}
+
+uint32_t pow_sum(int depth) {
+  uint32_t s = 0, p = 1;
+  for (int i = 1; i <= depth; i++) {
+    p *= 8;
+    s += p;
+  }
+  return s;
+}
+
+// Cell classification at `level` (coords in [0, 2^level)) against the leaf
+// grid at level `leaf`: geo = some leaf cell inside is solid, air = some is not.
+struct Scene {
+  int leaf = 0;
+  uint32_t seed = 0;
+  virtual ~Scene() = default;
+  virtual void classify(int level, uint32_t cx, uint32_t cy, uint32_t cz, bool &geo, bool &air) const = 0;
+  virtual void colour(int level, uint32_t cx, uint32_t cy, uint32_t cz, uint8_t rgb[3]) const = 0;
+};
+
+// Sphere of radius 0.2 (0.4 of the [-1,1] world) at the cube centre, displaced
+// by 3 octaves of seeded value noise of amplitude 0.025 (0.05 world). A leaf
+// cell is solid when the displaced SDF at its centre is <= 0. Coarser cells
+// use a Lipschitz bound of the SDF to decide whole cells at once.
+struct SphereScene final : Scene {
+  double cx = 0.5, cy = 0.5, cz = 0.5, radius = 0.2, amp = 0.025, f0 = 4.0;
+  double lip = 0.0;
+  SphereScene(uint32_t s, int leaf_level) {
+    seed = s;
+    leaf = leaf_level;
+    // |grad n| <= sqrt(3) * 1.875 * sum_o (2 a_o / sum a) f_o for value noise
+    // in [-1,1] with quintic fade (max slope 1.875).
+    double sum_a = 1.0 + 0.5 + 0.25, g = 0.0, f = f0, a = 1.0;
+    for (int o = 0; o < 3; o++, f *= 2.0, a *= 0.5) g += 2.0 * a / sum_a * 1.875 * f;
+    lip = (1.0 + amp * std::sqrt(3.0) * g) * 1.01;
+  }
+  double noise3(double x, double y, double z, uint32_t oct) const {
+    double fx = std::floor(x), fy = std::floor(y), fz = std::floor(z);
+    int32_t ix = (int32_t)fx, iy = (int32_t)fy, iz = (int32_t)fz;
+    double tx = quintic(x - fx), ty = quintic(y - fy), tz = quintic(z - fz);
+    double v[8];
+    for (int k = 0; k < 8; k++)
+      v[k] = unit_hash(hash4(seed, oct, (uint32_t)(ix + (k & 1)), (uint32_t)(iy + ((k >> 1) & 1)),
+                             (uint32_t)(iz + ((k >> 2) & 1))));
+    double x00 = v[0] + (v[1] - v[0]) * tx, x10 = v[2] + (v[3] - v[2]) * tx;
+    double x01 = v[4] + (v[5] - v[4]) * tx, x11 = v[6] + (v[7] - v[6]) * tx;
+    double y0 = x00 + (x10 - x00) * ty, y1 = x01 + (x11 - x01) * ty;
+    return y0 + (y1 - y0) * tz;
+  }
+  double sdf(double x, double y, double z) const {
+    double n = 0.0, f = f0, a = 1.0, sum_a = 1.75;
+    for (uint32_t o = 0; o < 3; o++, f *= 2.0, a *= 0.5) n += a * (2.0 * noise3(x * f, y * f, z * f, o) - 1.0);
+    n /= sum_a;
+    double dx = x - cx, dy = y - cy, dz = z - cz;
+    return std::sqrt(dx * dx + dy * dy + dz * dz) - radius - amp * n;
+  }
+  void classify(int level, uint32_t x, uint32_t y, uint32_t z, bool &geo, bool &air) const override {
+    geo = air = false;
+    classify_rec(level, x, y, z, geo, air);
+  }
+  void classify_rec(int level, uint32_t x, uint32_t y, uint32_t z, bool &geo, bool &air) const {
+    double s = std::ldexp(1.0, -level);
+    double f = sdf((x + 0.5) * s, (y + 0.5) * s, (z + 0.5) * s);
+    if (level >= leaf) {
+      if (f <= 0.0)
+        geo = true;
+      else
+        air = true;
+      return;
+    }
+    double r = std::sqrt(3.0) * (0.5 * s - std::ldexp(0.5, -leaf));
+    if (f < -lip * r) {
+      geo = true;
+      return;
+    }
+    if (f > lip * r) {
+      air = true;
+      return;
+    }
+    for (int k = 0; k < 8 && !(geo && air); k++)
+      classify_rec(level + 1, 2 * x + (k & 1), 2 * y + ((k >> 1) & 1), 2 * z + ((k >> 2) & 1), geo, air);
+  }
+  void colour(int level, uint32_t x, uint32_t y, uint32_t z, uint8_t rgb[3]) const override {
+    uint32_t h = hash4(seed ^ 0x51ed270bU, (uint32_t)level, x, y, z);
+    rgb[0] = (uint8_t)(h & 0xff);
+    rgb[1] = (uint8_t)((h >> 8) & 0xff);
+    rgb[2] = (uint8_t)((h >> 16) & 0xff);
+  }
+};
+
+// fBm heightfield: 6 octaves of seeded 2-D value noise, lacunarity 2, gain
+// 0.5, heights 0..0.3 of the domain. Up is -z (the reference's sky is lit
+// from -z, wavefront.cl:1756), so a column of height h is solid for
+// z >= 1 - h. Heights are quantised to whole leaf cells; min/max pyramids
+// over the columns make cell classification O(1).
+struct TerrainScene final : Scene {
+  uint32_t res = 0;  // 2^leaf columns per axis
+  double f0 = 6.0, hmax = 0.3;
+  std::vector<std::vector<uint16_t>> lo, hi;  // per level l: 4^l entries
+  TerrainScene(uint32_t s, int leaf_level, int threads) {
+    seed = s;
+    leaf = leaf_level;
+    res = 1u << leaf;
+    lo.resize(leaf + 1);
+    hi.resize(leaf + 1);
+    lo[leaf].resize((size_t)res * res);
+    hi[leaf].resize((size_t)res * res);
+    parallel_for(threads, res, [&](uint32_t j) {
+      for (uint32_t i = 0; i < res; i++) {
+        double h = height((i + 0.5) / res, (j + 0.5) / res);
+        uint32_t H = (uint32_t)std::floor(h * res + 0.5);
+        if (H > res) H = res;
+        lo[leaf][(size_t)j * res + i] = (uint16_t)H;
+        hi[leaf][(size_t)j * res + i] = (uint16_t)H;
+      }
+    });
+    for (int l = leaf - 1; l >= 0; l--) {
+      uint32_t n = 1u << l;
+      lo[l].resize((size_t)n * n);
+      hi[l].resize((size_t)n * n);
+      const auto &clo = lo[l + 1], &chi = hi[l + 1];
+      parallel_for(threads, n, [&, n, l](uint32_t j) {
+        for (uint32_t i = 0; i < n; i++) {
+          size_t a = (size_t)(2 * j) * (2 * n) + 2 * i, b = a + 2 * n;
+          lo[l][(size_t)j * n + i] = std::min(std::min(clo[a], clo[a + 1]), std::min(clo[b], clo[b + 1]));
+          hi[l][(size_t)j * n + i] = std::max(std::max(chi[a], chi[a + 1]), std::max(chi[b], chi[b + 1]));
+        }
+      });
+    }
+  }
+  template <class F>
+  static void parallel_for(int threads, uint32_t n, F f) {
+    std::atomic<uint32_t> next{0};
+    auto work = [&]() {
+      for (;;) {
+        uint32_t j = next.fetch_add(1);
+        if (j >= n) break;
+        f(j);
+      }
+    };
+    std::vector<std::thread> pool;
+    for (int t = 1; t < threads; t++) pool.emplace_back(work);
+    work();
+    for (auto &t : pool) t.join();
+  }
+  double noise2(double x, double y, uint32_t oct) const {
+    double fx = std::floor(x), fy = std::floor(y);
+    int32_t ix = (int32_t)fx, iy = (int32_t)fy;
+    double tx = quintic(x - fx), ty = quintic(y - fy);
+    double v00 = unit_hash(hash4(seed, oct, (uint32_t)ix, (uint32_t)iy, 7));
+    double v10 = unit_hash(hash4(seed, oct, (uint32_t)(ix + 1), (uint32_t)iy, 7));
+    double v01 = unit_hash(hash4(seed, oct, (uint32_t)ix, (uint32_t)(iy + 1), 7));
+    double v11 = unit_hash(hash4(seed, oct, (uint32_t)(ix + 1), (uint32_t)(iy + 1), 7));
+    double a = v00 + (v10 - v00) * tx, b = v01 + (v11 - v01) * tx;
+    return a + (b - a) * ty;
+  }
+  double height(double x, double y) const {
+    double n = 0.0, f = f0, a = 1.0, sum_a = 0.0;
+    for (uint32_t o = 0; o < 6; o++, f *= 2.0, a *= 0.5) {
+      n += a * noise2(x * f, y * f, o);
+      sum_a += a;
+    }
+    return hmax * (n / sum_a);
+  }
+  void classify(int level, uint32_t x, uint32_t y, uint32_t z, bool &geo, bool &air) const override {
+    size_t idx = (size_t)y * (1u << level) + x;
+    uint32_t s = 1u << (leaf - level);
+    uint32_t mx = hi[level][idx], mn = lo[level][idx];
+    // the deepest voxel row of the cell is solid somewhere / the top row is air somewhere
+    geo = (int64_t)mx > (int64_t)res - (int64_t)(z + 1) * s;
+    air = (int64_t)mn < (int64_t)res - (int64_t)z * s;
+  }
+  void colour(int level, uint32_t x, uint32_t y, uint32_t z, uint8_t rgb[3]) const override {
+    double zc = (z + 0.5) * std::ldexp(1.0, -level);
+    double h = 1.0 - zc;  // height above the bottom face
+    int base[3];
+    if (h < 0.06) {
+      base[0] = 194; base[1] = 178; base[2] = 128;  // sand
+    } else if (h < 0.14) {
+      base[0] = 86; base[1] = 125; base[2] = 70;    // grass
+    } else if (h < 0.22) {
+      base[0] = 120; base[1] = 110; base[2] = 100;  // rock
+    } else {
+      base[0] = 236; base[1] = 236; base[2] = 242;  // snow
+    }
+    uint32_t hsh = hash4(seed ^ 0x3c6ef372U, (uint32_t)level, x, y, z);
+    for (int k = 0; k < 3; k++) {
+      int j = (int)((hsh >> (8 * k)) % 17u) - 8;
+      int v = base[k] + j;
+      rgb[k] = (uint8_t)(v < 0 ? 0 : v > 255 ? 255 : v);
+    }
+  }
+};
+
+inline bool can_have_children(uint16_t chunk) {
+  for (int k = 0; k < 8; k++)
+    if (((chunk >> (2 * k)) & 3) == 3) return true;
+  return false;
+}
+
+// MakeChunk (TreeBuilder.cs:264-284) for the cell (x,y,z) at `level`.
+uint16_t make_chunk(const Scene &sc, int level, uint32_t x, uint32_t y, uint32_t z) {
+  uint16_t chunk = 0;
+  for (int k = 0; k < 8; k++) {
+    bool geo, air;
+    sc.classify(level + 1, 2 * x + (k & 1), 2 * y + ((k >> 1) & 1), 2 * z + ((k >> 2) & 1), geo, air);
+    chunk |= (uint16_t)((air ? 1 : 0) << (2 * k));
+    chunk |= (uint16_t)((geo ? 1 : 0) << (2 * k + 1));
+  }
+  return chunk;
+}
+
+svo_block make_block(const Scene &sc, int level, uint32_t x, uint32_t y, uint32_t z) {
+  svo_block b;
+  std::memset(&b, 0, sizeof(b));
+  b.child = SVO_NO_CHILD;
+  b.chunk = make_chunk(sc, level, x, y, z);
+  b.opacity = 255;
+  uint8_t rgb[3];
+  sc.colour(level, x, y, z, rgb);
+  b.colour_r = rgb[0];
+  b.colour_g = rgb[1];
+  b.colour_b = rgb[2];
+  return b;
+}
+
+// Colour of a node with children: integer mean over the children whose
+// octant holds geometry (the node's own colour otherwise).
+void mean_colour(svo_block &parent, const svo_block *children) {
+  uint32_t s[3] = {0, 0, 0}, n = 0;
+  for (int k = 0; k < 8; k++)
+    if ((parent.chunk >> (2 * k + 1)) & 1) {
+      s[0] += children[k].colour_r;
+      s[1] += children[k].colour_g;
+      s[2] += children[k].colour_b;
+      n++;
+    }
+  if (n) {
+    parent.colour_r = (uint8_t)(s[0] / n);
+    parent.colour_g = (uint8_t)(s[1] / n);
+    parent.colour_b = (uint8_t)(s[2] / n);
+  }
+}
+
+// One level-(B+2) subtree with local group numbers (child = local group,
+// SVO_NO_CHILD = none).
+struct Subtree {
+  std::vector<svo_block> blocks;  // 8 per local group, pre-order of groups
+};
+
+// BuildBlocks (TreeBuilder.cs:237-256) with local allocation: group numbers
+// 0,1,2,... are handed out in the order the queue would be dequeued.
+void build_children(const Scene &sc, Subtree &st, uint32_t group, int level, uint32_t px, uint32_t py, uint32_t pz,
+                    int max_depth) {
+  for (int i = 0; i < 8; i++) {
+    uint32_t x = 2 * px + (i & 1), y = 2 * py + ((i >> 1) & 1), z = 2 * pz + ((i >> 2) & 1);
+    svo_block b = make_block(sc, level, x, y, z);
+    if (level < max_depth && can_have_children(b.chunk)) {
+      uint32_t g = (uint32_t)(st.blocks.size() / 8);
+      st.blocks.resize(st.blocks.size() + 8);
+      b.child = g;
+      build_children(sc, st, g, level + 1, x, y, z, max_depth);
+      mean_colour(b, &st.blocks[(size_t)g * 8]);
+    }
+    st.blocks[(size_t)group * 8 + i] = b;
+  }
+}
+
+}  // namespace
+
+struct TreeHost {
+  uint8_t base_depth = 0;
+  uint32_t block_count = 0;  // TreeBuilder's BlockCount
+  std::vector<uint16_t> bases;
+  std::vector<svo_block> blocks;
+};
+
+svo_status build_tree(const svo_scene_params &p, TreeHost &tree) {
+  const int B = p.base_depth, D = p.max_depth;
+  if (B < 1 || B > 6) return fail(SVO_ERR_INVALID_ARGUMENT, "svo_tree_build: base_depth must be 1..6");
+  if (D < B + 2 || D > 16) return fail(SVO_ERR_INVALID_ARGUMENT, "svo_tree_build: max_depth must be base_depth+2..16");
+  int threads = p.threads > 0 ? p.threads : (int)std::max(1u, std::thread::hardware_concurrency());
+  const int leaf = D + 1;
+  std::unique_ptr<Scene> sc;
+  if (p.kind == SVO_SCENE_SPHERE)
+    sc.reset(new SphereScene(p.seed, leaf));
+  else if (p.kind == SVO_SCENE_TERRAIN)
+    sc.reset(new TerrainScene(p.seed, leaf, threads));
+  else
+    return fail(SVO_ERR_INVALID_ARGUMENT, "svo_tree_build: unknown scene kind");
+
+  uint64_t max_size = p.max_size ? p.max_size : 0xFFFFFFFFull / 64;
+  const uint64_t dense = 1ull << (3 * (B + 2));
+  if (max_size < dense) max_size = dense;  // TreeBuilder.cs:105
+  const uint64_t queue_end = max_size >> 3;
+
+  tree.base_depth = (uint8_t)B;
+  tree.bases.assign(pow_sum(B), 0);
+  // BuildBaseChunks, TreeBuilder.cs:152-172
+  for (int d = 1; d <= B; d++) {
+    uint32_t n = 1u << d, start = pow_sum(d - 1);
+    TerrainScene::parallel_for(threads, n, [&, n, start, d](uint32_t z) {
+      for (uint32_t y = 0; y < n; y++)
+        for (uint32_t x = 0; x < n; x++) tree.bases[start + morton3(x, y, z)] = make_chunk(*sc, d, x, y, z);
+    });
+  }
+
+  // PopulateInitialBlocks, TreeBuilder.cs:180-227
+  const uint32_t scan_n = 1u << (B + 1), base_start = pow_sum(B - 1);
+  std::vector<uint8_t> populated((size_t)1 << (3 * (B + 1)), 0);
+  for (uint32_t z = 0; z < scan_n; z++)
+    for (uint32_t y = 0; y < scan_n; y++)
+      for (uint32_t x = 0; x < scan_n; x++) {
+        uint32_t pos = morton3(x, y, z);
+        populated[pos] = ((tree.bases[base_start + (pos >> 3)] >> ((pos & 7) * 2)) & 3) == 3;
+      }
+  std::vector<uint32_t> empty_slots;
+  for (uint32_t pos = 0; pos < populated.size(); pos++)
+    if (!populated[pos]) empty_slots.push_back(pos);  // already sorted
+  std::vector<svo_block> level2(dense);
+  std::memset(level2.data(), 0, dense * sizeof(svo_block));
+  std::vector<uint8_t> need(dense, 0);
+  uint32_t block_count = 0;
+  const uint32_t n2 = 1u << (B + 2);
+  TerrainScene::parallel_for(threads, scan_n, [&](uint32_t z) {
+    for (uint32_t y = 0; y < scan_n; y++)
+      for (uint32_t x = 0; x < scan_n; x++) {
+        uint32_t pos = morton3(x, y, z);
+        if (!populated[pos]) continue;
+        for (int k = 0; k < 8; k++) {
+          uint32_t bx = 2 * x + (k & 1), by = 2 * y + ((k >> 1) & 1), bz = 2 * z + ((k >> 2) & 1);
+          uint32_t a = (pos << 3) + (uint32_t)k;
+          level2[a] = make_block(*sc, B + 2, bx, by, bz);
+          need[a] = D > B + 2 && can_have_children(level2[a].chunk);
+        }
+      }
+  });
+  for (uint32_t pos = 0; pos < populated.size(); pos++)
+    if (populated[pos]) block_count = std::max(block_count, (pos << 3) + 8);
+
+  // Level-(B+2) subtrees in TreeBuilder's x, y, z visiting order.
+  std::vector<uint32_t> roots;
+  for (uint32_t x = 0; x < n2; x++)
+    for (uint32_t y = 0; y < n2; y++)
+      for (uint32_t z = 0; z < n2; z++) {
+        uint32_t a = morton3(x, y, z);
+        if (need[a]) roots.push_back(a);
+      }
+  std::vector<Subtree> subs(roots.size());
+  TerrainScene::parallel_for(threads, (uint32_t)roots.size(), [&](uint32_t r) {
+    uint32_t a = roots[r];
+    uint32_t x = 0, y = 0, z = 0;
+    for (int i = 0; i < B + 2; i++) {
+      x |= ((a >> (3 * i)) & 1u) << i;
+      y |= ((a >> (3 * i + 1)) & 1u) << i;
+      z |= ((a >> (3 * i + 2)) & 1u) << i;
+    }
+    Subtree &st = subs[r];
+    st.blocks.resize(8);
+    build_children(*sc, st, 0, B + 3, x, y, z, D);
+    mean_colour(level2[a], st.blocks.data());
+  });
+
+  // Queue positions: subtree r owns [off[r], off[r] + groups_r).
+  std::vector<uint64_t> off(roots.size() + 1, 0);
+  for (size_t r = 0; r < roots.size(); r++) off[r + 1] = off[r] + subs[r].blocks.size() / 8;
+  const uint64_t capacity = empty_slots.size() + (queue_end > (1ull << (3 * (B + 1))) ? queue_end - (1ull << (3 * (B + 1))) : 0);
+  if (off.back() > capacity)
+    return fail(SVO_ERR_BUDGET, "svo_tree_build: tree needs " + std::to_string(off.back()) +
+                                    " block groups but max_size allows " + std::to_string(capacity));
+  auto queue_at = [&](uint64_t q) -> uint32_t {
+    return q < empty_slots.size() ? empty_slots[q] : (uint32_t)((1ull << (3 * (B + 1))) + (q - empty_slots.size()));
+  };
+  uint64_t max_group = dense / 8 - 1;
+  if (off.back() > 0) max_group = std::max<uint64_t>(max_group, queue_at(off.back() - 1));
+  for (uint64_t q = 0; q < off.back() && q < empty_slots.size(); q++) max_group = std::max<uint64_t>(max_group, queue_at(q));
+  tree.blocks.assign((max_group + 1) * 8, svo_block{});
+  std::memcpy(tree.blocks.data(), level2.data(), dense * sizeof(svo_block));
+  TerrainScene::parallel_for(threads, (uint32_t)roots.size(), [&](uint32_t r) {
+    const Subtree &st = subs[r];
+    tree.blocks[roots[r]].child = queue_at(off[r]) << 3;
+    size_t groups = st.blocks.size() / 8;
+    for (size_t g = 0; g < groups; g++) {
+      uint32_t dst = queue_at(off[r] + g) << 3;
+      for (int i = 0; i < 8; i++) {
+        svo_block b = st.blocks[g * 8 + i];
+        if (b.child != SVO_NO_CHILD) b.child = queue_at(off[r] + b.child) << 3;
+        tree.blocks[dst + i] = b;
+      }
+    }
+  });
+
+  // TreeBuilder's BlockCount bookkeeping (TreeBuilder.cs:216 and :254, with
+  // its "<" comparison) replayed in the order BuildBlocks writes nodes.
+  struct Rec {
+    static void walk(const std::vector<svo_block> &bl, uint32_t addr, uint32_t &bc) {
+      for (uint32_t i = 0; i < 8; i++) {
+        uint32_t c = bl[addr + i].child;
+        if (c != SVO_NO_CHILD) walk(bl, c, bc);
+        if (bc < addr + i) bc = addr + i + 1;
+      }
+    }
+  };
+  for (uint32_t a : roots) Rec::walk(tree.blocks, tree.blocks[a].child, block_count);
+  tree.block_count = block_count;
+  return SVO_OK;
+}
+
+}  // namespace svo
+
+using svo::TreeHost;
+
+extern "C" {
+
+SVO_API svo_status svo_tree_build(const svo_scene_params *params, void **tree) {
+  if (!params || !tree) return svo::fail(SVO_ERR_INVALID_ARGUMENT, "svo_tree_build: null argument");
+  try {
+    std::unique_ptr<TreeHost> t(new TreeHost);
+    svo_status st = svo::build_tree(*params, *t);
+    if (st != SVO_OK) return st;
+    *tree = t.release();
+    return SVO_OK;
+  } catch (const std::bad_alloc &) {
+    return svo::fail(SVO_ERR_OUT_OF_MEMORY, "svo_tree_build: out of host memory");
+  } catch (const std::exception &e) {
+    return svo::fail(SVO_ERR_INTERNAL, std::string("svo_tree_build: ") + e.what());
+  }
+}
+
+SVO_API svo_status svo_tree_info(void *tree, uint8_t *base_depth, size_t *n_bases, size_t *n_blocks,
+                                 uint32_t *block_count) {
+  if (!tree) return svo::fail(SVO_ERR_INVALID_ARGUMENT, "svo_tree_info: null tree");
+  auto *t = static_cast<TreeHost *>(tree);
+  if (base_depth) *base_depth = t->base_depth;
+  if (n_bases) *n_bases = t->bases.size();
+  if (n_blocks) *n_blocks = t->blocks.size();
+  if (block_count) *block_count = t->block_count;
+  return SVO_OK;
+}
+
+SVO_API svo_status svo_tree_data(void *tree, const uint16_t **bases, const svo_block **blocks) {
+  if (!tree) return svo::fail(SVO_ERR_INVALID_ARGUMENT, "svo_tree_data: null tree");
+  auto *t = static_cast<TreeHost *>(tree);
+  if (bases) *bases = t->bases.data();
+  if (blocks) *blocks = t->blocks.data();
+  return SVO_OK;
+}
+
+SVO_API svo_status svo_tree_free(void *tree) {
+  delete static_cast<TreeHost *>(tree);
+  return SVO_OK;
+}
+
+}  // extern "C"

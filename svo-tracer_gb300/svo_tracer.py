@@ -1,0 +1,400 @@
+"""Python host binding of libsvo (ctypes over include/svo.h).
+
+Mirrors the reference's host-side surface for the trace path:
+
+* ``Octree`` / ``TreeBuilder``: SvoTracer.Domain/Models/Octree.cs and
+  ITreeBuilder.BuildTree (SvoTracer.Domain/TreeBuilder.cs:102-150);
+* ``TraceInput``: SvoTracer.Domain/Models/TraceInput.cs with the OpenCL layout of
+  wavefront.cl:53-75;
+* ``Tracer``: the ComputeManager + MainWindow.RunWavefront pair
+  (SvoTracer.Kernel/ComputeManager.cs, SvoTracer.Window/MainWindow.cs:356-622).
+  Errors raise ``SvoError("{method}: {code}")`` like ComputeManager.HandleResultCode
+  (ComputeManager.cs:283-287).
+
+There is no CPU fallback: if libsvo.so or a CUDA device is missing, every call
+raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+import os
+from dataclasses import dataclass, field
+
+import numpy as np
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "lib", "libsvo.so")
+
+# ---- OpenCL struct layouts (include/svo.h) ---------------------------------------
+
+BLOCK_DTYPE = np.dtype([
+    ("child", "<u4"), ("chunk", "<u2"), ("normal_pitch", "<i2"), ("normal_yaw", "<i2"),
+    ("colour_r", "u1"), ("colour_g", "u1"), ("colour_b", "u1"), ("opacity", "u1"),
+    ("specularity", "u1"), ("gloss", "u1"),
+])
+USAGE_DTYPE = np.dtype([("tick", "<u2"), ("_pad", "<u2"), ("parent", "<u4")])
+CHILD_REQUEST_DTYPE = np.dtype([
+    ("address", "<u4"), ("tick", "<u2"), ("depth", "u1"), ("_pad0", "u1"),
+    ("location", "<u8", (3,)), ("tree_size", "u1"), ("_pad1", "u1", (7,)),
+])
+assert BLOCK_DTYPE.itemsize == 16 and USAGE_DTYPE.itemsize == 8 and CHILD_REQUEST_DTYPE.itemsize == 40
+
+NO_CHILD = 0xFFFFFFFF
+MISS = 0xFFFFFFFF
+
+STATUS_NAMES = {
+    0: "Success", 1: "InvalidArgument", 2: "CudaError", 3: "OutOfMemory", 4: "QueueFull", 5: "Timeout",
+    6: "NoTree", 7: "StepLimit", 8: "Budget", 9: "NoDevice", 10: "Internal",
+}
+SCENE_SPHERE, SCENE_TERRAIN = 0, 1
+
+
+class SvoError(RuntimeError):
+    def __init__(self, method: str, code: int, detail: str = ""):
+        self.method, self.code, self.detail = method, code, detail
+        super().__init__("%s: %s%s" % (method, STATUS_NAMES.get(code, str(code)), (" (%s)" % detail) if detail else ""))
+
+
+class TraceInputC(C.Structure):
+    _fields_ = [
+        ("origin", C.c_float * 3), ("facing", C.c_float * 9), ("fov", C.c_float * 2), ("dof", C.c_float * 2),
+        ("screen_size", C.c_uint32 * 2), ("max_opacity", C.c_uint8), ("base_depth", C.c_uint8),
+        ("tick", C.c_uint16), ("max_child_request_id", C.c_uint32), ("fov_multiplier", C.c_float),
+        ("fov_constant", C.c_float), ("weighting_multiplier", C.c_float), ("weighting_constant", C.c_float),
+        ("ambient_light_level", C.c_uint8), ("_pad", C.c_uint8 * 7),
+    ]
+
+
+class TraceOutputC(C.Structure):
+    _fields_ = [("hit_index", C.c_void_p), ("hit_depth", C.c_void_p), ("t", C.c_void_p), ("rgba", C.c_void_p),
+                ("on_device", C.c_int32), ("_pad", C.c_int32)]
+
+
+class TraceStatsC(C.Structure):
+    _fields_ = [(n, C.c_uint64) for n in ("rays", "hits", "base_steps", "block_node_reads", "block_steps",
+                                           "child_requests", "step_limited")]
+
+
+class TraceConfigC(C.Structure):
+    _fields_ = [(n, C.c_int32) for n in ("block_size", "ctas_per_sm", "refill_lanes", "cadence", "max_steps",
+                                          "collect_stats", "_pad0", "_pad1")]
+
+
+class SceneParamsC(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("seed", C.c_uint32), ("base_depth", C.c_uint8), ("max_depth", C.c_uint8),
+                ("_pad", C.c_uint8 * 2), ("threads", C.c_int32), ("max_size", C.c_uint64)]
+
+
+assert C.sizeof(TraceInputC) == 104
+
+_lib = None
+
+
+def load_library(path: str | None = None) -> C.CDLL:
+    """Loads libsvo.so (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise SvoError("load_library", 9, "libsvo.so not built at %s; run __graft_entry__.build()" % p)
+    lib = C.CDLL(p)
+    vp, sz = C.c_void_p, C.c_size_t
+    sig = {
+        "svo_last_error_string": ([], C.c_char_p),
+        "svo_version": ([], C.c_char_p),
+        "svo_create": ([C.c_int32, C.POINTER(vp)], C.c_int32),
+        "svo_destroy": ([vp], C.c_int32),
+        "svo_set_stream": ([vp, vp], C.c_int32),
+        "svo_synchronize": ([vp], C.c_int32),
+        "svo_set_trace_config": ([vp, C.POINTER(TraceConfigC)], C.c_int32),
+        "svo_get_trace_config": ([vp, C.POINTER(TraceConfigC)], C.c_int32),
+        "svo_upload_octree": ([vp, C.c_uint8, vp, sz, vp, sz, C.c_uint32], C.c_int32),
+        "svo_init_usage": ([vp], C.c_int32),
+        "svo_read_usage": ([vp, vp, sz], C.c_int32),
+        "svo_write_usage": ([vp, vp, sz], C.c_int32),
+        "svo_read_blocks": ([vp, vp, sz, sz], C.c_int32),
+        "svo_read_bases": ([vp, vp, sz], C.c_int32),
+        "svo_tree_size": ([vp, C.POINTER(C.c_uint8), C.POINTER(sz), C.POINTER(sz), C.POINTER(sz)], C.c_int32),
+        "svo_trace": ([vp, C.POINTER(TraceInputC), C.POINTER(TraceOutputC)], C.c_int32),
+        "svo_trace_batch": ([vp, C.POINTER(TraceInputC), C.c_int32, C.POINTER(TraceOutputC)], C.c_int32),
+        "svo_trace_batch_graph": ([vp, C.POINTER(TraceInputC), C.c_int32, C.POINTER(TraceOutputC)], C.c_int32),
+        "svo_last_trace_stats": ([vp, C.POINTER(TraceStatsC)], C.c_int32),
+        "svo_read_ray_counts": ([vp, vp, vp, sz], C.c_int32),
+        "svo_read_child_requests": ([vp, vp, C.c_uint32, C.POINTER(C.c_uint32)], C.c_int32),
+        "svo_tree_build": ([C.POINTER(SceneParamsC), C.POINTER(vp)], C.c_int32),
+        "svo_tree_info": ([vp, C.POINTER(C.c_uint8), C.POINTER(sz), C.POINTER(sz), C.POINTER(C.c_uint32)], C.c_int32),
+        "svo_tree_data": ([vp, C.POINTER(vp), C.POINTER(vp)], C.c_int32),
+        "svo_tree_free": ([vp], C.c_int32),
+    }
+    for name, (args, res) in sig.items():
+        f = getattr(lib, name)
+        f.argtypes = args
+        f.restype = res
+    _lib = lib
+    return lib
+
+
+def _check(method: str, status: int) -> None:
+    if status != 0:
+        detail = load_library().svo_last_error_string().decode(errors="replace")
+        raise SvoError(method, status, detail)
+
+
+def _ptr(a: np.ndarray | None):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+# ---- domain types ------------------------------------------------------------------
+
+
+@dataclass
+class Octree:
+    """SvoTracer.Domain/Models/Octree.cs: BaseDepth, BlockCount, BaseBlocks, Blocks."""
+    BaseDepth: int
+    BlockCount: int
+    BaseBlocks: np.ndarray  # uint16[powSum(BaseDepth)]
+    Blocks: np.ndarray      # BLOCK_DTYPE[n]
+
+    @property
+    def n_groups(self) -> int:
+        return len(self.Blocks) // 8
+
+
+def pow_sum(depth: int) -> int:
+    return sum(8 ** i for i in range(1, depth + 1))
+
+
+class TreeBuilder:
+    """ITreeBuilder over the seeded procedural scenes (sphere, terrain)."""
+
+    def __init__(self, scene: int = SCENE_SPHERE, seed: int = 1, threads: int = 0):
+        self.scene, self.seed, self.threads = scene, seed, threads
+
+    def BuildTree(self, baseDepth: int, maxDepth: int, maxSize: int = 0) -> Octree:
+        lib = load_library()
+        p = SceneParamsC(kind=self.scene, seed=self.seed, base_depth=baseDepth, max_depth=maxDepth,
+                         threads=self.threads, max_size=maxSize)
+        h = C.c_void_p()
+        _check("BuildTree", lib.svo_tree_build(C.byref(p), C.byref(h)))
+        try:
+            bd, nb, nk, bc = C.c_uint8(), C.c_size_t(), C.c_size_t(), C.c_uint32()
+            _check("BuildTree", lib.svo_tree_info(h, C.byref(bd), C.byref(nb), C.byref(nk), C.byref(bc)))
+            pb, pk = C.c_void_p(), C.c_void_p()
+            _check("BuildTree", lib.svo_tree_data(h, C.byref(pb), C.byref(pk)))
+            bases = np.ctypeslib.as_array(C.cast(pb, C.POINTER(C.c_uint16)), shape=(nb.value,)).copy()
+            raw = np.ctypeslib.as_array(C.cast(pk, C.POINTER(C.c_uint8)), shape=(nk.value * 16,)).copy()
+            blocks = raw.view(BLOCK_DTYPE)
+            return Octree(bd.value, bc.value, bases, blocks)
+        finally:
+            lib.svo_tree_free(h)
+
+    build_tree = BuildTree
+
+
+@dataclass
+class TraceInput:
+    """SvoTracer.Domain/Models/TraceInput.cs. Facing is column-major (forward, right, up columns)."""
+    Origin: tuple = (0.0, 0.0, 0.0)
+    Facing: tuple = (1, 0, 0, 0, 1, 0, 0, 0, 1)
+    FoV: tuple = (math.pi / 4, math.pi / 4)
+    DoF: tuple = (0.0, 0.0)
+    ScreenSize: tuple = (640, 480)
+    MaxOpacity: int = 200
+    BaseDepth: int = 0
+    Tick: int = 1
+    MaxChildRequestId: int = 6000
+    FovMultiplier: float = 0.2
+    FovConstant: float = 0.2
+    WeightingMultiplier: float = -0.05
+    WeightingConstant: float = 0.5
+    AmbientLightLevel: int = 100
+
+    def to_c(self) -> TraceInputC:
+        c = TraceInputC()
+        c.origin[:] = [float(v) for v in self.Origin]
+        c.facing[:] = [float(v) for v in self.Facing]
+        c.fov[:] = [float(v) for v in self.FoV]
+        c.dof[:] = [float(v) for v in self.DoF]
+        c.screen_size[:] = [int(v) for v in self.ScreenSize]
+        c.max_opacity = self.MaxOpacity
+        c.base_depth = self.BaseDepth
+        c.tick = self.Tick
+        c.max_child_request_id = self.MaxChildRequestId
+        c.fov_multiplier = self.FovMultiplier
+        c.fov_constant = self.FovConstant
+        c.weighting_multiplier = self.WeightingMultiplier
+        c.weighting_constant = self.WeightingConstant
+        c.ambient_light_level = self.AmbientLightLevel
+        return c
+
+    def to_bytes(self) -> bytes:
+        return bytes(self.to_c())
+
+
+def look_at(origin, target, width: int, height: int, fov_deg: float, up=(0.0, 0.0, -1.0), **kw) -> TraceInput:
+    """Camera at `origin` (unit-cube coordinates) looking at `target`.
+
+    World up is -z (the reference lights its sky from -z, wavefront.cl:1756). FoV[0]
+    is the horizontal angle and FoV[1] = FoV[0] * H / W (equi-angular rays)."""
+    o = np.asarray(origin, dtype=np.float64)
+    f = np.asarray(target, dtype=np.float64) - o
+    f /= np.linalg.norm(f)
+    u = np.asarray(up, dtype=np.float64)
+    r = np.cross(f, u)
+    if np.linalg.norm(r) < 1e-9:
+        r = np.cross(f, np.array([1.0, 0.0, 0.0]))
+    r /= np.linalg.norm(r)
+    u2 = np.cross(r, f)
+    facing = tuple(float(v) for v in np.concatenate([f, r, u2]).astype(np.float32))
+    fx = math.radians(fov_deg)
+    return TraceInput(Origin=tuple(float(v) for v in np.float32(o)), Facing=facing,
+                      FoV=(float(np.float32(fx)), float(np.float32(fx * height / width))),
+                      ScreenSize=(width, height), **kw)
+
+
+@dataclass
+class TraceResult:
+    hit_index: np.ndarray
+    hit_depth: np.ndarray
+    t: np.ndarray
+    rgba: np.ndarray
+
+
+class Tracer:
+    """Context of one GPU: octree residency, usage ticks, child requests, traces."""
+
+    def __init__(self, device: int = 0):
+        self._lib = load_library()
+        self._ctx = C.c_void_p()
+        self._req_cap = 0
+        _check("ComputeManagerFactory.Build", self._lib.svo_create(device, C.byref(self._ctx)))
+
+    # ComputeManager.Dispose
+    def close(self) -> None:
+        if self._ctx:
+            self._lib.svo_destroy(self._ctx)
+            self._ctx = C.c_void_p()
+
+    Dispose = close
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def handle(self) -> C.c_void_p:
+        return self._ctx
+
+    def set_stream(self, stream_ptr: int | None) -> None:
+        _check("SetStream", self._lib.svo_set_stream(self._ctx, C.c_void_p(stream_ptr or 0)))
+
+    def synchronize(self) -> None:
+        _check("Synchronize", self._lib.svo_synchronize(self._ctx))
+
+    def set_config(self, **kw) -> None:
+        cfg = self.get_config()
+        for k, v in kw.items():
+            setattr(cfg, k, int(v))
+        _check("SetTraceConfig", self._lib.svo_set_trace_config(self._ctx, C.byref(cfg)))
+
+    def get_config(self) -> TraceConfigC:
+        cfg = TraceConfigC()
+        _check("GetTraceConfig", self._lib.svo_get_trace_config(self._ctx, C.byref(cfg)))
+        return cfg
+
+    # MainWindow.SetupWavefrontKernels: InitReadBuffer(Bases, Blocks)
+    def upload(self, tree: Octree, block_budget: int = 0) -> None:
+        bases = np.ascontiguousarray(tree.BaseBlocks, dtype=np.uint16)
+        blocks = np.ascontiguousarray(tree.Blocks)
+        assert blocks.dtype == BLOCK_DTYPE
+        _check("InitReadBuffer", self._lib.svo_upload_octree(self._ctx, tree.BaseDepth, _ptr(bases), len(bases),
+                                                             _ptr(blocks), len(blocks), block_budget))
+
+    def init_usage(self) -> None:
+        _check("InitUsage", self._lib.svo_init_usage(self._ctx))
+
+    def tree_size(self):
+        bd, nb, nk, bu = C.c_uint8(), C.c_size_t(), C.c_size_t(), C.c_size_t()
+        _check("TreeSize", self._lib.svo_tree_size(self._ctx, C.byref(bd), C.byref(nb), C.byref(nk), C.byref(bu)))
+        return bd.value, nb.value, nk.value, bu.value
+
+    def read_usage(self, n_groups: int | None = None) -> np.ndarray:
+        if n_groups is None:
+            n_groups = self.tree_size()[3] // 8
+        out = np.zeros(n_groups, dtype=USAGE_DTYPE)
+        _check("ReadBuffer:Usages", self._lib.svo_read_usage(self._ctx, _ptr(out), n_groups))
+        return out
+
+    def write_usage(self, usage: np.ndarray) -> None:
+        u = np.ascontiguousarray(usage, dtype=USAGE_DTYPE)
+        _check("WriteBuffer:Usages", self._lib.svo_write_usage(self._ctx, _ptr(u), len(u)))
+
+    def read_blocks(self, first: int = 0, n: int | None = None) -> np.ndarray:
+        if n is None:
+            n = self.tree_size()[3] - first
+        out = np.zeros(n, dtype=BLOCK_DTYPE)
+        _check("ReadBuffer:Blocks", self._lib.svo_read_blocks(self._ctx, _ptr(out), first, n))
+        return out
+
+    @staticmethod
+    def _alloc(w: int, h: int) -> TraceResult:
+        n = w * h
+        return TraceResult(np.empty(n, np.uint32), np.empty(n, np.uint8), np.empty(n, np.float32),
+                           np.empty((n, 4), np.float32))
+
+    @staticmethod
+    def _out(r: TraceResult) -> TraceOutputC:
+        return TraceOutputC(_ptr(r.hit_index), _ptr(r.hit_depth), _ptr(r.t), _ptr(r.rgba), 0, 0)
+
+    # MainWindow.RunWavefront for one view, results in host memory
+    def trace(self, inp: TraceInput) -> TraceResult:
+        r = self._alloc(*inp.ScreenSize)
+        c_in, c_out = inp.to_c(), self._out(r)
+        self._req_cap = inp.MaxChildRequestId
+        _check("RunWavefront", self._lib.svo_trace(self._ctx, C.byref(c_in), C.byref(c_out)))
+        return r
+
+    def trace_batch(self, inputs, graph: bool = False):
+        res = [self._alloc(*i.ScreenSize) for i in inputs]
+        c_in = (TraceInputC * len(inputs))(*[i.to_c() for i in inputs])
+        c_out = (TraceOutputC * len(inputs))(*[self._out(r) for r in res])
+        fn = self._lib.svo_trace_batch_graph if graph else self._lib.svo_trace_batch
+        self._req_cap = max(i.MaxChildRequestId for i in inputs)
+        _check("RunWavefrontBatch", fn(self._ctx, c_in, len(inputs), c_out))
+        return res
+
+    def trace_device(self, inputs, outputs, graph: bool = False) -> None:
+        """Trace into caller-owned device buffers: outputs is a list of
+        (hit_index_ptr, hit_depth_ptr, t_ptr, rgba_ptr) device addresses (0 = skip)."""
+        c_in = (TraceInputC * len(inputs))(*[i.to_c() for i in inputs])
+        c_out = (TraceOutputC * len(inputs))(*[TraceOutputC(o[0] or None, o[1] or None, o[2] or None, o[3] or None, 1, 0)
+                                               for o in outputs])
+        fn = self._lib.svo_trace_batch_graph if graph else self._lib.svo_trace_batch
+        self._req_cap = max(i.MaxChildRequestId for i in inputs)
+        _check("RunWavefrontDevice", fn(self._ctx, c_in, len(inputs), c_out))
+
+    def stats(self) -> dict:
+        s = TraceStatsC()
+        _check("TraceStats", self._lib.svo_last_trace_stats(self._ctx, C.byref(s)))
+        return {n: getattr(s, n) for n, _ in TraceStatsC._fields_}
+
+    def ray_counts(self, n: int):
+        vb, vs = np.zeros(n, np.uint32), np.zeros(n, np.uint32)
+        _check("RayCounts", self._lib.svo_read_ray_counts(self._ctx, _ptr(vb), _ptr(vs), n))
+        return vb, vs
+
+    def read_child_requests(self, cap: int = 1 << 20):
+        out = np.zeros(cap, dtype=CHILD_REQUEST_DTYPE)
+        n = C.c_uint32()
+        _check("ReadBuffer:ChildRequests", self._lib.svo_read_child_requests(self._ctx, _ptr(out), cap, C.byref(n)))
+        return out[: min(n.value, cap, self._req_cap)], n.value
