@@ -1,0 +1,312 @@
+"""Benchmark: 1080p single-view wavefront trace over the depth-11 fBm terrain octree.
+
+One step = one full frame (1920x1080 primary rays: ray generation, base/block
+traversal with the cone LOD stop, usage stamping, child requests, shading and the
+final colour) over a ~48M-node tree resident in HBM.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints one JSON line. `value` is kernel-timed Mrays/s with the tree and outputs on
+the device (L2 flushed between steps); `e2e` is the same metric through the public
+API with host buffers (input upload and result download inside the timed region);
+`roofline` uses the algorithmic bytes of the reference's walk (16 B per node read of
+getBlockAddress + 2 B per base chunk read + 25 B of per-pixel output).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "svo-tracer_gb300"))
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+WIDTH, HEIGHT = 1920, 1080
+BASE_DEPTH, MAX_DEPTH, SEED = 4, 11, 5
+CAM_ORIGIN, CAM_TARGET, FOV = (0.08, 0.12, 0.62), (0.75, 0.8, 0.88), 60.0
+METRIC = "Mrays/s 1080p"
+OUT_BYTES = 4 + 1 + 4 + 16  # hit index, hit depth, t, float4 RGBA
+
+
+def workload(st):
+    tree = st.TreeBuilder(st.SCENE_TERRAIN, seed=SEED).BuildTree(BASE_DEPTH, MAX_DEPTH)
+    cam = st.look_at(CAM_ORIGIN, CAM_TARGET, WIDTH, HEIGHT, FOV, Tick=7, MaxChildRequestId=1 << 16)
+    return tree, cam
+
+
+def config_dict(tree, extra=None):
+    d = {"workload": "1920x1080 single view, depth-11 fBm terrain octree (seeded, 6 octaves)",
+         "width": WIDTH, "height": HEIGHT, "base_depth": BASE_DEPTH, "max_depth": MAX_DEPTH,
+         "nodes": int(len(tree.Blocks)), "tree_bytes": int(tree.Blocks.nbytes),
+         "l2": "flushed between steps (256 MiB write)"}
+    if extra:
+        d.update(extra)
+    return d
+
+
+class ClockSampler:
+    FIELDS = "clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown," \
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown," \
+             "clocks_event_reasons.sw_power_cap"
+
+    def __init__(self, index: int):
+        self.index, self.rows, self.proc = index, [], None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4) if len(r) > 4 + i and r[4 + i] == "Active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def measured_peak():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def ncu_traffic():
+    """dram bytes per launch of the trace kernel from the committed ncu summary."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "trace_kernel_terrain1080p_traffic.json")) as f:
+            d = json.load(f)
+        return float(d["dram_bytes_per_launch"])
+    except (OSError, KeyError, ValueError):
+        return None
+
+
+def cpu_sample(tree, cam, kind, budget_s=12.0):
+    """The CPU implementation over row bands of the same frame until ~budget_s."""
+    import pyoracle as po
+
+    threads = os.cpu_count() or 1
+    rows_per_band = 40 if kind == "reference" else 270
+    rays = 0
+    t0 = time.perf_counter()
+    band = 0
+    while True:
+        r0 = (band * rows_per_band) % HEIGHT
+        r1 = min(HEIGHT, r0 + rows_per_band)
+        if kind == "reference":
+            po.ref_trace_rows(tree, cam, r0, r1, threads=threads)
+        else:
+            po.trace_rows(tree, cam, r0, r1, threads=threads)
+        rays += (r1 - r0) * WIDTH
+        band += 1
+        el = time.perf_counter() - t0
+        if el >= budget_s or band * rows_per_band >= 4 * HEIGHT:
+            break
+    return {"value": rays / el / 1e6, "unit": "Mrays/s", "cores": threads, "kind": kind,
+            "sample": "%d rays in %d row bands of %d rows of the 1080p frame, %.1f s" % (rays, band, rows_per_band, el)}
+
+
+def run_reference(args, rank, world):
+    """The reference's own wavefront.cl kernels, built for the host CPU, on the same frame."""
+    if rank != 0:
+        return
+    import pyoracle as po
+    import svo_tracer as st
+
+    if not po.ref_available():
+        print(json.dumps({"impl": "reference", "unavailable": "reference kernels (oracle/_ref) not built on this host"}))
+        return
+    tree, cam = workload(st)
+    threads = os.cpu_count() or 1
+    rows = 24
+    times = []
+    for i in range(args.warmup + args.steps):
+        r0 = (i * rows) % HEIGHT
+        t0 = time.perf_counter()
+        po.ref_trace_rows(tree, cam, r0, r0 + rows, threads=threads)
+        if i >= args.warmup:
+            times.append(time.perf_counter() - t0)
+    total = sum(times)
+    value = rows * WIDTH * len(times) / total / 1e6
+    line = {"metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1000 * total / len(times), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32+u64", "data": "synthetic",
+            "config": config_dict(tree, {"sample_rows_per_step": rows}), "impl": "reference",
+            "cpu_baseline": {"value": value, "unit": "Mrays/s", "cores": threads, "kind": "reference",
+                             "sample": "%d rows (%d rays) of the 1080p frame per step" % (rows, rows * WIDTH)},
+            "e2e": {"value": value, "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def run_ours(args, rank, world):
+    import torch
+
+    import svo_tracer as st
+
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    tree, cam = workload(st)
+    tr = st.Tracer(dev)
+    stream = torch.cuda.Stream(device=dev)
+    tr.set_stream(stream.cuda_stream)
+    tr.upload(tree)
+    tr.init_usage()
+    n = WIDTH * HEIGHT
+
+    # algorithmic bytes of one frame (counting launch, untimed)
+    tr.set_config(collect_stats=1)
+    tr.trace(cam)
+    stats = tr.stats()
+    tr.set_config(collect_stats=0)
+    alg_bytes = 16 * stats["block_node_reads"] + 2 * stats["base_steps"] + OUT_BYTES * n
+
+    # device-resident outputs
+    o_idx = torch.empty(n, dtype=torch.int32, device=dev)
+    o_dep = torch.empty(n, dtype=torch.uint8, device=dev)
+    o_t = torch.empty(n, dtype=torch.float32, device=dev)
+    o_rgba = torch.empty(n * 4, dtype=torch.float32, device=dev)
+    outs = [(o_idx.data_ptr(), o_dep.data_ptr(), o_t.data_ptr(), o_rgba.data_ptr())]
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            flush.zero_()
+            tr.trace_device([cam], outs)
+        starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+        ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+        torch.cuda.synchronize(dev)
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize(dev)
+        with ClockSampler(dev) as clk:
+            t_wall = time.perf_counter()
+            for i in range(args.steps):
+                flush.zero_()
+                starts[i].record(stream)
+                tr.trace_device([cam], outs)
+                ends[i].record(stream)
+            torch.cuda.synchronize(dev)
+            t_wall = time.perf_counter() - t_wall
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize(dev)
+    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    total_ms = float(sum(step_ms))
+
+    # end to end through the public API with host buffers (pinned outputs)
+    h_idx = torch.empty(n, dtype=torch.int32, pin_memory=True).numpy().view(np.uint32)
+    h_dep = torch.empty(n, dtype=torch.uint8, pin_memory=True).numpy()
+    h_t = torch.empty(n, dtype=torch.float32, pin_memory=True).numpy()
+    h_rgba = torch.empty(n * 4, dtype=torch.float32, pin_memory=True).numpy().reshape(n, 4)
+    res = st.TraceResult(h_idx, h_dep, h_t, h_rgba)
+    for _ in range(max(1, args.warmup)):
+        tr.trace(cam, out=res)
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        tr.trace(cam, out=res)  # uploads view + trig tables, traces, downloads all outputs, synchronises
+    e2e_s = time.perf_counter() - t0
+
+    if dist:
+        t = torch.tensor([total_ms, e2e_s], dtype=torch.float64, device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms, e2e_s = float(t[0]), float(t[1])
+    if rank != 0:
+        tr.close()
+        if dist:
+            dist.destroy_process_group()
+        return
+
+    ms_per_step = total_ms / args.steps
+    value = world * n / (ms_per_step / 1000.0) / 1e6
+    peak, peak_kind = measured_peak()
+    achieved = alg_bytes / (ms_per_step / 1000.0) / 1e9
+    traffic = ncu_traffic()
+    h2d = 120 + 8 * (WIDTH + HEIGHT)  # view record + sin/cos tables
+    d2h = n * OUT_BYTES
+    line = {
+        "metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32+u64", "data": "synthetic",
+        "config": config_dict(tree, {"parallelism": "replicas" if world > 1 else "single GPU",
+                                     "step_ms_min": min(step_ms), "step_ms_max": max(step_ms),
+                                     "wall_s_timed_loop": t_wall}),
+        "e2e": {"value": world * n * args.steps / e2e_s / 1e6, "unit": "Mrays/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h},
+        "gpu_launches": args.steps,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": traffic, "peak_kind": peak_kind,
+                     "algorithmic_bytes_per_launch": int(alg_bytes),
+                     "bytes_per_ray": alg_bytes / n},
+        "clocks": clk.summary(),
+        "trace_stats": {k: int(v) for k, v in stats.items()},
+    }
+    if not args.no_cpu_baseline:
+        import pyoracle as po
+
+        kind = "reference" if po.ref_available() else "port"
+        line["cpu_baseline"] = cpu_sample(tree, cam, kind)
+    print(json.dumps(line))
+    tr.close()
+    if dist:
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(3, args.warmup)
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", str(args.gpus if args.impl == "reference" else 1)))
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+    else:
+        import __graft_entry__
+
+        if not os.path.exists(os.path.join(ROOT, "svo-tracer_gb300", "lib", "libsvo.so")):
+            __graft_entry__.build()
+        run_ours(args, rank, world)
+
+
+if __name__ == "__main__":
+    main()

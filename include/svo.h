@@ -171,7 +171,7 @@ typedef struct svo_trace_stats {
 
 /* Tuning of the persistent trace kernel (0 = library default). */
 typedef struct svo_trace_config {
-  int32_t block_size;   /* threads per CTA */
+  int32_t block_size;   /* threads per CTA, multiple of 32 up to 256 */
   int32_t ctas_per_sm;  /* resident CTAs per SM for the persistent grid */
   int32_t refill_lanes; /* idle lanes of a warp that trigger a ray-queue refill (1..32) */
   int32_t cadence;      /* steps between lane refills */
@@ -218,7 +218,7 @@ SVO_API svo_status svo_tree_size(void *ctx, uint8_t *base_depth, size_t *n_bases
  * MainWindow.RunWavefront, MainWindow.cs:356-426). Stamps usage ticks and
  * queues child requests (capped at max_child_request_id). */
 SVO_API svo_status svo_trace(void *ctx, const svo_trace_input *input, const svo_trace_output *out);
-/* n_views views in one persistent launch. out[i] receives view i. */
+/* n_views (<= 512) views in one persistent launch. out[i] receives view i. */
 SVO_API svo_status svo_trace_batch(void *ctx, const svo_trace_input *inputs, int32_t n_views, const svo_trace_output *out);
 /* Same, replayed from a CUDA graph captured on first use for this view set. */
 SVO_API svo_status svo_trace_batch_graph(void *ctx, const svo_trace_input *inputs, int32_t n_views,

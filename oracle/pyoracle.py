@@ -40,6 +40,8 @@ def oracle_lib() -> C.CDLL:
         lib.oracle_trace_view.argtypes = [_vp, C.c_uint8, _vp, C.c_size_t, _vp, C.c_size_t, C.c_char_p, C.c_int32,
                                           C.POINTER(_ViewOut), _vp, C.c_uint32, C.POINTER(C.c_uint32), C.c_int32]
         lib.oracle_trace_view.restype = C.c_int64
+        lib.oracle_trace_rows.argtypes = lib.oracle_trace_view.argtypes + [C.c_uint32, C.c_uint32]
+        lib.oracle_trace_rows.restype = C.c_int64
         lib.oracle_float_to_ulong.argtypes = [C.c_float]
         lib.oracle_float_to_ulong.restype = C.c_uint64
         lib.oracle_ulong_to_float.argtypes = [C.c_uint64]
@@ -75,6 +77,8 @@ def ref_lib() -> C.CDLL:
         lib.ref_trace_view.argtypes = [_vp, C.c_uint8, _vp, C.c_size_t, _vp, C.c_size_t, C.c_char_p, _vp, _vp, _vp,
                                        _vp, _vp, _vp, C.c_uint32, C.POINTER(C.c_uint32), C.c_int, C.c_long]
         lib.ref_trace_view.restype = C.c_long
+        lib.ref_trace_rows.argtypes = lib.ref_trace_view.argtypes + [C.c_uint, C.c_uint]
+        lib.ref_trace_rows.restype = C.c_long
         _ref = lib
     return _ref
 
@@ -142,3 +146,36 @@ def sort_requests(req: np.ndarray) -> np.ndarray:
     keys = (req["tree_size"], req["location"][:, 2], req["location"][:, 1], req["location"][:, 0], req["depth"],
             req["address"])
     return req[np.lexsort(keys)]
+
+
+def trace_rows(tree, inp: TraceInput, row_begin: int, row_end: int, threads: int = 0, max_steps: int = 1 << 16):
+    """Oracle over rows [row_begin, row_end) of a view (a bounded sample); returns the
+    per-pixel hit_index of the band."""
+    lib = oracle_lib()
+    w = inp.ScreenSize[0]
+    n = w * (row_end - row_begin)
+    hit = np.empty(n, np.uint32)
+    vo = _ViewOut(_p(hit), None, None, None, None, None, None, None)
+    bases = np.ascontiguousarray(tree.BaseBlocks, np.uint16)
+    blocks = np.ascontiguousarray(tree.Blocks)
+    nreq = C.c_uint32(0)
+    lib.oracle_trace_rows(_p(bases), tree.BaseDepth, _p(blocks), len(blocks), None, 0, inp.to_bytes(), max_steps,
+                          C.byref(vo), None, 0, C.byref(nreq), threads, row_begin, row_end)
+    return hit
+
+
+def ref_trace_rows(tree, inp: TraceInput, row_begin: int, row_end: int, threads: int = 0):
+    """The reference's kernels over rows [row_begin, row_end) of a view; returns the
+    full-image hit_index (rows outside the band are misses)."""
+    lib = ref_lib()
+    w, h = inp.ScreenSize
+    hit = np.empty(w * h, np.uint32)
+    bases = np.ascontiguousarray(tree.BaseBlocks, np.uint16)
+    blocks = np.ascontiguousarray(tree.Blocks)
+    nreq = C.c_uint32(0)
+    passes = lib.ref_trace_rows(_p(bases), tree.BaseDepth, _p(blocks), len(blocks), None, 0, inp.to_bytes(),
+                                _p(hit), None, None, None, None, None, 0, C.byref(nreq), threads, 1 << 20,
+                                row_begin, row_end)
+    if passes < 0:
+        raise RuntimeError("reference harness ran out of passes")
+    return hit

@@ -28,10 +28,13 @@ uint ref_image_width;
 
 static void *zalloc(size_t n) { return calloc(n ? n : 1, 1); }
 
-/* Returns the number of traversal passes, or -1 if max_passes ran out. */
-long ref_trace_view(const ushort *bases, uchar base_depth, const Block *blocks_in, size_t n_blocks, Usage *usage,
+/* Returns the number of traversal passes, or -1 if max_passes ran out.
+ * Only rows [row_begin, row_end) get an init work-item (a bounded sample of the
+ * view); per-pixel outputs still cover the whole W x H image. */
+long ref_trace_rows(const ushort *bases, uchar base_depth, const Block *blocks_in, size_t n_blocks, Usage *usage,
                     size_t n_groups, const TraceInput *in, uint *hit_index, uchar *hit_depth, float *t, float *rgba,
-                    uint *acc, ChildRequest *req_out, uint req_cap, uint *n_req, int threads, long max_passes) {
+                    uint *acc, ChildRequest *req_out, uint req_cap, uint *n_req, int threads, long max_passes,
+                    uint row_begin, uint row_end) {
   (void)n_groups;
   TraceInput input = *in;
   input.BaseDepth = base_depth;
@@ -63,10 +66,12 @@ long ref_trace_view(const ushort *bases, uchar base_depth, const Block *blocks_i
 
   ref_gsize[0] = W;
   ref_gsize[1] = H;
+  if (row_end > H) row_end = (uint)H;
+  if (row_begin > row_end) row_begin = row_end;
 #ifdef _OPENMP
 #pragma omp parallel for schedule(dynamic, 1024) num_threads(nt)
 #endif
-  for (size_t id = 0; id < N; id++) {
+  for (size_t id = (size_t)row_begin * W; id < (size_t)row_end * W; id++) {
     ref_gid[0] = id % W;
     ref_gid[1] = id / W;
     init(Origins, Directions, FoVs, Locations, Depths, BaseTraceQueue, &BaseTraceQueueID, BackgroundQueue,
@@ -187,4 +192,11 @@ long ref_trace_view(const ushort *bases, uchar base_depth, const Block *blocks_i
   free(BlockTraces); free(BlockTraceQueue); free(BackgroundQueue); free(MaterialQueue); free(FinalColourRs);
   free(FinalColourGs); free(FinalColourBs); free(FinalWeightings); free(ChildRequests);
   return passes;
+}
+
+long ref_trace_view(const ushort *bases, uchar base_depth, const Block *blocks_in, size_t n_blocks, Usage *usage,
+                    size_t n_groups, const TraceInput *in, uint *hit_index, uchar *hit_depth, float *t, float *rgba,
+                    uint *acc, ChildRequest *req_out, uint req_cap, uint *n_req, int threads, long max_passes) {
+  return ref_trace_rows(bases, base_depth, blocks_in, n_blocks, usage, n_groups, in, hit_index, hit_depth, t, rgba, acc,
+                        req_out, req_cap, n_req, threads, max_passes, 0, in->ScreenSize[1]);
 }

@@ -440,14 +440,24 @@ int64_t oracle_trace_view(const uint16_t *bases, uint8_t base_depth, const svo_b
                           svo_usage *usage, size_t n_groups, const svo_trace_input *in, int32_t max_steps,
                           const oracle_view_out *out, svo_child_request *req, uint32_t req_cap, uint32_t *n_req,
                           int32_t threads) {
+  return oracle_trace_rows(bases, base_depth, blocks, n_blocks, usage, n_groups, in, max_steps, out, req, req_cap, n_req,
+                           threads, 0, in->screen_size[1]);
+}
+
+int64_t oracle_trace_rows(const uint16_t *bases, uint8_t base_depth, const svo_block *blocks, size_t n_blocks,
+                          svo_usage *usage, size_t n_groups, const svo_trace_input *in, int32_t max_steps,
+                          const oracle_view_out *out, svo_child_request *req, uint32_t req_cap, uint32_t *n_req,
+                          int32_t threads, uint32_t row_begin, uint32_t row_end) {
   uint32_t W = in->screen_size[0], H = in->screen_size[1];
+  if (row_end > H) row_end = H;
+  if (row_begin > row_end) row_begin = row_end;
   float *su = (float *)malloc(sizeof(float) * (W + 1));
   float *cu = (float *)malloc(sizeof(float) * (W + 1));
   float *sv = (float *)malloc(sizeof(float) * (H + 1));
   float *cv = (float *)malloc(sizeof(float) * (H + 1));
   oracle_view_tables(in, su, cu, sv, cv);
   int64_t limited = 0;
-  int64_t n = (int64_t)W * H;
+  int64_t n = (int64_t)W * (row_end - row_begin);
 #ifdef _OPENMP
   int nt = threads > 0 ? threads : omp_get_max_threads();
 #pragma omp parallel for schedule(dynamic, 256) num_threads(nt) reduction(+ : limited)
@@ -455,7 +465,7 @@ int64_t oracle_trace_view(const uint16_t *bases, uint8_t base_depth, const svo_b
   for (int64_t id = 0; id < n; id++) {
     ray_result r;
     trace_ray(bases, base_depth, blocks, n_blocks, usage, n_groups, in, su, cu, sv, cv, (uint32_t)(id % W),
-              (uint32_t)(id / W), max_steps, req, req_cap, n_req, &r);
+              row_begin + (uint32_t)(id / W), max_steps, req, req_cap, n_req, &r);
     limited += r.step_limited;
     if (out->hit_index) out->hit_index[id] = r.hit_index;
     if (out->hit_depth) out->hit_depth[id] = r.hit_depth;

@@ -38,6 +38,12 @@ int64_t oracle_trace_view(const uint16_t *bases, uint8_t base_depth, const svo_b
                           svo_usage *usage, size_t n_groups, const svo_trace_input *in, int32_t max_steps,
                           const oracle_view_out *out, svo_child_request *req, uint32_t req_cap, uint32_t *n_req,
                           int32_t threads);
+/* Same for rows [row_begin, row_end) of the view only; per-pixel outputs are
+ * indexed within the band (pixel (x, y) at (y - row_begin) * W + x). */
+int64_t oracle_trace_rows(const uint16_t *bases, uint8_t base_depth, const svo_block *blocks, size_t n_blocks,
+                          svo_usage *usage, size_t n_groups, const svo_trace_input *in, int32_t max_steps,
+                          const oracle_view_out *out, svo_child_request *req, uint32_t req_cap, uint32_t *n_req,
+                          int32_t threads, uint32_t row_begin, uint32_t row_end);
 
 /* Ray-setup tables of the parity contract: sinU/cosU per column, sinV/cosV
  * per row, each (float)sin((double)angle). */

@@ -284,10 +284,14 @@ static svo_status prepare_launch(Context &c, int32_t n_views, uint32_t total_ray
   return SVO_OK;
 }
 
+// The view table lives in shared memory (120 B per view).
+constexpr int kMaxViews = 512;
+
 static svo_status run_trace(Context &c, const svo_trace_input *in, int32_t n, const svo_trace_output *out,
                             bool use_graph) {
   if (!c.has_tree) return fail(SVO_ERR_NO_TREE, "svo_trace: no octree uploaded");
   if (n <= 0 || !in || !out) return fail(SVO_ERR_INVALID_ARGUMENT, "svo_trace: bad view list");
+  if (n > kMaxViews) return fail(SVO_ERR_INVALID_ARGUMENT, "svo_trace_batch: at most 512 views per call");
   SVO_CUDA(cudaSetDevice(c.device), "cudaSetDevice");
   bool on_device = out[0].on_device != 0;
   for (int i = 1; i < n; i++)
@@ -466,8 +470,8 @@ SVO_API svo_status svo_set_trace_config(void *ctx, const svo_trace_config *cfg) 
   if (n.refill_lanes == 0) n.refill_lanes = d.refill_lanes;
   if (n.cadence == 0) n.cadence = d.cadence;
   if (n.max_steps == 0) n.max_steps = d.max_steps;
-  if (n.block_size % 32 || n.block_size < 32 || n.block_size > 1024)
-    return fail(SVO_ERR_INVALID_ARGUMENT, "svo_set_trace_config: block_size must be a multiple of 32 in 32..1024");
+  if (n.block_size % 32 || n.block_size < 32 || n.block_size > 256)
+    return fail(SVO_ERR_INVALID_ARGUMENT, "svo_set_trace_config: block_size must be a multiple of 32 in 32..256");
   if (n.refill_lanes < 1 || n.refill_lanes > 32 || n.cadence < 1 || n.max_steps < 1 || n.ctas_per_sm < 0 ||
       n.collect_stats < 0 || n.collect_stats > 2)
     return fail(SVO_ERR_INVALID_ARGUMENT, "svo_set_trace_config: value out of range");

@@ -166,7 +166,7 @@ struct SphereScene final : Scene {
 // over the columns make cell classification O(1).
 struct TerrainScene final : Scene {
   uint32_t res = 0;  // 2^leaf columns per axis
-  double f0 = 6.0, hmax = 0.3;
+  double f0 = 18.0, hmax = 0.3;
   std::vector<std::vector<uint16_t>> lo, hi;  // per level l: 4^l entries
   TerrainScene(uint32_t s, int leaf_level, int threads) {
     seed = s;

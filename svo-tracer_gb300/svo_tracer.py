@@ -357,8 +357,8 @@ class Tracer:
         return TraceOutputC(_ptr(r.hit_index), _ptr(r.hit_depth), _ptr(r.t), _ptr(r.rgba), 0, 0)
 
     # MainWindow.RunWavefront for one view, results in host memory
-    def trace(self, inp: TraceInput) -> TraceResult:
-        r = self._alloc(*inp.ScreenSize)
+    def trace(self, inp: TraceInput, out: TraceResult | None = None) -> TraceResult:
+        r = out if out is not None else self._alloc(*inp.ScreenSize)
         c_in, c_out = inp.to_c(), self._out(r)
         self._req_cap = inp.MaxChildRequestId
         _check("RunWavefront", self._lib.svo_trace(self._ctx, C.byref(c_in), C.byref(c_out)))

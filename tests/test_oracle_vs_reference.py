@@ -1,0 +1,72 @@
+"""The C restatement (oracle/svo_oracle.c) against the reference's own wavefront.cl
+kernels compiled for the CPU (oracle/_ref): every per-pixel output, the usage ticks and
+the child-request set must agree bit for bit."""
+import numpy as np
+import pytest
+
+import pyoracle as po
+import svo_tracer as st
+
+pytestmark = pytest.mark.skipif(not po.ref_available(), reason="reference kernels not available")
+
+CAMERAS = [
+    ("outside", (1.2, 0.75, 0.1), (0.5, 0.5, 0.5), 96, 72, 60.0, (0.0, 0.0)),
+    ("grazing", (0.5, -0.6, 0.5), (0.52, 0.5, 0.48), 80, 60, 45.0, (0.0, 0.0)),
+    ("inside_air", (0.9, 0.1, 0.15), (0.4, 0.6, 0.5), 64, 48, 80.0, (0.0, 0.0)),
+    ("dof", (0.1, 1.3, 0.3), (0.5, 0.5, 0.5), 64, 48, 60.0, (0.01, 0.7)),
+]
+
+
+def _compare(tree, cam):
+    u_ref = po.init_usage(tree)
+    u_orc = u_ref.copy()
+    ref = po.ref_trace_view(tree, cam, usage=u_ref)
+    orc = po.trace_view(tree, cam, usage=u_orc)
+    assert ref["passes"] > 0
+    for k in ("hit_index", "hit_depth", "t", "rgba", "acc"):
+        assert np.array_equal(ref[k], orc[k]), k
+    assert np.array_equal(u_ref["tick"], u_orc["tick"])
+    assert ref["n_requests"] == orc["n_requests"]
+    assert po.sort_requests(ref["requests"]).tobytes() == po.sort_requests(orc["requests"]).tobytes()
+    return orc
+
+
+@pytest.mark.parametrize("seed", [1, 2])
+@pytest.mark.parametrize("cam", CAMERAS, ids=[c[0] for c in CAMERAS])
+def test_sphere_matches_reference(seed, cam):
+    tree = st.TreeBuilder(st.SCENE_SPHERE, seed=seed).BuildTree(4, 8)
+    _, o, t, w, h, fov, dof = cam
+    out = _compare(tree, st.look_at(o, t, w, h, fov, DoF=dof, Tick=3 + seed))
+    assert (out["hit_index"] != st.MISS).any()
+
+
+@pytest.mark.parametrize("b,d", [(3, 8), (4, 9)])
+def test_terrain_matches_reference(b, d):
+    tree = st.TreeBuilder(st.SCENE_TERRAIN, seed=5).BuildTree(b, d)
+    out = _compare(tree, st.look_at((0.1, 0.15, 0.55), (0.7, 0.7, 0.9), 128, 72, 60.0, Tick=11))
+    assert (out["hit_index"] != st.MISS).mean() > 0.3
+
+
+def test_empty_scene_matches_reference():
+    tree = st.TreeBuilder(st.SCENE_SPHERE, seed=1).BuildTree(2, 4)
+    tree.BaseBlocks[:] = 0x5555  # every octant air only
+    tree.Blocks[:] = np.zeros(1, st.BLOCK_DTYPE)
+    out = _compare(tree, st.look_at((1.3, 0.2, 0.4), (0.5, 0.5, 0.5), 32, 24, 60.0))
+    assert (out["hit_index"] == st.MISS).all()
+
+
+def test_unset_cone_tree_size_is_saturated():
+    """A ray whose location equals the eye has cone 0 and ConeDepth = +inf; the
+    reference's (uchar)ConeDepth is then an out-of-range conversion (undefined). The
+    oracle saturates it, so TreeSize is 1; every other field still matches."""
+    tree = st.TreeBuilder(st.SCENE_SPHERE, seed=1).BuildTree(4, 8)
+    cam = st.look_at((0.52, 0.47, 0.5), (0.9, 0.2, 0.3), 32, 24, 75.0)  # eye inside the solid sphere
+    ref = po.ref_trace_view(tree, cam)
+    orc = po.trace_view(tree, cam)
+    for k in ("hit_index", "hit_depth", "t", "rgba", "acc"):
+        assert np.array_equal(ref[k], orc[k]), k
+    a, b = orc["requests"].copy(), ref["requests"].copy()
+    assert set(np.unique(a["tree_size"])) <= {0, 1}
+    a["tree_size"] = 0
+    b["tree_size"] = 0
+    assert po.sort_requests(a).tobytes() == po.sort_requests(b).tobytes()
