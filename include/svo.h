@@ -173,11 +173,10 @@ typedef struct svo_trace_stats {
 typedef struct svo_trace_config {
   int32_t block_size;   /* threads per CTA, multiple of 32 up to 256 */
   int32_t ctas_per_sm;  /* resident CTAs per SM for the persistent grid */
-  int32_t refill_lanes; /* idle lanes of a warp that trigger a ray-queue refill (1..32) */
-  int32_t cadence;      /* steps between lane refills */
+  int32_t ray_chunk;    /* rays a thread claims per ray-queue fetch (1..64) */
   int32_t max_steps;    /* per-ray step limit */
   int32_t collect_stats; /* 0 none, 1 totals (svo_last_trace_stats), 2 totals and per-ray counts */
-  int32_t _pad[2];
+  int32_t _pad[3];
 } svo_trace_config;
 
 /* ---- context ------------------------------------------------------------ */

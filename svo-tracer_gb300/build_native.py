@@ -25,6 +25,7 @@ NVCC_FLAGS = ARCH + [
     "-O3", "-lineinfo", "-std=c++17", "--fmad=false", "-prec-div=true", "-prec-sqrt=true",
     "-Xcompiler", "-fPIC,-ffp-contract=off,-fvisibility=hidden", "-I" + INCLUDE,
 ]
+NVCC_FLAGS += os.environ.get("SVO_NVCC_EXTRA", "").split()
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-fvisibility=hidden", "-pthread", "-I" + INCLUDE]
 
 

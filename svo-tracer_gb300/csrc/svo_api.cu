@@ -88,7 +88,7 @@ struct Context {
   DevBuf<svo_block> blocks;
   DevBuf<svo_usage> usage;
   // trace scratch
-  DevBuf<uint32_t> counters;  // [0] ray queue head, [1] child requests raised
+  DevBuf<uint32_t> counters;  // [0] ray queue head, [1] child requests raised, [4..9] kernel error record
   DevBuf<unsigned long long> stats;
   DevBuf<svo_child_request> requests;
   DevBuf<ViewParams> views;
@@ -138,8 +138,7 @@ static svo_trace_config default_config() {
   svo_trace_config c{};
   c.block_size = 256;
   c.ctas_per_sm = 0;  // occupancy-derived
-  c.refill_lanes = 16;
-  c.cadence = 4;
+  c.ray_chunk = 1;
   c.max_steps = 1 << 16;
   c.collect_stats = 0;
   return c;
@@ -259,6 +258,7 @@ static svo_status prepare_launch(Context &c, int32_t n_views, uint32_t total_ray
   a.requests = c.requests.p;
   a.request_cap = c.request_cap;
   a.ray_counter = c.counters.p;
+  a.error = c.counters.p + 4;
   a.request_count = c.counters.p + 1;
   a.stats = stats ? c.stats.p : nullptr;
   a.ray_v_block = (stats && c.cfg.collect_stats >= 2) ? c.ray_v_block.p : nullptr;
@@ -272,8 +272,7 @@ static svo_status prepare_launch(Context &c, int32_t n_views, uint32_t total_ray
   a.n_views = n_views;
   a.base_depth = c.base_depth;
   a.max_steps = c.cfg.max_steps;
-  a.cadence = std::max(1, c.cfg.cadence);
-  a.refill_lanes = std::min(32, std::max(1, c.cfg.refill_lanes));
+  a.ray_chunk = (uint32_t)std::max(1, c.cfg.ray_chunk);
   a.block_size = c.cfg.block_size;
   a.path_levels = std::max(1, c.tree_depth - (int)c.base_depth - 1);
   int occ = c.cfg.ctas_per_sm > 0 ? c.cfg.ctas_per_sm : trace_occupancy(a, stats);
@@ -286,6 +285,19 @@ static svo_status prepare_launch(Context &c, int32_t n_views, uint32_t total_ray
 
 // The view table lives in shared memory (120 B per view).
 constexpr int kMaxViews = 512;
+
+// Reads the kernel's error record (synchronises the stream).
+static svo_status check_kernel_error(Context &c) {
+  uint32_t e[6] = {0};
+  SVO_CUDA(cudaMemcpyAsync(e, c.counters.p + 4, sizeof(e), cudaMemcpyDeviceToHost, c.stream), "svo_trace: error record");
+  SVO_CUDA(cudaStreamSynchronize(c.stream), "svo_trace: synchronize");
+  if (e[0] == SVO_ERR_TIMEOUT)
+    return fail(SVO_ERR_TIMEOUT, "svo_trace: thread " + std::to_string(e[2]) + " of block " + std::to_string(e[1]) +
+                                     " exceeded its iteration bound on ray " + std::to_string(e[3]) + " (depth " +
+                                     std::to_string(e[4]) + ", steps " + std::to_string(e[5]) + ")");
+  if (e[0]) return fail((svo_status)e[0], "svo_trace: kernel reported an error");
+  return SVO_OK;
+}
 
 static svo_status run_trace(Context &c, const svo_trace_input *in, int32_t n, const svo_trace_output *out,
                             bool use_graph) {
@@ -328,7 +340,7 @@ static svo_status run_trace(Context &c, const svo_trace_input *in, int32_t n, co
              "svo_trace: view upload");
     SVO_CUDA(cudaMemcpyAsync(c.tables.p, c.h_tables.p, sizeof(float) * table_floats, cudaMemcpyHostToDevice, c.stream),
              "svo_trace: table upload");
-    SVO_CUDA(cudaMemsetAsync(c.counters.p, 0, 2 * sizeof(uint32_t), c.stream), "svo_trace: counter reset");
+    SVO_CUDA(cudaMemsetAsync(c.counters.p, 0, (4 + 8) * sizeof(uint32_t), c.stream), "svo_trace: counter reset");
     if (stats) SVO_CUDA(cudaMemsetAsync(c.stats.p, 0, 8 * sizeof(unsigned long long), c.stream), "svo_trace: stats reset");
     return launch_trace(a, stats, c.stream);
   };
@@ -390,6 +402,7 @@ static svo_status run_trace(Context &c, const svo_trace_input *in, int32_t n, co
       off += np;
     }
     SVO_CUDA(cudaStreamSynchronize(c.stream), "svo_trace: synchronize");
+    return check_kernel_error(c);
   }
   return SVO_OK;
 }
@@ -434,7 +447,7 @@ SVO_API svo_status svo_create(int32_t device, void **ctx) {
   SVO_CUDA(cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking), "svo_create: stream");
   c->stream = c->own_stream;
   c->cfg = svo::default_config();
-  SVO_CUDA(c->counters.reserve(4), "svo_create: counters");
+  SVO_CUDA(c->counters.reserve(4 + 8), "svo_create: counters");
   SVO_CUDA(c->stats.reserve(8), "svo_create: stats");
   SVO_CUDA(c->h_counters.reserve(4), "svo_create: pinned counters");
   *ctx = c.release();
@@ -467,12 +480,11 @@ SVO_API svo_status svo_set_trace_config(void *ctx, const svo_trace_config *cfg) 
   if (!cfg) return fail(SVO_ERR_INVALID_ARGUMENT, "svo_set_trace_config: null config");
   svo_trace_config d = svo::default_config(), n = *cfg;
   if (n.block_size == 0) n.block_size = d.block_size;
-  if (n.refill_lanes == 0) n.refill_lanes = d.refill_lanes;
-  if (n.cadence == 0) n.cadence = d.cadence;
+  if (n.ray_chunk == 0) n.ray_chunk = d.ray_chunk;
   if (n.max_steps == 0) n.max_steps = d.max_steps;
   if (n.block_size % 32 || n.block_size < 32 || n.block_size > 256)
     return fail(SVO_ERR_INVALID_ARGUMENT, "svo_set_trace_config: block_size must be a multiple of 32 in 32..256");
-  if (n.refill_lanes < 1 || n.refill_lanes > 32 || n.cadence < 1 || n.max_steps < 1 || n.ctas_per_sm < 0 ||
+  if (n.ray_chunk < 1 || n.ray_chunk > 64 || n.max_steps < 1 || n.ctas_per_sm < 0 ||
       n.collect_stats < 0 || n.collect_stats > 2)
     return fail(SVO_ERR_INVALID_ARGUMENT, "svo_set_trace_config: value out of range");
   c.cfg = n;

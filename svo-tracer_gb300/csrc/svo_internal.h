@@ -40,6 +40,7 @@ struct TraceLaunch {
   svo_child_request *requests;
   uint32_t *request_count;
   uint32_t *ray_counter;
+  uint32_t *error;            // [0] status, [1..3] diagnostics of a stopped warp
   unsigned long long *stats;  // 7 counters in svo_trace_stats order, or null
   uint32_t *ray_v_block;      // per-ray V_block (stats launches only), or null
   uint32_t *ray_v_base;
@@ -53,8 +54,7 @@ struct TraceLaunch {
   int32_t n_views;
   int32_t base_depth;
   int32_t max_steps;
-  int32_t cadence;
-  int32_t refill_lanes;
+  uint32_t ray_chunk;
   int32_t block_size;
   int32_t grid;
   int32_t path_levels;

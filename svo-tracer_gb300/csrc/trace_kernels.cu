@@ -8,10 +8,13 @@
 // persistent launch:
 //
 //  * The ray queue is the batch's ray index space with a device-side head
-//    counter. Each warp keeps 32 ray slots; idle lanes are refilled with one
-//    warp-aggregated atomicAdd (ballot + popc) every `cadence` steps once at
-//    least `refill_lanes` lanes are idle. Ray state stays in registers, so
-//    the reference's per-step reload of ~74 B of SoA state disappears.
+//    counter. A persistent grid of threads takes rays from it: whenever a
+//    thread finishes a ray it claims the next one, the threads of a warp that
+//    need rays at the same moment sharing one atomicAdd (coalesced group,
+//    `ray_chunk` rays per thread). No step depends on the warp staying
+//    converged, so a lane leaves the loop as soon as the queue is drained.
+//    Ray state stays in registers, so the reference's per-step reload of
+//    ~74 B of SoA state disappears.
 //  * Each step is runBaseTrace or runBlockTrace for one ray. The reference
 //    re-walks the block tree from level B+2 at every block step
 //    (getBlockAddress, wavefront.cl:296-304); here each lane keeps the node
@@ -32,14 +35,21 @@
 // round-to-nearest intrinsics (no contraction); ConeDepth comparisons
 // (-half_log2(c) against integers) are evaluated exactly as comparisons of
 // the cone size c with powers of two.
+#include <cooperative_groups.h>
+#include <cooperative_groups/reduce.h>
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#ifdef SVO_TRACE_DEBUG
+#include <cstdio>
+#endif
 
 #include "svo_internal.h"
 
 namespace svo {
 namespace {
+
+namespace cg = cooperative_groups;
 
 constexpr unsigned kFull = 0xffffffffu;
 constexpr uint64_t kAll = ~0ull;
@@ -167,7 +177,7 @@ __device__ __forceinline__ float cone_at(const Ray &r, float dof0, float dof1) {
 // traceIntoVolume (wavefront.cl:639-1088): enter the unit cube on the face of
 // the outside slab with the largest entry distance (ties x, then y); reject
 // when the entry point is outside the cube grown by the cone size.
-__device__ bool enter_volume(Ray &r) {
+__device__ __forceinline__ bool enter_volume(Ray &r) {
   const float o[3] = {r.ox, r.oy, r.oz};
   const float d[3] = {r.dx, r.dy, r.dz};
   const float iv[3] = {r.ix, r.iy, r.iz};
@@ -228,6 +238,15 @@ struct Stats {
   unsigned long long rays, hits, base_steps, block_reads, block_steps, requests, limited;
 };
 
+// Claims `n` consecutive slots of a device counter for the lanes of `g` with one
+// atomic; returns this lane's first slot. Only the lanes present in `g` take
+// part, so lanes may arrive here (or leave the kernel) independently.
+__device__ __forceinline__ uint32_t claim(cg::coalesced_group &g, uint32_t *counter, uint32_t per_lane) {
+  uint32_t base = 0;
+  if (g.thread_rank() == 0) base = atomicAdd(counter, g.size() * per_lane);
+  return g.shfl(base, 0) + g.thread_rank();
+}
+
 template <bool kStats, bool kSmemBases>
 __global__ void __launch_bounds__(256) trace_kernel(const TraceLaunch a) {
   extern __shared__ __align__(16) uint8_t smem[];
@@ -245,12 +264,11 @@ __global__ void __launch_bounds__(256) trace_kernel(const TraceLaunch a) {
   }
   __syncthreads();
 
-  const int lane = threadIdx.x & 31;
-  const unsigned lt_mask = (1u << lane) - 1u;
   const int B = a.base_depth;
   const uint4 *blocks = reinterpret_cast<const uint4 *>(a.blocks);
   uint32_t *path = s_path + threadIdx.x;  // path[level * blockDim.x]
   const int pstride = blockDim.x;
+  const uint32_t chunk = a.ray_chunk;
 
   Stats st = {0, 0, 0, 0, 0, 0, 0};
   Ray r;
@@ -258,254 +276,264 @@ __global__ void __launch_bounds__(256) trace_kernel(const TraceLaunch a) {
   r.steps = 0;
   uint32_t v_block = 0, v_base = 0;
   uint32_t cur_addr = kFull, cur_child = 0, cur_chunk = 0, last_group = kFull;
-  bool active = false, exhausted = false;
-  uint32_t ray_global = 0;
+  bool have = false;
+  uint32_t ray_global = 0, next_ray = 0, left_in_chunk = 0, chunk_stride = 0;
+  // Every pass either starts a ray or advances one by a step, so a thread runs
+  // at most total_rays * (max_steps + 2) + 64 passes; past that bound it
+  // records its state and stops instead of spinning.
+  const unsigned long long iter_limit =
+      (unsigned long long)a.total_rays * (unsigned long long)(a.max_steps + 2) + 64;
+  unsigned long long iters = 0;
 
   for (;;) {
-    // ---- refill idle lanes from the ray queue (warp-aggregated) ----------
-    unsigned idle = __ballot_sync(kFull, !active);
-    if (idle && !exhausted && (__popc(idle) >= a.refill_lanes || idle == kFull)) {
-      int n = __popc(idle);
-      int leader = __ffs(idle) - 1;
-      uint32_t base = 0;
-      if (lane == leader) base = atomicAdd(a.ray_counter, (uint32_t)n);
-      base = __shfl_sync(kFull, base, leader);
-      if (base + (uint32_t)n >= a.total_rays) exhausted = true;
-      if (!active) {
-        uint32_t my = base + __popc(idle & lt_mask);
-        if (my < a.total_rays) {
-          ray_global = my;
-          // find the view (views are sorted by ray_begin)
-          int lo = 0, hi = a.n_views - 1;
-          while (lo < hi) {
-            int mid = (lo + hi + 1) >> 1;
-            if (s_views[mid].ray_begin <= my) lo = mid; else hi = mid - 1;
-          }
-          const ViewParams &v = s_views[lo];
-          r.view = lo;
-          r.id = my - v.ray_begin;
-          uint32_t px = r.id % v.width, py = r.id / v.width;
-          const float *tb = a.tables + v.table_off;
-          float su = __ldg(tb + px), cu = __ldg(tb + v.width + px);
-          float sv = __ldg(tb + 2 * v.width + py), cv = __ldg(tb + 2 * v.width + v.height + py);
-          // setupInitialTrace (wavefront.cl:563-595)
-          float m0 = __fmul_rn(cu, cv);
-          float m1 = __fmul_rn(__fsub_rn(0.0f, su), cv);
-          float m2 = sv;
-          const float *F = v.facing;
-          r.dx = __fadd_rn(__fadd_rn(__fmul_rn(F[0], m0), __fmul_rn(F[3], m1)), __fmul_rn(F[6], m2));
-          r.dy = __fadd_rn(__fadd_rn(__fmul_rn(F[1], m0), __fmul_rn(F[4], m1)), __fmul_rn(F[7], m2));
-          r.dz = __fadd_rn(__fadd_rn(__fmul_rn(F[2], m0), __fmul_rn(F[5], m1)), __fmul_rn(F[8], m2));
-          r.ix = __frcp_rn(r.dx);
-          r.iy = __frcp_rn(r.dy);
-          r.iz = __frcp_rn(r.dz);
-          r.sx = r.dx >= 0.0f;
-          r.sy = r.dy >= 0.0f;
-          r.sz = r.dz >= 0.0f;
-          r.ox = v.origin[0];
-          r.oy = v.origin[1];
-          r.oz = v.origin[2];
-          r.fov = v.fov_px;
-          r.depth = 1;
-          r.steps = 0;
-          v_block = 0;
-          v_base = 0;
-          cur_addr = kFull;
-          last_group = kFull;
-          active = true;
-          if (!enter_volume(r)) r.depth = 0;  // background at once
-        }
+    if (++iters > iter_limit) {
+      if (a.error && atomicCAS(a.error, 0u, (unsigned)SVO_ERR_TIMEOUT) == 0u) {
+        a.error[1] = blockIdx.x;
+        a.error[2] = threadIdx.x;
+        a.error[3] = ray_global;
+        a.error[4] = (uint32_t)r.depth;
+        a.error[5] = (uint32_t)r.steps;
       }
+      break;
     }
-    if (!__any_sync(kFull, active)) {
-      if (exhausted) break;
-      continue;
+    if (!have) {
+      // ---- take the next ray from the queue --------------------------------
+      uint32_t my;
+      if (left_in_chunk == 0) {
+        // one atomic per group of idle lanes: each lane gets `chunk` rays,
+        // interleaved so that lanes of a group hold neighbouring pixels
+        cg::coalesced_group g = cg::coalesced_threads();
+        uint32_t first = claim(g, a.ray_counter, chunk);
+        uint32_t base = first - g.thread_rank();
+        chunk_stride = g.size();
+        my = first;
+        next_ray = base + g.thread_rank() + chunk_stride;
+        left_in_chunk = chunk - 1;
+      } else {
+        my = next_ray;
+        next_ray += chunk_stride;
+        left_in_chunk--;
+      }
+      // later rays of this chunk, and every later claim, are larger still
+      if (my >= a.total_rays) break;  // queue drained
+      ray_global = my;
+      // find the view (views are sorted by ray_begin)
+      int lo = 0, hi = a.n_views - 1;
+      while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (s_views[mid].ray_begin <= my)
+          lo = mid;
+        else
+          hi = mid - 1;
+      }
+      const ViewParams &v = s_views[lo];
+      r.view = lo;
+      r.id = my - v.ray_begin;
+      uint32_t px = r.id % v.width, py = r.id / v.width;
+      const float *tb = a.tables + v.table_off;
+      float su = __ldg(tb + px), cu = __ldg(tb + v.width + px);
+      float sv = __ldg(tb + 2 * v.width + py), cv = __ldg(tb + 2 * v.width + v.height + py);
+      // setupInitialTrace (wavefront.cl:563-595)
+      float m0 = __fmul_rn(cu, cv);
+      float m1 = __fmul_rn(__fsub_rn(0.0f, su), cv);
+      float m2 = sv;
+      const float *F = v.facing;
+      r.dx = __fadd_rn(__fadd_rn(__fmul_rn(F[0], m0), __fmul_rn(F[3], m1)), __fmul_rn(F[6], m2));
+      r.dy = __fadd_rn(__fadd_rn(__fmul_rn(F[1], m0), __fmul_rn(F[4], m1)), __fmul_rn(F[7], m2));
+      r.dz = __fadd_rn(__fadd_rn(__fmul_rn(F[2], m0), __fmul_rn(F[5], m1)), __fmul_rn(F[8], m2));
+      r.ix = __frcp_rn(r.dx);
+      r.iy = __frcp_rn(r.dy);
+      r.iz = __frcp_rn(r.dz);
+      r.sx = r.dx >= 0.0f;
+      r.sy = r.dy >= 0.0f;
+      r.sz = r.dz >= 0.0f;
+      r.ox = v.origin[0];
+      r.oy = v.origin[1];
+      r.oz = v.origin[2];
+      r.fov = v.fov_px;
+      r.depth = 1;
+      r.steps = 0;
+      v_block = 0;
+      v_base = 0;
+      cur_addr = kFull;
+      last_group = kFull;
+      have = true;
+      if (!enter_volume(r)) r.depth = 0;  // background at once
     }
 
-    for (int s = 0; s < a.cadence; s++) {
-      bool request = false;
-      int finish = 0;  // 1 = background, 2 = hit
-      if (active) {
-        const ViewParams &v = s_views[r.view];
-        if (r.depth == 0) {
-          finish = 1;
-        } else if (a.max_steps > 0 && r.steps >= a.max_steps) {
-          finish = 1;
-          if (kStats) st.limited++;
+    // ---- one traversal step (runBaseTrace / runBlockTrace) -------------------
+    bool request = false;
+    int finish = 0;  // 1 = background, 2 = hit
+    const ViewParams &v = s_views[r.view];
+    if (r.depth == 0) {
+      finish = 1;
+    } else if (a.max_steps > 0 && r.steps >= a.max_steps) {
+      finish = 1;
+      if (kStats) st.limited++;
+    } else {
+      r.steps++;
+      if (r.depth <= B) {
+        // runBaseTrace (wavefront.cl:1400-1463)
+        uint32_t idx = c_pow_sum[r.depth - 1] + cell_index(r.depth, r.lx, r.ly, r.lz);
+        uint32_t chunk_bits = kSmemBases ? s_bases[idx] : __ldg(a.bases + idx);
+        if (kStats) v_base++;
+        if (((chunk_bits >> (octant(r.depth, r.lx, r.ly, r.lz) * 2)) & 2) == 0) {
+          uint64_t px = r.lx, py = r.ly, pz = r.lz;
+          traverse(r, r.depth);
+          if (leaving(r))
+            finish = 1;
+          else
+            r.depth = pop_depth(r, r.depth, px, py, pz);
+        } else if (r.depth < B) {
+          r.depth++;
         } else {
-          r.steps++;
-          if (r.depth <= B) {
-            // runBaseTrace (wavefront.cl:1400-1463)
-            uint32_t idx = c_pow_sum[r.depth - 1] + cell_index(r.depth, r.lx, r.ly, r.lz);
-            uint32_t chunk = kSmemBases ? s_bases[idx] : __ldg(a.bases + idx);
-            if (kStats) v_base++;
-            if (((chunk >> (octant(r.depth, r.lx, r.ly, r.lz) * 2)) & 2) == 0) {
-              uint64_t px = r.lx, py = r.ly, pz = r.lz;
-              traverse(r, r.depth);
-              if (leaving(r))
-                finish = 1;
-              else
-                r.depth = pop_depth(r, r.depth, px, py, pz);
-            } else if (r.depth < B) {
-              r.depth++;
-            } else {
-              r.depth = B + 2;
-              path[0] = cell_index(B + 2, r.lx, r.ly, r.lz);
-            }
-          } else {
-            // runBlockTrace (wavefront.cl:1465-1566)
-            int lvl = r.depth - (B + 2);
-            uint32_t addr = path[lvl * pstride];
-            if (addr != cur_addr) {
-              uint4 nd = load_node(blocks, a.n_blocks, addr);
-              cur_addr = addr;
-              cur_child = nd.x;
-              cur_chunk = nd.y & 0xffffu;
-            }
-            if (kStats) {
-              v_block += (uint32_t)(r.depth - B - 1);
-              st.block_steps++;
-            }
-            uint32_t group = addr >> 3;
-            if (a.usage && group != last_group && group < a.n_groups) {
-              // updateUsage (wavefront.cl:377-381)
-              uint16_t *tick = reinterpret_cast<uint16_t *>(a.usage + group);
-              uint16_t now = v.tick;
-              uint16_t cur = *tick;
-              if (cur < 65534 && cur != now) *tick = now;
-              last_group = group;
-            }
-            if (((cur_chunk >> (octant(r.depth, r.lx, r.ly, r.lz) * 2)) & 2) == 0) {
-              uint64_t px = r.lx, py = r.ly, pz = r.lz;
-              traverse(r, r.depth);
-              if (leaving(r)) {
-                finish = 1;
-              } else {
-                int nd = pop_depth(r, r.depth, px, py, pz);
-                if (nd >= B + 2 && (((px ^ r.lx) | (py ^ r.ly) | (pz ^ r.lz)) >> (64 - nd)) != 0) {
-                  // an ancestor cell changed: rebuild the path like getBlockAddress
-                  uint32_t w = cell_index(B + 2, r.lx, r.ly, r.lz);
-                  path[0] = w;
-                  for (int d = B + 2; d < nd; d++) {
-                    uint4 n2 = load_node(blocks, a.n_blocks, w);
-                    w = n2.x + octant(d, r.lx, r.ly, r.lz);
-                    path[(d - B - 1) * pstride] = w;
-                  }
-                }
-                r.depth = nd == B + 1 ? B : nd;
-              }
-            } else {
-              float c = cone_at(r, v.dof[0], v.dof[1]);
-              if (c > pow2_neg(B + 2)) {
-                r.depth = B + 2;
-                finish = 2;
-              } else if (c > pow2_neg(r.depth)) {
-                r.depth--;
-                if (r.depth == B + 1) r.depth = B;
-              } else if (cur_child == SVO_NO_CHILD) {
-                request = true;
-                finish = 2;
-              } else if (c < pow2_neg(r.depth + 1) && lvl + 1 < a.path_levels) {
-                path[(lvl + 1) * pstride] = cur_child + octant(r.depth, r.lx, r.ly, r.lz);
-                r.depth++;
-              } else {
-                finish = 2;
-              }
-            }
-          }
+          r.depth = B + 2;
+          path[0] = cell_index(B + 2, r.lx, r.ly, r.lz);
         }
-      }
-
-      // ---- child requests: one atomic per warp (requestChild, wavefront.cl:362-375)
-      unsigned rm = __ballot_sync(kFull, request);
-      if (rm) {
-        int leader = __ffs(rm) - 1;
-        uint32_t base = 0;
-        if (lane == leader) base = atomicAdd(a.request_count, (uint32_t)__popc(rm));
-        base = __shfl_sync(kFull, base, leader);
-        if (request) {
-          uint32_t slot = base + __popc(rm & lt_mask);
-          if (kStats) st.requests++;
-          if (slot < a.request_cap && a.requests) {
-            svo_child_request q;
-            q.address = cur_addr;
-            q.tick = 0;  // TraceData.Tick is never set by resolveTrace
-            q.depth = (uint8_t)r.depth;
-            q._pad0 = 0;
-            q.location[0] = r.lx;
-            q.location[1] = r.ly;
-            q.location[2] = r.lz;
-            float c = cone_at(r, s_views[r.view].dof[0], s_views[r.view].dof[1]);
-            q.tree_size = c <= pow2_neg(r.depth + 1) ? 1 : 0;
-            for (int k = 0; k < 7; k++) q._pad1[k] = 0;
-            a.requests[slot] = q;
-          }
-        }
-      }
-
-      if (finish) {
-        // evaluateBackground / resolveRemainders + drawTrace
-        const ViewParams &v = s_views[r.view];
-        uint32_t hit_index = SVO_MISS, cr, cg, cb;
-        uint8_t hit_depth = 0;
-        float t = __int_as_float(0x7f800000);
-        if (finish == 2) {
-          uint32_t addr = path[(r.depth - B - 2) * pstride];
+      } else {
+        // runBlockTrace (wavefront.cl:1465-1566)
+        int lvl = r.depth - (B + 2);
+        uint32_t addr = path[lvl * pstride];
+        if (addr != cur_addr) {
           uint4 nd = load_node(blocks, a.n_blocks, addr);
-          hit_index = addr;
-          hit_depth = (uint8_t)r.depth;
-          cr = (nd.z >> 16) & 0xffu;
-          cg = nd.z >> 24;
-          cb = nd.w & 0xffu;
-          float x = __fsub_rn(ulong_to_unit(r.lx), r.ox);
-          float y = __fsub_rn(ulong_to_unit(r.ly), r.oy);
-          float z = __fsub_rn(ulong_to_unit(r.lz), r.oz);
-          t = __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(x, x), __fmul_rn(y, y)), __fmul_rn(z, z)));
-          if (kStats) {
-            v_block += (uint32_t)(r.depth - B - 1);
-            st.hits++;
+          cur_addr = addr;
+          cur_child = nd.x;
+          cur_chunk = nd.y & 0xffffu;
+        }
+        if (kStats) {
+          v_block += (uint32_t)(r.depth - B - 1);
+          st.block_steps++;
+        }
+        uint32_t group = addr >> 3;
+        if (a.usage && group != last_group && group < a.n_groups) {
+          // updateUsage (wavefront.cl:377-381)
+          uint16_t *tick = reinterpret_cast<uint16_t *>(a.usage + group);
+          uint16_t now = v.tick;
+          uint16_t cur = *tick;
+          if (cur < 65534 && cur != now) *tick = now;
+          last_group = group;
+        }
+        if (((cur_chunk >> (octant(r.depth, r.lx, r.ly, r.lz) * 2)) & 2) == 0) {
+          uint64_t px = r.lx, py = r.ly, pz = r.lz;
+          traverse(r, r.depth);
+          if (leaving(r)) {
+            finish = 1;
+          } else {
+            int nd = pop_depth(r, r.depth, px, py, pz);
+            if (nd >= B + 2 && (((px ^ r.lx) | (py ^ r.ly) | (pz ^ r.lz)) >> (64 - nd)) != 0) {
+              // an ancestor cell changed: rebuild the path like getBlockAddress
+              uint32_t w = cell_index(B + 2, r.lx, r.ly, r.lz);
+              path[0] = w;
+              for (int d = B + 2; d < nd; d++) {
+                uint4 n2 = load_node(blocks, a.n_blocks, w);
+                w = n2.x + octant(d, r.lx, r.ly, r.lz);
+                path[(d - B - 1) * pstride] = w;
+              }
+            }
+            r.depth = nd == B + 1 ? B : nd;
           }
         } else {
-          float dotp = __fadd_rn(__fadd_rn(__fmul_rn(r.dx, 0.0f), __fmul_rn(r.dy, 0.0f)), __fmul_rn(r.dz, -1.0f));
-          if (dotp > 0.8f) {
-            cr = cg = cb = 255;  // luminosity (uchar)(dot*200) >= 160 > 0
+          float c = cone_at(r, v.dof[0], v.dof[1]);
+          if (c > pow2_neg(B + 2)) {
+            r.depth = B + 2;
+            finish = 2;
+          } else if (c > pow2_neg(r.depth)) {
+            r.depth--;
+            if (r.depth == B + 1) r.depth = B;
+          } else if (cur_child == SVO_NO_CHILD) {
+            request = true;
+            finish = 2;
+          } else if (c < pow2_neg(r.depth + 1) && lvl + 1 < a.path_levels) {
+            path[(lvl + 1) * pstride] = cur_child + octant(r.depth, r.lx, r.ly, r.lz);
+            r.depth++;
           } else {
-            cr = 135;
-            cg = 206;
-            cb = 235;
+            finish = 2;
           }
         }
-        const float fw = 65025.0f;  // (float)255 * 255.0f
-        float4 px;
-        px.x = fminf(__fdiv_rn(__uint2float_rn(cr * 255u), fw), 1.0f);
-        px.y = fminf(__fdiv_rn(__uint2float_rn(cg * 255u), fw), 1.0f);
-        px.z = fminf(__fdiv_rn(__uint2float_rn(cb * 255u), fw), 1.0f);
-        px.w = 1.0f;
-        if (v.hit_index) v.hit_index[r.id] = hit_index;
-        if (v.hit_depth) v.hit_depth[r.id] = hit_depth;
-        if (v.t) v.t[r.id] = t;
-        if (v.rgba) reinterpret_cast<float4 *>(v.rgba)[r.id] = px;
-        if (kStats) {
-          st.rays++;
-          st.base_steps += v_base;
-          st.block_reads += v_block;
-          if (a.ray_v_block) a.ray_v_block[ray_global] = v_block;
-          if (a.ray_v_base) a.ray_v_base[ray_global] = v_base;
-        }
-        active = false;
       }
-      if (!__any_sync(kFull, active)) break;
+    }
+
+    if (request) {
+      // requestChild (wavefront.cl:362-375): one atomic per group of requesting lanes
+      cg::coalesced_group g = cg::coalesced_threads();
+      uint32_t slot = claim(g, a.request_count, 1);
+      if (kStats) st.requests++;
+      if (slot < a.request_cap && a.requests) {
+        svo_child_request q;
+        q.address = cur_addr;
+        q.tick = 0;  // TraceData.Tick is never set by resolveTrace
+        q.depth = (uint8_t)r.depth;
+        q._pad0 = 0;
+        q.location[0] = r.lx;
+        q.location[1] = r.ly;
+        q.location[2] = r.lz;
+        float c = cone_at(r, v.dof[0], v.dof[1]);
+        q.tree_size = c <= pow2_neg(r.depth + 1) ? 1 : 0;
+        for (int k = 0; k < 7; k++) q._pad1[k] = 0;
+        a.requests[slot] = q;
+      }
+    }
+
+    if (finish) {
+      // evaluateBackground / resolveRemainders + drawTrace
+      uint32_t hit_index = SVO_MISS, cr, cg_, cb;
+      uint8_t hit_depth = 0;
+      float t = __int_as_float(0x7f800000);
+      if (finish == 2) {
+        uint32_t addr = path[(r.depth - B - 2) * pstride];
+        uint4 nd = load_node(blocks, a.n_blocks, addr);
+        hit_index = addr;
+        hit_depth = (uint8_t)r.depth;
+        cr = (nd.z >> 16) & 0xffu;
+        cg_ = nd.z >> 24;
+        cb = nd.w & 0xffu;
+        float x = __fsub_rn(ulong_to_unit(r.lx), r.ox);
+        float y = __fsub_rn(ulong_to_unit(r.ly), r.oy);
+        float z = __fsub_rn(ulong_to_unit(r.lz), r.oz);
+        t = __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(x, x), __fmul_rn(y, y)), __fmul_rn(z, z)));
+        if (kStats) {
+          v_block += (uint32_t)(r.depth - B - 1);
+          st.hits++;
+        }
+      } else {
+        float dotp = __fadd_rn(__fadd_rn(__fmul_rn(r.dx, 0.0f), __fmul_rn(r.dy, 0.0f)), __fmul_rn(r.dz, -1.0f));
+        if (dotp > 0.8f) {
+          cr = cg_ = cb = 255;  // luminosity (uchar)(dot*200) >= 160 > 0
+        } else {
+          cr = 135;
+          cg_ = 206;
+          cb = 235;
+        }
+      }
+      const float fw = 65025.0f;  // (float)255 * 255.0f
+      float4 px;
+      px.x = fminf(__fdiv_rn(__uint2float_rn(cr * 255u), fw), 1.0f);
+      px.y = fminf(__fdiv_rn(__uint2float_rn(cg_ * 255u), fw), 1.0f);
+      px.z = fminf(__fdiv_rn(__uint2float_rn(cb * 255u), fw), 1.0f);
+      px.w = 1.0f;
+      if (v.hit_index) v.hit_index[r.id] = hit_index;
+      if (v.hit_depth) v.hit_depth[r.id] = hit_depth;
+      if (v.t) v.t[r.id] = t;
+      if (v.rgba) reinterpret_cast<float4 *>(v.rgba)[r.id] = px;
+      if (kStats) {
+        st.rays++;
+        st.base_steps += v_base;
+        st.block_reads += v_block;
+        if (a.ray_v_block) a.ray_v_block[ray_global] = v_block;
+        if (a.ray_v_base) a.ray_v_base[ray_global] = v_base;
+      }
+      have = false;
     }
   }
 
   if (kStats && a.stats) {
     unsigned long long vals[7] = {st.rays, st.hits, st.base_steps, st.block_reads, st.block_steps, st.requests,
                                   st.limited};
+    cg::coalesced_group g = cg::coalesced_threads();
 #pragma unroll
     for (int k = 0; k < 7; k++) {
-      unsigned long long x = vals[k];
-      for (int off = 16; off > 0; off >>= 1) x += __shfl_down_sync(kFull, x, off);
-      if (lane == 0 && x) atomicAdd(a.stats + k, x);
+      unsigned long long x = cg::reduce(g, vals[k], cg::plus<unsigned long long>());
+      if (g.thread_rank() == 0 && x) atomicAdd(a.stats + k, x);
     }
   }
 }

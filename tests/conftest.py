@@ -11,6 +11,11 @@ for p in (os.path.join(ROOT, "svo-tracer_gb300"), os.path.join(ROOT, "oracle"), 
 
 def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (sm_103a); parity tests through the C ABI")
+    # SVO_TEST_WATCHDOG=<seconds>: dump every thread's Python stack periodically
+    if os.environ.get("SVO_TEST_WATCHDOG"):
+        import faulthandler
+
+        faulthandler.dump_traceback_later(int(os.environ["SVO_TEST_WATCHDOG"]), repeat=True)
 
 
 @pytest.fixture(scope="session", autouse=True)

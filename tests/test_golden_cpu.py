@@ -39,4 +39,5 @@ def test_oracle_matches_golden(path):
         assert np.array_equal(out[k], z[k]), k
     assert np.array_equal(usage["tick"], z["usage_tick"])
     assert out["n_requests"] == int(z["n_requests"])
-    assert po.sort_requests(out["requests"]).view(np.uint8).reshape(-1, 40).tobytes() == z["requests"].tobytes()
+    same = po.sort_requests(out["requests"]).view(np.uint8).reshape(-1, 40).tobytes() == z["requests"].tobytes()
+    assert same, "child requests differ"

@@ -14,6 +14,12 @@ from test_golden_cpu import GOLDEN, load_case
 
 pytestmark = pytest.mark.gpu
 
+
+@pytest.fixture(autouse=True)
+def default_config(tracer):
+    tracer.set_config(block_size=256, ctas_per_sm=0, ray_chunk=1, max_steps=1 << 16, collect_stats=0)
+    yield
+
 T_RTOL = 1e-5  # the benchmark spec's tolerance for t and RGBA; the checks below are tighter (exact)
 
 
@@ -24,6 +30,17 @@ def assert_same(got, want, label=""):
         if k in ("t", "rgba"):
             np.testing.assert_allclose(a, b, rtol=T_RTOL, atol=0, err_msg=label + k)
         assert np.array_equal(a, b), "%s%s: %d pixels differ" % (label, k, int((a != b).sum()))
+
+
+def same_requests(a, b):
+    """(equal, short message) for two child-request arrays in any order."""
+    a, b = po.sort_requests(a), po.sort_requests(b)
+    if len(a) != len(b):
+        return False, "request count %d vs %d" % (len(a), len(b))
+    bad = np.nonzero((a.view(np.uint8).reshape(-1, 40) != b.view(np.uint8).reshape(-1, 40)).any(axis=1))[0]
+    if len(bad):
+        return False, "%d of %d requests differ, first %r vs %r" % (len(bad), len(a), a[bad[0]], b[bad[0]])
+    return True, ""
 
 
 def run_both(tracer, tree, cam, max_steps=1 << 16):
@@ -52,7 +69,8 @@ def test_golden_fixture(tracer, path):
     assert np.array_equal(usage["tick"], z["usage_tick"])
     req, n = tracer.read_child_requests()
     assert n == int(z["n_requests"])
-    assert po.sort_requests(req).view(np.uint8).reshape(-1, 40).tobytes() == z["requests"].tobytes()
+    ok, msg = same_requests(req, z["requests"].reshape(-1).view(st.CHILD_REQUEST_DTYPE))
+    assert ok, msg
 
 
 SCENES = [
@@ -71,12 +89,13 @@ def test_trace_matches_oracle(tracer, scene):
     cam = st.look_at(o, t, w, h, fov, DoF=dof, Tick=17, MaxChildRequestId=1 << 20)
     got, usage, req, n, stats, (vb, vs), want, u_ref = run_both(tracer, tree, cam)
     assert_same(got, want)
-    assert np.array_equal(usage["tick"], u_ref["tick"])
+    assert np.array_equal(usage["tick"], u_ref["tick"]), "%d usage ticks differ" % int((usage["tick"] != u_ref["tick"]).sum())
     assert n == want["n_requests"]
-    assert po.sort_requests(req).tobytes() == po.sort_requests(want["requests"]).tobytes()
+    ok, msg = same_requests(req, want["requests"])
+    assert ok, msg
     # algorithmic-byte accounting (V_block, V_base) matches the reference walk the oracle counts
-    assert np.array_equal(vb, want["v_block"])
-    assert np.array_equal(vs, want["v_base"])
+    assert np.array_equal(vb, want["v_block"]), "V_block differs for %d rays" % int((vb != want["v_block"]).sum())
+    assert np.array_equal(vs, want["v_base"]), "V_base differs for %d rays" % int((vs != want["v_base"]).sum())
     assert stats["rays"] == w * h
     assert stats["hits"] == int((want["hit_index"] != st.MISS).sum())
     assert stats["block_node_reads"] == int(want["v_block"].sum())
@@ -132,9 +151,9 @@ def test_batch_equals_single_views_and_graph(tracer):
         assert_same(s, want)
 
 
-@pytest.mark.parametrize("cfg", [dict(block_size=128, cadence=1, refill_lanes=1),
-                                 dict(block_size=256, cadence=16, refill_lanes=32),
-                                 dict(block_size=64, cadence=3, refill_lanes=7, ctas_per_sm=1)])
+@pytest.mark.parametrize("cfg", [dict(block_size=128, ray_chunk=1),
+                                 dict(block_size=256, ray_chunk=8),
+                                 dict(block_size=64, ray_chunk=3, ctas_per_sm=1)])
 def test_launch_shapes_do_not_change_results(tracer, cfg):
     tree = st.TreeBuilder(st.SCENE_SPHERE, seed=6).BuildTree(4, 8)
     cam = st.look_at((1.1, 0.2, 0.9), (0.5, 0.5, 0.5), 120, 90, 60.0)
@@ -143,7 +162,7 @@ def test_launch_shapes_do_not_change_results(tracer, cfg):
         tracer.upload(tree)
         got = tracer.trace(cam)
     finally:
-        tracer.set_config(block_size=256, cadence=4, refill_lanes=16, ctas_per_sm=0)
+        tracer.set_config(block_size=256, ray_chunk=1, ctas_per_sm=0)
     assert_same(got, po.trace_view(tree, cam))
 
 

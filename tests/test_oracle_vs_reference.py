@@ -27,7 +27,8 @@ def _compare(tree, cam):
         assert np.array_equal(ref[k], orc[k]), k
     assert np.array_equal(u_ref["tick"], u_orc["tick"])
     assert ref["n_requests"] == orc["n_requests"]
-    assert po.sort_requests(ref["requests"]).tobytes() == po.sort_requests(orc["requests"]).tobytes()
+    same = po.sort_requests(ref["requests"]).tobytes() == po.sort_requests(orc["requests"]).tobytes()
+    assert same, "child requests differ"
     return orc
 
 
@@ -69,4 +70,5 @@ def test_unset_cone_tree_size_is_saturated():
     assert set(np.unique(a["tree_size"])) <= {0, 1}
     a["tree_size"] = 0
     b["tree_size"] = 0
-    assert po.sort_requests(a).tobytes() == po.sort_requests(b).tobytes()
+    same = po.sort_requests(a).tobytes() == po.sort_requests(b).tobytes()
+    assert same, "child requests differ"

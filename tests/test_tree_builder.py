@@ -93,7 +93,8 @@ def test_deterministic_and_thread_independent():
     b = st.TreeBuilder(st.SCENE_TERRAIN, seed=4, threads=8).BuildTree(3, 7)
     assert a.BlockCount == b.BlockCount
     assert np.array_equal(a.BaseBlocks, b.BaseBlocks)
-    assert a.Blocks.tobytes() == b.Blocks.tobytes()
+    same = a.Blocks.tobytes() == b.Blocks.tobytes()
+    assert same, "blocks differ"
 
 
 def test_budget_and_argument_errors():
