@@ -229,6 +229,29 @@ SVO_API svo_status svo_read_ray_counts(void *ctx, uint32_t *v_block, uint32_t *v
 /* Child requests of the last trace. *n = requests raised (may exceed cap). */
 SVO_API svo_status svo_read_child_requests(void *ctx, svo_child_request *out, uint32_t cap, uint32_t *n);
 
+/* ---- tracing without allocation ------------------------------------------ */
+
+/* No counterpart in the reference. For callers that cannot allocate device
+ * memory (an engine that owns every GPU allocation through its own pool, a
+ * real-time host loop where cudaMalloc's synchronisation and latency are not
+ * allowed): traces one view of a tree the caller keeps in device memory
+ * (bases, blocks, usage) into caller-owned device outputs (out->on_device must
+ * be 1) and, optionally, a caller-owned child-request array. The call makes no
+ * cudaMalloc/cudaFree and needs no context: its scratch (queue counters, error
+ * record, view record, ray tables) is a 132 KiB static device array inside
+ * libsvo, so views are limited to width + height <= 16384. Every GPU that
+ * loads the library holds that array until the process exits. All calls share
+ * it: calls whose work overlaps on the GPU race and must not be issued. The
+ * first call on a device looks up the array's device address; make it before
+ * any stream capture. max_node_depth = deepest node level (0 = 24). The call
+ * returns after the trace completed on `stream`; *requests_raised (if not
+ * NULL) receives the number of child requests raised. */
+SVO_API svo_status svo_trace_noalloc(int32_t device, void *stream, uint8_t base_depth, const uint16_t *bases,
+                                     size_t n_bases, const svo_block *blocks, size_t n_blocks, svo_usage *usage,
+                                     size_t n_groups, int32_t max_node_depth, const svo_trace_input *input,
+                                     const svo_trace_output *out, svo_child_request *requests, uint32_t request_cap,
+                                     uint32_t *requests_raised);
+
 /* ---- procedural scenes and the tree builder (host) ----------------------- */
 
 enum { SVO_SCENE_SPHERE = 0, SVO_SCENE_TERRAIN = 1 };

@@ -1,0 +1,102 @@
+"""svo_trace_noalloc: tracing for callers that cannot allocate device memory.
+
+Such a caller (an engine that owns every GPU allocation through its own pool, a
+real-time host loop that may not call cudaMalloc) keeps the octree and the output
+buffers in memory it already owns and calls svo_trace_noalloc, whose only scratch is
+a fixed static array inside libsvo. This test gives it buffers allocated here (the
+test may allocate; the entry point does not) and checks two calls in a row against
+the context-based svo_trace entry point on the same tree and view: hit indices, hit
+depths, usage ticks and child requests bit for bit, t and RGBA within the tolerance
+the other GPU tests use (they are in fact bit-exact)."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import pyoracle as po
+import svo_tracer as st
+
+pytestmark = pytest.mark.gpu
+
+T_RTOL = 1e-5
+
+
+def _entry(lib):
+    f = lib.svo_trace_noalloc
+    f.argtypes = [C.c_int32, C.c_void_p, C.c_uint8, C.c_void_p, C.c_size_t, C.c_void_p, C.c_size_t, C.c_void_p,
+                  C.c_size_t, C.c_int32, C.POINTER(st.TraceInputC), C.POINTER(st.TraceOutputC), C.c_void_p,
+                  C.c_uint32, C.POINTER(C.c_uint32)]
+    f.restype = C.c_int32
+    return f
+
+
+def test_noalloc_matches_trace_on_two_calls():
+    torch = pytest.importorskip("torch")
+    lib = st.load_library()
+    trace_noalloc = _entry(lib)
+    tree = st.TreeBuilder(st.SCENE_TERRAIN, seed=5).BuildTree(4, 9)
+    W, H, cap = 320, 180, 1 << 16
+    cam = st.look_at((0.1, 0.15, 0.55), (0.7, 0.7, 0.9), W, H, 60.0, Tick=9, MaxChildRequestId=cap)
+    n_groups = len(tree.Blocks) // 8
+
+    with st.Tracer(0) as tr:  # the existing entry point
+        tr.upload(tree)
+        tr.init_usage()
+        usage0 = tr.read_usage(n_groups)
+        want = tr.trace(cam)
+        usage_want = tr.read_usage(n_groups)
+        req_want, n_want = tr.read_child_requests()
+    assert n_want > 0 and (want.hit_index != st.MISS).any()
+
+    dev = torch.device("cuda", 0)
+    d_bases = torch.from_numpy(tree.BaseBlocks.view(np.int16).copy()).to(dev)
+    d_blocks = torch.from_numpy(tree.Blocks.view(np.uint8).copy()).to(dev)
+    c_in = cam.to_c()
+    for call in range(2):
+        d_usage = torch.from_numpy(usage0.view(np.uint8).copy()).to(dev)
+        d_idx = torch.full((W * H,), -7, dtype=torch.int32, device=dev)
+        d_dep = torch.full((W * H,), 99, dtype=torch.uint8, device=dev)
+        d_t = torch.full((W * H,), -1.0, dtype=torch.float32, device=dev)
+        d_rgba = torch.full((W * H * 4,), -1.0, dtype=torch.float32, device=dev)
+        d_req = torch.zeros((cap * 40,), dtype=torch.uint8, device=dev)
+        out = st.TraceOutputC(d_idx.data_ptr(), d_dep.data_ptr(), d_t.data_ptr(), d_rgba.data_ptr(), 1, 0)
+        raised = C.c_uint32(0)
+        torch.cuda.synchronize()
+        status = trace_noalloc(0, None, tree.BaseDepth, d_bases.data_ptr(), len(tree.BaseBlocks), d_blocks.data_ptr(),
+                               len(tree.Blocks), d_usage.data_ptr(), n_groups, 9, C.byref(c_in), C.byref(out),
+                               d_req.data_ptr(), cap, C.byref(raised))
+        assert status == 0, lib.svo_last_error_string()
+        torch.cuda.synchronize()
+        idx = d_idx.cpu().numpy().view(np.uint32)
+        dep = d_dep.cpu().numpy()
+        t = d_t.cpu().numpy()
+        rgba = d_rgba.cpu().numpy().reshape(-1, 4)
+        assert np.array_equal(idx, want.hit_index), "call %d: hit_index" % call
+        assert np.array_equal(dep, want.hit_depth), "call %d: hit_depth" % call
+        np.testing.assert_allclose(t, want.t, rtol=T_RTOL, atol=0)
+        np.testing.assert_allclose(rgba, want.rgba, rtol=T_RTOL, atol=0)
+        usage = d_usage.cpu().numpy().view(st.USAGE_DTYPE)
+        assert np.array_equal(usage["tick"], usage_want["tick"]), "call %d: usage ticks" % call
+        assert raised.value == n_want
+        req = d_req.cpu().numpy().view(st.CHILD_REQUEST_DTYPE)[: min(raised.value, cap)]
+        same = po.sort_requests(req).tobytes() == po.sort_requests(req_want).tobytes()
+        assert same, "call %d: child requests differ" % call
+
+
+def test_noalloc_rejects_oversized_views_and_host_outputs():
+    lib = st.load_library()
+    trace_noalloc = _entry(lib)
+    bases = np.zeros(st.pow_sum(2), np.uint16)
+    blocks = np.zeros(8 ** 4, st.BLOCK_DTYPE)
+    out = st.TraceOutputC(1, None, None, None, 1, 0)  # never dereferenced: the call must refuse first
+    too_big = st.TraceInput(ScreenSize=(16000, 400)).to_c()
+    status = trace_noalloc(0, None, 2, bases.ctypes.data, len(bases), blocks.ctypes.data, len(blocks), None, 0, 0,
+                           C.byref(too_big), C.byref(out), None, 0, None)
+    assert status == 1
+    assert b"16384" in lib.svo_last_error_string()
+    host_out = st.TraceOutputC(1, None, None, None, 0, 0)
+    ok_size = st.TraceInput(ScreenSize=(64, 48)).to_c()
+    status = trace_noalloc(0, None, 2, bases.ctypes.data, len(bases), blocks.ctypes.data, len(blocks), None, 0, 0,
+                           C.byref(ok_size), C.byref(host_out), None, 0, None)
+    assert status == 1
+    assert b"device pointers" in lib.svo_last_error_string()
