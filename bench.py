@@ -28,10 +28,10 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.join(ROOT, "svo-tracer_gb300"))
 sys.path.insert(0, os.path.join(ROOT, "oracle"))
 
-WIDTH, HEIGHT = 1920, 1080
+WIDTH, HEIGHT = 1920, 1080  # the headline view; --width/--height trace a smaller view of the same scene
 BASE_DEPTH, MAX_DEPTH, SEED = 4, 11, 5
 CAM_ORIGIN, CAM_TARGET, FOV = (0.08, 0.12, 0.62), (0.75, 0.8, 0.88), 60.0
-METRIC = "Mrays/s 1080p"
+METRIC = "Mrays/s 1080p"  # reported for the 1920x1080 view
 OUT_BYTES = 4 + 1 + 4 + 16  # hit index, hit depth, t, float4 RGBA
 
 
@@ -42,7 +42,7 @@ def workload(st):
 
 
 def config_dict(tree, extra=None):
-    d = {"workload": "1920x1080 single view, depth-11 fBm terrain octree (seeded, 6 octaves)",
+    d = {"workload": "%dx%d single view, depth-11 fBm terrain octree (seeded, 6 octaves)" % (WIDTH, HEIGHT),
          "width": WIDTH, "height": HEIGHT, "base_depth": BASE_DEPTH, "max_depth": MAX_DEPTH,
          "nodes": int(len(tree.Blocks)), "tree_bytes": int(tree.Blocks.nbytes),
          "l2": "flushed between steps (256 MiB write)"}
@@ -294,7 +294,11 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--width", type=int, default=WIDTH)
+    ap.add_argument("--height", type=int, default=HEIGHT)
     args = ap.parse_args()
+    global WIDTH, HEIGHT
+    WIDTH, HEIGHT = args.width, args.height
     args.warmup = max(3, args.warmup)
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", str(args.gpus if args.impl == "reference" else 1)))
