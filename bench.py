@@ -288,6 +288,7 @@ def run_ours(args, rank, world):
 
 
 def main():
+    global WIDTH, HEIGHT
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
@@ -297,7 +298,6 @@ def main():
     ap.add_argument("--width", type=int, default=WIDTH)
     ap.add_argument("--height", type=int, default=HEIGHT)
     args = ap.parse_args()
-    global WIDTH, HEIGHT
     WIDTH, HEIGHT = args.width, args.height
     args.warmup = max(3, args.warmup)
     rank = int(os.environ.get("RANK", "0"))
