@@ -174,9 +174,10 @@ typedef struct svo_trace_config {
   int32_t block_size;   /* threads per CTA, multiple of 32 up to 256 */
   int32_t ctas_per_sm;  /* resident CTAs per SM for the persistent grid */
   int32_t ray_chunk;    /* rays a thread claims per ray-queue fetch (1..64) */
+  int32_t cadence;      /* steps a thread runs between ray retire/refill points (1..1024) */
   int32_t max_steps;    /* per-ray step limit */
   int32_t collect_stats; /* 0 none, 1 totals (svo_last_trace_stats), 2 totals and per-ray counts */
-  int32_t _pad[3];
+  int32_t _pad[2];
 } svo_trace_config;
 
 /* ---- context ------------------------------------------------------------ */

@@ -168,6 +168,7 @@ extern "C" SVO_API svo_status svo_trace_noalloc(int32_t device, void *stream, ui
   a.base_depth = base_depth;
   a.max_steps = 1 << 16;
   a.ray_chunk = 1;
+  a.cadence = 16;
   a.block_size = 256;
   a.path_levels = depth - base_depth - 1;
   int occ = trace_occupancy(a, false);

@@ -139,6 +139,7 @@ static svo_trace_config default_config() {
   c.block_size = 256;
   c.ctas_per_sm = 0;  // occupancy-derived
   c.ray_chunk = 1;
+  c.cadence = 16;
   c.max_steps = 1 << 16;
   c.collect_stats = 0;
   return c;
@@ -273,6 +274,7 @@ static svo_status prepare_launch(Context &c, int32_t n_views, uint32_t total_ray
   a.base_depth = c.base_depth;
   a.max_steps = c.cfg.max_steps;
   a.ray_chunk = (uint32_t)std::max(1, c.cfg.ray_chunk);
+  a.cadence = std::max(1, c.cfg.cadence);
   a.block_size = c.cfg.block_size;
   a.path_levels = std::max(1, c.tree_depth - (int)c.base_depth - 1);
   int occ = c.cfg.ctas_per_sm > 0 ? c.cfg.ctas_per_sm : trace_occupancy(a, stats);
@@ -481,10 +483,11 @@ SVO_API svo_status svo_set_trace_config(void *ctx, const svo_trace_config *cfg) 
   svo_trace_config d = svo::default_config(), n = *cfg;
   if (n.block_size == 0) n.block_size = d.block_size;
   if (n.ray_chunk == 0) n.ray_chunk = d.ray_chunk;
+  if (n.cadence == 0) n.cadence = d.cadence;
   if (n.max_steps == 0) n.max_steps = d.max_steps;
   if (n.block_size % 32 || n.block_size < 32 || n.block_size > 256)
     return fail(SVO_ERR_INVALID_ARGUMENT, "svo_set_trace_config: block_size must be a multiple of 32 in 32..256");
-  if (n.ray_chunk < 1 || n.ray_chunk > 64 || n.max_steps < 1 || n.ctas_per_sm < 0 ||
+  if (n.ray_chunk < 1 || n.ray_chunk > 64 || n.cadence < 1 || n.cadence > 1024 || n.max_steps < 1 || n.ctas_per_sm < 0 ||
       n.collect_stats < 0 || n.collect_stats > 2)
     return fail(SVO_ERR_INVALID_ARGUMENT, "svo_set_trace_config: value out of range");
   c.cfg = n;

@@ -55,6 +55,7 @@ struct TraceLaunch {
   int32_t base_depth;
   int32_t max_steps;
   uint32_t ray_chunk;
+  int32_t cadence;
   int32_t block_size;
   int32_t grid;
   int32_t path_levels;

@@ -11,7 +11,9 @@
 //    counter. A persistent grid of threads takes rays from it: whenever a
 //    thread finishes a ray it claims the next one, the threads of a warp that
 //    need rays at the same moment sharing one atomicAdd (coalesced group,
-//    `ray_chunk` rays per thread). No step depends on the warp staying
+//    `ray_chunk` rays per thread). A thread runs up to `cadence` steps of its
+//    ray per pass, so the rays of a warp that finish within the same window are
+//    retired and replaced together. No step depends on the warp staying
 //    converged, so a lane leaves the loop as soon as the queue is drained.
 //    Ray state stays in registers, so the reference's per-step reload of
 //    ~74 B of SoA state disappears.
@@ -238,17 +240,141 @@ struct Stats {
   unsigned long long rays, hits, base_steps, block_reads, block_steps, requests, limited;
 };
 
-// Claims `n` consecutive slots of a device counter for the lanes of `g` with one
-// atomic; returns this lane's first slot. Only the lanes present in `g` take
-// part, so lanes may arrive here (or leave the kernel) independently.
+// Claims `per_lane` consecutive slots of a device counter for every lane of `g`
+// with one atomic; returns this lane's first slot. Only the lanes present in `g`
+// take part, so lanes may arrive here (or leave the kernel) independently.
 __device__ __forceinline__ uint32_t claim(cg::coalesced_group &g, uint32_t *counter, uint32_t per_lane) {
   uint32_t base = 0;
   if (g.thread_rank() == 0) base = atomicAdd(counter, g.size() * per_lane);
   return g.shfl(base, 0) + g.thread_rank();
 }
 
+// Per-thread traversal state besides the ray itself.
+struct Walk {
+  uint32_t *path;  // path[level * stride]: node address of each level below B+2
+  int stride;
+  uint32_t cur_addr, cur_child, cur_chunk;  // last node read
+  uint32_t last_group;                      // last usage group stamped
+  uint32_t v_block, v_base;                 // reference-walk counters (stats launches)
+};
+
+enum : int { kStepOn = 0, kStepBackground = 1, kStepHit = 2 };
+
+// One runBaseTrace (wavefront.cl:1400-1463) or runBlockTrace (:1465-1566) step.
+// Both read a 2-bit octant pair from a chunk (a base chunk or the current
+// node's) and share the empty-octant stepping code, so lanes at base and block
+// levels run it together.
 template <bool kStats, bool kSmemBases>
-__global__ void __launch_bounds__(256) trace_kernel(const TraceLaunch a) {
+__device__ __forceinline__ int step(const TraceLaunch &a, const ViewParams &v, const uint16_t *s_bases,
+                                    const uint4 *blocks, int B, Ray &r, Walk &w, Stats &st) {
+  if (r.depth == 0) return kStepBackground;
+  if (a.max_steps > 0 && r.steps >= a.max_steps) {
+    if (kStats) st.limited++;
+    return kStepBackground;
+  }
+  r.steps++;
+  const bool block = r.depth > B;
+  const int lvl = r.depth - (B + 2);
+  uint32_t chunk;
+  if (!block) {
+    uint32_t idx = c_pow_sum[r.depth - 1] + cell_index(r.depth, r.lx, r.ly, r.lz);
+    chunk = kSmemBases ? s_bases[idx] : __ldg(a.bases + idx);
+    if (kStats) w.v_base++;
+  } else {
+    uint32_t addr = w.path[lvl * w.stride];
+    if (addr != w.cur_addr) {
+      uint4 nd = load_node(blocks, a.n_blocks, addr);
+      w.cur_addr = addr;
+      w.cur_child = nd.x;
+      w.cur_chunk = nd.y & 0xffffu;
+    }
+    chunk = w.cur_chunk;
+    if (kStats) {
+      w.v_block += (uint32_t)(r.depth - B - 1);
+      st.block_steps++;
+    }
+    uint32_t group = addr >> 3;
+    if (a.usage && group != w.last_group && group < a.n_groups) {
+      // updateUsage (wavefront.cl:377-381)
+      uint16_t *tick = reinterpret_cast<uint16_t *>(a.usage + group);
+      uint16_t cur = *tick;
+      if (cur < 65534 && cur != v.tick) *tick = v.tick;
+      w.last_group = group;
+    }
+  }
+  if (((chunk >> (octant(r.depth, r.lx, r.ly, r.lz) * 2)) & 2) == 0) {
+    // empty octant: step to the neighbouring cell and pop (traverseChunk, comparePositions)
+    uint64_t px = r.lx, py = r.ly, pz = r.lz;
+    traverse(r, r.depth);
+    if (leaving(r)) return kStepBackground;
+    int nd = pop_depth(r, r.depth, px, py, pz);
+    if (block && nd >= B + 2 && (((px ^ r.lx) | (py ^ r.ly) | (pz ^ r.lz)) >> (64 - nd)) != 0) {
+      // an ancestor cell changed: rebuild the path like getBlockAddress
+      uint32_t n = cell_index(B + 2, r.lx, r.ly, r.lz);
+      w.path[0] = n;
+      for (int d = B + 2; d < nd; d++) {
+        uint4 n2 = load_node(blocks, a.n_blocks, n);
+        n = n2.x + octant(d, r.lx, r.ly, r.lz);
+        w.path[(d - B - 1) * w.stride] = n;
+      }
+    }
+    r.depth = nd == B + 1 ? B : nd;
+    return kStepOn;
+  }
+  if (!block) {
+    // geometry below a base cell: descend, jumping from level B to B+2
+    if (r.depth < B) {
+      r.depth++;
+    } else {
+      r.depth = B + 2;
+      w.path[0] = cell_index(B + 2, r.lx, r.ly, r.lz);
+    }
+    return kStepOn;
+  }
+  // geometry below a node: the cone LOD decision (ConeDepth = -half_log2(c))
+  float c = cone_at(r, v.dof[0], v.dof[1]);
+  if (c > pow2_neg(B + 2)) {
+    r.depth = B + 2;
+    return kStepHit;
+  }
+  if (c > pow2_neg(r.depth)) {
+    r.depth--;
+    if (r.depth == B + 1) r.depth = B;
+    return kStepOn;
+  }
+  if (w.cur_child == SVO_NO_CHILD) {
+    // requestChild (wavefront.cl:362-375): one atomic per group of requesting lanes
+    cg::coalesced_group g = cg::coalesced_threads();
+    uint32_t slot = claim(g, a.request_count, 1);
+    if (kStats) st.requests++;
+    if (slot < a.request_cap && a.requests) {
+      svo_child_request q;
+      q.address = w.cur_addr;
+      q.tick = 0;  // TraceData.Tick is never set by resolveTrace
+      q.depth = (uint8_t)r.depth;
+      q._pad0 = 0;
+      q.location[0] = r.lx;
+      q.location[1] = r.ly;
+      q.location[2] = r.lz;
+      q.tree_size = c <= pow2_neg(r.depth + 1) ? 1 : 0;
+      for (int k = 0; k < 7; k++) q._pad1[k] = 0;
+      a.requests[slot] = q;
+    }
+    return kStepHit;
+  }
+  if (c < pow2_neg(r.depth + 1) && lvl + 1 < a.path_levels) {
+    w.path[(lvl + 1) * w.stride] = w.cur_child + octant(r.depth, r.lx, r.ly, r.lz);
+    r.depth++;
+    return kStepOn;
+  }
+  return kStepHit;
+}
+
+template <bool kStats, bool kSmemBases>
+#ifndef SVO_TRACE_MIN_CTAS
+#define SVO_TRACE_MIN_CTAS 1
+#endif
+__global__ void __launch_bounds__(256, SVO_TRACE_MIN_CTAS) trace_kernel(const TraceLaunch a) {
   extern __shared__ __align__(16) uint8_t smem[];
   ViewParams *s_views = reinterpret_cast<ViewParams *>(smem);
   uint16_t *s_bases = reinterpret_cast<uint16_t *>(smem + a.n_views * sizeof(ViewParams));
@@ -266,21 +392,28 @@ __global__ void __launch_bounds__(256) trace_kernel(const TraceLaunch a) {
 
   const int B = a.base_depth;
   const uint4 *blocks = reinterpret_cast<const uint4 *>(a.blocks);
-  uint32_t *path = s_path + threadIdx.x;  // path[level * blockDim.x]
-  const int pstride = blockDim.x;
   const uint32_t chunk = a.ray_chunk;
+  const int cadence = a.cadence;
 
   Stats st = {0, 0, 0, 0, 0, 0, 0};
+  Walk w;
+  w.path = s_path + threadIdx.x;
+  w.stride = blockDim.x;
+  w.cur_addr = kFull;
+  w.cur_child = 0;
+  w.cur_chunk = 0;
+  w.last_group = kFull;
+  w.v_block = 0;
+  w.v_base = 0;
   Ray r;
   r.depth = 0;
   r.steps = 0;
-  uint32_t v_block = 0, v_base = 0;
-  uint32_t cur_addr = kFull, cur_child = 0, cur_chunk = 0, last_group = kFull;
+  r.view = 0;
   bool have = false;
   uint32_t ray_global = 0, next_ray = 0, left_in_chunk = 0, chunk_stride = 0;
-  // Every pass either starts a ray or advances one by a step, so a thread runs
-  // at most total_rays * (max_steps + 2) + 64 passes; past that bound it
-  // records its state and stops instead of spinning.
+  // Every pass either starts a ray or advances it by at least one step, so a
+  // thread runs at most total_rays * (max_steps + 2) + 64 passes; past that
+  // bound it records its state and stops instead of spinning.
   const unsigned long long iter_limit =
       (unsigned long long)a.total_rays * (unsigned long long)(a.max_steps + 2) + 64;
   unsigned long long iters = 0;
@@ -304,10 +437,9 @@ __global__ void __launch_bounds__(256) trace_kernel(const TraceLaunch a) {
         // interleaved so that lanes of a group hold neighbouring pixels
         cg::coalesced_group g = cg::coalesced_threads();
         uint32_t first = claim(g, a.ray_counter, chunk);
-        uint32_t base = first - g.thread_rank();
         chunk_stride = g.size();
         my = first;
-        next_ray = base + g.thread_rank() + chunk_stride;
+        next_ray = first + chunk_stride;
         left_in_chunk = chunk - 1;
       } else {
         my = next_ray;
@@ -317,8 +449,7 @@ __global__ void __launch_bounds__(256) trace_kernel(const TraceLaunch a) {
       // later rays of this chunk, and every later claim, are larger still
       if (my >= a.total_rays) break;  // queue drained
       ray_global = my;
-      // find the view (views are sorted by ray_begin)
-      int lo = 0, hi = a.n_views - 1;
+      int lo = 0, hi = a.n_views - 1;  // views are sorted by ray_begin
       while (lo < hi) {
         int mid = (lo + hi + 1) >> 1;
         if (s_views[mid].ray_begin <= my)
@@ -353,177 +484,69 @@ __global__ void __launch_bounds__(256) trace_kernel(const TraceLaunch a) {
       r.fov = v.fov_px;
       r.depth = 1;
       r.steps = 0;
-      v_block = 0;
-      v_base = 0;
-      cur_addr = kFull;
-      last_group = kFull;
+      w.v_block = 0;
+      w.v_base = 0;
+      w.cur_addr = kFull;
+      w.last_group = kFull;
       have = true;
       if (!enter_volume(r)) r.depth = 0;  // background at once
     }
 
-    // ---- one traversal step (runBaseTrace / runBlockTrace) -------------------
-    bool request = false;
-    int finish = 0;  // 1 = background, 2 = hit
+    // ---- up to `cadence` traversal steps; retire finished rays together -------
     const ViewParams &v = s_views[r.view];
-    if (r.depth == 0) {
-      finish = 1;
-    } else if (a.max_steps > 0 && r.steps >= a.max_steps) {
-      finish = 1;
-      if (kStats) st.limited++;
-    } else {
-      r.steps++;
-      if (r.depth <= B) {
-        // runBaseTrace (wavefront.cl:1400-1463)
-        uint32_t idx = c_pow_sum[r.depth - 1] + cell_index(r.depth, r.lx, r.ly, r.lz);
-        uint32_t chunk_bits = kSmemBases ? s_bases[idx] : __ldg(a.bases + idx);
-        if (kStats) v_base++;
-        if (((chunk_bits >> (octant(r.depth, r.lx, r.ly, r.lz) * 2)) & 2) == 0) {
-          uint64_t px = r.lx, py = r.ly, pz = r.lz;
-          traverse(r, r.depth);
-          if (leaving(r))
-            finish = 1;
-          else
-            r.depth = pop_depth(r, r.depth, px, py, pz);
-        } else if (r.depth < B) {
-          r.depth++;
-        } else {
-          r.depth = B + 2;
-          path[0] = cell_index(B + 2, r.lx, r.ly, r.lz);
-        }
-      } else {
-        // runBlockTrace (wavefront.cl:1465-1566)
-        int lvl = r.depth - (B + 2);
-        uint32_t addr = path[lvl * pstride];
-        if (addr != cur_addr) {
-          uint4 nd = load_node(blocks, a.n_blocks, addr);
-          cur_addr = addr;
-          cur_child = nd.x;
-          cur_chunk = nd.y & 0xffffu;
-        }
-        if (kStats) {
-          v_block += (uint32_t)(r.depth - B - 1);
-          st.block_steps++;
-        }
-        uint32_t group = addr >> 3;
-        if (a.usage && group != last_group && group < a.n_groups) {
-          // updateUsage (wavefront.cl:377-381)
-          uint16_t *tick = reinterpret_cast<uint16_t *>(a.usage + group);
-          uint16_t now = v.tick;
-          uint16_t cur = *tick;
-          if (cur < 65534 && cur != now) *tick = now;
-          last_group = group;
-        }
-        if (((cur_chunk >> (octant(r.depth, r.lx, r.ly, r.lz) * 2)) & 2) == 0) {
-          uint64_t px = r.lx, py = r.ly, pz = r.lz;
-          traverse(r, r.depth);
-          if (leaving(r)) {
-            finish = 1;
-          } else {
-            int nd = pop_depth(r, r.depth, px, py, pz);
-            if (nd >= B + 2 && (((px ^ r.lx) | (py ^ r.ly) | (pz ^ r.lz)) >> (64 - nd)) != 0) {
-              // an ancestor cell changed: rebuild the path like getBlockAddress
-              uint32_t w = cell_index(B + 2, r.lx, r.ly, r.lz);
-              path[0] = w;
-              for (int d = B + 2; d < nd; d++) {
-                uint4 n2 = load_node(blocks, a.n_blocks, w);
-                w = n2.x + octant(d, r.lx, r.ly, r.lz);
-                path[(d - B - 1) * pstride] = w;
-              }
-            }
-            r.depth = nd == B + 1 ? B : nd;
-          }
-        } else {
-          float c = cone_at(r, v.dof[0], v.dof[1]);
-          if (c > pow2_neg(B + 2)) {
-            r.depth = B + 2;
-            finish = 2;
-          } else if (c > pow2_neg(r.depth)) {
-            r.depth--;
-            if (r.depth == B + 1) r.depth = B;
-          } else if (cur_child == SVO_NO_CHILD) {
-            request = true;
-            finish = 2;
-          } else if (c < pow2_neg(r.depth + 1) && lvl + 1 < a.path_levels) {
-            path[(lvl + 1) * pstride] = cur_child + octant(r.depth, r.lx, r.ly, r.lz);
-            r.depth++;
-          } else {
-            finish = 2;
-          }
-        }
-      }
-    }
+    int finish = kStepOn;
+    for (int k = 0; k < cadence && finish == kStepOn; k++)
+      finish = step<kStats, kSmemBases>(a, v, s_bases, blocks, B, r, w, st);
+    if (finish == kStepOn) continue;
 
-    if (request) {
-      // requestChild (wavefront.cl:362-375): one atomic per group of requesting lanes
-      cg::coalesced_group g = cg::coalesced_threads();
-      uint32_t slot = claim(g, a.request_count, 1);
-      if (kStats) st.requests++;
-      if (slot < a.request_cap && a.requests) {
-        svo_child_request q;
-        q.address = cur_addr;
-        q.tick = 0;  // TraceData.Tick is never set by resolveTrace
-        q.depth = (uint8_t)r.depth;
-        q._pad0 = 0;
-        q.location[0] = r.lx;
-        q.location[1] = r.ly;
-        q.location[2] = r.lz;
-        float c = cone_at(r, v.dof[0], v.dof[1]);
-        q.tree_size = c <= pow2_neg(r.depth + 1) ? 1 : 0;
-        for (int k = 0; k < 7; k++) q._pad1[k] = 0;
-        a.requests[slot] = q;
-      }
-    }
-
-    if (finish) {
-      // evaluateBackground / resolveRemainders + drawTrace
-      uint32_t hit_index = SVO_MISS, cr, cg_, cb;
-      uint8_t hit_depth = 0;
-      float t = __int_as_float(0x7f800000);
-      if (finish == 2) {
-        uint32_t addr = path[(r.depth - B - 2) * pstride];
-        uint4 nd = load_node(blocks, a.n_blocks, addr);
-        hit_index = addr;
-        hit_depth = (uint8_t)r.depth;
-        cr = (nd.z >> 16) & 0xffu;
-        cg_ = nd.z >> 24;
-        cb = nd.w & 0xffu;
-        float x = __fsub_rn(ulong_to_unit(r.lx), r.ox);
-        float y = __fsub_rn(ulong_to_unit(r.ly), r.oy);
-        float z = __fsub_rn(ulong_to_unit(r.lz), r.oz);
-        t = __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(x, x), __fmul_rn(y, y)), __fmul_rn(z, z)));
-        if (kStats) {
-          v_block += (uint32_t)(r.depth - B - 1);
-          st.hits++;
-        }
-      } else {
-        float dotp = __fadd_rn(__fadd_rn(__fmul_rn(r.dx, 0.0f), __fmul_rn(r.dy, 0.0f)), __fmul_rn(r.dz, -1.0f));
-        if (dotp > 0.8f) {
-          cr = cg_ = cb = 255;  // luminosity (uchar)(dot*200) >= 160 > 0
-        } else {
-          cr = 135;
-          cg_ = 206;
-          cb = 235;
-        }
-      }
-      const float fw = 65025.0f;  // (float)255 * 255.0f
-      float4 px;
-      px.x = fminf(__fdiv_rn(__uint2float_rn(cr * 255u), fw), 1.0f);
-      px.y = fminf(__fdiv_rn(__uint2float_rn(cg_ * 255u), fw), 1.0f);
-      px.z = fminf(__fdiv_rn(__uint2float_rn(cb * 255u), fw), 1.0f);
-      px.w = 1.0f;
-      if (v.hit_index) v.hit_index[r.id] = hit_index;
-      if (v.hit_depth) v.hit_depth[r.id] = hit_depth;
-      if (v.t) v.t[r.id] = t;
-      if (v.rgba) reinterpret_cast<float4 *>(v.rgba)[r.id] = px;
+    // evaluateBackground / resolveRemainders + drawTrace
+    uint32_t hit_index = SVO_MISS, cr, cg_, cb;
+    uint8_t hit_depth = 0;
+    float t = __int_as_float(0x7f800000);
+    if (finish == kStepHit) {
+      uint32_t addr = w.path[(r.depth - B - 2) * w.stride];
+      uint4 nd = load_node(blocks, a.n_blocks, addr);
+      hit_index = addr;
+      hit_depth = (uint8_t)r.depth;
+      cr = (nd.z >> 16) & 0xffu;
+      cg_ = nd.z >> 24;
+      cb = nd.w & 0xffu;
+      float x = __fsub_rn(ulong_to_unit(r.lx), r.ox);
+      float y = __fsub_rn(ulong_to_unit(r.ly), r.oy);
+      float z = __fsub_rn(ulong_to_unit(r.lz), r.oz);
+      t = __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(x, x), __fmul_rn(y, y)), __fmul_rn(z, z)));
       if (kStats) {
-        st.rays++;
-        st.base_steps += v_base;
-        st.block_reads += v_block;
-        if (a.ray_v_block) a.ray_v_block[ray_global] = v_block;
-        if (a.ray_v_base) a.ray_v_base[ray_global] = v_base;
+        w.v_block += (uint32_t)(r.depth - B - 1);
+        st.hits++;
       }
-      have = false;
+    } else {
+      float dotp = __fadd_rn(__fadd_rn(__fmul_rn(r.dx, 0.0f), __fmul_rn(r.dy, 0.0f)), __fmul_rn(r.dz, -1.0f));
+      if (dotp > 0.8f) {
+        cr = cg_ = cb = 255;  // luminosity (uchar)(dot*200) >= 160 > 0
+      } else {
+        cr = 135;
+        cg_ = 206;
+        cb = 235;
+      }
     }
+    const float fw = 65025.0f;  // (float)255 * 255.0f
+    float4 px;
+    px.x = fminf(__fdiv_rn(__uint2float_rn(cr * 255u), fw), 1.0f);
+    px.y = fminf(__fdiv_rn(__uint2float_rn(cg_ * 255u), fw), 1.0f);
+    px.z = fminf(__fdiv_rn(__uint2float_rn(cb * 255u), fw), 1.0f);
+    px.w = 1.0f;
+    if (v.hit_index) v.hit_index[r.id] = hit_index;
+    if (v.hit_depth) v.hit_depth[r.id] = hit_depth;
+    if (v.t) v.t[r.id] = t;
+    if (v.rgba) reinterpret_cast<float4 *>(v.rgba)[r.id] = px;
+    if (kStats) {
+      st.rays++;
+      st.base_steps += w.v_base;
+      st.block_reads += w.v_block;
+      if (a.ray_v_block) a.ray_v_block[ray_global] = w.v_block;
+      if (a.ray_v_base) a.ray_v_base[ray_global] = w.v_base;
+    }
+    have = false;
   }
 
   if (kStats && a.stats) {

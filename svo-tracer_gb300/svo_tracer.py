@@ -77,8 +77,8 @@ class TraceStatsC(C.Structure):
 
 
 class TraceConfigC(C.Structure):
-    _fields_ = [(n, C.c_int32) for n in ("block_size", "ctas_per_sm", "ray_chunk", "max_steps", "collect_stats",
-                                          "_pad0", "_pad1", "_pad2")]
+    _fields_ = [(n, C.c_int32) for n in ("block_size", "ctas_per_sm", "ray_chunk", "cadence", "max_steps",
+                                          "collect_stats", "_pad0", "_pad1")]
 
 
 class SceneParamsC(C.Structure):

@@ -17,7 +17,7 @@ pytestmark = pytest.mark.gpu
 
 @pytest.fixture(autouse=True)
 def default_config(tracer):
-    tracer.set_config(block_size=256, ctas_per_sm=0, ray_chunk=1, max_steps=1 << 16, collect_stats=0)
+    tracer.set_config(block_size=256, ctas_per_sm=0, ray_chunk=1, cadence=16, max_steps=1 << 16, collect_stats=0)
     yield
 
 T_RTOL = 1e-5  # the benchmark spec's tolerance for t and RGBA; the checks below are tighter (exact)
@@ -151,9 +151,9 @@ def test_batch_equals_single_views_and_graph(tracer):
         assert_same(s, want)
 
 
-@pytest.mark.parametrize("cfg", [dict(block_size=128, ray_chunk=1),
-                                 dict(block_size=256, ray_chunk=8),
-                                 dict(block_size=64, ray_chunk=3, ctas_per_sm=1)])
+@pytest.mark.parametrize("cfg", [dict(block_size=128, ray_chunk=1, cadence=1),
+                                 dict(block_size=256, ray_chunk=8, cadence=32),
+                                 dict(block_size=64, ray_chunk=3, cadence=5, ctas_per_sm=1)])
 def test_launch_shapes_do_not_change_results(tracer, cfg):
     tree = st.TreeBuilder(st.SCENE_SPHERE, seed=6).BuildTree(4, 8)
     cam = st.look_at((1.1, 0.2, 0.9), (0.5, 0.5, 0.5), 120, 90, 60.0)
@@ -162,7 +162,7 @@ def test_launch_shapes_do_not_change_results(tracer, cfg):
         tracer.upload(tree)
         got = tracer.trace(cam)
     finally:
-        tracer.set_config(block_size=256, ray_chunk=1, ctas_per_sm=0)
+        tracer.set_config(block_size=256, ray_chunk=1, cadence=16, ctas_per_sm=0)
     assert_same(got, po.trace_view(tree, cam))
 
 
