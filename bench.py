@@ -168,6 +168,63 @@ def run_reference(args, rank, world):
     print(json.dumps(line))
 
 
+def multiview(tr, torch, dev, stream, flush, args):
+    """64 mixed-resolution views over the same tree: one autotuned, CUDA-graph-replayed
+    persistent launch against 64 sequential plain launches, same device outputs."""
+    import svo_tracer as st
+
+    views = st.mixed_views(seed=4, Tick=7, MaxChildRequestId=1 << 16)
+    sizes = [v.ScreenSize[0] * v.ScreenSize[1] for v in views]
+    rays = sum(sizes)
+
+    def alloc():
+        o = [(torch.empty(n, dtype=torch.int32, device=dev), torch.empty(n, dtype=torch.uint8, device=dev),
+              torch.empty(n, dtype=torch.float32, device=dev), torch.empty(4 * n, dtype=torch.float32, device=dev))
+             for n in sizes]
+        return o, [tuple(x.data_ptr() for x in t) for t in o]
+
+    batched_t, batched_p = alloc()
+    plain_t, plain_p = alloc()
+    cfg0 = {n: getattr(tr.get_config(), n) for n in ("block_size", "ray_chunk", "cadence", "ctas_per_sm")}
+    with torch.cuda.stream(stream):
+        # plain: one launch per view with the default configuration
+        for _ in range(2):
+            for v, p in zip(views, plain_p):
+                tr.trace_device([v], [p])
+        plain_ms = []
+        for _ in range(max(3, args.steps // 4)):
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for v, p in zip(views, plain_p):
+                tr.trace_device([v], [p])
+            e1.record(stream)
+            plain_ms.append((e0, e1))
+        torch.cuda.synchronize(dev)
+        plain = sorted(a.elapsed_time(b) for a, b in plain_ms)[len(plain_ms) // 2]
+        tuned, tune_ms = tr.autotune(views, batched_p, repeats=2)
+        for _ in range(2):
+            tr.trace_device(views, batched_p, graph=True)
+        batch_ms = []
+        for _ in range(max(3, args.steps // 4)):
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            tr.trace_device(views, batched_p, graph=True)
+            e1.record(stream)
+            batch_ms.append((e0, e1))
+        torch.cuda.synchronize(dev)
+        batched = sorted(a.elapsed_time(b) for a, b in batch_ms)[len(batch_ms) // 2]
+    same = all(torch.equal(a[0], b[0]) and torch.equal(a[1], b[1]) and torch.equal(a[2], b[2])
+               and torch.equal(a[3], b[3]) for a, b in zip(batched_t, plain_t))
+    tr.set_config(**cfg0)
+    return {"views": len(views), "rays": rays, "batched_ms": batched, "plain_ms": plain,
+            "batched_mrays_s": rays / batched / 1e3, "plain_mrays_s": rays / plain / 1e3,
+            "speedup": plain / batched, "identical_outputs": bool(same), "autotuned": tuned,
+            "batched": "one persistent launch over all views, replayed from a CUDA graph",
+            "plain": "64 sequential single-view launches, same stream, default configuration"}
+
+
 def run_ours(args, rank, world):
     import torch
 
@@ -276,6 +333,8 @@ def run_ours(args, rank, world):
         "clocks": clk.summary(),
         "trace_stats": {k: int(v) for k, v in stats.items()},
     }
+    if not args.no_multiview:
+        line["multiview"] = multiview(tr, torch, dev, stream, flush, args)
     if not args.no_cpu_baseline:
         import pyoracle as po
 
@@ -295,6 +354,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-multiview", action="store_true")
     ap.add_argument("--width", type=int, default=WIDTH)
     ap.add_argument("--height", type=int, default=HEIGHT)
     args = ap.parse_args()

@@ -224,6 +224,14 @@ SVO_API svo_status svo_trace_batch(void *ctx, const svo_trace_input *inputs, int
 SVO_API svo_status svo_trace_batch_graph(void *ctx, const svo_trace_input *inputs, int32_t n_views,
                                          const svo_trace_output *out);
 SVO_API svo_status svo_last_trace_stats(void *ctx, svo_trace_stats *stats);
+/* Autotuner for a view set (no reference counterpart): times svo_trace_batch
+ * over block sizes {64,128,256} x ray chunks {1,2,4,8} x cadences {4,8,16,32}
+ * (best of `repeats` runs each; outputs must be device pointers), keeps the
+ * fastest configuration in the context and returns it. Results are identical
+ * for every configuration. */
+SVO_API svo_status svo_autotune(void *ctx, const svo_trace_input *inputs, int32_t n_views,
+                                const svo_trace_output *out, int32_t repeats, svo_trace_config *best,
+                                float *best_ms);
 /* Per-ray V_block / V_base of the last trace run with collect_stats = 2,
  * in batch ray order (view 0's pixels first). */
 SVO_API svo_status svo_read_ray_counts(void *ctx, uint32_t *v_block, uint32_t *v_base, size_t n);

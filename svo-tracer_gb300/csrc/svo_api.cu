@@ -106,6 +106,8 @@ struct Context {
   uint64_t last_rays = 0;
   bool last_stats_valid = false;
   svo_trace_config cfg{};
+  // recorded after the view/table uploads: the pinned staging may be rewritten once it fired
+  cudaEvent_t staged = nullptr;
   // graph cache for svo_trace_batch_graph
   cudaGraphExec_t graph_exec = nullptr;
   std::vector<uint32_t> graph_key;
@@ -113,6 +115,7 @@ struct Context {
   ~Context() {
     if (device >= 0) cudaSetDevice(device);
     if (graph_exec) cudaGraphExecDestroy(graph_exec);
+    if (staged) cudaEventDestroy(staged);
     bases.release();
     blocks.release();
     usage.release();
@@ -326,6 +329,8 @@ static svo_status run_trace(Context &c, const svo_trace_input *in, int32_t n, co
   c.request_cap = cap;
   uint32_t total_rays;
   size_t table_floats;
+  // the previous call's uploads must have read the pinned staging before it is rewritten
+  SVO_CUDA(cudaEventSynchronize(c.staged), "svo_trace: staging");
   svo_status st = stage_views(c, in, n, out, on_device, total_rays, table_floats);
   if (st) return st;
   bool stats = c.cfg.collect_stats > 0;
@@ -337,11 +342,13 @@ static svo_status run_trace(Context &c, const svo_trace_input *in, int32_t n, co
   st = prepare_launch(c, n, total_rays, a, stats);
   if (st) return st;
 
-  auto enqueue = [&]() -> svo_status {
+  auto enqueue = [&](bool capturing) -> svo_status {
     SVO_CUDA(cudaMemcpyAsync(c.views.p, c.h_views.p, sizeof(ViewParams) * n, cudaMemcpyHostToDevice, c.stream),
              "svo_trace: view upload");
     SVO_CUDA(cudaMemcpyAsync(c.tables.p, c.h_tables.p, sizeof(float) * table_floats, cudaMemcpyHostToDevice, c.stream),
              "svo_trace: table upload");
+    SVO_CUDA(cudaEventRecordWithFlags(c.staged, c.stream, capturing ? cudaEventRecordExternal : cudaEventRecordDefault),
+             "svo_trace: staging event");
     SVO_CUDA(cudaMemsetAsync(c.counters.p, 0, (4 + 8) * sizeof(uint32_t), c.stream), "svo_trace: counter reset");
     if (stats) SVO_CUDA(cudaMemsetAsync(c.stats.p, 0, 8 * sizeof(unsigned long long), c.stream), "svo_trace: stats reset");
     return launch_trace(a, stats, c.stream);
@@ -365,7 +372,7 @@ static svo_status run_trace(Context &c, const svo_trace_input *in, int32_t n, co
       c.graph_exec = nullptr;
       cudaStream_t cap_stream = c.stream;
       SVO_CUDA(cudaStreamBeginCapture(cap_stream, cudaStreamCaptureModeThreadLocal), "svo_trace_batch_graph: capture");
-      svo_status est = enqueue();
+      svo_status est = enqueue(true);
       cudaGraph_t g = nullptr;
       cudaError_t ce = cudaStreamEndCapture(cap_stream, &g);
       if (est) {
@@ -383,7 +390,7 @@ static svo_status run_trace(Context &c, const svo_trace_input *in, int32_t n, co
     }
     SVO_CUDA(cudaGraphLaunch(c.graph_exec, c.stream), "svo_trace_batch_graph: launch");
   } else {
-    st = enqueue();
+    st = enqueue(false);
     if (st) return st;
   }
   c.last_rays = total_rays;
@@ -447,6 +454,7 @@ SVO_API svo_status svo_create(int32_t device, void **ctx) {
   c->device = device;
   SVO_CUDA(cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, device), "svo_create: SM count");
   SVO_CUDA(cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking), "svo_create: stream");
+  SVO_CUDA(cudaEventCreateWithFlags(&c->staged, cudaEventDisableTiming), "svo_create: event");
   c->stream = c->own_stream;
   c->cfg = svo::default_config();
   SVO_CUDA(c->counters.reserve(4 + 8), "svo_create: counters");
@@ -638,6 +646,67 @@ SVO_API svo_status svo_trace_batch_graph(void *ctx, const svo_trace_input *input
   GUARD_BEGIN
   return svo::run_trace(c, inputs, n_views, out, true);
   GUARD_END("svo_trace_batch_graph")
+}
+
+SVO_API svo_status svo_autotune(void *ctx, const svo_trace_input *inputs, int32_t n_views,
+                                const svo_trace_output *out, int32_t repeats, svo_trace_config *best,
+                                float *best_ms) {
+  CTX_OR_FAIL(ctx, "svo_autotune");
+  GUARD_BEGIN
+  if (n_views <= 0 || !inputs || !out) return fail(SVO_ERR_INVALID_ARGUMENT, "svo_autotune: bad view list");
+  for (int i = 0; i < n_views; i++)
+    if (!out[i].on_device) return fail(SVO_ERR_INVALID_ARGUMENT, "svo_autotune: outputs must be device pointers");
+  if (repeats <= 0) repeats = 3;
+  SVO_CUDA(cudaSetDevice(c.device), "cudaSetDevice");
+  svo_trace_config base = c.cfg, chosen = c.cfg;
+  base.collect_stats = 0;
+  float chosen_ms = 1e30f;
+  cudaEvent_t e0, e1;
+  SVO_CUDA(cudaEventCreate(&e0), "svo_autotune: event");
+  SVO_CUDA(cudaEventCreate(&e1), "svo_autotune: event");
+  svo_status st = SVO_OK;
+  // Block size, rays claimed per queue fetch and steps between retire points;
+  // results do not depend on any of them, only the time does.
+  const int sizes[] = {64, 128, 256};
+  const int chunks[] = {1, 2, 4, 8};
+  const int cadences[] = {4, 8, 16, 32};
+  for (int bs : sizes)
+    for (int ch : chunks)
+      for (int cd : cadences) {
+        if (st) break;
+        svo_trace_config cfg = base;
+        cfg.block_size = bs;
+        cfg.ray_chunk = ch;
+        cfg.cadence = cd;
+        c.cfg = cfg;
+        st = svo::run_trace(c, inputs, n_views, out, false);  // warm-up
+        if (st) break;
+        float best_rep = 1e30f;
+        for (int r = 0; r < repeats && !st; r++) {
+          cudaEventRecord(e0, c.stream);
+          st = svo::run_trace(c, inputs, n_views, out, false);
+          cudaEventRecord(e1, c.stream);
+          if (cudaEventSynchronize(e1) != cudaSuccess) st = fail(SVO_ERR_CUDA, "svo_autotune: event sync");
+          float ms = 0.f;
+          cudaEventElapsedTime(&ms, e0, e1);
+          best_rep = std::min(best_rep, ms);
+        }
+        if (!st && best_rep < chosen_ms) {
+          chosen_ms = best_rep;
+          chosen = cfg;
+        }
+      }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  chosen.collect_stats = 0;
+  c.cfg = st ? base : chosen;
+  if (c.graph_exec) cudaGraphExecDestroy(c.graph_exec);
+  c.graph_exec = nullptr;
+  if (st) return st;
+  if (best) *best = chosen;
+  if (best_ms) *best_ms = chosen_ms;
+  return SVO_OK;
+  GUARD_END("svo_autotune")
 }
 
 SVO_API svo_status svo_last_trace_stats(void *ctx, svo_trace_stats *stats) {

@@ -121,6 +121,8 @@ def load_library(path: str | None = None) -> C.CDLL:
         "svo_trace_batch": ([vp, C.POINTER(TraceInputC), C.c_int32, C.POINTER(TraceOutputC)], C.c_int32),
         "svo_trace_batch_graph": ([vp, C.POINTER(TraceInputC), C.c_int32, C.POINTER(TraceOutputC)], C.c_int32),
         "svo_last_trace_stats": ([vp, C.POINTER(TraceStatsC)], C.c_int32),
+        "svo_autotune": ([vp, C.POINTER(TraceInputC), C.c_int32, C.POINTER(TraceOutputC), C.c_int32,
+                          C.POINTER(TraceConfigC), C.POINTER(C.c_float)], C.c_int32),
         "svo_read_ray_counts": ([vp, vp, vp, sz], C.c_int32),
         "svo_read_child_requests": ([vp, vp, C.c_uint32, C.POINTER(C.c_uint32)], C.c_int32),
         "svo_tree_build": ([C.POINTER(SceneParamsC), C.POINTER(vp)], C.c_int32),
@@ -254,6 +256,31 @@ def look_at(origin, target, width: int, height: int, fov_deg: float, up=(0.0, 0.
                       ScreenSize=(width, height), **kw)
 
 
+def mixed_views(seed: int = 4, n: int = 64, **kw):
+    """The batched multi-view workload: n cameras whose pixel counts are drawn
+    log-uniformly between 128x128 and 1920x1080 with aspect ratios in {1, 4/3, 16/9},
+    placed uniformly on spheres of radius 1.2-2.0 (world units, [-1,1]^3 maps to the
+    unit cube: radius 0.6-1.0 around its centre), looking at seeded targets within 0.2
+    world units of the centre, horizontal FoV uniform in 40-90 degrees."""
+    rng = np.random.default_rng(seed)
+    views = []
+    lo, hi = math.log(128 * 128), math.log(1920 * 1080)
+    for _ in range(n):
+        px = math.exp(rng.uniform(lo, hi))
+        aspect = [1.0, 4.0 / 3.0, 16.0 / 9.0][int(rng.integers(0, 3))]
+        h = max(1, int(round(math.sqrt(px / aspect))))
+        w = max(1, int(round(h * aspect)))
+        d = rng.normal(size=3)
+        d /= np.linalg.norm(d)
+        radius = rng.uniform(1.2, 2.0) * 0.5
+        t = rng.normal(size=3)
+        t *= rng.uniform(0.0, 0.2) * 0.5 / max(np.linalg.norm(t), 1e-12)
+        target = 0.5 + t
+        origin = 0.5 + radius * d
+        views.append(look_at(origin, target, w, h, rng.uniform(40.0, 90.0), **kw))
+    return views
+
+
 @dataclass
 class TraceResult:
     hit_index: np.ndarray
@@ -382,6 +409,19 @@ class Tracer:
         fn = self._lib.svo_trace_batch_graph if graph else self._lib.svo_trace_batch
         self._req_cap = max(i.MaxChildRequestId for i in inputs)
         _check("RunWavefrontDevice", fn(self._ctx, c_in, len(inputs), c_out))
+
+    def autotune(self, inputs, outputs, repeats: int = 3):
+        """Picks the fastest launch configuration for this view set (device outputs,
+        as for trace_device); returns (config dict, milliseconds)."""
+        c_in = (TraceInputC * len(inputs))(*[i.to_c() for i in inputs])
+        c_out = (TraceOutputC * len(inputs))(*[TraceOutputC(o[0] or None, o[1] or None, o[2] or None, o[3] or None, 1, 0)
+                                               for o in outputs])
+        best = TraceConfigC()
+        ms = C.c_float()
+        self._req_cap = max(i.MaxChildRequestId for i in inputs)
+        _check("Autotune", self._lib.svo_autotune(self._ctx, c_in, len(inputs), c_out, repeats, C.byref(best),
+                                                  C.byref(ms)))
+        return {n: getattr(best, n) for n, _ in TraceConfigC._fields_ if not n.startswith("_")}, ms.value
 
     def stats(self) -> dict:
         s = TraceStatsC()

@@ -166,6 +166,43 @@ def test_launch_shapes_do_not_change_results(tracer, cfg):
     assert_same(got, po.trace_view(tree, cam))
 
 
+def test_mixed_views_batched_graph_equals_plain_launches(tracer):
+    """The 64 mixed-resolution views traced in one (graph-replayed, autotuned) launch
+    give the same per-view results as 64 plain launches; a few views against the oracle."""
+    torch = pytest.importorskip("torch")
+    tree = st.TreeBuilder(st.SCENE_TERRAIN, seed=5).BuildTree(4, 10)
+    views = st.mixed_views(seed=4, Tick=3)
+    tracer.upload(tree)
+    sizes = [v.ScreenSize[0] * v.ScreenSize[1] for v in views]
+    dev_outs = []
+    keep = []
+    for n in sizes:
+        idx = torch.empty(n, dtype=torch.int32, device="cuda")
+        dep = torch.empty(n, dtype=torch.uint8, device="cuda")
+        tt = torch.empty(n, dtype=torch.float32, device="cuda")
+        rgba = torch.empty(4 * n, dtype=torch.float32, device="cuda")
+        keep.append((idx, dep, tt, rgba))
+        dev_outs.append((idx.data_ptr(), dep.data_ptr(), tt.data_ptr(), rgba.data_ptr()))
+    cfg, ms = tracer.autotune(views, dev_outs, repeats=1)
+    assert cfg["block_size"] in (64, 128, 256) and ms > 0
+    tracer.trace_device(views, dev_outs, graph=True)
+    tracer.trace_device(views, dev_outs, graph=True)  # replay
+    torch.cuda.synchronize()
+    batched = [tuple(x.cpu() for x in k) for k in keep]
+    tracer.set_config(block_size=256, ray_chunk=1, cadence=16)
+    for v, o in zip(views, dev_outs):
+        tracer.trace_device([v], [o])
+    torch.cuda.synchronize()
+    for b, k in zip(batched, keep):
+        for x, y in zip(b, k):
+            assert torch.equal(x, y.cpu())
+    small = sorted(range(len(views)), key=lambda i: sizes[i])[:3]
+    for i in small:
+        want = po.trace_view(tree, views[i])
+        assert np.array_equal(batched[i][0].numpy().view(np.uint32), want["hit_index"])
+        assert np.array_equal(batched[i][3].numpy().reshape(-1, 4), want["rgba"])
+
+
 def test_full_size_terrain_1080p(tracer):
     """The headline workload: 1920x1080 over the depth-11 terrain (~48M nodes),
     compared pixel for pixel with the oracle (OpenMP over all host cores)."""
