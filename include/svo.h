@@ -238,6 +238,62 @@ SVO_API svo_status svo_read_ray_counts(void *ctx, uint32_t *v_block, uint32_t *v
 /* Child requests of the last trace. *n = requests raised (may exceed cap). */
 SVO_API svo_status svo_read_child_requests(void *ctx, svo_child_request *out, uint32_t cap, uint32_t *n);
 
+/* ---- tree updates: usage, block GC, grafting, pruning --------------------- */
+
+/* Groups are the 8-node block groups (one svo_usage each). Dense-real groups
+ * (the level-B+2 nodes under air+geometry level-(B+1) cells) are never
+ * allocated or freed; every other group below the budget is allocatable. */
+typedef struct svo_gc_report {
+  uint64_t pruned; /* stale groups detached from their parent this call */
+  uint64_t freed;  /* groups that became free (unreachable) this call */
+  uint64_t free;   /* allocatable groups free after the call (the free list) */
+} svo_gc_report;
+
+typedef struct svo_graft_report {
+  uint32_t applied;  /* records grafted */
+  uint32_t skipped;  /* records skipped: bad payload range, missing target, or not enough free groups */
+  uint64_t claimed;  /* groups claimed from the free list */
+  uint64_t free_left;
+} svo_graft_report;
+
+typedef struct svo_prune_report {
+  uint64_t freed;    /* groups freed because CullChild orphaned them */
+  uint32_t requests; /* child requests raised by Location walks that met a missing child */
+  uint32_t _pad;
+} svo_prune_report;
+
+/* Streaming usage initialisation (no reference counterpart; the reference's
+ * rule is svo_init_usage): dense-real groups become inviolate, every group
+ * reachable through Child pointers gets {tick, parent node}, all others are
+ * free. */
+SVO_API svo_status svo_init_usage_tree(void *ctx, uint16_t tick);
+/* Block GC (the claim loop of graft, wavefront.cl:1279-1305): groups whose
+ * tick is older than in->offset ticks (wrapping tick space 1..65533, now =
+ * in->tick) are detached from their parent; every allocated group that is no
+ * longer reachable is freed; the free groups form an ascending free list that
+ * svo_graft consumes. */
+SVO_API svo_status svo_gc(void *ctx, const svo_update_input *in, svo_gc_report *report);
+/* The pruned, freed and free-list group indices of the last svo_gc (or of the
+ * sweep of the last svo_prune / svo_graft). */
+SVO_API svo_status svo_read_gc_lists(void *ctx, uint32_t *pruned, size_t cap_pruned, uint32_t *freed,
+                                     size_t cap_freed, uint32_t *free_list, size_t cap_free);
+/* Grafting (wavefront.cl:1306-1350, Grafting :38-43): records in order claim
+ * graft_total_size groups from the free list; payload group k (blocks
+ * graft_data_address + 8k .. +7, children given as payload block indices)
+ * becomes claimed group k; the target node (graft_address, or the Location
+ * graft_address of `locations` walked to `depth` when depth != 255) points at
+ * the first claimed group. Targets must be distinct. */
+SVO_API svo_status svo_graft(void *ctx, const svo_update_input *in, const svo_grafting *records, uint32_t n_records,
+                             const svo_block *payload, size_t n_payload, const uint64_t *locations,
+                             size_t n_locations, svo_graft_report *report);
+SVO_API svo_status svo_read_graft_claims(void *ctx, uint32_t *claimed, size_t cap);
+/* Pruning records (wavefront.cl:1215-1266, Pruning :24-36) applied in order;
+ * groups orphaned by CullChild are freed afterwards. Child requests of
+ * Location walks that meet a missing child go to the context's request queue. */
+SVO_API svo_status svo_prune(void *ctx, const svo_update_input *in, const svo_pruning *records, uint32_t n_records,
+                             const svo_block *surface, size_t n_surface, const uint64_t *locations,
+                             size_t n_locations, svo_prune_report *report);
+
 /* ---- tracing without allocation ------------------------------------------ */
 
 /* No counterpart in the reference. For callers that cannot allocate device
@@ -281,6 +337,21 @@ SVO_API svo_status svo_tree_info(void *tree, uint8_t *base_depth, size_t *n_base
                                  uint32_t *block_count);
 SVO_API svo_status svo_tree_data(void *tree, const uint16_t **bases, const svo_block **blocks);
 SVO_API svo_status svo_tree_free(void *tree);
+
+/* A persistent scene: the tree builder and the graft payload source of the
+ * streaming workflow (the host-side procedural generator behind
+ * WorldManager.UpdateGrafting, SvoTracer.Window/WorldManager.cs:84-103).
+ * params->max_depth is the deepest node level the scene can produce. */
+SVO_API svo_status svo_scene_create(const svo_scene_params *params, void **scene);
+SVO_API svo_status svo_scene_build_tree(void *scene, uint8_t max_depth, void **tree);
+/* One Grafting record per distinct requesting node (ascending address): its
+ * children, and their children when a request asked for TreeSize 1, with
+ * payload-relative child indices; feed the result to svo_graft. */
+SVO_API svo_status svo_scene_graft_payload(void *scene, const svo_child_request *requests, size_t n, void **graft);
+SVO_API svo_status svo_graft_payload_data(void *graft, const svo_grafting **records, size_t *n_records,
+                                          const svo_block **payload, size_t *n_payload);
+SVO_API svo_status svo_graft_payload_free(void *graft);
+SVO_API svo_status svo_scene_free(void *scene);
 
 #ifdef __cplusplus
 } /* extern "C" */

@@ -19,13 +19,13 @@ import build_ref  # noqa: E402
 
 
 def build_oracle(cc: str = "gcc") -> str:
-    src = os.path.join(HERE, "svo_oracle.c")
+    srcs = [os.path.join(HERE, "svo_oracle.c"), os.path.join(HERE, "svo_tree_oracle.c")]
     hdr = os.path.join(HERE, "svo_oracle.h")
     api = os.path.join(os.path.dirname(HERE), "include", "svo.h")
-    if os.path.exists(ORACLE_LIB) and all(os.path.getmtime(ORACLE_LIB) >= os.path.getmtime(d) for d in (src, hdr, api)):
+    if os.path.exists(ORACLE_LIB) and all(os.path.getmtime(ORACLE_LIB) >= os.path.getmtime(d) for d in srcs + [hdr, api]):
         return ORACLE_LIB
-    cmd = [cc, "-std=gnu11", "-O2", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off", "-fno-fast-math",
-           src, "-o", ORACLE_LIB + ".tmp", "-lm"]
+    cmd = [cc, "-std=gnu11", "-O2", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off", "-fno-fast-math"] + srcs + [
+        "-o", ORACLE_LIB + ".tmp", "-lm"]
     subprocess.run(cmd, check=True)
     os.replace(ORACLE_LIB + ".tmp", ORACLE_LIB)
     return ORACLE_LIB

@@ -18,7 +18,8 @@ import build_oracle  # noqa: E402
 import build_ref  # noqa: E402
 
 sys.path.insert(0, os.path.join(os.path.dirname(HERE), "svo-tracer_gb300"))
-from svo_tracer import BLOCK_DTYPE, CHILD_REQUEST_DTYPE, USAGE_DTYPE, TraceInput  # noqa: E402
+from svo_tracer import (BLOCK_DTYPE, CHILD_REQUEST_DTYPE, GRAFTING_DTYPE, PRUNING_DTYPE, USAGE_DTYPE,  # noqa: E402
+                        TraceInput)
 
 _vp = C.c_void_p
 _oracle = None
@@ -56,6 +57,14 @@ def oracle_lib() -> C.CDLL:
         lib.oracle_trace_into_volume.argtypes = [_vp, _vp, _vp, C.c_float, _vp, _vp]
         lib.oracle_trace_into_volume.restype = C.c_int
         lib.oracle_init_usage.argtypes = [_vp, C.c_uint8, _vp, C.c_size_t]
+        lib.oracle_init_usage_tree.argtypes = [_vp, C.c_int, _vp, C.c_size_t, _vp, C.c_uint16]
+        lib.oracle_gc.argtypes = [_vp, C.c_int, _vp, C.c_size_t, _vp, C.c_uint16, C.c_uint32, _vp, _vp, _vp, _vp]
+        lib.oracle_graft.argtypes = [C.c_int, _vp, C.c_size_t, _vp, C.c_uint16, _vp, C.c_uint32, _vp, C.c_size_t, _vp,
+                                     C.c_size_t, _vp, C.c_uint64, _vp, _vp]
+        lib.oracle_graft.restype = C.c_uint64
+        lib.oracle_prune.argtypes = [_vp, C.c_size_t, C.c_int, _vp, C.c_size_t, _vp, C.c_uint16, _vp, C.c_uint32, _vp,
+                                     C.c_size_t, _vp, C.c_size_t, _vp, C.c_uint32, C.POINTER(C.c_uint32), _vp]
+        lib.oracle_prune.restype = C.c_uint64
         _oracle = lib
     return _oracle
 
@@ -179,3 +188,61 @@ def ref_trace_rows(tree, inp: TraceInput, row_begin: int, row_end: int, threads:
     if passes < 0:
         raise RuntimeError("reference harness ran out of passes")
     return hit
+
+
+class TreeState:
+    """The oracle's copy of a resident tree padded to a block budget (whole groups),
+    with its usage array: the state the tree-update oracle edits in place."""
+
+    def __init__(self, tree, budget_groups: int):
+        n = max(budget_groups, (len(tree.Blocks) + 7) // 8)
+        self.B = tree.BaseDepth
+        self.bases = np.ascontiguousarray(tree.BaseBlocks, np.uint16).copy()
+        self.blocks = np.zeros(n * 8, BLOCK_DTYPE)
+        self.blocks[: len(tree.Blocks)] = tree.Blocks
+        self.usage = np.zeros(n, USAGE_DTYPE)
+        self.n_groups = n
+
+    def init_usage_tree(self, tick):
+        oracle_lib().oracle_init_usage_tree(_p(self.bases), self.B, _p(self.blocks), self.n_groups, _p(self.usage),
+                                            tick)
+
+    def gc(self, tick, threshold):
+        n = self.n_groups
+        pruned, freed, free = np.zeros(n, np.uint32), np.zeros(n, np.uint32), np.zeros(n, np.uint32)
+        out = (C.c_uint64 * 3)()
+        oracle_lib().oracle_gc(_p(self.bases), self.B, _p(self.blocks), n, _p(self.usage), tick, threshold, _p(pruned),
+                               _p(freed), _p(free), out)
+        self.free_list = free[: out[2]].copy()
+        self.free_used = 0
+        return pruned[: out[0]], freed[: out[1]], self.free_list
+
+    def graft(self, tick, records, payload, locations=None):
+        rec = np.ascontiguousarray(records, GRAFTING_DTYPE)
+        pay = np.ascontiguousarray(payload, BLOCK_DTYPE)
+        loc = None if locations is None else np.ascontiguousarray(locations, np.uint64)
+        free = self.free_list[self.free_used:]
+        claimed = np.zeros(len(free), np.uint32)
+        applied = np.zeros(len(rec), np.uint8)
+        q = oracle_lib().oracle_graft(self.B, _p(self.blocks), self.n_groups, _p(self.usage), tick, _p(rec), len(rec),
+                                      _p(pay), len(pay), _p(loc), 0 if loc is None else loc.size, _p(free), len(free),
+                                      _p(claimed), _p(applied))
+        self.free_used += int(q)
+        return claimed[: int(q)], applied
+
+    def prune(self, tick, records, surface=None, locations=None, req_cap=4096):
+        rec = np.ascontiguousarray(records, PRUNING_DTYPE)
+        sur = None if surface is None else np.ascontiguousarray(surface, BLOCK_DTYPE)
+        loc = None if locations is None else np.ascontiguousarray(locations, np.uint64)
+        req = np.zeros(req_cap, CHILD_REQUEST_DTYPE)
+        nreq = C.c_uint32(0)
+        freed = np.zeros(self.n_groups, np.uint32)
+        nf = oracle_lib().oracle_prune(_p(self.bases), len(self.bases), self.B, _p(self.blocks), self.n_groups,
+                                       _p(self.usage), tick, _p(rec), len(rec), _p(sur), 0 if sur is None else len(sur),
+                                       _p(loc), 0 if loc is None else loc.size, _p(req), req_cap, C.byref(nreq),
+                                       _p(freed))
+        return freed[: int(nf)], req[: min(nreq.value, req_cap)]
+
+    def as_octree(self):
+        from svo_tracer import Octree
+        return Octree(self.B, len(self.blocks), self.bases, self.blocks)

@@ -1,0 +1,152 @@
+// Context of libsvo (one GPU, one stream) and device-buffer helpers, shared by
+// the translation units of the C ABI.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <string>
+#include <vector>
+
+#include "svo_internal.h"
+
+namespace svo {
+
+#define SVO_CUDA(call, what)                                                                  \
+  do {                                                                                        \
+    cudaError_t e_ = (call);                                                                  \
+    if (e_ != cudaSuccess) return fail(SVO_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+template <class T>
+struct DevBuf {
+  T *p = nullptr;
+  size_t n = 0;
+  cudaError_t reserve(size_t want) {
+    if (want <= n && p) return cudaSuccess;
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+    cudaError_t e = cudaMalloc(&p, std::max<size_t>(want, 1) * sizeof(T));
+    if (e == cudaSuccess) n = want;
+    return e;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+};
+
+template <class T>
+struct PinBuf {
+  T *p = nullptr;
+  size_t n = 0;
+  cudaError_t reserve(size_t want) {
+    if (want <= n && p) return cudaSuccess;
+    if (p) cudaFreeHost(p);
+    p = nullptr;
+    n = 0;
+    cudaError_t e = cudaMallocHost(&p, std::max<size_t>(want, 1) * sizeof(T));
+    if (e == cudaSuccess) n = want;
+    return e;
+  }
+  void release() {
+    if (p) cudaFreeHost(p);
+    p = nullptr;
+    n = 0;
+  }
+};
+
+struct Context {
+  int device = 0;
+  int sm_count = 0;
+  cudaStream_t own_stream = nullptr;
+  cudaStream_t stream = nullptr;
+  // resident tree
+  bool has_tree = false;
+  uint8_t base_depth = 0;
+  size_t n_bases = 0, n_blocks = 0, budget = 0, n_groups = 0;
+  int tree_depth = 0;
+  DevBuf<uint16_t> bases;
+  DevBuf<svo_block> blocks;
+  DevBuf<svo_usage> usage;
+  // trace scratch
+  DevBuf<uint32_t> counters;  // [0] ray queue head, [1] child requests raised, [4..9] kernel error record
+  DevBuf<unsigned long long> stats;
+  DevBuf<svo_child_request> requests;
+  DevBuf<ViewParams> views;
+  DevBuf<float> tables;
+  DevBuf<uint32_t> ray_v_block, ray_v_base;
+  PinBuf<ViewParams> h_views;
+  PinBuf<float> h_tables;
+  PinBuf<uint32_t> h_counters;
+  // library-owned outputs for host-memory results
+  DevBuf<uint32_t> o_index;
+  DevBuf<uint8_t> o_depth;
+  DevBuf<float> o_t;
+  DevBuf<float> o_rgba;
+  uint32_t request_cap = 0;
+  uint64_t last_rays = 0;
+  bool last_stats_valid = false;
+  svo_trace_config cfg{};
+  // recorded after the view/table uploads: the pinned staging may be rewritten once it fired
+  cudaEvent_t staged = nullptr;
+  // tree updates: reachability marks, stale/freed flags, free list
+  DevBuf<uint32_t> reach, parent_min, frontier_a, frontier_b, scan_tmp;
+  DevBuf<uint8_t> flags;
+  DevBuf<uint32_t> free_list, pruned_list, freed_list, claimed_list;
+  DevBuf<svo_block> payload;
+  DevBuf<svo_grafting> graft_records;
+  DevBuf<uint32_t> graft_jobs, graft_targets;
+  DevBuf<svo_pruning> prune_records;
+  DevBuf<uint64_t> locations;
+  uint64_t n_free = 0, free_used = 0, n_pruned = 0, n_freed = 0, n_claimed = 0;
+  bool free_valid = false;
+  // graph cache for svo_trace_batch_graph
+  cudaGraphExec_t graph_exec = nullptr;
+  std::vector<uint32_t> graph_key;
+
+  ~Context() {
+    if (device >= 0) cudaSetDevice(device);
+    if (graph_exec) cudaGraphExecDestroy(graph_exec);
+    if (staged) cudaEventDestroy(staged);
+    bases.release();
+    blocks.release();
+    usage.release();
+    counters.release();
+    stats.release();
+    requests.release();
+    views.release();
+    tables.release();
+    ray_v_block.release();
+    ray_v_base.release();
+    h_views.release();
+    h_tables.release();
+    h_counters.release();
+    o_index.release();
+    o_depth.release();
+    o_t.release();
+    o_rgba.release();
+    reach.release();
+    parent_min.release();
+    frontier_a.release();
+    frontier_b.release();
+    scan_tmp.release();
+    flags.release();
+    free_list.release();
+    pruned_list.release();
+    freed_list.release();
+    claimed_list.release();
+    payload.release();
+    graft_records.release();
+    graft_jobs.release();
+    graft_targets.release();
+    prune_records.release();
+    locations.release();
+    if (own_stream) cudaStreamDestroy(own_stream);
+  }
+};
+
+
+}  // namespace svo

@@ -346,19 +346,41 @@ struct TreeHost {
   std::vector<svo_block> blocks;
 };
 
-svo_status build_tree(const svo_scene_params &p, TreeHost &tree) {
+// A scene whose leaf grid lies one level below node level `scene_depth`.
+struct SceneHost {
+  std::unique_ptr<Scene> scene;
+  int scene_depth = 0;
+  int threads = 1;
+  uint8_t base_depth = 0;
+  uint64_t max_size = 0;
+};
+
+svo_status make_scene(const svo_scene_params &p, SceneHost &out) {
   const int B = p.base_depth, D = p.max_depth;
   if (B < 1 || B > 6) return fail(SVO_ERR_INVALID_ARGUMENT, "svo_tree_build: base_depth must be 1..6");
   if (D < B + 2 || D > 16) return fail(SVO_ERR_INVALID_ARGUMENT, "svo_tree_build: max_depth must be base_depth+2..16");
-  int threads = p.threads > 0 ? p.threads : (int)std::max(1u, std::thread::hardware_concurrency());
-  const int leaf = D + 1;
-  std::unique_ptr<Scene> sc;
+  out.threads = p.threads > 0 ? p.threads : (int)std::max(1u, std::thread::hardware_concurrency());
+  out.scene_depth = D;
+  out.base_depth = (uint8_t)B;
+  out.max_size = p.max_size;
   if (p.kind == SVO_SCENE_SPHERE)
-    sc.reset(new SphereScene(p.seed, leaf));
+    out.scene.reset(new SphereScene(p.seed, D + 1));
   else if (p.kind == SVO_SCENE_TERRAIN)
-    sc.reset(new TerrainScene(p.seed, leaf, threads));
+    out.scene.reset(new TerrainScene(p.seed, D + 1, out.threads));
   else
     return fail(SVO_ERR_INVALID_ARGUMENT, "svo_tree_build: unknown scene kind");
+  return SVO_OK;
+}
+
+// TreeBuilder.BuildTree with nodes down to level D (<= the scene's depth).
+svo_status build_tree_with(const SceneHost &scene, int D, TreeHost &tree) {
+  const int B = scene.base_depth;
+  if (D < B + 2 || D > scene.scene_depth)
+    return fail(SVO_ERR_INVALID_ARGUMENT, "svo_scene_build_tree: max_depth must be base_depth+2..the scene's depth");
+  const int threads = scene.threads;
+  const Scene *sc = scene.scene.get();
+  svo_scene_params p{};
+  p.max_size = scene.max_size;
 
   uint64_t max_size = p.max_size ? p.max_size : 0xFFFFFFFFull / 64;
   const uint64_t dense = 1ull << (3 * (B + 2));
@@ -419,7 +441,7 @@ svo_status build_tree(const svo_scene_params &p, TreeHost &tree) {
       }
   std::vector<Subtree> subs(roots.size());
   TerrainScene::parallel_for(threads, (uint32_t)roots.size(), [&](uint32_t r) {
-    uint32_t a = roots[r];
+    uint32_t a = roots[r];  // level-(B+2) node
     uint32_t x = 0, y = 0, z = 0;
     for (int i = 0; i < B + 2; i++) {
       x |= ((a >> (3 * i)) & 1u) << i;
@@ -477,8 +499,87 @@ svo_status build_tree(const svo_scene_params &p, TreeHost &tree) {
   return SVO_OK;
 }
 
+svo_status build_tree(const svo_scene_params &p, TreeHost &tree) {
+  SceneHost scene;
+  svo_status st = make_scene(p, scene);
+  if (st) return st;
+  return build_tree_with(scene, p.max_depth, tree);
+}
+
+// Graft payloads for child requests: one record per distinct requesting node
+// (ascending node address, largest TreeSize of its requests); the payload is
+// the node's children (and, for TreeSize 1, their children), built like
+// BuildBlocks with local pre-order groups and children given as payload block
+// indices (what WorldManager.UpdateGrafting hands to the graft kernel,
+// SvoTracer.Window/WorldManager.cs:84-103).
+struct GraftHost {
+  std::vector<svo_grafting> records;
+  std::vector<svo_block> payload;
+};
+
+svo_status graft_payload(const SceneHost &scene, const svo_child_request *req, size_t n, GraftHost &out) {
+  std::vector<std::pair<uint32_t, size_t>> order;
+  order.reserve(n);
+  for (size_t i = 0; i < n; i++) order.push_back({req[i].address, i});
+  std::sort(order.begin(), order.end());
+  struct Job {
+    uint32_t address;
+    int depth;
+    int limit;
+    uint32_t x, y, z;
+  };
+  std::vector<Job> jobs;
+  for (size_t k = 0; k < order.size();) {
+    size_t e = k;
+    uint8_t ts = 0;
+    while (e < order.size() && order[e].first == order[k].first) ts = std::max(ts, req[order[e++].second].tree_size);
+    const svo_child_request &r = req[order[k].second];
+    int d = r.depth;
+    if (d >= scene.base_depth + 2 && d < scene.scene_depth) {
+      Job j;
+      j.address = r.address;
+      j.depth = d;
+      j.limit = std::min(scene.scene_depth, d + 1 + (ts ? 1 : 0));
+      j.x = (uint32_t)(r.location[0] >> (64 - d));
+      j.y = (uint32_t)(r.location[1] >> (64 - d));
+      j.z = (uint32_t)(r.location[2] >> (64 - d));
+      jobs.push_back(j);
+    }
+    k = e;
+  }
+  std::vector<Subtree> subs(jobs.size());
+  TerrainScene::parallel_for(scene.threads, (uint32_t)jobs.size(), [&](uint32_t i) {
+    const Job &j = jobs[i];
+    subs[i].blocks.resize(8);
+    build_children(*scene.scene, subs[i], 0, j.depth + 1, j.x, j.y, j.z, j.limit);
+  });
+  size_t total = 0;
+  for (auto &st : subs) total += st.blocks.size();
+  out.payload.resize(total);
+  out.records.resize(jobs.size());
+  size_t at = 0;
+  for (size_t i = 0; i < jobs.size(); i++) {
+    const Subtree &st = subs[i];
+    svo_grafting g{};
+    g.graft_data_address = (uint32_t)at;
+    g.graft_total_size = (uint32_t)(st.blocks.size() / 8);
+    g.depth = 255;
+    g.graft_address = jobs[i].address;
+    out.records[i] = g;
+    for (size_t b = 0; b < st.blocks.size(); b++) {
+      svo_block blk = st.blocks[b];
+      if (blk.child != SVO_NO_CHILD) blk.child = (uint32_t)at + 8u * blk.child;
+      out.payload[at + b] = blk;
+    }
+    at += st.blocks.size();
+  }
+  return SVO_OK;
+}
+
 }  // namespace svo
 
+using svo::GraftHost;
+using svo::SceneHost;
 using svo::TreeHost;
 
 extern "C" {
@@ -519,6 +620,66 @@ SVO_API svo_status svo_tree_data(void *tree, const uint16_t **bases, const svo_b
 
 SVO_API svo_status svo_tree_free(void *tree) {
   delete static_cast<TreeHost *>(tree);
+  return SVO_OK;
+}
+
+SVO_API svo_status svo_scene_create(const svo_scene_params *params, void **scene) {
+  if (!params || !scene) return svo::fail(SVO_ERR_INVALID_ARGUMENT, "svo_scene_create: null argument");
+  try {
+    std::unique_ptr<SceneHost> s(new SceneHost);
+    svo_status st = svo::make_scene(*params, *s);
+    if (st) return st;
+    *scene = s.release();
+    return SVO_OK;
+  } catch (const std::bad_alloc &) {
+    return svo::fail(SVO_ERR_OUT_OF_MEMORY, "svo_scene_create: out of host memory");
+  }
+}
+
+SVO_API svo_status svo_scene_build_tree(void *scene, uint8_t max_depth, void **tree) {
+  if (!scene || !tree) return svo::fail(SVO_ERR_INVALID_ARGUMENT, "svo_scene_build_tree: null argument");
+  try {
+    std::unique_ptr<TreeHost> t(new TreeHost);
+    svo_status st = svo::build_tree_with(*static_cast<SceneHost *>(scene), max_depth, *t);
+    if (st) return st;
+    *tree = t.release();
+    return SVO_OK;
+  } catch (const std::bad_alloc &) {
+    return svo::fail(SVO_ERR_OUT_OF_MEMORY, "svo_scene_build_tree: out of host memory");
+  }
+}
+
+SVO_API svo_status svo_scene_graft_payload(void *scene, const svo_child_request *requests, size_t n, void **graft) {
+  if (!scene || !graft || (n && !requests)) return svo::fail(SVO_ERR_INVALID_ARGUMENT, "svo_scene_graft_payload: null");
+  try {
+    std::unique_ptr<GraftHost> g(new GraftHost);
+    svo_status st = svo::graft_payload(*static_cast<SceneHost *>(scene), requests, n, *g);
+    if (st) return st;
+    *graft = g.release();
+    return SVO_OK;
+  } catch (const std::bad_alloc &) {
+    return svo::fail(SVO_ERR_OUT_OF_MEMORY, "svo_scene_graft_payload: out of host memory");
+  }
+}
+
+SVO_API svo_status svo_graft_payload_data(void *graft, const svo_grafting **records, size_t *n_records,
+                                          const svo_block **payload, size_t *n_payload) {
+  if (!graft) return svo::fail(SVO_ERR_INVALID_ARGUMENT, "svo_graft_payload_data: null");
+  auto *g = static_cast<GraftHost *>(graft);
+  if (records) *records = g->records.data();
+  if (n_records) *n_records = g->records.size();
+  if (payload) *payload = g->payload.data();
+  if (n_payload) *n_payload = g->payload.size();
+  return SVO_OK;
+}
+
+SVO_API svo_status svo_graft_payload_free(void *graft) {
+  delete static_cast<GraftHost *>(graft);
+  return SVO_OK;
+}
+
+SVO_API svo_status svo_scene_free(void *scene) {
+  delete static_cast<SceneHost *>(scene);
   return SVO_OK;
 }
 

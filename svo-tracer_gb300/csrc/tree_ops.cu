@@ -1,0 +1,642 @@
+// Tree updates on the device: usage initialisation, block GC, grafting and
+// pruning (the reference's prune/graft kernels, SvoTracer.Kernel/wavefront.cl:
+// 1097-1350, restated as a specification the oracle shares):
+//
+//  * groups: 8-node block groups, one svo_usage each (Tick 0 free, 1..65533
+//    last frame used, 65534 multi-parent, 65535 inviolate);
+//  * dense-real groups: the level-(B+2) groups under air+geometry
+//    level-(B+1) cells, addressed by baseLocation; never allocated or freed;
+//  * reachable: an allocatable group whose first node is the Child of a node
+//    of a dense-real or reachable group.
+//
+// GC detaches stale groups (age > threshold in the wrapping tick space) from
+// their parent node, then frees every allocated group that is no longer
+// reachable, and compacts the free groups into an ascending free list. Grafts
+// claim groups from that list in record order. Pruning applies the reference's
+// Pruning records in order and frees the groups CullChild orphaned. The
+// reference serialises its dereferencing through a global spin lock
+// (wavefront.cl:226-231); here reachability is recomputed breadth-first with
+// one pass per tree level, so no thread ever waits on another.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <memory>
+#include <new>
+#include <set>
+#include <string>
+#include <vector>
+
+#include "context.h"
+
+namespace svo {
+namespace {
+
+constexpr uint32_t kNone = 0xFFFFFFFFu;
+
+struct TreeView {
+  const uint16_t *bases;
+  svo_block *blocks;
+  svo_usage *usage;
+  uint32_t n_groups;
+  uint32_t base_start;    // powSum(B-1): first level-B base chunk
+  uint32_t dense_groups;  // 8^(B+1)
+  int32_t base_depth;
+};
+
+__device__ __forceinline__ bool dense_real(const TreeView &t, uint32_t g) {
+  if (g >= t.dense_groups) return false;
+  uint16_t chunk = t.bases[t.base_start + (g >> 3)];
+  return ((chunk >> ((g & 7) * 2)) & 3) == 3;
+}
+
+__device__ __forceinline__ uint32_t tick_age(uint32_t t, uint32_t now) {
+  return now >= t ? now - t : now + 65533u - t;
+}
+
+__global__ void k_reach_seed(TreeView t, uint32_t *reach, uint32_t *parent_min, uint32_t *frontier,
+                             uint32_t *count) {
+  for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < t.n_groups; g += gridDim.x * blockDim.x) {
+    reach[g] = 0;
+    parent_min[g] = kNone;
+    if (dense_real(t, g)) frontier[atomicAdd(count, 1u)] = g;
+  }
+}
+
+// One breadth-first level: every node of every frontier group marks its child group.
+__global__ void k_reach_expand(TreeView t, const uint32_t *frontier, const uint32_t *n_in, uint32_t *next,
+                               uint32_t *n_out, uint32_t *reach, uint32_t *parent_min) {
+  uint64_t total = 8ull * *n_in;
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < total; i += (uint64_t)gridDim.x * blockDim.x) {
+    uint32_t node = frontier[i >> 3] * 8u + (uint32_t)(i & 7);
+    uint32_t c = t.blocks[node].child;
+    if (c == kNone || (c & 7u)) continue;
+    uint32_t h = c >> 3;
+    if (h >= t.n_groups || dense_real(t, h)) continue;
+    atomicMin(parent_min + h, node);
+    if (atomicExch(reach + h, 1u) == 0u) next[atomicAdd(n_out, 1u)] = h;
+  }
+}
+
+__global__ void k_init_usage_tree(TreeView t, const uint32_t *reach, const uint32_t *parent_min, uint16_t tick) {
+  for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < t.n_groups; g += gridDim.x * blockDim.x) {
+    svo_usage u;
+    u._pad = 0;
+    if (dense_real(t, g)) {
+      u.tick = 65535;
+      u.parent = kNone;
+    } else if (reach[g]) {
+      u.tick = tick;
+      u.parent = parent_min[g];
+    } else {
+      u.tick = 0;
+      u.parent = kNone;
+    }
+    t.usage[g] = u;
+  }
+}
+
+// Stale groups: flag and detach from the parent node that still points at them.
+__global__ void k_stale_detach(TreeView t, uint16_t now, uint32_t threshold, uint8_t *flags) {
+  for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < t.n_groups; g += gridDim.x * blockDim.x) {
+    uint8_t f = 0;
+    uint32_t tk = t.usage[g].tick;
+    if (tk >= 1 && tk <= 65533 && !dense_real(t, g) && tick_age(tk, now) > threshold) {
+      f = 1;
+      uint32_t p = t.usage[g].parent;
+      if (p != kNone && p < t.n_groups * 8u && t.blocks[p].child == g * 8u) t.blocks[p].child = kNone;
+    }
+    flags[g] = f;
+  }
+}
+
+// Frees allocated groups that are no longer reachable; flags them.
+__global__ void k_sweep(TreeView t, const uint32_t *reach, uint8_t *flags) {
+  for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < t.n_groups; g += gridDim.x * blockDim.x) {
+    uint8_t f = 0;
+    uint32_t tk = t.usage[g].tick;
+    if (tk >= 1 && tk <= 65533 && !reach[g] && !dense_real(t, g)) {
+      svo_usage u;
+      u.tick = 0;
+      u._pad = 0;
+      u.parent = kNone;
+      t.usage[g] = u;
+      f = 1;
+    }
+    flags[g] = f;
+  }
+}
+
+__global__ void k_free_flags(TreeView t, uint8_t *flags) {
+  for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < t.n_groups; g += gridDim.x * blockDim.x)
+    flags[g] = (t.usage[g].tick == 0 && !dense_real(t, g)) ? 1 : 0;
+}
+
+// ---- stream compaction of a flag array into the ascending list of indices ----
+constexpr int kScanBlock = 1024;
+
+__global__ void k_count(const uint8_t *flags, uint32_t n, uint32_t *block_counts) {
+  uint32_t i = blockIdx.x * kScanBlock + threadIdx.x;
+  int c = __syncthreads_count(i < n && flags[i]);
+  if (threadIdx.x == 0) block_counts[blockIdx.x] = (uint32_t)c;
+}
+
+// Exclusive scan of n block counts (in place) by one CTA; writes the total.
+__global__ void k_scan_counts(uint32_t *counts, uint32_t n, uint32_t *total) {
+  __shared__ uint32_t part[kScanBlock];
+  uint32_t per = (n + kScanBlock - 1) / kScanBlock;
+  uint32_t b = threadIdx.x * per, e = min(n, b + per), s = 0;
+  for (uint32_t i = b; i < e; i++) s += counts[i];
+  part[threadIdx.x] = s;
+  __syncthreads();
+  for (int off = 1; off < kScanBlock; off <<= 1) {
+    uint32_t v = threadIdx.x >= (uint32_t)off ? part[threadIdx.x - off] : 0;
+    __syncthreads();
+    part[threadIdx.x] += v;
+    __syncthreads();
+  }
+  uint32_t run = part[threadIdx.x] - s;  // exclusive prefix of this thread's range
+  for (uint32_t i = b; i < e; i++) {
+    uint32_t c = counts[i];
+    counts[i] = run;
+    run += c;
+  }
+  if (threadIdx.x == kScanBlock - 1) *total = part[kScanBlock - 1];
+}
+
+__global__ void k_scatter(const uint8_t *flags, uint32_t n, const uint32_t *offsets, uint32_t *out) {
+  __shared__ uint32_t warp_base[kScanBlock / 32];
+  uint32_t i = blockIdx.x * kScanBlock + threadIdx.x;
+  bool f = i < n && flags[i];
+  unsigned m = __ballot_sync(0xffffffffu, f);
+  int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0) warp_base[warp] = __popc(m);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    uint32_t run = 0;
+    for (int w = 0; w < kScanBlock / 32; w++) {
+      uint32_t c = warp_base[w];
+      warp_base[w] = run;
+      run += c;
+    }
+  }
+  __syncthreads();
+  if (f) out[offsets[blockIdx.x] + warp_base[warp] + __popc(m & ((1u << lane) - 1u))] = i;
+}
+
+// ---- grafting ------------------------------------------------------------------
+struct GraftJob {
+  uint32_t payload_block;  // first payload block of this group
+  uint32_t record;
+  uint32_t k;              // group index within the record's subtree
+};
+
+struct GraftRec {
+  uint32_t P, G, q, target;  // payload block, groups, first free-list slot, target node
+};
+
+__global__ void k_graft_usage(TreeView t, const GraftJob *jobs, uint32_t n_jobs, const GraftRec *recs,
+                              const uint32_t *free_list, uint16_t now) {
+  for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n_jobs; j += gridDim.x * blockDim.x) {
+    uint32_t g = free_list[recs[jobs[j].record].q + jobs[j].k];
+    svo_usage u;
+    u.tick = now;
+    u._pad = 0;
+    u.parent = kNone;
+    t.usage[g] = u;
+  }
+}
+
+__global__ void k_graft_nodes(TreeView t, const GraftJob *jobs, uint32_t n_jobs, const GraftRec *recs,
+                              const uint32_t *free_list, const svo_block *payload) {
+  for (uint64_t x = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; x < 8ull * n_jobs;
+       x += (uint64_t)gridDim.x * blockDim.x) {
+    const GraftJob jb = jobs[x >> 3];
+    const GraftRec r = recs[jb.record];
+    uint32_t i = (uint32_t)(x & 7);
+    svo_block b = payload[jb.payload_block + i];
+    uint32_t node = free_list[r.q + jb.k] * 8u + i;
+    uint32_t c = b.child;
+    if (c != kNone) {
+      uint32_t rel = c - r.P;
+      if (c < r.P || (rel & 7u) || rel / 8u >= r.G) {
+        b.child = kNone;
+      } else {
+        uint32_t h = free_list[r.q + rel / 8u];
+        b.child = h * 8u;
+        atomicMin(&t.usage[h].parent, node);
+      }
+    }
+    t.blocks[node] = b;
+  }
+}
+
+__global__ void k_graft_link(TreeView t, const GraftRec *recs, uint32_t n, const uint32_t *free_list) {
+  for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
+    uint32_t g = free_list[recs[r].q];
+    t.usage[g].parent = recs[r].target;
+    t.blocks[recs[r].target].child = g * 8u;
+  }
+}
+
+__device__ __forceinline__ uint32_t loc_octant(const uint64_t *loc, int d) {
+  int s = 63 - d;
+  return (uint32_t)(((loc[0] >> s) & 1) | (((loc[1] >> s) & 1) << 1) | (((loc[2] >> s) & 1) << 2));
+}
+
+// Location walk of getBlockAddress for graft targets given by Location.
+__global__ void k_resolve_targets(TreeView t, const svo_grafting *rec, uint32_t n, const uint64_t *locs,
+                                  uint64_t n_locs, uint32_t *targets) {
+  for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
+    if (rec[r].depth == 255) {
+      targets[r] = rec[r].graft_address;
+      continue;
+    }
+    if ((uint64_t)rec[r].graft_address * 3 + 3 > n_locs) {
+      targets[r] = kNone;
+      continue;
+    }
+    const uint64_t *loc = locs + 3ull * rec[r].graft_address;
+    uint32_t a = 0;
+    for (int i = 0; i < t.base_depth + 2; i++) a = (a << 3) + loc_octant(loc, i);
+    for (int d = t.base_depth + 2; d < rec[r].depth; d++) {
+      if (a >= t.n_groups * 8u || t.blocks[a].child == kNone) {
+        a = kNone;
+        break;
+      }
+      a = t.blocks[a].child + loc_octant(loc, d);
+    }
+    targets[r] = a;
+  }
+}
+
+// ---- pruning: the records are applied in order by one thread -------------------
+__global__ void k_prune(TreeView t, uint16_t *bases_rw, uint32_t n_bases, uint16_t now, const svo_pruning *rec,
+                        uint32_t n_rec, const svo_block *surface, uint32_t n_surface, const uint64_t *locs,
+                        uint64_t n_locs, svo_child_request *req, uint32_t req_cap, uint32_t *n_req,
+                        uint32_t *culled) {
+  if (blockIdx.x != 0 || threadIdx.x != 0) return;
+  uint32_t n_blocks = t.n_groups * 8u;
+  for (uint32_t r = 0; r < n_rec; r++) {
+    const svo_pruning p = rec[r];
+    uint32_t address = p.address;
+    if ((p.properties >> 4) & 1) {  // BaseBlock
+      if (address < n_bases) bases_rw[address] = p.chunk;
+      continue;
+    }
+    if (p.depth != 255) {  // findAddress (wavefront.cl:1191-1211)
+      if ((uint64_t)address * 3 + 3 > n_locs) continue;
+      const uint64_t *loc = locs + 3ull * address;
+      uint32_t a = 0;
+      for (int i = 0; i < t.base_depth + 2; i++) a = (a << 3) + loc_octant(loc, i);
+      bool missing = false;
+      for (int i = t.base_depth + 2; i < p.depth; i++) {
+        if (a >= n_blocks) {
+          missing = true;
+          break;
+        }
+        if (t.usage[a >> 3].tick < 65534) t.usage[a >> 3].tick = now;
+        if (t.blocks[a].child == kNone) {
+          uint32_t slot = (*n_req)++;
+          if (req && slot < req_cap) {
+            svo_child_request q;
+            memset(&q, 0, sizeof(q));
+            q.address = a;
+            q.tick = now;
+            q.depth = (uint8_t)i;
+            q.location[0] = loc[0];
+            q.location[1] = loc[1];
+            q.location[2] = loc[2];
+            q.tree_size = (uint8_t)(p.depth - i);
+            req[slot] = q;
+          }
+          missing = true;
+          break;
+        }
+        a = t.blocks[a].child + loc_octant(loc, i);
+      }
+      if (missing) continue;
+      address = a;
+    } else {
+      if (address >= n_blocks || t.usage[address >> 3].tick == 0) continue;  // dereferenced
+      if (t.usage[address >> 3].tick < 65534) t.usage[address >> 3].tick = now;
+    }
+    if (address >= n_blocks) continue;
+    if (p.properties & 1) {  // CullChild
+      t.blocks[address].child = p.child_address;
+      *culled = 1;
+    }
+    uint32_t v = (p.properties >> 1) & 3;  // AlterViolability / MakeInviolate
+    if (v == 3)
+      t.usage[address >> 3].tick = 65535;
+    else if (v == 1)
+      t.usage[address >> 3].tick = now;
+    if ((p.properties >> 3) & 1) {  // UpdateChunk
+      if (p.colour_address < n_surface) t.blocks[address] = surface[p.colour_address];
+      t.blocks[address].chunk = p.chunk;
+    }
+  }
+}
+
+int grid_for(uint64_t n, int bs = 256) {
+  uint64_t g = (n + bs - 1) / bs;
+  return (int)std::max<uint64_t>(1, std::min<uint64_t>(g, 152ull * 64));
+}
+
+TreeView view_of(Context &c) {
+  TreeView t;
+  t.bases = c.bases.p;
+  t.blocks = c.blocks.p;
+  t.usage = c.usage.p;
+  t.n_groups = (uint32_t)c.n_groups;
+  uint32_t s = 0, p = 1;
+  for (int i = 1; i <= c.base_depth - 1; i++) s += (p *= 8);
+  t.base_start = s;
+  t.dense_groups = 1u << (3 * (c.base_depth + 1));
+  t.base_depth = c.base_depth;
+  return t;
+}
+
+svo_status ensure_tree_buffers(Context &c) {
+  size_t g = c.n_groups;
+  size_t nb = (g + kScanBlock - 1) / kScanBlock + 1;
+  if (c.reach.reserve(g) || c.parent_min.reserve(g) || c.frontier_a.reserve(g) || c.frontier_b.reserve(g) ||
+      c.flags.reserve(g) || c.scan_tmp.reserve(nb + 8) || c.free_list.reserve(g) || c.pruned_list.reserve(g) ||
+      c.freed_list.reserve(g))
+    return fail(SVO_ERR_OUT_OF_MEMORY, "tree update: device allocation failed");
+  return SVO_OK;
+}
+
+// Breadth-first reachability from the dense-real groups (one launch per level).
+svo_status reachability(Context &c, const TreeView &t) {
+  // scan_tmp = [block counts | ... | n-8, n-7: frontier sizes | n-6: compact total | n-5: prune flag]
+  uint32_t *cnt = c.scan_tmp.p + (c.scan_tmp.n - 8);
+  SVO_CUDA(cudaMemsetAsync(cnt, 0, 2 * sizeof(uint32_t), c.stream), "reachability: reset");
+  k_reach_seed<<<grid_for(t.n_groups), 256, 0, c.stream>>>(t, c.reach.p, c.parent_min.p, c.frontier_a.p, cnt);
+  uint32_t *in = c.frontier_a.p, *out = c.frontier_b.p;
+  uint32_t *n_in = cnt, *n_out = cnt + 1;
+  for (int level = 0; level < SVO_MAX_TREE_DEPTH + 2; level++) {
+    uint32_t n = 0;
+    SVO_CUDA(cudaMemcpyAsync(&n, n_in, 4, cudaMemcpyDeviceToHost, c.stream), "reachability: frontier size");
+    SVO_CUDA(cudaStreamSynchronize(c.stream), "reachability: synchronize");
+    if (n == 0) return SVO_OK;
+    SVO_CUDA(cudaMemsetAsync(n_out, 0, 4, c.stream), "reachability: reset");
+    k_reach_expand<<<grid_for(8ull * n), 256, 0, c.stream>>>(t, in, n_in, out, n_out, c.reach.p, c.parent_min.p);
+    SVO_CUDA(cudaGetLastError(), "reachability: expand");
+    std::swap(in, out);
+    std::swap(n_in, n_out);
+  }
+  return fail(SVO_ERR_INTERNAL, "reachability: tree deeper than SVO_MAX_TREE_DEPTH");
+}
+
+// Ascending indices of flags[i] != 0 into out; returns the count.
+svo_status compact(Context &c, const uint8_t *flags, uint32_t n, uint32_t *out, uint64_t *count) {
+  uint32_t nb = (n + kScanBlock - 1) / kScanBlock;
+  uint32_t *counts = c.scan_tmp.p, *total = c.scan_tmp.p + (c.scan_tmp.n - 6);
+  if (nb == 0) {
+    *count = 0;
+    return SVO_OK;
+  }
+  k_count<<<nb, kScanBlock, 0, c.stream>>>(flags, n, counts);
+  k_scan_counts<<<1, kScanBlock, 0, c.stream>>>(counts, nb, total);
+  k_scatter<<<nb, kScanBlock, 0, c.stream>>>(flags, n, counts, out);
+  SVO_CUDA(cudaGetLastError(), "compact");
+  uint32_t t = 0;
+  SVO_CUDA(cudaMemcpyAsync(&t, total, 4, cudaMemcpyDeviceToHost, c.stream), "compact: total");
+  SVO_CUDA(cudaStreamSynchronize(c.stream), "compact: synchronize");
+  *count = t;
+  return SVO_OK;
+}
+
+svo_status sweep_and_free_list(Context &c, const TreeView &t, uint64_t *n_freed) {
+  svo_status st = reachability(c, t);
+  if (st) return st;
+  k_sweep<<<grid_for(t.n_groups), 256, 0, c.stream>>>(t, c.reach.p, c.flags.p);
+  st = compact(c, c.flags.p, t.n_groups, c.freed_list.p, n_freed);
+  if (st) return st;
+  k_free_flags<<<grid_for(t.n_groups), 256, 0, c.stream>>>(t, c.flags.p);
+  st = compact(c, c.flags.p, t.n_groups, c.free_list.p, &c.n_free);
+  if (st) return st;
+  c.free_used = 0;
+  c.free_valid = true;
+  return SVO_OK;
+}
+
+}  // namespace
+}  // namespace svo
+
+using svo::Context;
+using svo::fail;
+
+#define CTX(ptr, fn)                                                                          \
+  if (!(ptr)) return fail(SVO_ERR_INVALID_ARGUMENT, std::string(fn) + ": null context"); \
+  Context &c = *static_cast<Context *>(ptr);                                                \
+  if (!c.has_tree) return fail(SVO_ERR_NO_TREE, std::string(fn) + ": no octree uploaded");   \
+  SVO_CUDA(cudaSetDevice(c.device), "cudaSetDevice")
+
+extern "C" {
+
+SVO_API svo_status svo_init_usage_tree(void *ctx, uint16_t tick) {
+  CTX(ctx, "svo_init_usage_tree");
+  if (tick < 1 || tick > 65533) return fail(SVO_ERR_INVALID_ARGUMENT, "svo_init_usage_tree: tick must be 1..65533");
+  svo_status st = svo::ensure_tree_buffers(c);
+  if (st) return st;
+  svo::TreeView t = svo::view_of(c);
+  st = svo::reachability(c, t);
+  if (st) return st;
+  svo::k_init_usage_tree<<<svo::grid_for(t.n_groups), 256, 0, c.stream>>>(t, c.reach.p, c.parent_min.p, tick);
+  SVO_CUDA(cudaGetLastError(), "svo_init_usage_tree");
+  SVO_CUDA(cudaStreamSynchronize(c.stream), "svo_init_usage_tree: synchronize");
+  c.free_valid = false;
+  return SVO_OK;
+}
+
+SVO_API svo_status svo_gc(void *ctx, const svo_update_input *in, svo_gc_report *report) {
+  CTX(ctx, "svo_gc");
+  if (!in) return fail(SVO_ERR_INVALID_ARGUMENT, "svo_gc: null input");
+  if (in->tick < 1 || in->tick > 65533) return fail(SVO_ERR_INVALID_ARGUMENT, "svo_gc: tick must be 1..65533");
+  svo_status st = svo::ensure_tree_buffers(c);
+  if (st) return st;
+  svo::TreeView t = svo::view_of(c);
+  svo::k_stale_detach<<<svo::grid_for(t.n_groups), 256, 0, c.stream>>>(t, in->tick, in->offset, c.flags.p);
+  st = svo::compact(c, c.flags.p, t.n_groups, c.pruned_list.p, &c.n_pruned);
+  if (st) return st;
+  st = svo::sweep_and_free_list(c, t, &c.n_freed);
+  if (st) return st;
+  if (report) {
+    report->pruned = c.n_pruned;
+    report->freed = c.n_freed;
+    report->free = c.n_free;
+  }
+  return SVO_OK;
+}
+
+SVO_API svo_status svo_read_gc_lists(void *ctx, uint32_t *pruned, size_t cap_pruned, uint32_t *freed,
+                                     size_t cap_freed, uint32_t *free_list, size_t cap_free) {
+  CTX(ctx, "svo_read_gc_lists");
+  SVO_CUDA(cudaStreamSynchronize(c.stream), "svo_read_gc_lists: synchronize");
+  size_t np = std::min<size_t>(cap_pruned, c.n_pruned), nf = std::min<size_t>(cap_freed, c.n_freed);
+  size_t nl = c.free_valid ? std::min<size_t>(cap_free, c.n_free - c.free_used) : 0;
+  if (pruned && np) SVO_CUDA(cudaMemcpy(pruned, c.pruned_list.p, np * 4, cudaMemcpyDeviceToHost), "svo_read_gc_lists");
+  if (freed && nf) SVO_CUDA(cudaMemcpy(freed, c.freed_list.p, nf * 4, cudaMemcpyDeviceToHost), "svo_read_gc_lists");
+  if (free_list && nl)
+    SVO_CUDA(cudaMemcpy(free_list, c.free_list.p + c.free_used, nl * 4, cudaMemcpyDeviceToHost), "svo_read_gc_lists");
+  return SVO_OK;
+}
+
+SVO_API svo_status svo_graft(void *ctx, const svo_update_input *in, const svo_grafting *records, uint32_t n_records,
+                             const svo_block *payload, size_t n_payload, const uint64_t *locations,
+                             size_t n_locations, svo_graft_report *report) {
+  CTX(ctx, "svo_graft");
+  if (!in || (n_records && !records) || (n_payload && !payload))
+    return fail(SVO_ERR_INVALID_ARGUMENT, "svo_graft: null argument");
+  if (in->tick < 1 || in->tick > 65533) return fail(SVO_ERR_INVALID_ARGUMENT, "svo_graft: tick must be 1..65533");
+  if (n_payload > 0xFFFFFFF0ull) return fail(SVO_ERR_INVALID_ARGUMENT, "svo_graft: payload too large");
+  svo_status st = svo::ensure_tree_buffers(c);
+  if (st) return st;
+  svo::TreeView t = svo::view_of(c);
+  if (!c.free_valid) {  // no GC ran since the tree changed: build the free list now
+    uint64_t dummy = 0;
+    st = svo::sweep_and_free_list(c, t, &dummy);
+    if (st) return st;
+    c.n_freed = dummy;
+  }
+  if (report) std::memset(report, 0, sizeof(*report));
+  if (n_records == 0) return SVO_OK;
+  // resolve targets on the device (Location walks), then assign free-list ranges in record order
+  if (c.graft_records.reserve(n_records) || c.graft_targets.reserve(n_records) ||
+      (n_locations && c.locations.reserve(n_locations)))
+    return fail(SVO_ERR_OUT_OF_MEMORY, "svo_graft: device allocation failed");
+  SVO_CUDA(cudaMemcpyAsync(c.graft_records.p, records, sizeof(svo_grafting) * n_records, cudaMemcpyHostToDevice,
+                           c.stream), "svo_graft: records");
+  if (n_locations)
+    SVO_CUDA(cudaMemcpyAsync(c.locations.p, locations, sizeof(uint64_t) * n_locations, cudaMemcpyHostToDevice,
+                             c.stream), "svo_graft: locations");
+  svo::k_resolve_targets<<<svo::grid_for(n_records), 256, 0, c.stream>>>(
+      t, c.graft_records.p, n_records, c.locations.p, n_locations, c.graft_targets.p);
+  std::vector<uint32_t> targets(n_records);
+  SVO_CUDA(cudaMemcpyAsync(targets.data(), c.graft_targets.p, 4ull * n_records, cudaMemcpyDeviceToHost, c.stream),
+           "svo_graft: targets");
+  SVO_CUDA(cudaStreamSynchronize(c.stream), "svo_graft: synchronize");
+  std::vector<svo::GraftRec> recs;
+  std::vector<svo::GraftJob> jobs;
+  std::vector<uint8_t> applied(n_records, 0);
+  std::set<uint32_t> seen;
+  uint64_t q = c.free_used;
+  uint64_t n_blocks = (uint64_t)c.n_groups * 8;
+  for (uint32_t r = 0; r < n_records; r++) {
+    uint32_t G = records[r].graft_total_size, P = records[r].graft_data_address;
+    if (G == 0 || (P & 7u) || (uint64_t)P + 8ull * G > n_payload) continue;
+    if (q + G > c.n_free) continue;
+    uint32_t target = targets[r];
+    if (target == svo::kNone || target >= n_blocks) continue;
+    if (!seen.insert(target).second)
+      return fail(SVO_ERR_INVALID_ARGUMENT, "svo_graft: two records graft onto node " + std::to_string(target));
+    svo::GraftRec gr{P, G, (uint32_t)q, target};
+    uint32_t rec_index = (uint32_t)recs.size();
+    recs.push_back(gr);
+    for (uint32_t k = 0; k < G; k++) jobs.push_back(svo::GraftJob{P + 8 * k, rec_index, k});
+    applied[r] = 1;
+    q += G;
+  }
+  uint64_t claimed = q - c.free_used;
+  if (!recs.empty()) {
+    static_assert(sizeof(svo::GraftJob) == 12 && sizeof(svo::GraftRec) == 16, "graft job layout");
+    size_t job_words = jobs.size() * 3, rec_words = recs.size() * 4;
+    if (c.payload.reserve(n_payload) || c.graft_jobs.reserve(job_words + rec_words) ||
+        c.claimed_list.reserve(std::max<uint64_t>(claimed, 1)))
+      return fail(SVO_ERR_OUT_OF_MEMORY, "svo_graft: device allocation failed");
+    svo::GraftRec *d_recs = reinterpret_cast<svo::GraftRec *>(c.graft_jobs.p + job_words);
+    SVO_CUDA(cudaMemcpyAsync(c.payload.p, payload, sizeof(svo_block) * n_payload, cudaMemcpyHostToDevice, c.stream),
+             "svo_graft: payload");
+    SVO_CUDA(cudaMemcpyAsync(c.graft_jobs.p, jobs.data(), sizeof(svo::GraftJob) * jobs.size(),
+                             cudaMemcpyHostToDevice, c.stream), "svo_graft: jobs");
+    SVO_CUDA(cudaMemcpyAsync(d_recs, recs.data(), sizeof(svo::GraftRec) * recs.size(), cudaMemcpyHostToDevice,
+                             c.stream), "svo_graft: records");
+    const svo::GraftJob *d_jobs = reinterpret_cast<const svo::GraftJob *>(c.graft_jobs.p);
+    uint32_t nj = (uint32_t)jobs.size();
+    svo::k_graft_usage<<<svo::grid_for(nj), 256, 0, c.stream>>>(t, d_jobs, nj, d_recs, c.free_list.p, in->tick);
+    svo::k_graft_nodes<<<svo::grid_for(8ull * nj), 256, 0, c.stream>>>(t, d_jobs, nj, d_recs, c.free_list.p,
+                                                                      c.payload.p);
+    svo::k_graft_link<<<svo::grid_for(recs.size()), 256, 0, c.stream>>>(t, d_recs, (uint32_t)recs.size(),
+                                                                        c.free_list.p);
+    SVO_CUDA(cudaGetLastError(), "svo_graft: kernels");
+    SVO_CUDA(cudaMemcpyAsync(c.claimed_list.p, c.free_list.p + c.free_used, claimed * 4, cudaMemcpyDeviceToDevice,
+                             c.stream), "svo_graft: claimed list");
+    SVO_CUDA(cudaStreamSynchronize(c.stream), "svo_graft: synchronize");
+  }
+  c.n_claimed = claimed;
+  c.free_used = q;
+  // grafted subtrees can reach below the deepest level seen at upload
+  if (claimed) c.tree_depth = SVO_MAX_TREE_DEPTH;
+  if (report) {
+    report->applied = (uint32_t)recs.size();
+    report->skipped = n_records - (uint32_t)recs.size();
+    report->claimed = claimed;
+    report->free_left = c.n_free - c.free_used;
+  }
+  return SVO_OK;
+}
+
+SVO_API svo_status svo_read_graft_claims(void *ctx, uint32_t *claimed, size_t cap) {
+  CTX(ctx, "svo_read_graft_claims");
+  SVO_CUDA(cudaStreamSynchronize(c.stream), "svo_read_graft_claims: synchronize");
+  size_t n = std::min<size_t>(cap, c.n_claimed);
+  if (claimed && n)
+    SVO_CUDA(cudaMemcpy(claimed, c.claimed_list.p, n * 4, cudaMemcpyDeviceToHost), "svo_read_graft_claims");
+  return SVO_OK;
+}
+
+SVO_API svo_status svo_prune(void *ctx, const svo_update_input *in, const svo_pruning *records, uint32_t n_records,
+                             const svo_block *surface, size_t n_surface, const uint64_t *locations,
+                             size_t n_locations, svo_prune_report *report) {
+  CTX(ctx, "svo_prune");
+  if (!in || (n_records && !records)) return fail(SVO_ERR_INVALID_ARGUMENT, "svo_prune: null argument");
+  if (in->tick < 1 || in->tick > 65533) return fail(SVO_ERR_INVALID_ARGUMENT, "svo_prune: tick must be 1..65533");
+  svo_status st = svo::ensure_tree_buffers(c);
+  if (st) return st;
+  svo::TreeView t = svo::view_of(c);
+  if (report) std::memset(report, 0, sizeof(*report));
+  if (n_records == 0) return SVO_OK;
+  uint32_t cap = std::max<uint32_t>(c.request_cap, 4096);
+  if (c.prune_records.reserve(n_records) || c.payload.reserve(std::max<size_t>(n_surface, 1)) ||
+      (n_locations && c.locations.reserve(n_locations)) || c.requests.reserve(cap))
+    return fail(SVO_ERR_OUT_OF_MEMORY, "svo_prune: device allocation failed");
+  c.request_cap = cap;
+  SVO_CUDA(cudaMemcpyAsync(c.prune_records.p, records, sizeof(svo_pruning) * n_records, cudaMemcpyHostToDevice,
+                           c.stream), "svo_prune: records");
+  if (n_surface)
+    SVO_CUDA(cudaMemcpyAsync(c.payload.p, surface, sizeof(svo_block) * n_surface, cudaMemcpyHostToDevice, c.stream),
+             "svo_prune: surface");
+  if (n_locations)
+    SVO_CUDA(cudaMemcpyAsync(c.locations.p, locations, sizeof(uint64_t) * n_locations, cudaMemcpyHostToDevice,
+                             c.stream), "svo_prune: locations");
+  uint32_t *culled = c.scan_tmp.p + (c.scan_tmp.n - 5);
+  uint32_t before = 0;
+  SVO_CUDA(cudaMemcpyAsync(&before, c.counters.p + 1, 4, cudaMemcpyDeviceToHost, c.stream), "svo_prune: requests");
+  SVO_CUDA(cudaMemsetAsync(culled, 0, 4, c.stream), "svo_prune: reset");
+  svo::k_prune<<<1, 1, 0, c.stream>>>(t, c.bases.p, (uint32_t)c.n_bases, in->tick, c.prune_records.p, n_records,
+                                     c.payload.p, (uint32_t)n_surface, c.locations.p, n_locations, c.requests.p, cap,
+                                     c.counters.p + 1, culled);
+  SVO_CUDA(cudaGetLastError(), "svo_prune: kernel");
+  uint32_t was_culled = 0, after = 0;
+  SVO_CUDA(cudaMemcpyAsync(&was_culled, culled, 4, cudaMemcpyDeviceToHost, c.stream), "svo_prune: flag");
+  SVO_CUDA(cudaMemcpyAsync(&after, c.counters.p + 1, 4, cudaMemcpyDeviceToHost, c.stream), "svo_prune: requests");
+  SVO_CUDA(cudaStreamSynchronize(c.stream), "svo_prune: synchronize");
+  uint64_t freed = 0;
+  if (was_culled) {
+    st = svo::sweep_and_free_list(c, t, &freed);
+    if (st) return st;
+  } else {
+    c.free_valid = false;
+  }
+  c.n_freed = freed;
+  c.n_pruned = 0;
+  if (report) {
+    report->freed = freed;
+    report->requests = after - before;
+  }
+  return SVO_OK;
+}
+
+}  // extern "C"

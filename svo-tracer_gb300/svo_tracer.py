@@ -38,7 +38,12 @@ CHILD_REQUEST_DTYPE = np.dtype([
     ("address", "<u4"), ("tick", "<u2"), ("depth", "u1"), ("_pad0", "u1"),
     ("location", "<u8", (3,)), ("tree_size", "u1"), ("_pad1", "u1", (7,)),
 ])
+GRAFTING_DTYPE = np.dtype([("graft_data_address", "<u4"), ("graft_total_size", "<u4"), ("depth", "u1"),
+                           ("_pad", "u1", (3,)), ("graft_address", "<u4")])
+PRUNING_DTYPE = np.dtype([("properties", "u1"), ("depth", "u1"), ("_pad0", "u1", (2,)), ("address", "<u4"),
+                          ("chunk", "<u2"), ("_pad1", "u1", (2,)), ("colour_address", "<u4"), ("child_address", "<u4")])
 assert BLOCK_DTYPE.itemsize == 16 and USAGE_DTYPE.itemsize == 8 and CHILD_REQUEST_DTYPE.itemsize == 40
+assert GRAFTING_DTYPE.itemsize == 16 and PRUNING_DTYPE.itemsize == 20
 
 NO_CHILD = 0xFFFFFFFF
 MISS = 0xFFFFFFFF
@@ -86,7 +91,25 @@ class SceneParamsC(C.Structure):
                 ("_pad", C.c_uint8 * 2), ("threads", C.c_int32), ("max_size", C.c_uint64)]
 
 
-assert C.sizeof(TraceInputC) == 104
+class UpdateInputC(C.Structure):
+    _fields_ = [("base_depth", C.c_uint8), ("_pad", C.c_uint8), ("tick", C.c_uint16),
+                ("max_child_request_id", C.c_uint32), ("memory_size", C.c_uint32), ("offset", C.c_uint32),
+                ("graft_size", C.c_uint32)]
+
+
+class GcReportC(C.Structure):
+    _fields_ = [("pruned", C.c_uint64), ("freed", C.c_uint64), ("free", C.c_uint64)]
+
+
+class GraftReportC(C.Structure):
+    _fields_ = [("applied", C.c_uint32), ("skipped", C.c_uint32), ("claimed", C.c_uint64), ("free_left", C.c_uint64)]
+
+
+class PruneReportC(C.Structure):
+    _fields_ = [("freed", C.c_uint64), ("requests", C.c_uint32), ("_pad", C.c_uint32)]
+
+
+assert C.sizeof(TraceInputC) == 104 and C.sizeof(UpdateInputC) == 20
 
 _lib = None
 
@@ -129,6 +152,18 @@ def load_library(path: str | None = None) -> C.CDLL:
         "svo_tree_info": ([vp, C.POINTER(C.c_uint8), C.POINTER(sz), C.POINTER(sz), C.POINTER(C.c_uint32)], C.c_int32),
         "svo_tree_data": ([vp, C.POINTER(vp), C.POINTER(vp)], C.c_int32),
         "svo_tree_free": ([vp], C.c_int32),
+        "svo_init_usage_tree": ([vp, C.c_uint16], C.c_int32),
+        "svo_gc": ([vp, C.POINTER(UpdateInputC), C.POINTER(GcReportC)], C.c_int32),
+        "svo_read_gc_lists": ([vp, vp, sz, vp, sz, vp, sz], C.c_int32),
+        "svo_graft": ([vp, C.POINTER(UpdateInputC), vp, C.c_uint32, vp, sz, vp, sz, C.POINTER(GraftReportC)], C.c_int32),
+        "svo_read_graft_claims": ([vp, vp, sz], C.c_int32),
+        "svo_prune": ([vp, C.POINTER(UpdateInputC), vp, C.c_uint32, vp, sz, vp, sz, C.POINTER(PruneReportC)], C.c_int32),
+        "svo_scene_create": ([C.POINTER(SceneParamsC), C.POINTER(vp)], C.c_int32),
+        "svo_scene_build_tree": ([vp, C.c_uint8, C.POINTER(vp)], C.c_int32),
+        "svo_scene_graft_payload": ([vp, vp, sz, C.POINTER(vp)], C.c_int32),
+        "svo_graft_payload_data": ([vp, C.POINTER(vp), C.POINTER(sz), C.POINTER(vp), C.POINTER(sz)], C.c_int32),
+        "svo_graft_payload_free": ([vp], C.c_int32),
+        "svo_scene_free": ([vp], C.c_int32),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)
@@ -166,6 +201,66 @@ class Octree:
 
 def pow_sum(depth: int) -> int:
     return sum(8 ** i for i in range(1, depth + 1))
+
+
+def _tree_from_handle(lib, h) -> "Octree":
+    try:
+        bd, nb, nk, bc = C.c_uint8(), C.c_size_t(), C.c_size_t(), C.c_uint32()
+        _check("BuildTree", lib.svo_tree_info(h, C.byref(bd), C.byref(nb), C.byref(nk), C.byref(bc)))
+        pb, pk = C.c_void_p(), C.c_void_p()
+        _check("BuildTree", lib.svo_tree_data(h, C.byref(pb), C.byref(pk)))
+        bases = np.ctypeslib.as_array(C.cast(pb, C.POINTER(C.c_uint16)), shape=(nb.value,)).copy()
+        raw = np.ctypeslib.as_array(C.cast(pk, C.POINTER(C.c_uint8)), shape=(nk.value * 16,)).copy()
+        return Octree(bd.value, bc.value, bases, raw.view(BLOCK_DTYPE))
+    finally:
+        lib.svo_tree_free(h)
+
+
+class Scene:
+    """A persistent procedural scene: builds the resident tree and the graft
+    payloads of the streaming workflow (depth = deepest node level it produces)."""
+
+    def __init__(self, scene: int = SCENE_TERRAIN, seed: int = 1, base_depth: int = 4, depth: int = 12,
+                 threads: int = 0):
+        self._lib = load_library()
+        self._h = C.c_void_p()
+        p = SceneParamsC(kind=scene, seed=seed, base_depth=base_depth, max_depth=depth, threads=threads, max_size=0)
+        _check("SceneCreate", self._lib.svo_scene_create(C.byref(p), C.byref(self._h)))
+        self.base_depth, self.depth = base_depth, depth
+
+    def close(self):
+        if self._h:
+            self._lib.svo_scene_free(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def build_tree(self, max_depth: int) -> "Octree":
+        h = C.c_void_p()
+        _check("BuildTree", self._lib.svo_scene_build_tree(self._h, max_depth, C.byref(h)))
+        return _tree_from_handle(self._lib, h)
+
+    def graft_payload(self, requests: np.ndarray):
+        req = np.ascontiguousarray(requests, dtype=CHILD_REQUEST_DTYPE)
+        h = C.c_void_p()
+        _check("GraftPayload", self._lib.svo_scene_graft_payload(self._h, _ptr(req), len(req), C.byref(h)))
+        try:
+            pr, nr, pp, npay = C.c_void_p(), C.c_size_t(), C.c_void_p(), C.c_size_t()
+            _check("GraftPayload", self._lib.svo_graft_payload_data(h, C.byref(pr), C.byref(nr), C.byref(pp),
+                                                                      C.byref(npay)))
+            rec = np.zeros(nr.value, GRAFTING_DTYPE)
+            pay = np.zeros(npay.value, BLOCK_DTYPE)
+            if nr.value:
+                C.memmove(rec.ctypes.data, pr.value, nr.value * 16)
+            if npay.value:
+                C.memmove(pay.ctypes.data, pp.value, npay.value * 16)
+            return rec, pay
+        finally:
+            self._lib.svo_graft_payload_free(h)
 
 
 class TreeBuilder:
@@ -279,6 +374,36 @@ def mixed_views(seed: int = 4, n: int = 64, **kw):
         origin = 0.5 + radius * d
         views.append(look_at(origin, target, w, h, rng.uniform(40.0, 90.0), **kw))
     return views
+
+
+def camera_path(seed: int = 3, frames: int = 120, width: int = 1920, height: int = 1080, fov: float = 60.0,
+                n_points: int = 8, **kw):
+    """The streaming workload's camera: a Catmull-Rom spline through n_points seeded
+    control points at heights 0.35-0.6 above the terrain's base (unit-cube z = 1 - h,
+    up is -z), sampled at `frames` evenly spaced parameters; each frame looks ahead
+    along the path and down towards the terrain. Frame f carries Tick f + 1."""
+    rng = np.random.default_rng(seed)
+    pts = np.stack([rng.uniform(0.1, 0.9, n_points), rng.uniform(0.1, 0.9, n_points),
+                    1.0 - rng.uniform(0.35, 0.6, n_points)], axis=1)
+
+    def spline(u):
+        seg = min(int(u), n_points - 4)
+        t = u - seg
+        p0, p1, p2, p3 = pts[seg], pts[seg + 1], pts[seg + 2], pts[seg + 3]
+        return 0.5 * ((2 * p1) + (-p0 + p2) * t + (2 * p0 - 5 * p1 + 4 * p2 - p3) * t * t +
+                      (-p0 + 3 * p1 - 3 * p2 + p3) * t * t * t)
+
+    span = n_points - 3
+    out = []
+    for f in range(frames):
+        u = span * f / max(frames - 1, 1)
+        pos = spline(u)
+        ahead = spline(min(span, u + 0.05 * span))
+        if np.linalg.norm(ahead - pos) < 1e-6:
+            ahead = pos + (pts[-2] - pts[1])
+        target = ahead + np.array([0.0, 0.0, 0.25])
+        out.append(look_at(pos, target, width, height, fov, Tick=f + 1, **kw))
+    return out
 
 
 @dataclass
@@ -432,6 +557,55 @@ class Tracer:
         vb, vs = np.zeros(n, np.uint32), np.zeros(n, np.uint32)
         _check("RayCounts", self._lib.svo_read_ray_counts(self._ctx, _ptr(vb), _ptr(vs), n))
         return vb, vs
+
+    # ---- tree updates --------------------------------------------------------
+    @staticmethod
+    def _update(tick: int, offset: int = 0) -> UpdateInputC:
+        return UpdateInputC(0, 0, tick, 0, 0, offset, 0)
+
+    def init_usage_tree(self, tick: int) -> None:
+        _check("InitUsageTree", self._lib.svo_init_usage_tree(self._ctx, tick))
+
+    def gc(self, tick: int, threshold: int) -> dict:
+        rep = GcReportC()
+        _check("GC", self._lib.svo_gc(self._ctx, C.byref(self._update(tick, threshold)), C.byref(rep)))
+        return {"pruned": rep.pruned, "freed": rep.freed, "free": rep.free}
+
+    def gc_lists(self, n_pruned: int, n_freed: int, n_free: int):
+        a, b, c = (np.zeros(max(n, 1), np.uint32) for n in (n_pruned, n_freed, n_free))
+        _check("GcLists", self._lib.svo_read_gc_lists(self._ctx, _ptr(a), n_pruned, _ptr(b), n_freed, _ptr(c), n_free))
+        return a[:n_pruned], b[:n_freed], c[:n_free]
+
+    def graft(self, tick: int, records: np.ndarray, payload: np.ndarray, locations: np.ndarray | None = None) -> dict:
+        rec = np.ascontiguousarray(records, dtype=GRAFTING_DTYPE)
+        pay = np.ascontiguousarray(payload, dtype=BLOCK_DTYPE)
+        loc = None if locations is None else np.ascontiguousarray(locations, dtype=np.uint64)
+        rep = GraftReportC()
+        _check("Graft", self._lib.svo_graft(self._ctx, C.byref(self._update(tick)), _ptr(rec), len(rec), _ptr(pay),
+                                            len(pay), _ptr(loc), 0 if loc is None else loc.size, C.byref(rep)))
+        return {"applied": rep.applied, "skipped": rep.skipped, "claimed": rep.claimed, "free_left": rep.free_left}
+
+    def graft_claims(self, n: int) -> np.ndarray:
+        out = np.zeros(max(n, 1), np.uint32)
+        _check("GraftClaims", self._lib.svo_read_graft_claims(self._ctx, _ptr(out), n))
+        return out[:n]
+
+    def prune(self, tick: int, records: np.ndarray, surface: np.ndarray | None = None,
+              locations: np.ndarray | None = None) -> dict:
+        rec = np.ascontiguousarray(records, dtype=PRUNING_DTYPE)
+        sur = None if surface is None else np.ascontiguousarray(surface, dtype=BLOCK_DTYPE)
+        loc = None if locations is None else np.ascontiguousarray(locations, dtype=np.uint64)
+        rep = PruneReportC()
+        _check("Prune", self._lib.svo_prune(self._ctx, C.byref(self._update(tick)), _ptr(rec), len(rec), _ptr(sur),
+                                            0 if sur is None else len(sur), _ptr(loc), 0 if loc is None else loc.size,
+                                            C.byref(rep)))
+        return {"freed": rep.freed, "requests": rep.requests}
+
+    def read_bases(self) -> np.ndarray:
+        n = self.tree_size()[1]
+        out = np.zeros(n, np.uint16)
+        _check("ReadBuffer:Bases", self._lib.svo_read_bases(self._ctx, _ptr(out), n))
+        return out
 
     def read_child_requests(self, cap: int = 1 << 20):
         out = np.zeros(cap, dtype=CHILD_REQUEST_DTYPE)

@@ -1,0 +1,155 @@
+"""Tree-update kernels (usage initialisation, block GC, grafting, pruning) against the
+oracle, through the C ABI. Every set the specification defines (pruned, freed,
+free-list and claimed groups) and the whole block and usage arrays must be bit-exact."""
+import numpy as np
+import pytest
+
+import pyoracle as po
+import svo_tracer as st
+
+pytestmark = pytest.mark.gpu
+NONE = 0xFFFFFFFF
+
+
+@pytest.fixture(autouse=True)
+def default_config(tracer):
+    tracer.set_config(block_size=256, ctas_per_sm=0, ray_chunk=1, cadence=16, max_steps=1 << 16, collect_stats=0)
+    yield
+
+
+def gpu_state(tr, n_groups):
+    return tr.read_blocks(0, n_groups * 8), tr.read_usage(n_groups)
+
+
+def assert_state(tr, oracle, label):
+    blocks, usage = gpu_state(tr, oracle.n_groups)
+    bad_b = int((blocks.view(np.uint8).reshape(-1, 16) != oracle.blocks.view(np.uint8).reshape(-1, 16)).any(1).sum())
+    bad_u = int((usage.view(np.uint8).reshape(-1, 8) != oracle.usage.view(np.uint8).reshape(-1, 8)).any(1).sum())
+    assert bad_b == 0 and bad_u == 0, "%s: %d nodes and %d usage entries differ" % (label, bad_b, bad_u)
+
+
+def test_init_usage_tree_matches_oracle(tracer):
+    scene = st.Scene(st.SCENE_TERRAIN, seed=5, base_depth=3, depth=9)
+    tree = scene.build_tree(8)
+    budget = 1 << 16
+    tracer.upload(tree, block_budget=budget * 8)
+    tracer.init_usage_tree(11)
+    oracle = po.TreeState(tree, budget)
+    oracle.init_usage_tree(11)
+    assert_state(tracer, oracle, "init")
+
+
+@pytest.mark.parametrize("base_depth,depth,initial,budget,threshold", [(3, 9, 7, 1 << 15, 3), (2, 8, 6, 1 << 13, 2)])
+def test_stream_matches_oracle(tracer, base_depth, depth, initial, budget, threshold):
+    """Frames of the streaming workflow: trace (usage stamps + child requests), graft
+    payloads from the procedural scene, GC of groups unused for `threshold` frames,
+    grafting into freed groups; GPU and oracle evolve their own copies of the tree."""
+    scene = st.Scene(st.SCENE_TERRAIN, seed=5, base_depth=base_depth, depth=depth)
+    tree = scene.build_tree(initial)
+    tracer.upload(tree, block_budget=budget * 8)
+    tracer.init_usage_tree(1)
+    oracle = po.TreeState(tree, budget)
+    oracle.init_usage_tree(1)
+    cams = st.camera_path(seed=3, frames=10, width=160, height=90, MaxChildRequestId=1 << 16)
+    grafted_total = pruned_total = 0
+    for f, cam in enumerate(cams):
+        tick = f + 1
+        got = tracer.trace(cam)
+        want = po.trace_view(oracle.as_octree(), cam, usage=oracle.usage)
+        for k in ("hit_index", "hit_depth", "t", "rgba"):
+            assert np.array_equal(getattr(got, k), want[k]), "frame %d: %s" % (f, k)
+        req, n = tracer.read_child_requests()
+        assert n == want["n_requests"]
+        same = po.sort_requests(req).tobytes() == po.sort_requests(want["requests"]).tobytes()
+        assert same, "frame %d: child requests differ" % f
+        rec, pay = scene.graft_payload(req)
+        rep = tracer.gc(tick, threshold)
+        g_pruned, g_freed, g_free = tracer.gc_lists(rep["pruned"], rep["freed"], rep["free"])
+        o_pruned, o_freed, o_free = oracle.gc(tick, threshold)
+        assert np.array_equal(g_pruned, o_pruned), "frame %d: pruned sets differ" % f
+        assert np.array_equal(g_freed, o_freed), "frame %d: freed sets differ" % f
+        assert np.array_equal(g_free, o_free), "frame %d: free lists differ" % f
+        grep = tracer.graft(tick, rec, pay)
+        claims = tracer.graft_claims(grep["claimed"])
+        o_claims, applied = oracle.graft(tick, rec, pay)
+        assert np.array_equal(claims, o_claims), "frame %d: grafted groups differ" % f
+        assert grep["applied"] == int(applied.sum())
+        assert_state(tracer, oracle, "frame %d" % f)
+        grafted_total += len(claims)
+        pruned_total += len(g_pruned)
+    assert grafted_total > 0 and pruned_total > 0
+
+
+def test_prune_matches_oracle(tracer):
+    scene = st.Scene(st.SCENE_TERRAIN, seed=8, base_depth=3, depth=9)
+    tree = scene.build_tree(8)
+    budget = 1 << 16
+    tracer.upload(tree, block_budget=budget * 8)
+    tracer.init_usage_tree(5)
+    oracle = po.TreeState(tree, budget)
+    oracle.init_usage_tree(5)
+    rng = np.random.default_rng(1)
+    live = np.nonzero(oracle.usage["tick"] == 5)[0]
+    n = 64
+    rec = np.zeros(n, st.PRUNING_DTYPE)
+    locs = rng.integers(0, 2 ** 63, size=(n, 3), dtype=np.uint64) * 2
+    for i in range(n):
+        kind = i % 5
+        rec[i]["properties"] = [1, 0b110, 0b010, 0b1000, 0b10000][kind] | (1 if i % 7 == 0 else 0)
+        if i % 3 == 0:
+            rec[i]["depth"] = rng.integers(3 + 2, 9)  # Location walk
+            rec[i]["address"] = i
+        else:
+            rec[i]["depth"] = 255
+            rec[i]["address"] = int(rng.choice(live)) * 8 + int(rng.integers(0, 8))
+        if kind == 4:
+            rec[i]["address"] = int(rng.integers(0, st.pow_sum(3)))
+        rec[i]["chunk"] = int(rng.integers(0, 65536))
+        rec[i]["colour_address"] = int(rng.integers(0, 4))
+        rec[i]["child_address"] = NONE
+    surface = np.zeros(4, st.BLOCK_DTYPE)
+    surface["child"] = NONE
+    surface["colour_r"] = [10, 20, 30, 40]
+    rep = tracer.prune(9, rec, surface, locs.reshape(-1))
+    o_freed, o_req = oracle.prune(9, rec, surface, locs.reshape(-1))
+    assert rep["freed"] == len(o_freed)
+    assert_state(tracer, oracle, "prune")
+    assert np.array_equal(tracer.read_bases(), oracle.bases)
+    _, g_freed, _ = tracer.gc_lists(0, rep["freed"], 0)
+    assert np.array_equal(g_freed, o_freed)
+    assert rep["requests"] == len(o_req)
+
+
+def test_graft_location_targets_and_budget(tracer):
+    scene = st.Scene(st.SCENE_TERRAIN, seed=5, base_depth=3, depth=9)
+    tree = scene.build_tree(7)
+    budget = (len(tree.Blocks) + 7) // 8 + 64  # only a few free groups beyond the tree
+    tracer.upload(tree, block_budget=budget * 8)
+    tracer.init_usage_tree(1)
+    oracle = po.TreeState(tree, budget)
+    oracle.init_usage_tree(1)
+    cam = st.look_at((0.1, 0.15, 0.55), (0.7, 0.7, 0.9), 96, 54, 60.0, Tick=1)
+    tracer.trace(cam)
+    req, n = tracer.read_child_requests()
+    assert n > 0
+    rec, pay = scene.graft_payload(req)
+    # address half of the records by Location (walk to the requesting node's depth)
+    uniq = {}
+    for r in po.sort_requests(req):
+        uniq.setdefault(int(r["address"]), r)
+    locs = []
+    for i, r in enumerate(rec):
+        if i % 2:
+            q = uniq[int(r["graft_address"])]
+            r["depth"] = q["depth"]
+            r["graft_address"] = len(locs) // 3
+            locs.extend(int(v) for v in q["location"])
+    locs = np.array(locs, np.uint64)
+    rep = tracer.gc(2, 100)
+    oracle.gc(2, 100)
+    grep = tracer.graft(2, rec, pay, locs)
+    o_claims, applied = oracle.graft(2, rec, pay, locs)
+    assert grep["skipped"] > 0  # the budget runs out
+    assert grep["applied"] == int(applied.sum()) > 0
+    assert np.array_equal(tracer.graft_claims(grep["claimed"]), o_claims)
+    assert_state(tracer, oracle, "graft")
