@@ -225,6 +225,65 @@ def multiview(tr, torch, dev, stream, flush, args):
             "plain": "64 sequential single-view launches, same stream, default configuration"}
 
 
+def stream_workload(torch, dev, args):
+    """The pruning/grafting/GC stream: 120 frames along a Catmull-Rom camera path at
+    1080p over the depth-12 terrain scene behind a budget of 2^22 block groups. Each
+    frame: trace (usage stamps, child requests capped at 65536), graft payloads from
+    the host generator, GC of groups unused for more than 30 frames, grafts into the
+    freed groups. Wall time per frame covers all of it (host generation included)."""
+    import svo_tracer as st
+
+    frames = args.stream_frames
+    t0 = time.perf_counter()
+    scene = st.Scene(st.SCENE_TERRAIN, seed=SEED, base_depth=BASE_DEPTH, depth=12)
+    tree = scene.build_tree(10)
+    setup_s = time.perf_counter() - t0
+    budget = 1 << 22
+    tr = st.Tracer(dev)
+    tr.upload(tree, block_budget=budget * 8)
+    tr.init_usage_tree(1)
+    cams = st.camera_path(seed=3, frames=frames, width=WIDTH, height=HEIGHT, MaxChildRequestId=1 << 16)
+    n = WIDTH * HEIGHT
+    o = [torch.empty(n, dtype=torch.int32, device=dev), torch.empty(n, dtype=torch.uint8, device=dev),
+         torch.empty(n, dtype=torch.float32, device=dev), torch.empty(4 * n, dtype=torch.float32, device=dev)]
+    outs = [tuple(x.data_ptr() for x in o)]
+    totals = {"requests": 0, "grafted_groups": 0, "graft_records": 0, "pruned_groups": 0, "freed_groups": 0}
+    phase = {"trace": 0.0, "generate": 0.0, "gc": 0.0, "graft": 0.0}
+    t_loop = time.perf_counter()
+    for f, cam in enumerate(cams):
+        tick = f + 1
+        a = time.perf_counter()
+        tr.trace_device([cam], outs)
+        req, n_req = tr.read_child_requests(cap=1 << 16)
+        b = time.perf_counter()
+        rec, pay = scene.graft_payload(req)
+        c = time.perf_counter()
+        rep = tr.gc(tick, 30)
+        d = time.perf_counter()
+        grep = tr.graft(tick, rec, pay)
+        e = time.perf_counter()
+        phase["trace"] += b - a
+        phase["generate"] += c - b
+        phase["gc"] += d - c
+        phase["graft"] += e - d
+        totals["requests"] += n_req
+        totals["grafted_groups"] += grep["claimed"]
+        totals["graft_records"] += grep["applied"]
+        totals["pruned_groups"] += rep["pruned"]
+        totals["freed_groups"] += rep["freed"]
+    loop_s = time.perf_counter() - t_loop
+    usage = tr.read_usage(budget)
+    resident = int(((usage["tick"] >= 1) & (usage["tick"] <= 65533)).sum())
+    tr.close()
+    return {"frames": frames, "width": WIDTH, "height": HEIGHT, "scene_depth": 12, "initial_depth": 10,
+            "budget_groups": budget, "stale_frames": 30, "request_cap": 1 << 16,
+            "frames_per_s": frames / loop_s, "ms_per_frame": 1000 * loop_s / frames,
+            "mrays_s_with_updates": frames * n / loop_s / 1e6,
+            "ms_per_frame_by_phase": {k: 1000 * v / frames for k, v in phase.items()},
+            "totals": totals, "resident_groups_end": resident, "setup_s": setup_s,
+            "timing": "host wall clock per frame, synchronous pipeline (generation on host cores)"}
+
+
 def run_ours(args, rank, world):
     import torch
 
@@ -335,6 +394,8 @@ def run_ours(args, rank, world):
     }
     if not args.no_multiview:
         line["multiview"] = multiview(tr, torch, dev, stream, flush, args)
+    if args.stream_frames > 0:
+        line["stream"] = stream_workload(torch, dev, args)
     if not args.no_cpu_baseline:
         import pyoracle as po
 
@@ -355,6 +416,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-multiview", action="store_true")
+    ap.add_argument("--stream-frames", type=int, default=120)
     ap.add_argument("--width", type=int, default=WIDTH)
     ap.add_argument("--height", type=int, default=HEIGHT)
     args = ap.parse_args()
