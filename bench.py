@@ -284,6 +284,84 @@ def stream_workload(torch, dev, args):
             "timing": "host wall clock per frame, synchronous pipeline (generation on host cores)"}
 
 
+def diff_workload(torch, dev, flush, args):
+    """Differentiable colour fitting: the depth-9 SDF sphere (512^3 leaf grid), 16
+    views of 512x512 around it, FP32 per-node RGBA initialised uniform in [0, 1],
+    targets rendered from the seeded sinusoid ground-truth field (opacity 0.9).
+    One step = forward colour + backward (loss and dL/dRGBA per node, traversal
+    recomputed once, the forward's colour reused), device-resident; L2 flushed
+    between steps. `e2e` is one fitting
+    step through the host API: parameters uploaded, forward colour read back,
+    backward with the loss and the gradients read back."""
+    import svo_tracer as st
+
+    tree = st.TreeBuilder(st.SCENE_SPHERE, seed=1).BuildTree(4, 9)
+    views = st.orbit_views(seed=7, n=16, width=512, height=512)
+    rays = sum(v.ScreenSize[0] * v.ScreenSize[1] for v in views)
+    nodes = len(tree.Blocks)
+    tr = st.Tracer(dev)
+    stream = torch.cuda.Stream(device=dev)  # events, flush and kernels all on this stream
+    tr.set_stream(stream.cuda_stream)
+    tr.upload(tree)
+    tr.set_config(max_hits=16)
+    with torch.cuda.stream(stream):
+        return _diff_timed(tr, torch, dev, stream, flush, args, tree, views, rays, nodes)
+
+
+def _diff_timed(tr, torch, dev, stream, flush, args, tree, views, rays, nodes):
+    import svo_tracer as st
+
+    gt = torch.from_numpy(st.sinusoid_field(tree, seed=9)).to(dev)
+    params = torch.from_numpy(np.random.default_rng(3).uniform(0.0, 1.0, (nodes, 4)).astype(np.float32)).to(dev)
+    target = torch.empty(rays * 3, dtype=torch.float32, device=dev)
+    rgb = torch.empty(rays * 3, dtype=torch.float32, device=dev)
+    tr.diff_set_params_device(gt.data_ptr(), nodes)
+    tr.diff_forward_device(views, target.data_ptr())
+    tr.diff_set_params_device(params.data_ptr(), nodes)
+    torch.cuda.synchronize()
+
+    def timed(fn, steps):
+        ms = []
+        for _ in range(steps):
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+            e1.synchronize()
+            ms.append(e0.elapsed_time(e1))
+        return float(np.median(ms))
+
+    steps = max(5, args.steps // 2)
+    for _ in range(3):
+        tr.diff_forward_device(views, rgb.data_ptr())
+        tr.diff_backward_device(views, target.data_ptr())
+    fwd_ms = timed(lambda: tr.diff_forward_device(views, rgb.data_ptr()), steps)
+    bwd_ms = timed(lambda: tr.diff_backward_device(views, target.data_ptr(), use_saved=True), steps)
+    bwd_recompute_ms = timed(lambda: tr.diff_backward_device(views, target.data_ptr()), steps)
+    step_ms = timed(lambda: (tr.diff_forward_device(views, rgb.data_ptr()),
+                             tr.diff_backward_device(views, target.data_ptr(), use_saved=True)), steps)
+    host_params = params.cpu().numpy()
+    host_target = target.cpu().numpy()
+    loss0 = tr.diff_backward(views, host_target)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        tr.diff_set_params(host_params)
+        tr.diff_forward(views)
+        tr.diff_backward(views, host_target, use_saved=True)
+        tr.diff_grads(nodes)
+    e2e_s = (time.perf_counter() - t0) / steps
+    tr.close()
+    return {"workload": "depth-9 SDF sphere, 16 views 512x512, FP32 per-node RGBA, max 16 hits per ray",
+            "nodes": nodes, "rays": rays, "fwd_ms": fwd_ms, "bwd_ms": bwd_ms, "fwd_bwd_ms": step_ms,
+            "bwd_recompute_colour_ms": bwd_recompute_ms,
+            "fwd_bwd_mrays_s": rays / step_ms / 1e3, "fwd_mrays_s": rays / fwd_ms / 1e3,
+            "bwd_mrays_s": rays / bwd_ms / 1e3, "initial_loss": loss0,
+            "e2e": {"value": rays / e2e_s / 1e6, "unit": "Mrays/s (fwd+bwd)",
+                    "h2d_bytes_per_step": nodes * 16 + rays * 12, "d2h_bytes_per_step": rays * 12 + nodes * 16 + 8},
+            "l2": "flushed between steps (256 MiB write)"}
+
+
 def run_ours(args, rank, world):
     import torch
 
@@ -394,6 +472,8 @@ def run_ours(args, rank, world):
     }
     if not args.no_multiview:
         line["multiview"] = multiview(tr, torch, dev, stream, flush, args)
+    if not args.no_diff:
+        line["diff"] = diff_workload(torch, dev, flush, args)
     if args.stream_frames > 0:
         line["stream"] = stream_workload(torch, dev, args)
     if not args.no_cpu_baseline:
@@ -416,6 +496,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-multiview", action="store_true")
+    ap.add_argument("--no-diff", action="store_true")
     ap.add_argument("--stream-frames", type=int, default=120)
     ap.add_argument("--width", type=int, default=WIDTH)
     ap.add_argument("--height", type=int, default=HEIGHT)

@@ -177,7 +177,8 @@ typedef struct svo_trace_config {
   int32_t cadence;      /* steps a thread runs between ray retire/refill points (1..1024) */
   int32_t max_steps;    /* per-ray step limit */
   int32_t collect_stats; /* 0 none, 1 totals (svo_last_trace_stats), 2 totals and per-ray counts */
-  int32_t _pad[2];
+  int32_t max_hits;     /* differentiable forward: LOD hits composited per ray (1..1024) */
+  int32_t _pad;
 } svo_trace_config;
 
 /* ---- context ------------------------------------------------------------ */
@@ -293,6 +294,29 @@ SVO_API svo_status svo_read_graft_claims(void *ctx, uint32_t *claimed, size_t ca
 SVO_API svo_status svo_prune(void *ctx, const svo_update_input *in, const svo_pruning *records, uint32_t n_records,
                              const svo_block *surface, size_t n_surface, const uint64_t *locations,
                              size_t n_locations, svo_prune_report *report);
+
+/* ---- differentiable colour fitting (no reference counterpart) ------------ */
+
+/* Per-node RGBA parameters (4 floats per node, nodes 0..n_nodes-1 of the
+ * resident tree; n_nodes <= the block budget, missing nodes are zero). A ray
+ * composites the parameters of its LOD hits front to back (C += T a rgb,
+ * T *= 1 - a), continuing past each hit, up to max_hits hits, then the sky
+ * colour times the remaining transmittance. The geometry (and so the hit
+ * sequence) is fixed. Pointers are device memory when on_device != 0. */
+SVO_API svo_status svo_diff_set_params(void *ctx, const float *rgba, size_t n_nodes, int32_t on_device);
+/* Gradients of the last svo_diff_backward, 4 floats per node. */
+SVO_API svo_status svo_diff_get_grads(void *ctx, float *grad_rgba, size_t n_nodes, int32_t on_device);
+/* Composited colour, 3 floats per ray, views concatenated in order. */
+SVO_API svo_status svo_diff_forward(void *ctx, const svo_trace_input *views, int32_t n_views, float *rgb,
+                                    int32_t on_device);
+/* L = sum over rays and channels of (C - target)^2 / rays; recomputes the
+ * traversal (no per-ray hit lists are stored) and writes dL/d(params) into the
+ * gradient buffer. use_saved != 0 takes C from the last svo_diff_forward
+ * (which must have run on the same views, parameters and max_hits, else
+ * SVO_ERR_INVALID_ARGUMENT): one traversal per ray instead of two. *loss (may
+ * be NULL: no synchronisation) receives L. */
+SVO_API svo_status svo_diff_backward(void *ctx, const svo_trace_input *views, int32_t n_views, const float *target,
+                                     int32_t use_saved, int32_t on_device, double *loss);
 
 /* ---- tracing without allocation ------------------------------------------ */
 

@@ -57,6 +57,12 @@ def oracle_lib() -> C.CDLL:
         lib.oracle_trace_into_volume.argtypes = [_vp, _vp, _vp, C.c_float, _vp, _vp]
         lib.oracle_trace_into_volume.restype = C.c_int
         lib.oracle_init_usage.argtypes = [_vp, C.c_uint8, _vp, C.c_size_t]
+        lib.oracle_hit_lists.argtypes = [_vp, C.c_uint8, _vp, C.c_size_t, C.c_char_p, C.c_int32, C.c_int32, _vp, _vp,
+                                         _vp, _vp, C.c_int32]
+        lib.oracle_diff_eval.argtypes = [_vp, _vp, _vp, _vp, C.c_int64, C.c_int32, _vp, _vp, _vp, _vp, C.c_int32]
+        lib.oracle_diff_eval.restype = C.c_double
+        lib.oracle_diff_fd.argtypes = [_vp, _vp, _vp, _vp, C.c_int64, C.c_int32, _vp, _vp, _vp, C.c_int32, C.c_double,
+                                       _vp, C.c_int32]
         lib.oracle_init_usage_tree.argtypes = [_vp, C.c_int, _vp, C.c_size_t, _vp, C.c_uint16]
         lib.oracle_gc.argtypes = [_vp, C.c_int, _vp, C.c_size_t, _vp, C.c_uint16, C.c_uint32, _vp, _vp, _vp, _vp]
         lib.oracle_graft.argtypes = [C.c_int, _vp, C.c_size_t, _vp, C.c_uint16, _vp, C.c_uint32, _vp, C.c_size_t, _vp,
@@ -246,3 +252,58 @@ class TreeState:
     def as_octree(self):
         from svo_tracer import Octree
         return Octree(self.B, len(self.blocks), self.bases, self.blocks)
+
+
+class HitLists:
+    """FP64 reference of the differentiable forward model: the per-ray LOD hit
+    lists of a set of views (fixed geometry), then compositing, loss and gradient
+    in double precision over any parameter array."""
+
+    def __init__(self, tree, views, max_hits=16, max_steps=1 << 16, threads=0):
+        lib = oracle_lib()
+        bases = np.ascontiguousarray(tree.BaseBlocks, np.uint16)
+        blocks = np.ascontiguousarray(tree.Blocks)
+        parts = []
+        for v in views:
+            n = v.ScreenSize[0] * v.ScreenSize[1]
+            hits = np.zeros((n, max_hits), np.uint32)
+            nh = np.zeros(n, np.uint8)
+            lv = np.zeros(n, np.uint8)
+            sky = np.zeros((n, 3), np.float32)
+            lib.oracle_hit_lists(_p(bases), tree.BaseDepth, _p(blocks), len(blocks), v.to_bytes(), max_steps,
+                                 max_hits, _p(hits), _p(nh), _p(lv), _p(sky), threads)
+            parts.append((hits, nh, lv, sky))
+        self.hits = np.concatenate([p[0] for p in parts])
+        self.n_hits = np.concatenate([p[1] for p in parts])
+        self.leaves = np.concatenate([p[2] for p in parts])
+        self.sky = np.concatenate([p[3] for p in parts])
+        self.max_hits = max_hits
+        self.n_rays = len(self.n_hits)
+        self.threads = threads
+
+    def eval(self, params, target=None, want_rgb=False, want_grad=False):
+        params = np.ascontiguousarray(params, np.float64)
+        tgt = None if target is None else np.ascontiguousarray(target, np.float64)
+        rgb = np.zeros((self.n_rays, 3)) if want_rgb else None
+        grad = np.zeros_like(params) if want_grad else None
+        loss = oracle_lib().oracle_diff_eval(_p(self.hits), _p(self.n_hits), _p(self.leaves), _p(self.sky),
+                                             self.n_rays, self.max_hits, _p(params), _p(tgt), _p(rgb), _p(grad),
+                                             self.threads)
+        return loss, rgb, grad
+
+    def finite_differences(self, params, target, nodes, h=1e-4):
+        """FP64 central differences of the loss with respect to the 4 parameters
+        of each listed node, step h; [len(nodes), 4]."""
+        params = np.ascontiguousarray(params, np.float64)
+        tgt = np.ascontiguousarray(target, np.float64)
+        nodes = np.asarray(nodes, np.uint32)
+        order = np.argsort(nodes, kind="stable")
+        srt = np.ascontiguousarray(nodes[order])
+        assert len(np.unique(srt)) == len(srt), "nodes must be distinct"
+        fd = np.zeros((len(nodes), 4))
+        oracle_lib().oracle_diff_fd(_p(self.hits), _p(self.n_hits), _p(self.leaves), _p(self.sky), self.n_rays,
+                                    self.max_hits, _p(params), _p(tgt), _p(srt), len(srt), h, _p(fd),
+                                    self.threads)
+        out = np.zeros_like(fd)
+        out[order] = fd
+        return out

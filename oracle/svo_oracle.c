@@ -498,3 +498,234 @@ int64_t oracle_trace_rows(const uint16_t *bases, uint8_t base_depth, const svo_b
   free(cv);
   return limited;
 }
+
+
+/* ---- differentiable forward model: LOD hit lists ------------------------- */
+
+/* For each ray of the view: the sequence of LOD hit nodes (up to max_hits),
+ * continuing past every hit as if its octant were empty (the traversal of
+ * svo_diff_forward), whether the ray ended by leaving the cube (then the sky
+ * colour contributes) and that sky colour (drawTrace's float of c/255). */
+void oracle_hit_lists(const uint16_t *bases, uint8_t B, const svo_block *blocks, size_t n_blocks,
+                      const svo_trace_input *in, int32_t max_steps, int32_t max_hits, uint32_t *hits, uint8_t *n_hits,
+                      uint8_t *leaves, float *sky, int32_t threads) {
+  uint32_t W = in->screen_size[0], H = in->screen_size[1];
+  float *su = (float *)malloc(sizeof(float) * (W + 1));
+  float *cu = (float *)malloc(sizeof(float) * (W + 1));
+  float *sv = (float *)malloc(sizeof(float) * (H + 1));
+  float *cv = (float *)malloc(sizeof(float) * (H + 1));
+  oracle_view_tables(in, su, cu, sv, cv);
+  int64_t n = (int64_t)W * H;
+#ifdef _OPENMP
+  int nt = threads > 0 ? threads : omp_get_max_threads();
+#pragma omp parallel for schedule(dynamic, 256) num_threads(nt)
+#endif
+  for (int64_t id = 0; id < n; id++) {
+    uint32_t px = (uint32_t)(id % W), py = (uint32_t)(id / W);
+    float m0 = cu[px] * cv[py], m1 = (0.0f - su[px]) * cv[py], m2 = sv[py];
+    const float *F = in->facing;
+    float dir[3], inv[3], o[3];
+    int sign[3];
+    dir[0] = F[0] * m0 + F[3] * m1 + F[6] * m2;
+    dir[1] = F[1] * m0 + F[4] * m1 + F[7] * m2;
+    dir[2] = F[2] * m0 + F[5] * m1 + F[8] * m2;
+    for (int k = 0; k < 3; k++) {
+      inv[k] = 1.0f / dir[k];
+      sign[k] = dir[k] >= 0;
+      o[k] = in->origin[k];
+    }
+    float fov = in->fov[0] / (float)in->screen_size[0];
+    const float zero_dof[2] = {0.0f, 0.0f};
+    uint64_t loc[3];
+    int nh = 0, leave = 0, steps = 0;
+    uint32_t reads = 0;
+    uint8_t depth = 1;
+    if (!oracle_trace_into_volume(o, dir, inv, fov, zero_dof, loc)) {
+      leave = 1;
+    } else {
+      for (;;) {
+        if (max_steps > 0 && steps >= max_steps) {
+          leave = 1;
+          break;
+        }
+        steps++;
+        int occupied, block = depth > B, hit = 0;
+        uint32_t addr = 0;
+        const svo_block *blk = &zero_block;
+        if (!block) {
+          uint16_t chunk = bases[oracle_pow_sum((uint8_t)(depth - 1)) + oracle_base_location(depth, loc)];
+          occupied = ((chunk >> (oracle_chunk_position(depth, loc) * 2)) & 2) == 2;
+        } else {
+          addr = block_address(blocks, n_blocks, B, depth, loc, &reads);
+          blk = node_at(blocks, n_blocks, addr);
+          occupied = ((blk->chunk >> (oracle_chunk_position(depth, loc) * 2)) & 2) == 2;
+        }
+        if (occupied && !block) {
+          depth = depth < B ? (uint8_t)(depth + 1) : (uint8_t)(B + 2);
+          continue;
+        }
+        if (occupied) {
+          float c = cone_size(cone_distance(o, loc), fov, in->dof);
+          if (c > pow2_neg(B + 2)) {
+            depth = (uint8_t)(B + 2);
+            hit = 1;
+          } else if (c > pow2_neg(depth)) {
+            depth--;
+            if (depth == B + 1) depth = B;
+            continue;
+          } else if (blk->child == SVO_NO_CHILD) {
+            hit = 1;
+          } else if (c < pow2_neg(depth + 1)) {
+            depth++;
+            continue;
+          } else {
+            hit = 1;
+          }
+          if (hit) {
+            hits[id * max_hits + nh] = block_address(blocks, n_blocks, B, depth, loc, &reads);
+            if (++nh >= max_hits) break;
+          }
+        }
+        /* empty octant, or stepping past a hit */
+        uint64_t prev[3] = {loc[0], loc[1], loc[2]};
+        oracle_traverse_chunk(depth, dir, inv, sign, loc);
+        if (leaving(loc, sign)) {
+          leave = 1;
+          break;
+        }
+        depth = oracle_compare_positions(depth, prev, loc, sign);
+        if (depth == B + 1) depth = B;
+      }
+    }
+    n_hits[id] = (uint8_t)nh;
+    leaves[id] = (uint8_t)leave;
+    float dotp = dir[0] * 0.0f + dir[1] * 0.0f + dir[2] * -1.0f;
+    uint32_t cr = 135, cg = 206, cb = 235;
+    if (dotp > 0.8f) cr = cg = cb = 255;
+    sky[3 * id + 0] = (float)(cr * 255u) / 65025.0f;
+    sky[3 * id + 1] = (float)(cg * 255u) / 65025.0f;
+    sky[3 * id + 2] = (float)(cb * 255u) / 65025.0f;
+  }
+  free(su);
+  free(cu);
+  free(sv);
+  free(cv);
+}
+
+/* FP64 compositing over hit lists: colour, loss sum((C - target)^2) / rays and,
+ * if grad != NULL, its gradient with respect to the per-node RGBA (4 doubles
+ * per node, accumulated). rgb (3 doubles per ray) may be NULL. */
+double oracle_diff_eval(const uint32_t *hits, const uint8_t *n_hits, const uint8_t *leaves, const float *sky,
+                        int64_t n_rays, int32_t max_hits, const double *params, const double *target, double *rgb,
+                        double *grad, int32_t threads) {
+  double loss = 0.0;
+  double inv_n = 1.0 / (double)n_rays;
+#ifdef _OPENMP
+  int nt = threads > 0 ? threads : omp_get_max_threads();
+#pragma omp parallel for schedule(dynamic, 1024) num_threads(nt) reduction(+ : loss)
+#endif
+  for (int64_t r = 0; r < n_rays; r++) {
+    const uint32_t *h = hits + r * max_hits;
+    double C[3] = {0, 0, 0}, T = 1.0;
+    for (int i = 0; i < n_hits[r]; i++) {
+      const double *p = params + 4ull * h[i];
+      for (int k = 0; k < 3; k++) C[k] += T * p[3] * p[k];
+      T *= 1.0 - p[3];
+    }
+    if (leaves[r])
+      for (int k = 0; k < 3; k++) C[k] += T * (double)sky[3 * r + k];
+    double G[3];
+    for (int k = 0; k < 3; k++) {
+      double e = C[k] - (target ? target[3 * r + k] : 0.0);
+      loss += e * e * inv_n;
+      G[k] = 2.0 * e * inv_n;
+      if (rgb) rgb[3 * r + k] = C[k];
+    }
+    if (!grad) continue;
+    double S[3] = {0, 0, 0};
+    T = 1.0;
+    for (int i = 0; i < n_hits[r]; i++) {
+      const double *p = params + 4ull * h[i];
+      double *g = grad + 4ull * h[i];
+      double a = p[3], ta = T * a, da = 0.0;
+      for (int k = 0; k < 3; k++) {
+        S[k] += ta * p[k];
+        double behind = C[k] - S[k];
+        da += G[k] * (T * p[k] - (1.0 - a > 0.0 ? behind / (1.0 - a) : 0.0));
+        double gk = ta * G[k];
+#ifdef _OPENMP
+#pragma omp atomic
+#endif
+        g[k] += gk;
+      }
+#ifdef _OPENMP
+#pragma omp atomic
+#endif
+      g[3] += da;
+      T *= 1.0 - a;
+    }
+  }
+  return loss;
+}
+
+/* FP64 central finite differences of the loss of oracle_diff_eval with respect
+ * to the 4 parameters of each node in `nodes` (step h). Only the rays whose hit
+ * list holds the node change with its parameters, so each difference is summed
+ * over those rays alone; nodes[] must be sorted ascending and fd receives 4
+ * doubles per listed node. */
+void oracle_diff_fd(const uint32_t *hits, const uint8_t *n_hits, const uint8_t *leaves, const float *sky,
+                    int64_t n_rays, int32_t max_hits, const double *params, const double *target, const uint32_t *nodes,
+                    int32_t n_nodes, double h, double *fd, int32_t threads) {
+  double inv_n = 1.0 / (double)n_rays;
+  memset(fd, 0, sizeof(double) * 4 * (size_t)n_nodes);
+#ifdef _OPENMP
+  int nt = threads > 0 ? threads : omp_get_max_threads();
+#pragma omp parallel for schedule(dynamic, 1024) num_threads(nt)
+#endif
+  for (int64_t r = 0; r < n_rays; r++) {
+    const uint32_t *hl = hits + r * max_hits;
+    for (int i0 = 0; i0 < n_hits[r]; i0++) {
+      /* nodes[] is sorted ascending; each listed node is differenced once per ray */
+      int32_t lo = 0, hi = n_nodes;
+      while (lo < hi) {
+        int32_t mid = (lo + hi) / 2;
+        if (nodes[mid] < hl[i0])
+          lo = mid + 1;
+        else
+          hi = mid;
+      }
+      if (lo >= n_nodes || nodes[lo] != hl[i0]) continue;
+      int seen = 0;
+      for (int i = 0; i < i0; i++) seen |= hl[i] == hl[i0];
+      if (seen) continue;
+      int32_t j = lo;
+      for (int ch = 0; ch < 4; ch++) {
+        double side[2];
+        for (int sgn = 0; sgn < 2; sgn++) {
+          double delta = sgn ? -h : h;
+          double C[3] = {0, 0, 0}, T = 1.0;
+          for (int i = 0; i < n_hits[r]; i++) {
+            double p[4];
+            for (int k = 0; k < 4; k++) p[k] = params[4ull * hl[i] + k];
+            if (hl[i] == nodes[j]) p[ch] += delta;
+            for (int k = 0; k < 3; k++) C[k] += T * p[3] * p[k];
+            T *= 1.0 - p[3];
+          }
+          if (leaves[r])
+            for (int k = 0; k < 3; k++) C[k] += T * (double)sky[3 * r + k];
+          double l = 0.0;
+          for (int k = 0; k < 3; k++) {
+            double e = C[k] - target[3 * r + k];
+            l += e * e * inv_n;
+          }
+          side[sgn] = l;
+        }
+        double v = (side[0] - side[1]) / (2.0 * h);
+#ifdef _OPENMP
+#pragma omp atomic
+#endif
+        fd[4 * j + ch] += v;
+      }
+    }
+  }
+}

@@ -66,6 +66,20 @@ int oracle_trace_into_volume(const float origin[3], const float dir[3], const fl
 /* Usage initialisation rule of MainWindow.cs:129-141. */
 void oracle_init_usage(const uint16_t *bases, uint8_t base_depth, svo_usage *usage, size_t n_groups);
 
+/* Differentiable forward model (no reference counterpart): per-ray LOD hit
+ * lists of one view, the ray continuing past each hit as if its octant were
+ * empty; then FP64 compositing, loss, analytic gradient and central finite
+ * differences over those lists. */
+void oracle_hit_lists(const uint16_t *bases, uint8_t base_depth, const svo_block *blocks, size_t n_blocks,
+                      const svo_trace_input *in, int32_t max_steps, int32_t max_hits, uint32_t *hits, uint8_t *n_hits,
+                      uint8_t *leaves, float *sky, int32_t threads);
+double oracle_diff_eval(const uint32_t *hits, const uint8_t *n_hits, const uint8_t *leaves, const float *sky,
+                        int64_t n_rays, int32_t max_hits, const double *params, const double *target, double *rgb,
+                        double *grad, int32_t threads);
+void oracle_diff_fd(const uint32_t *hits, const uint8_t *n_hits, const uint8_t *leaves, const float *sky,
+                    int64_t n_rays, int32_t max_hits, const double *params, const double *target, const uint32_t *nodes,
+                    int32_t n_nodes, double h, double *fd, int32_t threads);
+
 #ifdef __cplusplus
 }
 #endif

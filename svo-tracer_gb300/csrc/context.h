@@ -5,6 +5,8 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <array>
+#include <map>
 #include <string>
 #include <vector>
 
@@ -101,6 +103,20 @@ struct Context {
   DevBuf<uint32_t> graft_jobs, graft_targets;
   DevBuf<svo_pruning> prune_records;
   DevBuf<uint64_t> locations;
+  // ray-setup tables (sin/cos per column and row) by (fov bits, width, height)
+  std::map<std::array<uint32_t, 4>, std::vector<float>> table_cache;
+
+  // differentiable colour fitting: per-node RGBA parameters and gradients
+  DevBuf<float> params, grads, diff_rgb, diff_target;
+  DevBuf<float> diff_saved;  // forward colour as (hi, lo) float pairs, 6 per ray
+  DevBuf<double> diff_loss;
+  bool has_params = false;
+  uint64_t params_gen = 0;   // bumped by every parameter upload
+  // what diff_saved holds: the views, parameter generation and max_hits of the last forward
+  std::vector<svo_trace_input> saved_views;
+  uint64_t saved_params_gen = 0;
+  int32_t saved_max_hits = 0;
+  bool saved_valid = false;
   uint64_t n_free = 0, free_used = 0, n_pruned = 0, n_freed = 0, n_claimed = 0;
   bool free_valid = false;
   // graph cache for svo_trace_batch_graph
@@ -144,9 +160,19 @@ struct Context {
     graft_targets.release();
     prune_records.release();
     locations.release();
+    params.release();
+    grads.release();
+    diff_rgb.release();
+    diff_target.release();
+    diff_saved.release();
+    diff_loss.release();
     if (own_stream) cudaStreamDestroy(own_stream);
   }
 };
 
+
+svo_status stage_views(Context &c, const svo_trace_input *in, int32_t n, const svo_trace_output *out,
+                       bool outputs_on_device, uint32_t &total_rays, size_t &table_floats);
+svo_status prepare_launch(Context &c, int32_t n_views, uint32_t total_rays, TraceLaunch &a, bool stats);
 
 }  // namespace svo

@@ -36,6 +36,7 @@ static svo_trace_config default_config() {
   c.cadence = 16;
   c.max_steps = 1 << 16;
   c.collect_stats = 0;
+  c.max_hits = 16;
   return c;
 }
 
@@ -79,7 +80,7 @@ static int scan_tree_depth(const svo_block *blocks, size_t n_blocks, int B) {
 }
 
 // Builds the view table and trig tables for `n` views in pinned staging.
-static svo_status stage_views(Context &c, const svo_trace_input *in, int32_t n, const svo_trace_output *out,
+svo_status stage_views(Context &c, const svo_trace_input *in, int32_t n, const svo_trace_output *out,
                               bool outputs_on_device, uint32_t &total_rays, size_t &table_floats) {
   total_rays = 0;
   table_floats = 0;
@@ -126,18 +127,30 @@ static svo_status stage_views(Context &c, const svo_trace_input *in, int32_t n, 
       v.rgba = out[i].rgba ? c.o_rgba.p + 4 * out_off : nullptr;
     }
     // Ray-setup angles (wavefront.cl:566-572); sin/cos are (float)sin((double)a).
+    // Views of the same field of view and size share their tables.
     float *tb = c.h_tables.p + toff;
-    float fw = (float)W, fh = (float)H;
-    for (uint32_t x = 0; x < W; x++) {
-      float u = t.fov[0] * ((fw / 2.0f - (float)x) / fw);
-      tb[x] = (float)std::sin((double)u);
-      tb[W + x] = (float)std::cos((double)u);
+    uint32_t f0, f1;
+    std::memcpy(&f0, &t.fov[0], 4);
+    std::memcpy(&f1, &t.fov[1], 4);
+    const std::array<uint32_t, 4> key{f0, f1, W, H};
+    auto it = c.table_cache.find(key);
+    if (it == c.table_cache.end()) {
+      if (c.table_cache.size() >= 256) c.table_cache.clear();
+      std::vector<float> tab(2 * ((size_t)W + H));
+      float fw = (float)W, fh = (float)H;
+      for (uint32_t x = 0; x < W; x++) {
+        float u = t.fov[0] * ((fw / 2.0f - (float)x) / fw);
+        tab[x] = (float)std::sin((double)u);
+        tab[W + x] = (float)std::cos((double)u);
+      }
+      for (uint32_t y = 0; y < H; y++) {
+        float vv = t.fov[1] * ((fh / 2.0f - (float)y) / fh);
+        tab[2 * W + y] = (float)std::sin((double)vv);
+        tab[2 * W + H + y] = (float)std::cos((double)vv);
+      }
+      it = c.table_cache.emplace(key, std::move(tab)).first;
     }
-    for (uint32_t y = 0; y < H; y++) {
-      float vv = t.fov[1] * ((fh / 2.0f - (float)y) / fh);
-      tb[2 * W + y] = (float)std::sin((double)vv);
-      tb[2 * W + H + y] = (float)std::cos((double)vv);
-    }
+    std::memcpy(tb, it->second.data(), it->second.size() * sizeof(float));
     toff += 2 * ((size_t)W + H);
     out_off += (size_t)W * H;
     ray += W * H;
@@ -145,7 +158,7 @@ static svo_status stage_views(Context &c, const svo_trace_input *in, int32_t n, 
   return SVO_OK;
 }
 
-static svo_status prepare_launch(Context &c, int32_t n_views, uint32_t total_rays, TraceLaunch &a, bool stats) {
+svo_status prepare_launch(Context &c, int32_t n_views, uint32_t total_rays, TraceLaunch &a, bool stats) {
   a = TraceLaunch{};
   a.bases = c.bases.p;
   a.blocks = c.blocks.p;
@@ -384,10 +397,11 @@ SVO_API svo_status svo_set_trace_config(void *ctx, const svo_trace_config *cfg) 
   if (n.ray_chunk == 0) n.ray_chunk = d.ray_chunk;
   if (n.cadence == 0) n.cadence = d.cadence;
   if (n.max_steps == 0) n.max_steps = d.max_steps;
+  if (n.max_hits == 0) n.max_hits = d.max_hits;
   if (n.block_size % 32 || n.block_size < 32 || n.block_size > 256)
     return fail(SVO_ERR_INVALID_ARGUMENT, "svo_set_trace_config: block_size must be a multiple of 32 in 32..256");
   if (n.ray_chunk < 1 || n.ray_chunk > 64 || n.cadence < 1 || n.cadence > 1024 || n.max_steps < 1 || n.ctas_per_sm < 0 ||
-      n.collect_stats < 0 || n.collect_stats > 2)
+      n.collect_stats < 0 || n.collect_stats > 2 || n.max_hits < 1 || n.max_hits > 1024)
     return fail(SVO_ERR_INVALID_ARGUMENT, "svo_set_trace_config: value out of range");
   c.cfg = n;
   if (c.graph_exec) cudaGraphExecDestroy(c.graph_exec);
@@ -421,6 +435,7 @@ SVO_API svo_status svo_upload_octree(void *ctx, uint8_t base_depth, const uint16
   if (c.graph_exec) cudaGraphExecDestroy(c.graph_exec);
   c.graph_exec = nullptr;
   c.has_tree = false;
+  c.has_params = false;  // per-node parameters belong to the previous tree
   if (c.bases.reserve(n_bases) || c.blocks.reserve(budget) || c.usage.reserve(budget / 8))
     return fail(SVO_ERR_OUT_OF_MEMORY, "svo_upload_octree: device allocation failed");
   SVO_CUDA(cudaMemcpyAsync(c.bases.p, bases, n_bases * 2, cudaMemcpyHostToDevice, c.stream), "svo_upload_octree: bases");

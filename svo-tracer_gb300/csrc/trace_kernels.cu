@@ -42,337 +42,15 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
-#ifdef SVO_TRACE_DEBUG
-#include <cstdio>
-#endif
 
-#include "svo_internal.h"
+#include "trace_core.cuh"
 
 namespace svo {
 namespace {
 
-namespace cg = cooperative_groups;
-
-constexpr unsigned kFull = 0xffffffffu;
-constexpr uint64_t kAll = ~0ull;
-
-__constant__ uint32_t c_pow_sum[12] = {0,      8,       72,       584,       4680,       37448,
-                                       299592, 2396744, 19173960, 153391688, 1227133512, 0};
-
-__device__ __forceinline__ float ulong_to_unit(uint64_t x) { return __fmul_rn(__ull2float_rn(x), 0x1p-64f); }
-
-// floatToUlong (wavefront.cl:200-207); out-of-range products saturate, NaN -> 0.
-__device__ __forceinline__ uint64_t unit_to_ulong(float x) {
-  if (x >= 0.999999911f) return kAll;
-  float v = __fmul_rn(fabsf(x), 0x1p64f);
-  if (v != v) return 0;
-  if (!(v < 0x1p64f)) return kAll;
-  return __float2ull_rz(v);
-}
-
-// roundUlong (wavefront.cl:211-221)
-__device__ __forceinline__ uint64_t round_ulong(uint64_t v, int d, bool up) {
-  uint64_t mask = ~(kAll >> (d + 1));
-  if (up) return ((v & mask) + (0x8000000000000000ull >> d)) - v;
-  uint64_t out = v - ((v & mask) - 1);
-  return out >= v ? v : out;
-}
-
-__device__ __forceinline__ uint32_t spread3(uint32_t v) {
-  v &= 0x3ffu;
-  v = (v | (v << 16)) & 0x030000FFu;
-  v = (v | (v << 8)) & 0x0300F00Fu;
-  v = (v | (v << 4)) & 0x030C30C3u;
-  v = (v | (v << 2)) & 0x09249249u;
-  return v;
-}
-
-// baseLocation (wavefront.cl:405-411) for 1 <= depth <= 10.
-__device__ __forceinline__ uint32_t cell_index(int depth, uint64_t x, uint64_t y, uint64_t z) {
-  int s = 64 - depth;
-  return spread3((uint32_t)(x >> s)) | (spread3((uint32_t)(y >> s)) << 1) | (spread3((uint32_t)(z >> s)) << 2);
-}
-
-// chunkPosition (wavefront.cl:428-430)
-__device__ __forceinline__ uint32_t octant(int depth, uint64_t x, uint64_t y, uint64_t z) {
-  int s = 63 - depth;
-  return (uint32_t)(((x >> s) & 1) | (((y >> s) & 1) << 1) | (((z >> s) & 1) << 2));
-}
-
-__device__ __forceinline__ float pow2_neg(int k) { return __int_as_float((127 - k) << 23); }
-
-struct Ray {
-  uint64_t lx, ly, lz;
-  float dx, dy, dz;
-  float ix, iy, iz;
-  float ox, oy, oz;
-  float fov;
-  uint32_t id;   // pixel index within its view
-  int view;
-  int depth;
-  int steps;
-  bool sx, sy, sz;
-};
-
-struct Node {
-  uint32_t child;
-  uint32_t chunk;
-};
-
-__device__ __forceinline__ uint4 load_node(const uint4 *blocks, uint32_t n_blocks, uint32_t addr) {
-  if (addr >= n_blocks) return make_uint4(0, 0, 0, 0);
-  return __ldg(blocks + addr);
-}
-
-// traverseChunk (wavefront.cl:440-497) without the trailing setConeDepth.
-__device__ __forceinline__ void traverse(Ray &r, int depth) {
-  uint64_t d0 = round_ulong(r.lx, depth, r.sx);
-  uint64_t d1 = round_ulong(r.ly, depth, r.sy);
-  uint64_t d2 = round_ulong(r.lz, depth, r.sz);
-  float a0 = fabsf(__fmul_rn(__ull2float_rn(d0), r.ix));
-  float a1 = fabsf(__fmul_rn(__ull2float_rn(d1), r.iy));
-  float a2 = fabsf(__fmul_rn(__ull2float_rn(d2), r.iz));
-  int ax = (a0 <= a1 && a0 <= a2) ? 0 : ((a1 <= a0 && a1 <= a2) ? 1 : 2);
-  float inv = ax == 0 ? r.ix : (ax == 1 ? r.iy : r.iz);
-  float u = ulong_to_unit(ax == 0 ? d0 : (ax == 1 ? d1 : d2));
-  if (ax != 0) d0 = unit_to_ulong(__fmul_rn(__fmul_rn(r.dx, inv), u));
-  if (ax != 1) d1 = unit_to_ulong(__fmul_rn(__fmul_rn(r.dy, inv), u));
-  if (ax != 2) d2 = unit_to_ulong(__fmul_rn(__fmul_rn(r.dz, inv), u));
-  uint64_t x = r.sx ? r.lx + d0 : r.lx - d0;
-  uint64_t y = r.sy ? r.ly + d1 : r.ly - d1;
-  uint64_t z = r.sz ? r.lz + d2 : r.lz - d2;
-  if (r.sx && x == 0) x = kAll; else if (!r.sx && x == kAll) x = 0;
-  if (r.sy && y == 0) y = kAll; else if (!r.sy && y == kAll) y = 0;
-  if (r.sz && z == 0) z = kAll; else if (!r.sz && z == kAll) z = 0;
-  r.lx = x;
-  r.ly = y;
-  r.lz = z;
-}
-
-// comparePositions (wavefront.cl:413-426): the loop pops one level for every
-// consecutive level, counted upwards from `depth`, whose octant bit flipped
-// against the travel direction on some axis; it stops at level 1.
-__device__ __forceinline__ int pop_depth(const Ray &r, int depth, uint64_t px, uint64_t py, uint64_t pz) {
-  uint64_t m = (r.sx ? (px & ~r.lx) : (~px & r.lx)) | (r.sy ? (py & ~r.ly) : (~py & r.ly)) |
-               (r.sz ? (pz & ~r.lz) : (~pz & r.lz));
-  uint64_t run = ~(m >> (63 - depth));
-  int ones = __ffsll((long long)run) - 1;
-  return ones < depth ? depth - ones : 1;
-}
-
-__device__ __forceinline__ bool leaving(const Ray &r) {
-  return (!r.sx && r.lx == 0) || (!r.sy && r.ly == 0) || (!r.sz && r.lz == 0) || (r.sx && r.lx == kAll) ||
-         (r.sy && r.ly == kAll) || (r.sz && r.lz == kAll);
-}
-
-// coneSize (wavefront.cl:387-391) at the distance setConeDepth uses (:394-399).
-__device__ __forceinline__ float cone_at(const Ray &r, float dof0, float dof1) {
-  float x = __fsub_rn(r.ox, ulong_to_unit(r.lx));
-  float y = __fsub_rn(r.oy, ulong_to_unit(r.ly));
-  float z = __fsub_rn(r.oz, ulong_to_unit(r.lz));
-  float m = fabsf(__fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(x, x), __fmul_rn(y, y)), __fmul_rn(z, z))));
-  float eye = __fmul_rn(r.fov, m);
-  float f = fabsf(__fmul_rn(dof0, __fsub_rn(dof1, m)));
-  return eye < f ? f : eye;
-}
-
-// traceIntoVolume (wavefront.cl:639-1088): enter the unit cube on the face of
-// the outside slab with the largest entry distance (ties x, then y); reject
-// when the entry point is outside the cube grown by the cone size.
-__device__ __forceinline__ bool enter_volume(Ray &r) {
-  const float o[3] = {r.ox, r.oy, r.oz};
-  const float d[3] = {r.dx, r.dy, r.dz};
-  const float iv[3] = {r.ix, r.iy, r.iz};
-  bool lo[3], hi[3], any = false;
-#pragma unroll
-  for (int k = 0; k < 3; k++) {
-    lo[k] = o[k] < 0.0f;
-    hi[k] = o[k] > 1.0f;
-    any |= lo[k] | hi[k];
-  }
-  if (!any) {
-    r.lx = unit_to_ulong(o[0]);
-    r.ly = unit_to_ulong(o[1]);
-    r.lz = unit_to_ulong(o[2]);
-    return true;
-  }
-#pragma unroll
-  for (int k = 0; k < 3; k++)
-    if ((lo[k] || hi[k]) && d[k] == 0.0f) return false;
-#pragma unroll
-  for (int k = 0; k < 3; k++) {
-    bool pos = d[k] >= 0.0f;
-    if ((lo[k] && !pos) || (hi[k] && pos)) return false;
-  }
-  float mk[3];
-#pragma unroll
-  for (int k = 0; k < 3; k++) mk[k] = (lo[k] || hi[k]) ? fabsf(__fmul_rn(__fsub_rn(hi[k] ? 1.0f : 0.0f, o[k]), iv[k])) : 0.0f;
-  bool ox = lo[0] || hi[0], oy = lo[1] || hi[1], oz = lo[2] || hi[2];
-  int axis;
-  if (ox && oy && oz)
-    axis = (mk[0] >= mk[1] && mk[0] >= mk[2]) ? 0 : ((mk[1] >= mk[0] && mk[1] >= mk[2]) ? 1 : 2);
-  else if (ox && oy)
-    axis = mk[0] >= mk[1] ? 0 : 1;
-  else if (ox && oz)
-    axis = mk[0] >= mk[2] ? 0 : 2;
-  else if (oy && oz)
-    axis = mk[1] >= mk[2] ? 1 : 2;
-  else
-    axis = ox ? 0 : (oy ? 1 : 2);
-  float m = mk[axis];
-  float p[3];
-#pragma unroll
-  for (int k = 0; k < 3; k++) p[k] = (k == axis) ? (hi[k] ? 1.0f : 0.0f) : __fadd_rn(o[k], __fmul_rn(d[k], m));
-  r.lx = unit_to_ulong(p[0]);
-  r.ly = unit_to_ulong(p[1]);
-  r.lz = unit_to_ulong(p[2]);
-  // DoF of a fresh TraceData is zero (setupInitialTrace leaves it unset).
-  float eye = __fmul_rn(r.fov, m);
-  float f = fabsf(__fmul_rn(0.0f, __fsub_rn(0.0f, m)));
-  float c = eye < f ? f : eye;
-#pragma unroll
-  for (int k = 0; k < 3; k++)
-    if (p[k] < -c || p[k] > __fadd_rn(1.0f, c)) return false;
-  return true;
-}
-
-struct Stats {
-  unsigned long long rays, hits, base_steps, block_reads, block_steps, requests, limited;
-};
-
-// Claims `per_lane` consecutive slots of a device counter for every lane of `g`
-// with one atomic; returns this lane's first slot. Only the lanes present in `g`
-// take part, so lanes may arrive here (or leave the kernel) independently.
-__device__ __forceinline__ uint32_t claim(cg::coalesced_group &g, uint32_t *counter, uint32_t per_lane) {
-  uint32_t base = 0;
-  if (g.thread_rank() == 0) base = atomicAdd(counter, g.size() * per_lane);
-  return g.shfl(base, 0) + g.thread_rank();
-}
-
-// Per-thread traversal state besides the ray itself.
-struct Walk {
-  uint32_t *path;  // path[level * stride]: node address of each level below B+2
-  int stride;
-  uint32_t cur_addr, cur_child, cur_chunk;  // last node read
-  uint32_t last_group;                      // last usage group stamped
-  uint32_t v_block, v_base;                 // reference-walk counters (stats launches)
-};
-
-enum : int { kStepOn = 0, kStepBackground = 1, kStepHit = 2 };
-
-// One runBaseTrace (wavefront.cl:1400-1463) or runBlockTrace (:1465-1566) step.
-// Both read a 2-bit octant pair from a chunk (a base chunk or the current
-// node's) and share the empty-octant stepping code, so lanes at base and block
-// levels run it together.
-template <bool kStats, bool kSmemBases>
-__device__ __forceinline__ int step(const TraceLaunch &a, const ViewParams &v, const uint16_t *s_bases,
-                                    const uint4 *blocks, int B, Ray &r, Walk &w, Stats &st) {
-  if (r.depth == 0) return kStepBackground;
-  if (a.max_steps > 0 && r.steps >= a.max_steps) {
-    if (kStats) st.limited++;
-    return kStepBackground;
-  }
-  r.steps++;
-  const bool block = r.depth > B;
-  const int lvl = r.depth - (B + 2);
-  uint32_t chunk;
-  if (!block) {
-    uint32_t idx = c_pow_sum[r.depth - 1] + cell_index(r.depth, r.lx, r.ly, r.lz);
-    chunk = kSmemBases ? s_bases[idx] : __ldg(a.bases + idx);
-    if (kStats) w.v_base++;
-  } else {
-    uint32_t addr = w.path[lvl * w.stride];
-    if (addr != w.cur_addr) {
-      uint4 nd = load_node(blocks, a.n_blocks, addr);
-      w.cur_addr = addr;
-      w.cur_child = nd.x;
-      w.cur_chunk = nd.y & 0xffffu;
-    }
-    chunk = w.cur_chunk;
-    if (kStats) {
-      w.v_block += (uint32_t)(r.depth - B - 1);
-      st.block_steps++;
-    }
-    uint32_t group = addr >> 3;
-    if (a.usage && group != w.last_group && group < a.n_groups) {
-      // updateUsage (wavefront.cl:377-381)
-      uint16_t *tick = reinterpret_cast<uint16_t *>(a.usage + group);
-      uint16_t cur = *tick;
-      if (cur < 65534 && cur != v.tick) *tick = v.tick;
-      w.last_group = group;
-    }
-  }
-  if (((chunk >> (octant(r.depth, r.lx, r.ly, r.lz) * 2)) & 2) == 0) {
-    // empty octant: step to the neighbouring cell and pop (traverseChunk, comparePositions)
-    uint64_t px = r.lx, py = r.ly, pz = r.lz;
-    traverse(r, r.depth);
-    if (leaving(r)) return kStepBackground;
-    int nd = pop_depth(r, r.depth, px, py, pz);
-    if (block && nd >= B + 2 && (((px ^ r.lx) | (py ^ r.ly) | (pz ^ r.lz)) >> (64 - nd)) != 0) {
-      // an ancestor cell changed: rebuild the path like getBlockAddress
-      uint32_t n = cell_index(B + 2, r.lx, r.ly, r.lz);
-      w.path[0] = n;
-      for (int d = B + 2; d < nd; d++) {
-        uint4 n2 = load_node(blocks, a.n_blocks, n);
-        n = n2.x + octant(d, r.lx, r.ly, r.lz);
-        w.path[(d - B - 1) * w.stride] = n;
-      }
-    }
-    r.depth = nd == B + 1 ? B : nd;
-    return kStepOn;
-  }
-  if (!block) {
-    // geometry below a base cell: descend, jumping from level B to B+2
-    if (r.depth < B) {
-      r.depth++;
-    } else {
-      r.depth = B + 2;
-      w.path[0] = cell_index(B + 2, r.lx, r.ly, r.lz);
-    }
-    return kStepOn;
-  }
-  // geometry below a node: the cone LOD decision (ConeDepth = -half_log2(c))
-  float c = cone_at(r, v.dof[0], v.dof[1]);
-  if (c > pow2_neg(B + 2)) {
-    r.depth = B + 2;
-    return kStepHit;
-  }
-  if (c > pow2_neg(r.depth)) {
-    r.depth--;
-    if (r.depth == B + 1) r.depth = B;
-    return kStepOn;
-  }
-  if (w.cur_child == SVO_NO_CHILD) {
-    // requestChild (wavefront.cl:362-375): one atomic per group of requesting lanes
-    cg::coalesced_group g = cg::coalesced_threads();
-    uint32_t slot = claim(g, a.request_count, 1);
-    if (kStats) st.requests++;
-    if (slot < a.request_cap && a.requests) {
-      svo_child_request q;
-      q.address = w.cur_addr;
-      q.tick = 0;  // TraceData.Tick is never set by resolveTrace
-      q.depth = (uint8_t)r.depth;
-      q._pad0 = 0;
-      q.location[0] = r.lx;
-      q.location[1] = r.ly;
-      q.location[2] = r.lz;
-      q.tree_size = c <= pow2_neg(r.depth + 1) ? 1 : 0;
-      for (int k = 0; k < 7; k++) q._pad1[k] = 0;
-      a.requests[slot] = q;
-    }
-    return kStepHit;
-  }
-  if (c < pow2_neg(r.depth + 1) && lvl + 1 < a.path_levels) {
-    w.path[(lvl + 1) * w.stride] = w.cur_child + octant(r.depth, r.lx, r.ly, r.lz);
-    r.depth++;
-    return kStepOn;
-  }
-  return kStepHit;
-}
-
 template <bool kStats, bool kSmemBases>
 #ifndef SVO_TRACE_MIN_CTAS
-#define SVO_TRACE_MIN_CTAS 1
+#define SVO_TRACE_MIN_CTAS 4
 #endif
 __global__ void __launch_bounds__(256, SVO_TRACE_MIN_CTAS) trace_kernel(const TraceLaunch a) {
   extern __shared__ __align__(16) uint8_t smem[];
@@ -449,47 +127,12 @@ __global__ void __launch_bounds__(256, SVO_TRACE_MIN_CTAS) trace_kernel(const Tr
       // later rays of this chunk, and every later claim, are larger still
       if (my >= a.total_rays) break;  // queue drained
       ray_global = my;
-      int lo = 0, hi = a.n_views - 1;  // views are sorted by ray_begin
-      while (lo < hi) {
-        int mid = (lo + hi + 1) >> 1;
-        if (s_views[mid].ray_begin <= my)
-          lo = mid;
-        else
-          hi = mid - 1;
-      }
-      const ViewParams &v = s_views[lo];
-      r.view = lo;
-      r.id = my - v.ray_begin;
-      uint32_t px = r.id % v.width, py = r.id / v.width;
-      const float *tb = a.tables + v.table_off;
-      float su = __ldg(tb + px), cu = __ldg(tb + v.width + px);
-      float sv = __ldg(tb + 2 * v.width + py), cv = __ldg(tb + 2 * v.width + v.height + py);
-      // setupInitialTrace (wavefront.cl:563-595)
-      float m0 = __fmul_rn(cu, cv);
-      float m1 = __fmul_rn(__fsub_rn(0.0f, su), cv);
-      float m2 = sv;
-      const float *F = v.facing;
-      r.dx = __fadd_rn(__fadd_rn(__fmul_rn(F[0], m0), __fmul_rn(F[3], m1)), __fmul_rn(F[6], m2));
-      r.dy = __fadd_rn(__fadd_rn(__fmul_rn(F[1], m0), __fmul_rn(F[4], m1)), __fmul_rn(F[7], m2));
-      r.dz = __fadd_rn(__fadd_rn(__fmul_rn(F[2], m0), __fmul_rn(F[5], m1)), __fmul_rn(F[8], m2));
-      r.ix = __frcp_rn(r.dx);
-      r.iy = __frcp_rn(r.dy);
-      r.iz = __frcp_rn(r.dz);
-      r.sx = r.dx >= 0.0f;
-      r.sy = r.dy >= 0.0f;
-      r.sz = r.dz >= 0.0f;
-      r.ox = v.origin[0];
-      r.oy = v.origin[1];
-      r.oz = v.origin[2];
-      r.fov = v.fov_px;
-      r.depth = 1;
-      r.steps = 0;
+      setup_ray(a, s_views, my, r);
       w.v_block = 0;
       w.v_base = 0;
       w.cur_addr = kFull;
       w.last_group = kFull;
       have = true;
-      if (!enter_volume(r)) r.depth = 0;  // background at once
     }
 
     // ---- up to `cadence` traversal steps; retire finished rays together -------
@@ -520,14 +163,7 @@ __global__ void __launch_bounds__(256, SVO_TRACE_MIN_CTAS) trace_kernel(const Tr
         st.hits++;
       }
     } else {
-      float dotp = __fadd_rn(__fadd_rn(__fmul_rn(r.dx, 0.0f), __fmul_rn(r.dy, 0.0f)), __fmul_rn(r.dz, -1.0f));
-      if (dotp > 0.8f) {
-        cr = cg_ = cb = 255;  // luminosity (uchar)(dot*200) >= 160 > 0
-      } else {
-        cr = 135;
-        cg_ = 206;
-        cb = 235;
-      }
+      sky_colour(r, cr, cg_, cb);
     }
     const float fw = 65025.0f;  // (float)255 * 255.0f
     float4 px;

@@ -83,7 +83,7 @@ class TraceStatsC(C.Structure):
 
 class TraceConfigC(C.Structure):
     _fields_ = [(n, C.c_int32) for n in ("block_size", "ctas_per_sm", "ray_chunk", "cadence", "max_steps",
-                                          "collect_stats", "_pad0", "_pad1")]
+                                          "collect_stats", "max_hits", "_pad0")]
 
 
 class SceneParamsC(C.Structure):
@@ -153,6 +153,12 @@ def load_library(path: str | None = None) -> C.CDLL:
         "svo_tree_data": ([vp, C.POINTER(vp), C.POINTER(vp)], C.c_int32),
         "svo_tree_free": ([vp], C.c_int32),
         "svo_init_usage_tree": ([vp, C.c_uint16], C.c_int32),
+        "svo_diff_set_params": ([vp, vp, sz, C.c_int32], C.c_int32),
+        "svo_diff_get_grads": ([vp, vp, sz, C.c_int32], C.c_int32),
+        "svo_diff_forward": ([vp, C.POINTER(TraceInputC), C.c_int32, vp, C.c_int32], C.c_int32),
+        "svo_diff_backward": ([vp, C.POINTER(TraceInputC), C.c_int32, vp, C.c_int32, C.c_int32,
+                               C.POINTER(C.c_double)],
+                              C.c_int32),
         "svo_gc": ([vp, C.POINTER(UpdateInputC), C.POINTER(GcReportC)], C.c_int32),
         "svo_read_gc_lists": ([vp, vp, sz, vp, sz, vp, sz], C.c_int32),
         "svo_graft": ([vp, C.POINTER(UpdateInputC), vp, C.c_uint32, vp, sz, vp, sz, C.POINTER(GraftReportC)], C.c_int32),
@@ -406,6 +412,81 @@ def camera_path(seed: int = 3, frames: int = 120, width: int = 1920, height: int
     return out
 
 
+def node_cells(tree: Octree):
+    """Integer cell coordinates (at the node's own depth) and depth of every node
+    reachable from the dense level B+2; unreachable nodes get depth 0. The dense
+    level is indexed by baseLocation(B + 2) (wavefront.cl:405-411), but only the
+    groups below a mixed level-(B+1) base octant hold level-(B+2) nodes
+    (PopulateInitialBlocks, TreeBuilder.cs:180-227); the others are reused for
+    deeper groups. Node `child + o` of a depth-d node is the octant
+    o = x + 2y + 4z (chunkPosition, wavefront.cl:428-430) of its cell at depth d + 1."""
+    B = tree.BaseDepth
+    d0 = B + 2
+    n = len(tree.Blocks)
+    child = tree.Blocks["child"]
+    cells = np.zeros((n, 3), np.int64)
+    depth = np.zeros(n, np.uint8)
+    pos = np.arange(8 ** (B + 1), dtype=np.int64)
+    chunk = tree.BaseBlocks[pow_sum(B - 1) + (pos >> 3)].astype(np.int64)
+    populated = pos[((chunk >> ((pos & 7) * 2)) & 3) == 3]
+    front = (populated[:, None] * 8 + np.arange(8)).reshape(-1)
+    front = front[front < n]
+    xyz = np.zeros((len(front), 3), np.int64)
+    for i in range(d0):
+        dig = (front >> (3 * (d0 - 1 - i))) & 7
+        xyz = xyz * 2 + np.stack([dig & 1, (dig >> 1) & 1, (dig >> 2) & 1], axis=1)
+    cells[front] = xyz
+    depth[front] = d0
+    octs = np.array([[o & 1, (o >> 1) & 1, (o >> 2) & 1] for o in range(8)], np.int64)
+    d = d0
+    while len(front):
+        ch = child[front]
+        keep = ch != 0xFFFFFFFF
+        par, first = front[keep], ch[keep].astype(np.int64)
+        kids = (first[:, None] + np.arange(8)).reshape(-1)
+        kc = (cells[par][:, None, :] * 2 + octs[None]).reshape(-1, 3)
+        ok = (kids < n) & (depth[np.minimum(kids, n - 1)] == 0)
+        kids, kc = kids[ok], kc[ok]
+        cells[kids] = kc
+        depth[kids] = d + 1
+        front = kids
+        d += 1
+    return cells, depth
+
+
+def sinusoid_field(tree: Octree, seed: int = 9, opacity: float = 0.9) -> np.ndarray:
+    """Ground-truth per-node RGBA of the differentiable colour-fitting workload:
+    channel k = 0.5 + 0.5 sin(2 pi f_k (u_k . x) + phi_k) at the node's cell
+    centre x, with a seeded frequency f_k uniform in [1, 4], a seeded unit
+    direction u_k and phase phi_k; alpha = `opacity`. float32 [n_nodes, 4]."""
+    rng = np.random.default_rng(seed)
+    cells, depth = node_cells(tree)
+    centre = (cells + 0.5) / np.exp2(depth.astype(np.float64))[:, None]
+    out = np.zeros((len(cells), 4), np.float32)
+    for k in range(3):
+        u = rng.normal(size=3)
+        u /= np.linalg.norm(u)
+        f = rng.uniform(1.0, 4.0)
+        phi = rng.uniform(0.0, 2.0 * math.pi)
+        out[:, k] = 0.5 + 0.5 * np.sin(2.0 * math.pi * f * (centre @ u) + phi)
+    out[:, 3] = opacity
+    out[depth == 0] = 0.0
+    return out
+
+
+def orbit_views(seed: int = 11, n: int = 16, width: int = 512, height: int = 512, distance: float = 1.5,
+                fov: float = 60.0, centre=(0.5, 0.5, 0.5), **kw):
+    """n pinhole views at `distance` from `centre` on seeded directions, looking
+    at the centre (the colour-fitting workload's target views)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(n):
+        u = rng.normal(size=3)
+        u /= np.linalg.norm(u)
+        out.append(look_at(np.asarray(centre) + distance * u, centre, width, height, fov, **kw))
+    return out
+
+
 @dataclass
 class TraceResult:
     hit_index: np.ndarray
@@ -557,6 +638,49 @@ class Tracer:
         vb, vs = np.zeros(n, np.uint32), np.zeros(n, np.uint32)
         _check("RayCounts", self._lib.svo_read_ray_counts(self._ctx, _ptr(vb), _ptr(vs), n))
         return vb, vs
+
+    # ---- differentiable colour fitting ----------------------------------------
+    def diff_set_params(self, rgba: np.ndarray) -> None:
+        p = np.ascontiguousarray(rgba, np.float32).reshape(-1, 4)
+        _check("DiffSetParams", self._lib.svo_diff_set_params(self._ctx, _ptr(p), len(p), 0))
+
+    def diff_grads(self, n_nodes: int) -> np.ndarray:
+        g = np.zeros((n_nodes, 4), np.float32)
+        _check("DiffGrads", self._lib.svo_diff_get_grads(self._ctx, _ptr(g), n_nodes, 0))
+        return g
+
+    def diff_forward(self, views) -> np.ndarray:
+        n = sum(v.ScreenSize[0] * v.ScreenSize[1] for v in views)
+        out = np.zeros((n, 3), np.float32)
+        c_in = (TraceInputC * len(views))(*[v.to_c() for v in views])
+        _check("DiffForward", self._lib.svo_diff_forward(self._ctx, c_in, len(views), _ptr(out), 0))
+        return out
+
+    def diff_backward(self, views, target: np.ndarray, use_saved: bool = False) -> float:
+        """Loss and per-node gradients (read with diff_grads). use_saved: take the
+        colour from the last diff_forward over the same views and parameters
+        (one traversal per ray instead of two)."""
+        t = np.ascontiguousarray(target, np.float32).reshape(-1, 3)
+        loss = C.c_double()
+        c_in = (TraceInputC * len(views))(*[v.to_c() for v in views])
+        _check("DiffBackward", self._lib.svo_diff_backward(self._ctx, c_in, len(views), _ptr(t), int(use_saved), 0,
+                                                           C.byref(loss)))
+        return loss.value
+
+    def diff_set_params_device(self, ptr: int, n_nodes: int) -> None:
+        _check("DiffSetParams", self._lib.svo_diff_set_params(self._ctx, C.c_void_p(ptr), n_nodes, 1))
+
+    def diff_forward_device(self, views, rgb_ptr: int) -> None:
+        """Forward colour into a caller-owned device buffer (3 floats per ray)."""
+        c_in = (TraceInputC * len(views))(*[v.to_c() for v in views])
+        _check("DiffForward", self._lib.svo_diff_forward(self._ctx, c_in, len(views), C.c_void_p(rgb_ptr), 1))
+
+    def diff_backward_device(self, views, target_ptr: int, use_saved: bool = False) -> None:
+        """Backward against a device-resident target; the loss stays on the device
+        (no synchronisation) and the gradients in the context."""
+        c_in = (TraceInputC * len(views))(*[v.to_c() for v in views])
+        _check("DiffBackward", self._lib.svo_diff_backward(self._ctx, c_in, len(views), C.c_void_p(target_ptr),
+                                                           int(use_saved), 1, None))
 
     # ---- tree updates --------------------------------------------------------
     @staticmethod

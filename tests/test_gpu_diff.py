@@ -1,0 +1,171 @@
+"""Differentiable colour fitting through the C ABI against the FP64 oracle:
+forward colour, loss, the per-node RGBA gradient against the FP64 analytic
+gradient and FP64 central finite differences (h = 1e-4, 256 random hit nodes),
+and a descent step that lowers the loss."""
+import numpy as np
+import pytest
+
+import pyoracle as po
+import svo_tracer as st
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(autouse=True)
+def default_config(tracer):
+    tracer.set_config(block_size=256, ctas_per_sm=0, ray_chunk=1, cadence=16, max_steps=1 << 16, collect_stats=0,
+                      max_hits=16)
+    yield
+    tracer.set_config(max_hits=16)
+
+
+@pytest.fixture(scope="module")
+def fitting():
+    """The colour-fitting workload at test size: the depth-9 SDF sphere, 4 views of
+    128x96 around it, FP32 parameters uniform in [0, 1], targets rendered in FP64
+    from the sinusoid ground-truth field (opacity 0.9)."""
+    tree = st.TreeBuilder(st.SCENE_SPHERE, seed=1).BuildTree(4, 9)
+    views = st.orbit_views(seed=7, n=4, width=128, height=96)
+    hl = po.HitLists(tree, views, max_hits=16)
+    rng = np.random.default_rng(3)
+    params = rng.uniform(0.0, 1.0, size=(len(tree.Blocks), 4)).astype(np.float32)
+    _, target, _ = hl.eval(st.sinusoid_field(tree).astype(np.float64), want_rgb=True)
+    return tree, views, hl, params, target.astype(np.float32)
+
+
+def test_forward_matches_fp64(tracer, fitting):
+    tree, views, hl, params, _ = fitting
+    tracer.upload(tree)
+    tracer.diff_set_params(params)
+    rgb = tracer.diff_forward(views)
+    _, want, _ = hl.eval(params.astype(np.float64), want_rgb=True)
+    err = np.abs(rgb - want)
+    assert err.max() <= 1e-5, "max |C - C64| = %g" % err.max()
+    assert (hl.n_hits > 1).sum() > 1000  # the rays composite several hits
+
+
+def test_alpha_one_forward_is_the_trace_image(tracer, fitting):
+    """With alpha = 1 compositing stops at the first hit, so the forward colour is
+    the trace's shaded RGBA (node colour, sky where the ray misses)."""
+    tree, views, _, _, _ = fitting
+    tracer.upload(tree)
+    p = np.zeros((len(tree.Blocks), 4), np.float32)
+    p[:, 0] = tree.Blocks["colour_r"] / np.float32(255)
+    p[:, 1] = tree.Blocks["colour_g"] / np.float32(255)
+    p[:, 2] = tree.Blocks["colour_b"] / np.float32(255)
+    p[:, 3] = 1.0
+    tracer.diff_set_params(p)
+    rgb = tracer.diff_forward(views)
+    off = 0
+    for v in views:
+        n = v.ScreenSize[0] * v.ScreenSize[1]
+        img = tracer.trace(v).rgba.reshape(n, 4)[:, :3]
+        err = np.abs(rgb[off:off + n] - img).max()
+        assert err <= 1e-6, "max |C - trace rgba| = %g" % err
+        off += n
+
+
+def test_backward_matches_fp64_gradient(tracer, fitting):
+    tree, views, hl, params, target = fitting
+    tracer.upload(tree)
+    tracer.diff_set_params(params)
+    loss = tracer.diff_backward(views, target)
+    grad = tracer.diff_grads(len(tree.Blocks))
+    want_loss, _, want = hl.eval(params.astype(np.float64), target.astype(np.float64), want_grad=True)
+    assert abs(loss - want_loss) <= 1e-9 * want_loss, (loss, want_loss)
+    scale = np.abs(want).max()
+    err = np.abs(grad - want)
+    ok = err <= 1e-4 * np.abs(want) + 1e-6 * scale
+    assert ok.all(), "%d of %d entries off, max err %g (scale %g)" % ((~ok).sum(), ok.size, err.max(), scale)
+    assert not grad[np.abs(want).sum(1) == 0].any()
+
+
+def test_backward_matches_fp64_finite_differences(tracer, fitting):
+    """The acceptance check of the adjoint: within 1e-3 relative of FP64 central
+    differences (h = 1e-4) on 256 random nodes that rays hit. Entries below
+    1e-5 of the largest are held to 1e-3 of that absolute floor instead, where
+    the FP32 gradient sums cancel."""
+    tree, views, hl, params, target = fitting
+    tracer.upload(tree)
+    tracer.diff_set_params(params)
+    tracer.diff_backward(views, target)
+    grad = tracer.diff_grads(len(tree.Blocks))
+    touched = np.unique(hl.hits[np.arange(hl.max_hits)[None] < hl.n_hits[:, None]])
+    nodes = np.random.default_rng(11).choice(touched, 256, replace=False)
+    fd = hl.finite_differences(params.astype(np.float64), target.astype(np.float64), nodes, h=1e-4)
+    g = grad[nodes].astype(np.float64)
+    floor = 1e-5 * np.abs(fd).max()
+    rel = np.abs(g - fd) / np.maximum(np.abs(fd), floor)
+    assert rel.max() <= 1e-3, "max relative error %g" % rel.max()
+    assert (np.abs(fd) > floor).mean() > 0.6  # most entries are held to the relative bound
+
+
+def test_backward_with_saved_forward_colour(tracer, fitting):
+    """The backward fed with the forward's saved colour (one traversal) gives the
+    recomputing backward's loss and gradients; a saved colour of other views or
+    other parameters is refused."""
+    tree, views, hl, params, target = fitting
+    tracer.upload(tree)
+    tracer.diff_set_params(params)
+    loss_r = tracer.diff_backward(views, target)
+    grad_r = tracer.diff_grads(len(tree.Blocks))
+    with pytest.raises(st.SvoError):
+        tracer.diff_backward(views, target, use_saved=True)  # no forward yet for these parameters
+    tracer.diff_forward(views)
+    loss_s = tracer.diff_backward(views, target, use_saved=True)
+    grad_s = tracer.diff_grads(len(tree.Blocks))
+    assert abs(loss_s - loss_r) <= 1e-12 * loss_r
+    scale = np.abs(grad_r).max()
+    assert np.abs(grad_s - grad_r).max() <= 1e-6 * scale  # the same sums in another atomic order
+    with pytest.raises(st.SvoError):
+        tracer.diff_backward(views[:2], target[:2 * 128 * 96], use_saved=True)
+    tracer.diff_set_params(params)
+    with pytest.raises(st.SvoError):
+        tracer.diff_backward(views, target, use_saved=True)
+
+
+def test_descent_lowers_loss(tracer, fitting):
+    tree, views, _, params, target = fitting
+    tracer.upload(tree)
+    p = params.copy()
+    losses = []
+    for _ in range(6):
+        tracer.diff_set_params(p)
+        losses.append(tracer.diff_backward(views, target))
+        g = tracer.diff_grads(len(tree.Blocks))
+        hit = np.abs(g).sum(1) > 0
+        # per-node normalised step (each node's gradient scales with the pixels it covers)
+        step = g / np.maximum(np.abs(g).max(1, keepdims=True), 1e-30)
+        p[hit] = np.clip(p[hit] - 0.02 * step[hit], 0.0, 1.0)
+    assert all(b < a for a, b in zip(losses, losses[1:])), losses
+    assert losses[-1] < 0.9 * losses[0]
+
+
+def test_multi_view_batch_equals_single_views(tracer, fitting):
+    tree, views, _, params, target = fitting
+    tracer.upload(tree)
+    tracer.diff_set_params(params)
+    both = tracer.diff_forward(views[:2])
+    n0 = views[0].ScreenSize[0] * views[0].ScreenSize[1]
+    assert np.array_equal(both[:n0], tracer.diff_forward(views[:1]))
+    assert np.array_equal(both[n0:], tracer.diff_forward(views[1:2]))
+
+
+def test_max_hits_limits_compositing(tracer, fitting):
+    tree, views, _, params, _ = fitting
+    tracer.upload(tree)
+    tracer.diff_set_params(params)
+    tracer.set_config(max_hits=2)
+    rgb = tracer.diff_forward(views[:1])
+    hl2 = po.HitLists(tree, views[:1], max_hits=2)
+    _, want, _ = hl2.eval(params.astype(np.float64), want_rgb=True)
+    assert np.abs(rgb - want).max() <= 1e-5
+    with pytest.raises(st.SvoError):
+        tracer.set_config(max_hits=2000)  # 1..1024; 0 keeps the current value
+
+
+def test_diff_without_params_fails(tracer):
+    tree = st.TreeBuilder(st.SCENE_SPHERE, seed=2).BuildTree(2, 5)
+    tracer.upload(tree)
+    with pytest.raises(st.SvoError):
+        tracer.diff_forward(st.orbit_views(n=1, width=8, height=8))
