@@ -296,7 +296,7 @@ def diff_workload(torch, dev, flush, args):
     import svo_tracer as st
 
     tree = st.TreeBuilder(st.SCENE_SPHERE, seed=1).BuildTree(4, 9)
-    views = st.orbit_views(seed=7, n=16, width=512, height=512)
+    views = st.orbit_views(seed=7, n=args.diff_views, width=args.diff_size, height=args.diff_size)
     rays = sum(v.ScreenSize[0] * v.ScreenSize[1] for v in views)
     nodes = len(tree.Blocks)
     tr = st.Tracer(dev)
@@ -352,7 +352,8 @@ def _diff_timed(tr, torch, dev, stream, flush, args, tree, views, rays, nodes):
         tr.diff_grads(nodes)
     e2e_s = (time.perf_counter() - t0) / steps
     tr.close()
-    return {"workload": "depth-9 SDF sphere, 16 views 512x512, FP32 per-node RGBA, max 16 hits per ray",
+    return {"workload": "depth-9 SDF sphere, %d views %dx%d, FP32 per-node RGBA, max 16 hits per ray"
+                        % (len(views), views[0].ScreenSize[0], views[0].ScreenSize[1]),
             "nodes": nodes, "rays": rays, "fwd_ms": fwd_ms, "bwd_ms": bwd_ms, "fwd_bwd_ms": step_ms,
             "bwd_recompute_colour_ms": bwd_recompute_ms,
             "fwd_bwd_mrays_s": rays / step_ms / 1e3, "fwd_mrays_s": rays / fwd_ms / 1e3,
@@ -380,6 +381,8 @@ def run_ours(args, rank, world):
     tr.set_stream(stream.cuda_stream)
     tr.upload(tree)
     tr.init_usage()
+    if args.schedule:
+        tr.set_config(schedule={"lane": st.SCHEDULE_LANE, "warp": st.SCHEDULE_WARP}[args.schedule])
     n = WIDTH * HEIGHT
 
     # algorithmic bytes of one frame (counting launch, untimed)
@@ -497,6 +500,9 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-multiview", action="store_true")
     ap.add_argument("--no-diff", action="store_true")
+    ap.add_argument("--schedule", choices=["lane", "warp"], default=None)
+    ap.add_argument("--diff-views", type=int, default=16)
+    ap.add_argument("--diff-size", type=int, default=512)
     ap.add_argument("--stream-frames", type=int, default=120)
     ap.add_argument("--width", type=int, default=WIDTH)
     ap.add_argument("--height", type=int, default=HEIGHT)

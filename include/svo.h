@@ -47,7 +47,8 @@ enum {
   SVO_ERR_STEP_LIMIT = 7,  /* a ray exceeded the per-ray step limit */
   SVO_ERR_BUDGET = 8,      /* block budget exhausted (builder, graft) */
   SVO_ERR_NO_DEVICE = 9,   /* no usable CUDA device / kernel image */
-  SVO_ERR_INTERNAL = 10
+  SVO_ERR_INTERNAL = 10,
+  SVO_ERR_IO = 11          /* a file could not be opened, read or written, or is truncated */
 };
 
 /* Sentinels of the reference format. */
@@ -178,8 +179,14 @@ typedef struct svo_trace_config {
   int32_t max_steps;    /* per-ray step limit */
   int32_t collect_stats; /* 0 none, 1 totals (svo_last_trace_stats), 2 totals and per-ray counts */
   int32_t max_hits;     /* differentiable forward: LOD hits composited per ray (1..1024) */
-  int32_t _pad;
+  int32_t schedule;     /* SVO_SCHEDULE_LANE or SVO_SCHEDULE_WARP */
 } svo_trace_config;
+
+/* Ray scheduling of the persistent trace kernel. LANE: each thread claims rays
+ * on its own and finished rays are replaced every `cadence` steps. WARP: each
+ * warp claims 32 consecutive rays, runs them to the end and regroups before the
+ * next claim (ray_chunk and cadence unused). Results are identical. */
+enum { SVO_SCHEDULE_LANE = 1, SVO_SCHEDULE_WARP = 2 };
 
 /* ---- context ------------------------------------------------------------ */
 
@@ -361,6 +368,18 @@ SVO_API svo_status svo_tree_info(void *tree, uint8_t *base_depth, size_t *n_base
                                  uint32_t *block_count);
 SVO_API svo_status svo_tree_data(void *tree, const uint16_t **bases, const svo_block **blocks);
 SVO_API svo_status svo_tree_free(void *tree);
+
+/* The .oct tree file of OctreeSerializer (SvoTracer.Domain/Serializers/
+ * OctreeSerializer.cs:13-45, BlockSerializer.cs), little-endian: BaseDepth (1
+ * byte), BlockCount (uint32), powSum(BaseDepth) base chunks (uint16 each),
+ * then 16-byte blocks. svo_oct_write writes every block given (the reference
+ * writes its whole Blocks array); svo_oct_read reads BlockCount blocks and
+ * ignores anything after them, like the reference's Deserialize, and returns a
+ * tree handle for svo_tree_info / svo_tree_data / svo_tree_free (TreeManager.
+ * SaveTree / LoadTree, SvoTracer.Domain/TreeManager.cs:29-58). */
+SVO_API svo_status svo_oct_write(const char *path, uint8_t base_depth, uint32_t block_count, const uint16_t *bases,
+                                 size_t n_bases, const svo_block *blocks, size_t n_blocks);
+SVO_API svo_status svo_oct_read(const char *path, void **tree);
 
 /* A persistent scene: the tree builder and the graft payload source of the
  * streaming workflow (the host-side procedural generator behind

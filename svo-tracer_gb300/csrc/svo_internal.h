@@ -57,6 +57,7 @@ struct TraceLaunch {
   uint32_t ray_chunk;
   int32_t cadence;
   int32_t block_size;
+  int32_t schedule;  // SVO_SCHEDULE_LANE / SVO_SCHEDULE_WARP
   int32_t grid;
   int32_t path_levels;
 };

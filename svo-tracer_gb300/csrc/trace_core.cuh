@@ -22,6 +22,10 @@ constexpr uint64_t kAll = ~0ull;
 __constant__ uint32_t c_pow_sum[12] = {0,      8,       72,       584,       4680,       37448,
                                        299592, 2396744, 19173960, 153391688, 1227133512, 0};
 
+// (float)x of a 64-bit fixed-point value (ulongToFloat, wavefront.cl:209,
+// without the 2^-64 scaling).
+__device__ __forceinline__ float ulong_to_float(uint64_t x) { return __ull2float_rn(x); }
+// ulongToFloat (wavefront.cl:209): (float)x * 2^-64, the scaling exact.
 __device__ __forceinline__ float ulong_to_unit(uint64_t x) { return __fmul_rn(__ull2float_rn(x), 0x1p-64f); }
 
 // floatToUlong (wavefront.cl:200-207); out-of-range products saturate, NaN -> 0.
@@ -92,12 +96,14 @@ __device__ __forceinline__ void traverse(Ray &r, int depth) {
   uint64_t d0 = round_ulong(r.lx, depth, r.sx);
   uint64_t d1 = round_ulong(r.ly, depth, r.sy);
   uint64_t d2 = round_ulong(r.lz, depth, r.sz);
-  float a0 = fabsf(__fmul_rn(__ull2float_rn(d0), r.ix));
-  float a1 = fabsf(__fmul_rn(__ull2float_rn(d1), r.iy));
-  float a2 = fabsf(__fmul_rn(__ull2float_rn(d2), r.iz));
+  const float f0 = ulong_to_float(d0), f1 = ulong_to_float(d1), f2 = ulong_to_float(d2);
+  float a0 = fabsf(__fmul_rn(f0, r.ix));
+  float a1 = fabsf(__fmul_rn(f1, r.iy));
+  float a2 = fabsf(__fmul_rn(f2, r.iz));
   int ax = (a0 <= a1 && a0 <= a2) ? 0 : ((a1 <= a0 && a1 <= a2) ? 1 : 2);
   float inv = ax == 0 ? r.ix : (ax == 1 ? r.iy : r.iz);
-  float u = ulong_to_unit(ax == 0 ? d0 : (ax == 1 ? d1 : d2));
+  // ulongToFloat of the chosen distance: its float conversion times 2^-64 (exact)
+  float u = __fmul_rn(ax == 0 ? f0 : (ax == 1 ? f1 : f2), 0x1p-64f);
   if (ax != 0) d0 = unit_to_ulong(__fmul_rn(__fmul_rn(r.dx, inv), u));
   if (ax != 1) d1 = unit_to_ulong(__fmul_rn(__fmul_rn(r.dy, inv), u));
   if (ax != 2) d2 = unit_to_ulong(__fmul_rn(__fmul_rn(r.dz, inv), u));

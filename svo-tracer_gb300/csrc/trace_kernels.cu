@@ -48,10 +48,10 @@
 namespace svo {
 namespace {
 
-template <bool kStats, bool kSmemBases>
 #ifndef SVO_TRACE_MIN_CTAS
 #define SVO_TRACE_MIN_CTAS 4
 #endif
+template <bool kStats, bool kSmemBases, bool kWarpBatch>
 __global__ void __launch_bounds__(256, SVO_TRACE_MIN_CTAS) trace_kernel(const TraceLaunch a) {
   extern __shared__ __align__(16) uint8_t smem[];
   ViewParams *s_views = reinterpret_cast<ViewParams *>(smem);
@@ -70,8 +70,6 @@ __global__ void __launch_bounds__(256, SVO_TRACE_MIN_CTAS) trace_kernel(const Tr
 
   const int B = a.base_depth;
   const uint4 *blocks = reinterpret_cast<const uint4 *>(a.blocks);
-  const uint32_t chunk = a.ray_chunk;
-  const int cadence = a.cadence;
 
   Stats st = {0, 0, 0, 0, 0, 0, 0};
   Walk w;
@@ -87,62 +85,32 @@ __global__ void __launch_bounds__(256, SVO_TRACE_MIN_CTAS) trace_kernel(const Tr
   r.depth = 0;
   r.steps = 0;
   r.view = 0;
-  bool have = false;
-  uint32_t ray_global = 0, next_ray = 0, left_in_chunk = 0, chunk_stride = 0;
+  uint32_t ray_global = 0;
   // Every pass either starts a ray or advances it by at least one step, so a
   // thread runs at most total_rays * (max_steps + 2) + 64 passes; past that
   // bound it records its state and stops instead of spinning.
   const unsigned long long iter_limit =
       (unsigned long long)a.total_rays * (unsigned long long)(a.max_steps + 2) + 64;
   unsigned long long iters = 0;
-
-  for (;;) {
-    if (++iters > iter_limit) {
-      if (a.error && atomicCAS(a.error, 0u, (unsigned)SVO_ERR_TIMEOUT) == 0u) {
-        a.error[1] = blockIdx.x;
-        a.error[2] = threadIdx.x;
-        a.error[3] = ray_global;
-        a.error[4] = (uint32_t)r.depth;
-        a.error[5] = (uint32_t)r.steps;
-      }
-      break;
+  auto record_timeout = [&]() {
+    if (a.error && atomicCAS(a.error, 0u, (unsigned)SVO_ERR_TIMEOUT) == 0u) {
+      a.error[1] = blockIdx.x;
+      a.error[2] = threadIdx.x;
+      a.error[3] = ray_global;
+      a.error[4] = (uint32_t)r.depth;
+      a.error[5] = (uint32_t)r.steps;
     }
-    if (!have) {
-      // ---- take the next ray from the queue --------------------------------
-      uint32_t my;
-      if (left_in_chunk == 0) {
-        // one atomic per group of idle lanes: each lane gets `chunk` rays,
-        // interleaved so that lanes of a group hold neighbouring pixels
-        cg::coalesced_group g = cg::coalesced_threads();
-        uint32_t first = claim(g, a.ray_counter, chunk);
-        chunk_stride = g.size();
-        my = first;
-        next_ray = first + chunk_stride;
-        left_in_chunk = chunk - 1;
-      } else {
-        my = next_ray;
-        next_ray += chunk_stride;
-        left_in_chunk--;
-      }
-      // later rays of this chunk, and every later claim, are larger still
-      if (my >= a.total_rays) break;  // queue drained
-      ray_global = my;
-      setup_ray(a, s_views, my, r);
-      w.v_block = 0;
-      w.v_base = 0;
-      w.cur_addr = kFull;
-      w.last_group = kFull;
-      have = true;
-    }
-
-    // ---- up to `cadence` traversal steps; retire finished rays together -------
-    const ViewParams &v = s_views[r.view];
-    int finish = kStepOn;
-    for (int k = 0; k < cadence && finish == kStepOn; k++)
-      finish = step<kStats, kSmemBases>(a, v, s_bases, blocks, B, r, w, st);
-    if (finish == kStepOn) continue;
-
-    // evaluateBackground / resolveRemainders + drawTrace
+  };
+  auto start_ray = [&](uint32_t my) {
+    ray_global = my;
+    setup_ray(a, s_views, my, r);
+    w.v_block = 0;
+    w.v_base = 0;
+    w.cur_addr = kFull;
+    w.last_group = kFull;
+  };
+  // evaluateBackground / resolveRemainders + drawTrace for a finished ray
+  auto finish_ray = [&](const ViewParams &v, int finish) {
     uint32_t hit_index = SVO_MISS, cr, cg_, cb;
     uint8_t hit_depth = 0;
     float t = __int_as_float(0x7f800000);
@@ -182,7 +150,78 @@ __global__ void __launch_bounds__(256, SVO_TRACE_MIN_CTAS) trace_kernel(const Tr
       if (a.ray_v_block) a.ray_v_block[ray_global] = w.v_block;
       if (a.ray_v_base) a.ray_v_base[ray_global] = w.v_base;
     }
-    have = false;
+  };
+
+  if (kWarpBatch) {
+    // ---- warp batches: 32 consecutive rays per warp, regrouped between batches
+    const uint32_t lane = threadIdx.x & 31u;
+    bool timed_out = false;
+    for (;;) {
+      uint32_t base = 0;
+      if (lane == 0) base = atomicAdd(a.ray_counter, 32u);
+      base = __shfl_sync(kFull, base, 0);
+      if (base >= a.total_rays) break;
+      const uint32_t my = base + lane;
+      if (my < a.total_rays && !timed_out) {
+        start_ray(my);
+        const ViewParams &v = s_views[r.view];
+        int finish = kStepOn;
+        while (finish == kStepOn) {
+          if (++iters > iter_limit) {
+            record_timeout();
+            timed_out = true;
+            break;
+          }
+          finish = step<kStats, kSmemBases>(a, v, s_bases, blocks, B, r, w, st);
+        }
+        if (!timed_out) finish_ray(v, finish);
+      }
+      // every lane of the warp arrives here on every iteration
+      if (__any_sync(kFull, timed_out)) break;
+    }
+  } else {
+    // ---- lanes: each thread claims rays on its own ------------------------------
+    const uint32_t chunk = a.ray_chunk;
+    const int cadence = a.cadence;
+    bool have = false;
+    uint32_t next_ray = 0, left_in_chunk = 0, chunk_stride = 0;
+    for (;;) {
+      if (++iters > iter_limit) {
+        record_timeout();
+        break;
+      }
+      if (!have) {
+        // ---- take the next ray from the queue --------------------------------
+        uint32_t my;
+        if (left_in_chunk == 0) {
+          // one atomic per group of idle lanes: each lane gets `chunk` rays,
+          // interleaved so that lanes of a group hold neighbouring pixels
+          cg::coalesced_group g = cg::coalesced_threads();
+          uint32_t first = claim(g, a.ray_counter, chunk);
+          chunk_stride = g.size();
+          my = first;
+          next_ray = first + chunk_stride;
+          left_in_chunk = chunk - 1;
+        } else {
+          my = next_ray;
+          next_ray += chunk_stride;
+          left_in_chunk--;
+        }
+        // later rays of this chunk, and every later claim, are larger still
+        if (my >= a.total_rays) break;  // queue drained
+        start_ray(my);
+        have = true;
+      }
+
+      // ---- up to `cadence` traversal steps; retire finished rays together -----
+      const ViewParams &v = s_views[r.view];
+      int finish = kStepOn;
+      for (int k = 0; k < cadence && finish == kStepOn; k++)
+        finish = step<kStats, kSmemBases>(a, v, s_bases, blocks, B, r, w, st);
+      if (finish == kStepOn) continue;
+      finish_ray(v, finish);
+      have = false;
+    }
   }
 
   if (kStats && a.stats) {
@@ -208,35 +247,43 @@ size_t trace_smem_bytes(const TraceLaunch &a, bool bases_in_smem) {
 
 static bool bases_fit(const TraceLaunch &a) { return (size_t)a.n_bases * 2 <= 96 * 1024; }
 
-template <bool S, bool M>
+template <bool S, bool M, bool W>
 static cudaError_t launch_one(const TraceLaunch &a, size_t smem, cudaStream_t stream) {
-  auto k = trace_kernel<S, M>;
+  auto k = trace_kernel<S, M, W>;
   cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   k<<<a.grid, a.block_size, smem, stream>>>(a);
   return cudaGetLastError();
 }
 
+template <bool W>
+static const void *kernel_for(bool stats, bool m) {
+  return stats ? (m ? (const void *)trace_kernel<true, true, W> : (const void *)trace_kernel<true, false, W>)
+               : (m ? (const void *)trace_kernel<false, true, W> : (const void *)trace_kernel<false, false, W>);
+}
+
 int trace_occupancy(const TraceLaunch &a, bool with_stats) {
   bool m = bases_fit(a);
   size_t smem = trace_smem_bytes(a, m);
   int n = 0;
-  const void *k = with_stats ? (m ? (const void *)trace_kernel<true, true> : (const void *)trace_kernel<true, false>)
-                             : (m ? (const void *)trace_kernel<false, true> : (const void *)trace_kernel<false, false>);
+  const void *k = a.schedule == SVO_SCHEDULE_WARP ? kernel_for<true>(with_stats, m) : kernel_for<false>(with_stats, m);
   cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, a.block_size, smem) != cudaSuccess) return 0;
   return n;
+}
+
+template <bool W>
+static cudaError_t launch_sched(const TraceLaunch &a, bool with_stats, bool m, size_t smem, cudaStream_t s) {
+  if (with_stats) return m ? launch_one<true, true, W>(a, smem, s) : launch_one<true, false, W>(a, smem, s);
+  return m ? launch_one<false, true, W>(a, smem, s) : launch_one<false, false, W>(a, smem, s);
 }
 
 svo_status launch_trace(const TraceLaunch &a, bool with_stats, void *stream) {
   bool m = bases_fit(a);
   size_t smem = trace_smem_bytes(a, m);
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  cudaError_t e;
-  if (with_stats)
-    e = m ? launch_one<true, true>(a, smem, s) : launch_one<true, false>(a, smem, s);
-  else
-    e = m ? launch_one<false, true>(a, smem, s) : launch_one<false, false>(a, smem, s);
+  cudaError_t e = a.schedule == SVO_SCHEDULE_WARP ? launch_sched<true>(a, with_stats, m, smem, s)
+                                                  : launch_sched<false>(a, with_stats, m, smem, s);
   if (e != cudaSuccess) return fail(SVO_ERR_CUDA, std::string("trace kernel launch: ") + cudaGetErrorString(e));
   return SVO_OK;
 }

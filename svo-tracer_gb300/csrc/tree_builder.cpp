@@ -24,6 +24,7 @@
 #include <atomic>
 #include <cmath>
 #include <cstdint>
+#include <cstdio>
 #include <cstring>
 #include <memory>
 #include <new>
@@ -496,6 +497,11 @@ svo_status build_tree_with(const SceneHost &scene, int D, TreeHost &tree) {
   };
   for (uint32_t a : roots) Rec::walk(tree.blocks, tree.blocks[a].child, block_count);
   tree.block_count = block_count;
+  // "Trim final tree size down to populated volume" (TreeBuilder.cs:144-145):
+  // Blocks = Blocks.Take(BlockCount). With the bookkeeping's "<" comparison the
+  // count can stop one short of the last node written, which the reference
+  // then drops; reads of it see a missing node, here as in the reference.
+  if (tree.blocks.size() > block_count) tree.blocks.resize(block_count);
   return SVO_OK;
 }
 
@@ -620,6 +626,84 @@ SVO_API svo_status svo_tree_data(void *tree, const uint16_t **bases, const svo_b
 
 SVO_API svo_status svo_tree_free(void *tree) {
   delete static_cast<TreeHost *>(tree);
+  return SVO_OK;
+}
+
+namespace {
+
+// powSum (TreeBuilder.PowSum): base chunks of levels 1..depth.
+uint64_t oct_pow_sum(int depth) {
+  uint64_t s = 0, p = 1;
+  for (int i = 1; i <= depth; i++) s += (p *= 8);
+  return s;
+}
+
+struct FileCloser {
+  void operator()(FILE *f) const {
+    if (f) std::fclose(f);
+  }
+};
+
+// Base depths whose chunk table a file can reasonably hold (powSum(8) = 19.2M).
+constexpr int kMaxOctBaseDepth = 8;
+
+}  // namespace
+
+SVO_API svo_status svo_oct_write(const char *path, uint8_t base_depth, uint32_t block_count, const uint16_t *bases,
+                                 size_t n_bases, const svo_block *blocks, size_t n_blocks) {
+  if (!path || (!bases && n_bases) || (!blocks && n_blocks))
+    return svo::fail(SVO_ERR_INVALID_ARGUMENT, "svo_oct_write: null argument");
+  if (base_depth > kMaxOctBaseDepth || n_bases != oct_pow_sum(base_depth))
+    return svo::fail(SVO_ERR_INVALID_ARGUMENT, "svo_oct_write: n_bases must be powSum(base_depth)");
+  std::unique_ptr<FILE, FileCloser> f(std::fopen(path, "wb"));
+  if (!f) return svo::fail(SVO_ERR_IO, std::string("svo_oct_write: cannot create ") + path);
+  uint8_t head[5];
+  head[0] = base_depth;
+  for (int k = 0; k < 4; k++) head[1 + k] = (uint8_t)(block_count >> (8 * k));
+  bool ok = std::fwrite(head, 1, 5, f.get()) == 5;
+  // both hosts this library builds for are little-endian, like BinaryWriter
+  ok = ok && std::fwrite(bases, 2, n_bases, f.get()) == n_bases;
+  ok = ok && std::fwrite(blocks, sizeof(svo_block), n_blocks, f.get()) == n_blocks;
+  ok = (std::fflush(f.get()) == 0) && ok;
+  if (!ok) return svo::fail(SVO_ERR_IO, std::string("svo_oct_write: write failed: ") + path);
+  return SVO_OK;
+}
+
+SVO_API svo_status svo_oct_read(const char *path, void **tree) {
+  if (!path || !tree) return svo::fail(SVO_ERR_INVALID_ARGUMENT, "svo_oct_read: null argument");
+  std::unique_ptr<FILE, FileCloser> f(std::fopen(path, "rb"));
+  if (!f) return svo::fail(SVO_ERR_IO, std::string("svo_oct_read: cannot open ") + path);
+  uint8_t head[5];
+  if (std::fread(head, 1, 5, f.get()) != 5) return svo::fail(SVO_ERR_IO, "svo_oct_read: truncated header");
+  const int base_depth = head[0];
+  uint32_t block_count = 0;
+  for (int k = 0; k < 4; k++) block_count |= (uint32_t)head[1 + k] << (8 * k);
+  if (base_depth > kMaxOctBaseDepth)
+    return svo::fail(SVO_ERR_INVALID_ARGUMENT, "svo_oct_read: base depth " + std::to_string(base_depth) +
+                                                   " is larger than " + std::to_string(kMaxOctBaseDepth));
+  // the file must hold what the header announces before anything is allocated
+  if (std::fseek(f.get(), 0, SEEK_END) != 0) return svo::fail(SVO_ERR_IO, "svo_oct_read: cannot seek");
+  long long size = std::ftell(f.get());
+  const uint64_t n_bases = oct_pow_sum(base_depth);
+  const uint64_t need = 5 + 2 * n_bases + (uint64_t)sizeof(svo_block) * block_count;
+  if (size < 0 || (uint64_t)size < need)
+    return svo::fail(SVO_ERR_IO, "svo_oct_read: file holds " + std::to_string(size) + " bytes, the header needs " +
+                                     std::to_string(need));
+  if (std::fseek(f.get(), 5, SEEK_SET) != 0) return svo::fail(SVO_ERR_IO, "svo_oct_read: cannot seek");
+  std::unique_ptr<TreeHost> t(new (std::nothrow) TreeHost);
+  if (!t) return svo::fail(SVO_ERR_OUT_OF_MEMORY, "svo_oct_read: allocation failed");
+  try {
+    t->bases.resize(n_bases);
+    t->blocks.resize(block_count);
+  } catch (const std::bad_alloc &) {
+    return svo::fail(SVO_ERR_OUT_OF_MEMORY, "svo_oct_read: allocation failed");
+  }
+  if (std::fread(t->bases.data(), 2, n_bases, f.get()) != n_bases ||
+      std::fread(t->blocks.data(), sizeof(svo_block), block_count, f.get()) != block_count)
+    return svo::fail(SVO_ERR_IO, "svo_oct_read: read failed");
+  t->base_depth = (uint8_t)base_depth;
+  t->block_count = block_count;
+  *tree = t.release();
   return SVO_OK;
 }
 

@@ -53,6 +53,7 @@ STATUS_NAMES = {
     6: "NoTree", 7: "StepLimit", 8: "Budget", 9: "NoDevice", 10: "Internal",
 }
 SCENE_SPHERE, SCENE_TERRAIN = 0, 1
+SCHEDULE_LANE, SCHEDULE_WARP = 1, 2
 
 
 class SvoError(RuntimeError):
@@ -83,7 +84,7 @@ class TraceStatsC(C.Structure):
 
 class TraceConfigC(C.Structure):
     _fields_ = [(n, C.c_int32) for n in ("block_size", "ctas_per_sm", "ray_chunk", "cadence", "max_steps",
-                                          "collect_stats", "max_hits", "_pad0")]
+                                          "collect_stats", "max_hits", "schedule")]
 
 
 class SceneParamsC(C.Structure):
@@ -153,6 +154,8 @@ def load_library(path: str | None = None) -> C.CDLL:
         "svo_tree_data": ([vp, C.POINTER(vp), C.POINTER(vp)], C.c_int32),
         "svo_tree_free": ([vp], C.c_int32),
         "svo_init_usage_tree": ([vp, C.c_uint16], C.c_int32),
+        "svo_oct_write": ([C.c_char_p, C.c_uint8, C.c_uint32, vp, sz, vp, sz], C.c_int32),
+        "svo_oct_read": ([C.c_char_p, C.POINTER(C.c_void_p)], C.c_int32),
         "svo_diff_set_params": ([vp, vp, sz, C.c_int32], C.c_int32),
         "svo_diff_get_grads": ([vp, vp, sz, C.c_int32], C.c_int32),
         "svo_diff_forward": ([vp, C.POINTER(TraceInputC), C.c_int32, vp, C.c_int32], C.c_int32),
@@ -215,11 +218,56 @@ def _tree_from_handle(lib, h) -> "Octree":
         _check("BuildTree", lib.svo_tree_info(h, C.byref(bd), C.byref(nb), C.byref(nk), C.byref(bc)))
         pb, pk = C.c_void_p(), C.c_void_p()
         _check("BuildTree", lib.svo_tree_data(h, C.byref(pb), C.byref(pk)))
-        bases = np.ctypeslib.as_array(C.cast(pb, C.POINTER(C.c_uint16)), shape=(nb.value,)).copy()
-        raw = np.ctypeslib.as_array(C.cast(pk, C.POINTER(C.c_uint8)), shape=(nk.value * 16,)).copy()
+        bases = np.zeros(nb.value, np.uint16)
+        raw = np.zeros(nk.value * 16, np.uint8)
+        if nb.value:
+            C.memmove(bases.ctypes.data, pb.value, bases.nbytes)
+        if nk.value:
+            C.memmove(raw.ctypes.data, pk.value, raw.nbytes)
         return Octree(bd.value, bc.value, bases, raw.view(BLOCK_DTYPE))
     finally:
         lib.svo_tree_free(h)
+
+
+def write_oct(path: str, tree: Octree) -> None:
+    """OctreeSerializer.Serialize (SvoTracer.Domain/Serializers/OctreeSerializer.cs:13-21)."""
+    lib = load_library()
+    bases = np.ascontiguousarray(tree.BaseBlocks, np.uint16)
+    blocks = np.ascontiguousarray(tree.Blocks)
+    assert blocks.dtype == BLOCK_DTYPE
+    _check("SaveTree", lib.svo_oct_write(os.fsencode(path), tree.BaseDepth, tree.BlockCount, _ptr(bases), len(bases),
+                                         _ptr(blocks), len(blocks)))
+
+
+def read_oct(path: str) -> Octree:
+    """OctreeSerializer.Deserialize (OctreeSerializer.cs:23-44): BlockCount blocks."""
+    lib = load_library()
+    h = C.c_void_p()
+    _check("LoadTree", lib.svo_oct_read(os.fsencode(path), C.byref(h)))
+    return _tree_from_handle(lib, h)
+
+
+class TreeManager:
+    """ITreeManager over `{path}/{fileName}.oct` (SvoTracer.Domain/TreeManager.cs)."""
+
+    def __init__(self, path: str):
+        self._path = path
+
+    def _file(self, fileName: str) -> str:
+        return os.path.join(self._path, fileName + ".oct")
+
+    def TreeExists(self, fileName: str) -> bool:
+        return os.path.exists(self._file(fileName))
+
+    def DeleteTree(self, fileName: str) -> None:
+        os.remove(self._file(fileName))
+
+    def LoadTree(self, fileName: str) -> Octree:
+        return read_oct(self._file(fileName))
+
+    def SaveTree(self, fileName: str, tree: Octree) -> None:
+        os.makedirs(self._path, exist_ok=True)
+        write_oct(self._file(fileName), tree)
 
 
 class Scene:

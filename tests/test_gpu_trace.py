@@ -17,7 +17,8 @@ pytestmark = pytest.mark.gpu
 
 @pytest.fixture(autouse=True)
 def default_config(tracer):
-    tracer.set_config(block_size=256, ctas_per_sm=0, ray_chunk=1, cadence=16, max_steps=1 << 16, collect_stats=0)
+    tracer.set_config(block_size=256, ctas_per_sm=0, ray_chunk=1, cadence=16, max_steps=1 << 16, collect_stats=0,
+                      schedule=st.SCHEDULE_LANE)
     yield
 
 T_RTOL = 1e-5  # the benchmark spec's tolerance for t and RGBA; the checks below are tighter (exact)
@@ -82,9 +83,11 @@ SCENES = [
 ]
 
 
+@pytest.mark.parametrize("schedule", [st.SCHEDULE_LANE, st.SCHEDULE_WARP], ids=["lane", "warp"])
 @pytest.mark.parametrize("scene", SCENES, ids=[s[0] for s in SCENES])
-def test_trace_matches_oracle(tracer, scene):
+def test_trace_matches_oracle(tracer, scene, schedule):
     _, kind, seed, b, d, o, t, w, h, fov, dof = scene
+    tracer.set_config(schedule=schedule)
     tree = st.TreeBuilder(kind, seed=seed).BuildTree(b, d)
     cam = st.look_at(o, t, w, h, fov, DoF=dof, Tick=17, MaxChildRequestId=1 << 20)
     got, usage, req, n, stats, (vb, vs), want, u_ref = run_both(tracer, tree, cam)
@@ -103,7 +106,9 @@ def test_trace_matches_oracle(tracer, scene):
     assert stats["step_limited"] == 0
 
 
-def test_step_limit_matches_oracle(tracer):
+@pytest.mark.parametrize("schedule", [st.SCHEDULE_LANE, st.SCHEDULE_WARP], ids=["lane", "warp"])
+def test_step_limit_matches_oracle(tracer, schedule):
+    tracer.set_config(schedule=schedule)
     tree = st.TreeBuilder(st.SCENE_TERRAIN, seed=5).BuildTree(3, 8)
     cam = st.look_at((0.1, 0.15, 0.55), (0.7, 0.7, 0.9), 64, 36, 60.0)
     got, usage, req, n, stats, _, want, u_ref = run_both(tracer, tree, cam, max_steps=12)
@@ -153,7 +158,9 @@ def test_batch_equals_single_views_and_graph(tracer):
 
 @pytest.mark.parametrize("cfg", [dict(block_size=128, ray_chunk=1, cadence=1),
                                  dict(block_size=256, ray_chunk=8, cadence=32),
-                                 dict(block_size=64, ray_chunk=3, cadence=5, ctas_per_sm=1)])
+                                 dict(block_size=64, ray_chunk=3, cadence=5, ctas_per_sm=1),
+                                 dict(block_size=128, schedule=st.SCHEDULE_WARP),
+                                 dict(block_size=64, schedule=st.SCHEDULE_WARP, ctas_per_sm=1)])
 def test_launch_shapes_do_not_change_results(tracer, cfg):
     tree = st.TreeBuilder(st.SCENE_SPHERE, seed=6).BuildTree(4, 8)
     cam = st.look_at((1.1, 0.2, 0.9), (0.5, 0.5, 0.5), 120, 90, 60.0)
@@ -162,7 +169,7 @@ def test_launch_shapes_do_not_change_results(tracer, cfg):
         tracer.upload(tree)
         got = tracer.trace(cam)
     finally:
-        tracer.set_config(block_size=256, ray_chunk=1, cadence=16, ctas_per_sm=0)
+        tracer.set_config(block_size=256, ray_chunk=1, cadence=16, ctas_per_sm=0, schedule=st.SCHEDULE_LANE)
     assert_same(got, po.trace_view(tree, cam))
 
 
@@ -189,7 +196,7 @@ def test_mixed_views_batched_graph_equals_plain_launches(tracer):
     tracer.trace_device(views, dev_outs, graph=True)  # replay
     torch.cuda.synchronize()
     batched = [tuple(x.cpu() for x in k) for k in keep]
-    tracer.set_config(block_size=256, ray_chunk=1, cadence=16)
+    tracer.set_config(block_size=256, ray_chunk=1, cadence=16, schedule=st.SCHEDULE_LANE)
     for v, o in zip(views, dev_outs):
         tracer.trace_device([v], [o])
     torch.cuda.synchronize()
@@ -242,4 +249,6 @@ def test_errors(tracer):
         tracer.trace(st.TraceInput(ScreenSize=(8, 8), BaseDepth=3))
     with pytest.raises(st.SvoError):
         tracer.set_config(block_size=100)
+    with pytest.raises(st.SvoError):
+        tracer.set_config(schedule=3)
     assert lib is not None

@@ -49,12 +49,14 @@ def test_dense_level_and_allocation_order(tree):
         pair = (int(t.BaseBlocks[base_start + (pos >> 3)]) >> ((pos & 7) * 2)) & 3
         populated.append(pair == 3)
     empty = [p for p in range(8 ** (b + 1)) if not populated[p]]
-    queue = empty + list(range(8 ** (b + 1), 8 ** (b + 1) + len(bl) // 8))
+    queue = empty + list(range(8 ** (b + 1), 8 ** (b + 1) + (len(bl) + 7) // 8))
     seq = []
 
     def visit(group):
         seq.append(group)
         for i in range(8):
+            if group * 8 + i >= len(bl):
+                continue  # dropped by the trim to BlockCount
             c = int(bl[group * 8 + i]["child"])
             if c != st.NO_CHILD:
                 assert c % 8 == 0
@@ -65,15 +67,21 @@ def test_dense_level_and_allocation_order(tree):
         for y in range(n2):
             for z in range(n2):
                 a = morton(x, y, z, b + 2)
-                node = bl[a]
                 if not populated[a >> 3]:
                     continue
+                node = bl[a]
                 if d > b + 2 and can_have_children(int(node["chunk"])):
                     assert int(node["child"]) != st.NO_CHILD
                     visit(int(node["child"]) // 8)
                 else:
                     assert int(node["child"]) == st.NO_CHILD
     assert seq == queue[: len(seq)]
+
+
+def test_blocks_trimmed_to_block_count(tree):
+    """BuildTree ends with Blocks = Blocks.Take(BlockCount) (TreeBuilder.cs:144-145)."""
+    t, b, d = tree
+    assert len(t.Blocks) == t.BlockCount
 
 
 def test_check_tree(tree):
@@ -84,7 +92,7 @@ def test_check_tree(tree):
     for a in np.nonzero((bl["child"] != st.NO_CHILD) & (bl["chunk"] != 0))[0][:20000]:
         c = int(bl[a]["child"])
         for k in range(8):
-            if ((int(bl[a]["chunk"]) >> (2 * k)) & 3) != 1:
+            if ((int(bl[a]["chunk"]) >> (2 * k)) & 3) != 1 and c + k < len(bl):
                 assert int(bl[c + k]["chunk"]) != 0x5555
 
 
