@@ -171,8 +171,12 @@ struct Context {
 };
 
 
+// Views, ray-setup tables and outputs of a batch into pinned staging. With
+// `tiled`, each view's ray slots cover whole 8x4 pixel tiles (total_rays then
+// exceeds total_pixels by the padding slots).
 svo_status stage_views(Context &c, const svo_trace_input *in, int32_t n, const svo_trace_output *out,
-                       bool outputs_on_device, uint32_t &total_rays, size_t &table_floats);
+                       bool outputs_on_device, bool tiled, uint32_t &total_rays, uint32_t &total_pixels,
+                       size_t &table_floats);
 svo_status prepare_launch(Context &c, int32_t n_views, uint32_t total_rays, TraceLaunch &a, bool stats);
 
 }  // namespace svo

@@ -34,8 +34,9 @@
 // lowest of them sums the group's gradients through shared memory and issues
 // one 16-byte atomic add (a lane alone adds directly).
 //
-// Scheduling: a persistent grid whose warps claim 32 consecutive rays at a
-// time from a device counter; lane i takes ray base + i, and the warp regroups
+// Scheduling: a persistent grid whose warps claim 32 consecutive ray slots at
+// a time from a device counter (one 8x4 pixel tile: the views are staged
+// tiled, outputs stay indexed by pixel); lane i takes slot base + i, and the warp regroups
 // with __syncwarp() between the walks of a ray and before the next claim, so
 // lanes do not drift apart over rays and phases (measured 2-3x faster than a
 // free per-thread grid-stride loop).
@@ -179,7 +180,10 @@ __global__ void __launch_bounds__(256, kBackward ? SVO_DIFF_BWD_MIN_CTAS : SVO_D
     base = __shfl_sync(kFull, base, 0);
     if (base >= a.total_rays) break;
     const uint32_t ray = base + lane;
-    const bool live = ray < a.total_rays;
+    int view = 0;
+    uint32_t px = 0, py = 0;
+    const bool live = ray < a.total_rays && ray_slot(a, s_views, ray, view, px, py);  // not a padding slot
+    const uint32_t pixel = live ? s_views[view].pixel_begin + py * s_views[view].width + px : 0;
     Composite full;
     full.init();
     if (live && (!kBackward || !d.use_saved)) {
@@ -193,11 +197,11 @@ __global__ void __launch_bounds__(256, kBackward ? SVO_DIFF_BWD_MIN_CTAS : SVO_D
     __syncwarp();
     if (!kBackward) {
       if (live && d.rgb)
-        for (int k = 0; k < 3; k++) d.rgb[3ull * ray + k] = __fadd_rn(full.hi[k], full.lo[k]);
+        for (int k = 0; k < 3; k++) d.rgb[3ull * pixel + k] = __fadd_rn(full.hi[k], full.lo[k]);
       if (live && d.saved)
         for (int k = 0; k < 3; k++) {
-          d.saved[6ull * ray + 2 * k] = full.hi[k];
-          d.saved[6ull * ray + 2 * k + 1] = full.lo[k];
+          d.saved[6ull * pixel + 2 * k] = full.hi[k];
+          d.saved[6ull * pixel + 2 * k + 1] = full.lo[k];
         }
       continue;
     }
@@ -205,10 +209,10 @@ __global__ void __launch_bounds__(256, kBackward ? SVO_DIFF_BWD_MIN_CTAS : SVO_D
     if (live) {
       if (d.use_saved)
         for (int k = 0; k < 3; k++) {
-          full.hi[k] = __ldg(d.saved + 6ull * ray + 2 * k);
-          full.lo[k] = __ldg(d.saved + 6ull * ray + 2 * k + 1);
+          full.hi[k] = __ldg(d.saved + 6ull * pixel + 2 * k);
+          full.lo[k] = __ldg(d.saved + 6ull * pixel + 2 * k + 1);
         }
-      const float *tg = d.target + 3ull * ray;
+      const float *tg = d.target + 3ull * pixel;
       for (int k = 0; k < 3; k++) {
         double e = ((double)full.hi[k] - (double)__ldg(tg + k)) + (double)full.lo[k];
         loss_part += e * e * d.inv_pixels;
@@ -282,9 +286,9 @@ svo_status run_diff(Context &c, const svo_trace_input *views, int32_t n, const f
   std::memset(outs.data(), 0, sizeof(svo_trace_output) * n);
   for (auto &o : outs) o.on_device = 1;
   SVO_CUDA(cudaEventSynchronize(c.staged), "svo_diff: staging");
-  uint32_t total = 0;
+  uint32_t total = 0, pixels = 0;
   size_t table_floats = 0;
-  svo_status st = stage_views(c, views, n, outs.data(), true, total, table_floats);
+  svo_status st = stage_views(c, views, n, outs.data(), true, /*tiled=*/true, total, pixels, table_floats);
   if (st) return st;
   if (kBackward && use_saved &&
       !(c.saved_valid && c.saved_params_gen == c.params_gen && c.saved_max_hits == c.cfg.max_hits &&
@@ -292,7 +296,7 @@ svo_status run_diff(Context &c, const svo_trace_input *views, int32_t n, const f
     return fail(SVO_ERR_INVALID_ARGUMENT,
                 "svo_diff_backward: no saved forward colour for these views, parameters and max_hits");
   if (c.views.reserve(n) || c.tables.reserve(table_floats) || c.diff_loss.reserve(1) ||
-      (!kBackward && c.diff_saved.reserve(6ull * total)))
+      (!kBackward && c.diff_saved.reserve(6ull * pixels)))
     return fail(SVO_ERR_OUT_OF_MEMORY, "svo_diff: allocation failed");
   DiffLaunch d{};
   st = prepare_launch(c, n, total, d.t, false);
@@ -307,7 +311,7 @@ svo_status run_diff(Context &c, const svo_trace_input *views, int32_t n, const f
   d.saved = c.diff_saved.p;
   d.use_saved = use_saved ? 1 : 0;
   d.loss = c.diff_loss.p;
-  d.inv_pixels = 1.0 / (double)total;
+  d.inv_pixels = 1.0 / (double)pixels;
   d.max_hits = c.cfg.max_hits;
   d.t.block_size = 256;
   size_t smem = (size_t)n * sizeof(ViewParams) + ((c.n_bases * 2 + 15) & ~(size_t)15) +
@@ -341,7 +345,7 @@ svo_status run_diff(Context &c, const svo_trace_input *views, int32_t n, const f
     c.saved_max_hits = c.cfg.max_hits;
     c.saved_valid = true;
   }
-  c.last_rays = total;
+  c.last_rays = pixels;
   return SVO_OK;
 }
 

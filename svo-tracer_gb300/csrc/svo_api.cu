@@ -82,8 +82,10 @@ static int scan_tree_depth(const svo_block *blocks, size_t n_blocks, int B) {
 
 // Builds the view table and trig tables for `n` views in pinned staging.
 svo_status stage_views(Context &c, const svo_trace_input *in, int32_t n, const svo_trace_output *out,
-                              bool outputs_on_device, uint32_t &total_rays, size_t &table_floats) {
+                       bool outputs_on_device, bool tiled, uint32_t &total_rays, uint32_t &total_pixels,
+                       size_t &table_floats) {
   total_rays = 0;
+  total_pixels = 0;
   table_floats = 0;
   for (int i = 0; i < n; i++) {
     uint64_t w = in[i].screen_size[0], h = in[i].screen_size[1];
@@ -91,9 +93,11 @@ svo_status stage_views(Context &c, const svo_trace_input *in, int32_t n, const s
       return fail(SVO_ERR_INVALID_ARGUMENT, "svo_trace: screen_size must be 1..65536 per axis");
     if (in[i].base_depth != 0 && in[i].base_depth != c.base_depth)
       return fail(SVO_ERR_INVALID_ARGUMENT, "svo_trace: input base_depth differs from the resident tree's");
-    if ((uint64_t)total_rays + w * h > 0xF0000000ull)
+    uint64_t slots = tiled ? ((w + 7) / 8) * ((h + 3) / 4) * 32 : w * h;
+    if ((uint64_t)total_rays + slots > 0xF0000000ull)
       return fail(SVO_ERR_INVALID_ARGUMENT, "svo_trace: too many rays in one call");
-    total_rays += (uint32_t)(w * h);
+    total_rays += (uint32_t)slots;
+    total_pixels += (uint32_t)(w * h);
     table_floats += 2 * (w + h);
   }
   if (c.h_views.reserve(n) != cudaSuccess || c.h_tables.reserve(table_floats) != cudaSuccess)
@@ -114,6 +118,8 @@ svo_status stage_views(Context &c, const svo_trace_input *in, int32_t n, const s
     v.width = W;
     v.height = H;
     v.ray_begin = ray;
+    v.pixel_begin = (uint32_t)out_off;
+    v.tile = tiled ? 1 : 0;
     v.table_off = (uint32_t)toff;
     v.tick = t.tick;
     if (outputs_on_device) {
@@ -154,7 +160,7 @@ svo_status stage_views(Context &c, const svo_trace_input *in, int32_t n, const s
     std::memcpy(tb, it->second.data(), it->second.size() * sizeof(float));
     toff += 2 * ((size_t)W + H);
     out_off += (size_t)W * H;
-    ray += W * H;
+    ray += tiled ? ((W + 7) / 8) * ((H + 3) / 4) * 32 : W * H;
   }
   return SVO_OK;
 }
@@ -233,16 +239,18 @@ static svo_status run_trace(Context &c, const svo_trace_input *in, int32_t n, co
   }
   if (c.requests.reserve(cap) != cudaSuccess) return fail(SVO_ERR_OUT_OF_MEMORY, "svo_trace: request queue allocation");
   c.request_cap = cap;
-  uint32_t total_rays;
+  uint32_t total_rays, total_pixels;
   size_t table_floats;
   // the previous call's uploads must have read the pinned staging before it is rewritten
   SVO_CUDA(cudaEventSynchronize(c.staged), "svo_trace: staging");
-  svo_status st = stage_views(c, in, n, out, on_device, total_rays, table_floats);
+  // warp batches take 8x4 pixel tiles
+  svo_status st = stage_views(c, in, n, out, on_device, c.cfg.schedule == SVO_SCHEDULE_WARP, total_rays,
+                              total_pixels, table_floats);
   if (st) return st;
   bool stats = c.cfg.collect_stats > 0;
   if (c.views.reserve(n) || c.tables.reserve(table_floats))
     return fail(SVO_ERR_OUT_OF_MEMORY, "svo_trace: view table allocation failed");
-  if (stats && c.cfg.collect_stats >= 2 && (c.ray_v_block.reserve(total_rays) || c.ray_v_base.reserve(total_rays)))
+  if (stats && c.cfg.collect_stats >= 2 && (c.ray_v_block.reserve(total_pixels) || c.ray_v_base.reserve(total_pixels)))
     return fail(SVO_ERR_OUT_OF_MEMORY, "svo_trace: per-ray counter allocation failed");
   TraceLaunch a;
   st = prepare_launch(c, n, total_rays, a, stats);
@@ -299,7 +307,7 @@ static svo_status run_trace(Context &c, const svo_trace_input *in, int32_t n, co
     st = enqueue(false);
     if (st) return st;
   }
-  c.last_rays = total_rays;
+  c.last_rays = total_pixels;
   c.last_stats_valid = stats;
 
   if (!on_device) {

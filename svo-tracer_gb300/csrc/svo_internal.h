@@ -24,8 +24,8 @@ struct ViewParams {
   uint32_t ray_begin;  // first ray of this view in the batch's ray index space
   uint32_t table_off;  // sinU, cosU at [off, off+W); sinV, cosV at [off+2W, off+2W+2H)
   uint16_t tick;
-  uint16_t _pad0;
-  uint32_t _pad1;
+  uint16_t tile;         // 1: the view's rays are claimed in 8x4 pixel tiles (ray slots padded to whole tiles)
+  uint32_t pixel_begin;  // first pixel of this view in the batch's concatenated pixel space
   uint32_t *hit_index;
   uint8_t *hit_depth;
   float *t;

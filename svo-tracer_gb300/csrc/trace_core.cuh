@@ -340,10 +340,13 @@ __device__ __forceinline__ int step(const TraceLaunch &a, const ViewParams &v, c
 }
 
 
-// setupInitialTrace (wavefront.cl:563-595) for ray `my` of the batch, then
-// traceIntoVolume; a ray that misses the cube gets depth 0 (background).
-__device__ __forceinline__ void setup_ray(const TraceLaunch &a, const ViewParams *s_views, uint32_t my, Ray &r) {
-  int lo = 0, hi = a.n_views - 1;  // views are sorted by ray_begin
+// Slot `my` of the batch's ray index space: its view and pixel. Views are
+// sorted by ray_begin. A tiled view's slots run over 8x4 pixel tiles, row of
+// tiles by row of tiles, so the 32 slots a warp takes form one tile; the slots
+// of a tile that fall outside the image are padding (returns false).
+__device__ __forceinline__ bool ray_slot(const TraceLaunch &a, const ViewParams *s_views, uint32_t my, int &view,
+                                         uint32_t &px, uint32_t &py) {
+  int lo = 0, hi = a.n_views - 1;
   while (lo < hi) {
     int mid = (lo + hi + 1) >> 1;
     if (s_views[mid].ray_begin <= my)
@@ -352,9 +355,29 @@ __device__ __forceinline__ void setup_ray(const TraceLaunch &a, const ViewParams
       hi = mid - 1;
   }
   const ViewParams &v = s_views[lo];
-  r.view = lo;
-  r.id = my - v.ray_begin;
-  uint32_t px = r.id % v.width, py = r.id / v.width;
+  view = lo;
+  const uint32_t rel = my - v.ray_begin;
+  if (v.tile) {
+    const uint32_t tiles_x = (v.width + 7) >> 3, t = rel >> 5, l = rel & 31u;
+    py = (t / tiles_x) * 4 + (l >> 3);
+    px = (t % tiles_x) * 8 + (l & 7u);
+    return px < v.width && py < v.height;
+  }
+  px = rel % v.width;
+  py = rel / v.width;
+  return true;
+}
+
+// setupInitialTrace (wavefront.cl:563-595) for ray slot `my` of the batch,
+// then traceIntoVolume; a ray that misses the cube gets depth 0 (background).
+// Returns false (and sets nothing else) for a padding slot.
+__device__ __forceinline__ bool setup_ray(const TraceLaunch &a, const ViewParams *s_views, uint32_t my, Ray &r) {
+  int view;
+  uint32_t px, py;
+  if (!ray_slot(a, s_views, my, view, px, py)) return false;
+  const ViewParams &v = s_views[view];
+  r.view = view;
+  r.id = py * v.width + px;
   const float *tb = a.tables + v.table_off;
   float su = __ldg(tb + px), cu = __ldg(tb + v.width + px);
   float sv = __ldg(tb + 2 * v.width + py), cv = __ldg(tb + 2 * v.width + v.height + py);
@@ -378,6 +401,7 @@ __device__ __forceinline__ void setup_ray(const TraceLaunch &a, const ViewParams
   r.depth = 1;
   r.steps = 0;
   if (!enter_volume(r)) r.depth = 0;
+  return true;
 }
 
 // Continues a ray past a hit as if the hit octant held no geometry (the

@@ -101,13 +101,15 @@ __global__ void __launch_bounds__(256, SVO_TRACE_MIN_CTAS) trace_kernel(const Tr
       a.error[5] = (uint32_t)r.steps;
     }
   };
-  auto start_ray = [&](uint32_t my) {
+  // false for the padding slots of tiled views
+  auto start_ray = [&](uint32_t my) -> bool {
     ray_global = my;
-    setup_ray(a, s_views, my, r);
+    if (!setup_ray(a, s_views, my, r)) return false;
     w.v_block = 0;
     w.v_base = 0;
     w.cur_addr = kFull;
     w.last_group = kFull;
+    return true;
   };
   // evaluateBackground / resolveRemainders + drawTrace for a finished ray
   auto finish_ray = [&](const ViewParams &v, int finish) {
@@ -147,13 +149,15 @@ __global__ void __launch_bounds__(256, SVO_TRACE_MIN_CTAS) trace_kernel(const Tr
       st.rays++;
       st.base_steps += w.v_base;
       st.block_reads += w.v_block;
-      if (a.ray_v_block) a.ray_v_block[ray_global] = w.v_block;
-      if (a.ray_v_base) a.ray_v_base[ray_global] = w.v_base;
+      const uint32_t pixel = v.pixel_begin + r.id;  // per-ray counters by pixel of the batch
+      if (a.ray_v_block) a.ray_v_block[pixel] = w.v_block;
+      if (a.ray_v_base) a.ray_v_base[pixel] = w.v_base;
     }
   };
 
   if (kWarpBatch) {
-    // ---- warp batches: 32 consecutive rays per warp, regrouped between batches
+    // ---- warp batches: 32 consecutive ray slots (one 8x4 pixel tile of a tiled
+    // view) per warp, regrouped between batches
     const uint32_t lane = threadIdx.x & 31u;
     bool timed_out = false;
     for (;;) {
@@ -162,8 +166,7 @@ __global__ void __launch_bounds__(256, SVO_TRACE_MIN_CTAS) trace_kernel(const Tr
       base = __shfl_sync(kFull, base, 0);
       if (base >= a.total_rays) break;
       const uint32_t my = base + lane;
-      if (my < a.total_rays && !timed_out) {
-        start_ray(my);
+      if (my < a.total_rays && !timed_out && start_ray(my)) {
         const ViewParams &v = s_views[r.view];
         int finish = kStepOn;
         while (finish == kStepOn) {
@@ -209,7 +212,7 @@ __global__ void __launch_bounds__(256, SVO_TRACE_MIN_CTAS) trace_kernel(const Tr
         }
         // later rays of this chunk, and every later claim, are larger still
         if (my >= a.total_rays) break;  // queue drained
-        start_ray(my);
+        if (!start_ray(my)) continue;   // padding slot of a tiled view
         have = true;
       }
 
