@@ -295,6 +295,13 @@ SVO_API svo_status svo_graft(void *ctx, const svo_update_input *in, const svo_gr
                              const svo_block *payload, size_t n_payload, const uint64_t *locations,
                              size_t n_locations, svo_graft_report *report);
 SVO_API svo_status svo_read_graft_claims(void *ctx, uint32_t *claimed, size_t cap);
+/* The child requests of the last trace answered on the device: the payload
+ * svo_scene_graft_payload builds for them from `scene` (a terrain scene;
+ * WorldManager.UpdateGrafting's generator, SvoTracer.Window/WorldManager.cs:
+ * 84-103), grafted with svo_graft's rules and the same result node for node,
+ * without reading the requests back or sending a payload. The scene's column
+ * height pyramids are copied to the device on the first call with a scene. */
+SVO_API svo_status svo_graft_generate(void *ctx, void *scene, const svo_update_input *in, svo_graft_report *report);
 /* Pruning records (wavefront.cl:1215-1266, Pruning :24-36) applied in order;
  * groups orphaned by CullChild are freed afterwards. Child requests of
  * Location walks that meet a missing child go to the context's request queue. */

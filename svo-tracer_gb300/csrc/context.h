@@ -106,6 +106,14 @@ struct Context {
   // ray-setup tables (sin/cos per column and row) by (fov bits, width, height)
   std::map<std::array<uint32_t, 4>, std::vector<float>> table_cache;
 
+  // graft payloads generated on the device: the terrain's column pyramids (all
+  // levels concatenated) of the scene `terrain_id`, a per-node request marker
+  // (kept zero between calls), compaction counts, jobs and counters
+  DevBuf<uint16_t> terrain_lo, terrain_hi;
+  uint64_t terrain_id = 0;
+  DevBuf<uint32_t> gen_marker, gen_counts, gen_addr, gen_scalars;
+  DevBuf<uint8_t> gen_jobs;
+
   // differentiable colour fitting: per-node RGBA parameters and gradients
   DevBuf<float> params, grads, diff_rgb, diff_target;
   DevBuf<float> diff_saved;  // forward colour as (hi, lo) float pairs, 6 per ray
@@ -164,6 +172,13 @@ struct Context {
     grads.release();
     diff_rgb.release();
     diff_target.release();
+    terrain_lo.release();
+    terrain_hi.release();
+    gen_marker.release();
+    gen_counts.release();
+    gen_addr.release();
+    gen_scalars.release();
+    gen_jobs.release();
     diff_saved.release();
     diff_loss.release();
     if (own_stream) cudaStreamDestroy(own_stream);

@@ -93,7 +93,7 @@ svo_status stage_views(Context &c, const svo_trace_input *in, int32_t n, const s
       return fail(SVO_ERR_INVALID_ARGUMENT, "svo_trace: screen_size must be 1..65536 per axis");
     if (in[i].base_depth != 0 && in[i].base_depth != c.base_depth)
       return fail(SVO_ERR_INVALID_ARGUMENT, "svo_trace: input base_depth differs from the resident tree's");
-    uint64_t slots = tiled ? ((w + 7) / 8) * ((h + 3) / 4) * 32 : w * h;
+    uint64_t slots = tiled ? ((w + kTileW - 1) / kTileW) * ((h + kTileH - 1) / kTileH) * 32 : w * h;
     if ((uint64_t)total_rays + slots > 0xF0000000ull)
       return fail(SVO_ERR_INVALID_ARGUMENT, "svo_trace: too many rays in one call");
     total_rays += (uint32_t)slots;
@@ -160,7 +160,7 @@ svo_status stage_views(Context &c, const svo_trace_input *in, int32_t n, const s
     std::memcpy(tb, it->second.data(), it->second.size() * sizeof(float));
     toff += 2 * ((size_t)W + H);
     out_off += (size_t)W * H;
-    ray += tiled ? ((W + 7) / 8) * ((H + 3) / 4) * 32 : W * H;
+    ray += tiled ? ((W + kTileW - 1) / kTileW) * ((H + kTileH - 1) / kTileH) * 32 : W * H;
   }
   return SVO_OK;
 }

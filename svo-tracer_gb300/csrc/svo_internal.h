@@ -14,6 +14,13 @@ svo_status fail(svo_status status, const std::string &message);
 struct TreeHost;
 
 // Per-view constants of one trace, as the kernel reads them.
+// Pixel tile of a warp batch (kTileW x kTileH = 32 rays).
+#ifndef SVO_TILE_W
+#define SVO_TILE_W 8
+#endif
+constexpr uint32_t kTileW = SVO_TILE_W, kTileH = 32 / SVO_TILE_W;
+static_assert(kTileW * kTileH == 32, "a tile is one warp of rays");
+
 struct ViewParams {
   float origin[3];
   float facing[9];
@@ -67,5 +74,17 @@ svo_status launch_trace(const TraceLaunch &a, bool with_stats, void *stream);
 // Dynamic shared memory the launch needs.
 size_t trace_smem_bytes(const TraceLaunch &a, bool bases_in_smem);
 int trace_occupancy(const TraceLaunch &a, bool with_stats);
+
+// A terrain scene's column height pyramids, for generating graft payloads on
+// the device (tree_builder.cpp holds the scene).
+constexpr int kMaxTerrainLevels = 18;
+struct TerrainInfo {
+  uint64_t id;  // unique per scene object of this process
+  int base_depth, scene_depth, leaf;
+  uint32_t res, seed;
+  const uint16_t *lo[kMaxTerrainLevels], *hi[kMaxTerrainLevels];  // level l: 4^l columns, min / max height
+};
+// False when `scene` (an svo_scene_create handle) is not a terrain scene.
+bool scene_terrain_info(const void *scene, TerrainInfo *out);
 
 }  // namespace svo

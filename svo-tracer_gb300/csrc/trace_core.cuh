@@ -358,9 +358,9 @@ __device__ __forceinline__ bool ray_slot(const TraceLaunch &a, const ViewParams 
   view = lo;
   const uint32_t rel = my - v.ray_begin;
   if (v.tile) {
-    const uint32_t tiles_x = (v.width + 7) >> 3, t = rel >> 5, l = rel & 31u;
-    py = (t / tiles_x) * 4 + (l >> 3);
-    px = (t % tiles_x) * 8 + (l & 7u);
+    const uint32_t tiles_x = (v.width + kTileW - 1) / kTileW, t = rel >> 5, l = rel & 31u;
+    py = (t / tiles_x) * kTileH + l / kTileW;
+    px = (t % tiles_x) * kTileW + l % kTileW;
     return px < v.width && py < v.height;
   }
   px = rel % v.width;

@@ -34,28 +34,13 @@
 #include <vector>
 
 #include "../../include/svo.h"
+#include "scene_common.h"
 #include "svo_internal.h"
 
 namespace svo {
 namespace {
 
-inline uint32_t mix32(uint32_t h) {
-  h ^= h >> 16;
-  h *= 0x7feb352dU;
-  h ^= h >> 15;
-  h *= 0x846ca68bU;
-  h ^= h >> 16;
-  return h;
-}
-
-inline uint32_t hash4(uint32_t seed, uint32_t a, uint32_t b, uint32_t c, uint32_t d) {
-  uint32_t h = mix32(seed ^ 0x9e3779b9U);
-  h = mix32(h ^ a);
-  h = mix32(h + 0x632be5abU ^ b);
-  h = mix32(h + 0x85157af5U ^ c);
-  h = mix32(h + 0x2545f491U ^ d);
-  return h;
-}
+using scene::hash4;
 
 inline double unit_hash(uint32_t h) { return (h >> 8) * (1.0 / 16777216.0); }
 
@@ -236,39 +221,14 @@ struct TerrainScene final : Scene {
   }
   void classify(int level, uint32_t x, uint32_t y, uint32_t z, bool &geo, bool &air) const override {
     size_t idx = (size_t)y * (1u << level) + x;
-    uint32_t s = 1u << (leaf - level);
-    uint32_t mx = hi[level][idx], mn = lo[level][idx];
-    // the deepest voxel row of the cell is solid somewhere / the top row is air somewhere
-    geo = (int64_t)mx > (int64_t)res - (int64_t)(z + 1) * s;
-    air = (int64_t)mn < (int64_t)res - (int64_t)z * s;
+    scene::terrain_classify(hi[level][idx], lo[level][idx], res, leaf, level, z, geo, air);
   }
   void colour(int level, uint32_t x, uint32_t y, uint32_t z, uint8_t rgb[3]) const override {
-    double zc = (z + 0.5) * std::ldexp(1.0, -level);
-    double h = 1.0 - zc;  // height above the bottom face
-    int base[3];
-    if (h < 0.06) {
-      base[0] = 194; base[1] = 178; base[2] = 128;  // sand
-    } else if (h < 0.14) {
-      base[0] = 86; base[1] = 125; base[2] = 70;    // grass
-    } else if (h < 0.22) {
-      base[0] = 120; base[1] = 110; base[2] = 100;  // rock
-    } else {
-      base[0] = 236; base[1] = 236; base[2] = 242;  // snow
-    }
-    uint32_t hsh = hash4(seed ^ 0x3c6ef372U, (uint32_t)level, x, y, z);
-    for (int k = 0; k < 3; k++) {
-      int j = (int)((hsh >> (8 * k)) % 17u) - 8;
-      int v = base[k] + j;
-      rgb[k] = (uint8_t)(v < 0 ? 0 : v > 255 ? 255 : v);
-    }
+    scene::terrain_colour(seed, level, x, y, z, rgb);
   }
 };
 
-inline bool can_have_children(uint16_t chunk) {
-  for (int k = 0; k < 8; k++)
-    if (((chunk >> (2 * k)) & 3) == 3) return true;
-  return false;
-}
+using scene::can_have_children;
 
 // MakeChunk (TreeBuilder.cs:264-284) for the cell (x,y,z) at `level`.
 uint16_t make_chunk(const Scene &sc, int level, uint32_t x, uint32_t y, uint32_t z) {
@@ -349,6 +309,7 @@ struct TreeHost {
 
 // A scene whose leaf grid lies one level below node level `scene_depth`.
 struct SceneHost {
+  uint64_t id = 0;  // unique per scene object (keys device copies of its data)
   std::unique_ptr<Scene> scene;
   int scene_depth = 0;
   int threads = 1;
@@ -360,6 +321,8 @@ svo_status make_scene(const svo_scene_params &p, SceneHost &out) {
   const int B = p.base_depth, D = p.max_depth;
   if (B < 1 || B > 6) return fail(SVO_ERR_INVALID_ARGUMENT, "svo_tree_build: base_depth must be 1..6");
   if (D < B + 2 || D > 16) return fail(SVO_ERR_INVALID_ARGUMENT, "svo_tree_build: max_depth must be base_depth+2..16");
+  static std::atomic<uint64_t> next_id{1};
+  out.id = next_id.fetch_add(1);
   out.threads = p.threads > 0 ? p.threads : (int)std::max(1u, std::thread::hardware_concurrency());
   out.scene_depth = D;
   out.base_depth = (uint8_t)B;
@@ -580,6 +543,23 @@ svo_status graft_payload(const SceneHost &scene, const svo_child_request *req, s
     at += st.blocks.size();
   }
   return SVO_OK;
+}
+
+bool scene_terrain_info(const void *scene, TerrainInfo *out) {
+  const SceneHost *sh = static_cast<const SceneHost *>(scene);
+  const TerrainScene *t = dynamic_cast<const TerrainScene *>(sh->scene.get());
+  if (!t || t->leaf >= kMaxTerrainLevels) return false;
+  out->id = sh->id;
+  out->base_depth = sh->base_depth;
+  out->scene_depth = sh->scene_depth;
+  out->leaf = t->leaf;
+  out->res = t->res;
+  out->seed = t->seed;
+  for (int l = 0; l <= t->leaf; l++) {
+    out->lo[l] = t->lo[l].data();
+    out->hi[l] = t->hi[l].data();
+  }
+  return true;
 }
 
 }  // namespace svo

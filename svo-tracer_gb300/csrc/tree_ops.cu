@@ -28,6 +28,7 @@
 #include <vector>
 
 #include "context.h"
+#include "scene_common.h"
 
 namespace svo {
 namespace {
@@ -135,7 +136,8 @@ __global__ void k_free_flags(TreeView t, uint8_t *flags) {
 // ---- stream compaction of a flag array into the ascending list of indices ----
 constexpr int kScanBlock = 1024;
 
-__global__ void k_count(const uint8_t *flags, uint32_t n, uint32_t *block_counts) {
+template <class T>
+__global__ void k_count(const T *flags, uint32_t n, uint32_t *block_counts) {
   uint32_t i = blockIdx.x * kScanBlock + threadIdx.x;
   int c = __syncthreads_count(i < n && flags[i]);
   if (threadIdx.x == 0) block_counts[blockIdx.x] = (uint32_t)c;
@@ -164,7 +166,8 @@ __global__ void k_scan_counts(uint32_t *counts, uint32_t n, uint32_t *total) {
   if (threadIdx.x == kScanBlock - 1) *total = part[kScanBlock - 1];
 }
 
-__global__ void k_scatter(const uint8_t *flags, uint32_t n, const uint32_t *offsets, uint32_t *out) {
+template <class T>
+__global__ void k_scatter(const T *flags, uint32_t n, const uint32_t *offsets, uint32_t *out) {
   __shared__ uint32_t warp_base[kScanBlock / 32];
   uint32_t i = blockIdx.x * kScanBlock + threadIdx.x;
   bool f = i < n && flags[i];
@@ -422,6 +425,221 @@ svo_status sweep_and_free_list(Context &c, const TreeView &t, uint64_t *n_freed)
   return SVO_OK;
 }
 
+// ---- graft payloads generated on the device (terrain scenes) -------------------
+//
+// The same payload the host generator builds for a frame's child requests
+// (one job per distinct requesting node in ascending address order, its eight
+// children and, for TreeSize 1, the children of those that can have children,
+// BuildBlocks-style), grafted with svo_graft's rules, but without the host
+// round trip: requests are deduplicated through a per-node marker, jobs sized
+// and claimed from the free list in record order, and the nodes generated
+// straight into the claimed groups from the terrain's column pyramids.
+
+struct DevTerrain {
+  const uint16_t *lo, *hi;  // all levels concatenated
+  uint64_t off[kMaxTerrainLevels];
+  int leaf;
+  uint32_t res, seed;
+};
+
+struct GenJob {
+  uint32_t address;  // requesting node: the graft target
+  uint32_t x, y, z;  // its cell at `depth`
+  uint32_t q;        // first free-list slot of its groups, or kNone when skipped
+  uint8_t depth, mask, groups, _pad;  // mask: children that get a group of their own
+};
+static_assert(sizeof(GenJob) == 24, "GenJob layout");
+
+__device__ __forceinline__ uint16_t terrain_chunk(const DevTerrain &T, int level, uint32_t x, uint32_t y, uint32_t z) {
+  // MakeChunk: classify the eight level+1 cells
+  const int l1 = level + 1;
+  uint16_t chunk = 0;
+  for (int k = 0; k < 8; k++) {
+    const uint32_t cx = 2 * x + (k & 1), cy = 2 * y + ((k >> 1) & 1), cz = 2 * z + ((k >> 2) & 1);
+    const uint64_t idx = T.off[l1] + (uint64_t)cy * (1u << l1) + cx;
+    bool geo, air;
+    scene::terrain_classify(T.hi[idx], T.lo[idx], T.res, T.leaf, l1, cz, geo, air);
+    chunk |= (uint16_t)((air ? 1 : 0) << (2 * k));
+    chunk |= (uint16_t)((geo ? 1 : 0) << (2 * k + 1));
+  }
+  return chunk;
+}
+
+// MakeBlock of the host builder for a terrain cell (no children yet).
+__device__ __forceinline__ svo_block terrain_block(const DevTerrain &T, int level, uint32_t x, uint32_t y, uint32_t z) {
+  svo_block b;
+  b.child = kNone;
+  b.chunk = terrain_chunk(T, level, x, y, z);
+  b.normal_pitch = 0;
+  b.normal_yaw = 0;
+  uint8_t rgb[3];
+  scene::terrain_colour(T.seed, level, x, y, z, rgb);
+  b.colour_r = rgb[0];
+  b.colour_g = rgb[1];
+  b.colour_b = rgb[2];
+  b.opacity = 255;
+  b.specularity = 0;
+  b.gloss = 0;
+  return b;
+}
+
+// Marks every requesting node with (TreeSize != 0) << 31 | (request + 1),
+// keeping the largest: any request of a node gives its depth and cell.
+__global__ void k_gen_mark(const svo_child_request *req, const uint32_t *n_req, uint32_t cap, uint32_t *marker,
+                           uint32_t n_nodes, int min_depth, int scene_depth) {
+  const uint32_t n = min(*n_req, cap);
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const svo_child_request r = req[i];
+    if (r.depth >= min_depth && r.depth < scene_depth && r.address < n_nodes)
+      atomicMax(&marker[r.address], ((r.tree_size ? 1u : 0u) << 31) | (i + 1));
+  }
+}
+
+// One job per marked node (ascending): its cell, depth and groups; clears the marker.
+__global__ void k_gen_size(const DevTerrain T, const uint32_t *addr, const uint32_t *n_jobs, uint32_t cap,
+                           uint32_t *marker, const svo_child_request *req, int scene_depth, GenJob *jobs) {
+  const uint32_t n = min(*n_jobs, cap);
+  for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+    const uint32_t a = addr[j];
+    const uint32_t m = marker[a];
+    marker[a] = 0;
+    const svo_child_request r = req[(m & 0x7FFFFFFFu) - 1];
+    const int d = r.depth;
+    GenJob g;
+    g.address = a;
+    g.x = (uint32_t)(r.location[0] >> (64 - d));
+    g.y = (uint32_t)(r.location[1] >> (64 - d));
+    g.z = (uint32_t)(r.location[2] >> (64 - d));
+    g.q = kNone;
+    g.depth = (uint8_t)d;
+    g._pad = 0;
+    const int limit = min(scene_depth, d + 1 + (int)(m >> 31));
+    uint32_t mask = 0;
+    if (d + 1 < limit)
+      for (int o = 0; o < 8; o++) {
+        uint16_t ch = terrain_chunk(T, d + 1, 2 * g.x + (o & 1), 2 * g.y + ((o >> 1) & 1), 2 * g.z + ((o >> 2) & 1));
+        if (scene::can_have_children(ch)) mask |= 1u << o;
+      }
+    g.mask = (uint8_t)mask;
+    g.groups = (uint8_t)(1 + __popc(mask));
+    jobs[j] = g;
+  }
+}
+
+// Claims, one CTA: jobs in order take `groups` free-list slots each; a job that
+// no longer fits is skipped and later ones still try (svo_graft's rule).
+// Before the first job that overflows, claims are a prefix sum; from it on one
+// thread applies the rule in order. scalars[1] = applied jobs, [2] = groups.
+__global__ void __launch_bounds__(1024) k_gen_claim(GenJob *jobs, const uint32_t *n_jobs, uint32_t cap,
+                                                    uint64_t avail, uint32_t *scalars) {
+  __shared__ uint32_t part[1024];
+  __shared__ uint32_t first_over, used_at_first;
+  const uint32_t n = min(*n_jobs, cap);
+  const uint32_t per = (n + 1023) / 1024, b = threadIdx.x * per, e = min(n, b + per);
+  uint32_t sum = 0;
+  for (uint32_t j = b; j < e; j++) sum += jobs[j].groups;
+  part[threadIdx.x] = sum;
+  if (threadIdx.x == 0) {
+    first_over = n;
+    used_at_first = 0;
+  }
+  __syncthreads();
+  for (int off = 1; off < 1024; off <<= 1) {
+    uint32_t v = threadIdx.x >= (uint32_t)off ? part[threadIdx.x - off] : 0;
+    __syncthreads();
+    part[threadIdx.x] += v;
+    __syncthreads();
+  }
+  const uint32_t excl = part[threadIdx.x] - sum;
+  uint64_t run = excl;
+  for (uint32_t j = b; j < e; j++) {
+    run += jobs[j].groups;
+    if (run > avail) {
+      atomicMin(&first_over, j);
+      break;
+    }
+  }
+  __syncthreads();
+  const uint32_t k = first_over;
+  run = excl;
+  for (uint32_t j = b; j < e && j <= k; j++) {
+    if (j == k) {
+      used_at_first = (uint32_t)run;
+      break;
+    }
+    jobs[j].q = (uint32_t)run;
+    run += jobs[j].groups;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    uint64_t used = k < n ? used_at_first : (n ? part[1023] : 0);
+    uint32_t applied = k;
+    for (uint32_t j = k; j < n; j++) {
+      const uint32_t gsz = jobs[j].groups;
+      if (used + gsz <= avail) {
+        jobs[j].q = (uint32_t)used;
+        used += gsz;
+        applied++;
+      }
+    }
+    scalars[1] = applied;
+    scalars[2] = (uint32_t)used;
+  }
+}
+
+// Eight threads per claimed job: child o of the requesting node, its own
+// children when it gets a group, usage entries and the link to the target.
+__global__ void k_gen_write(const DevTerrain T, TreeView t, const GenJob *jobs, const uint32_t *n_jobs, uint32_t cap,
+                            const uint32_t *free_list, uint64_t free_base, uint16_t now) {
+  const uint32_t n = min(*n_jobs, cap);
+  for (uint64_t x = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; x < 8ull * n;
+       x += (uint64_t)gridDim.x * blockDim.x) {
+    const GenJob g = jobs[x >> 3];
+    if (g.q == kNone) continue;
+    const uint32_t o = (uint32_t)(x & 7);
+    const uint32_t g0 = free_list[free_base + g.q];
+    const uint32_t node = g0 * 8u + o;
+    const int level = g.depth + 1;
+    const uint32_t cx = 2 * g.x + (o & 1), cy = 2 * g.y + ((o >> 1) & 1), cz = 2 * g.z + ((o >> 2) & 1);
+    svo_block b = terrain_block(T, level, cx, cy, cz);
+    if ((g.mask >> o) & 1u) {
+      const uint32_t k = 1 + __popc(g.mask & ((1u << o) - 1u));
+      const uint32_t gk = free_list[free_base + g.q + k];
+      uint32_t sr = 0, sg = 0, sb = 0, cnt = 0;
+      for (int i = 0; i < 8; i++) {
+        svo_block c = terrain_block(T, level + 1, 2 * cx + (i & 1), 2 * cy + ((i >> 1) & 1), 2 * cz + ((i >> 2) & 1));
+        t.blocks[gk * 8u + i] = c;
+        if ((b.chunk >> (2 * i + 1)) & 1) {  // the mean over the geometry octants
+          sr += c.colour_r;
+          sg += c.colour_g;
+          sb += c.colour_b;
+          cnt++;
+        }
+      }
+      svo_usage u;
+      u.tick = now;
+      u._pad = 0;
+      u.parent = node;
+      t.usage[gk] = u;
+      b.child = gk * 8u;
+      if (cnt) {
+        b.colour_r = (uint8_t)(sr / cnt);
+        b.colour_g = (uint8_t)(sg / cnt);
+        b.colour_b = (uint8_t)(sb / cnt);
+      }
+    }
+    t.blocks[node] = b;
+    if (o == 0) {
+      svo_usage u;
+      u.tick = now;
+      u._pad = 0;
+      u.parent = g.address;
+      t.usage[g0] = u;
+      t.blocks[g.address].child = g0 * 8u;
+    }
+  }
+}
+
 }  // namespace
 }  // namespace svo
 
@@ -640,3 +858,101 @@ SVO_API svo_status svo_prune(void *ctx, const svo_update_input *in, const svo_pr
 }
 
 }  // extern "C"
+
+SVO_API svo_status svo_graft_generate(void *ctx, void *scene, const svo_update_input *in, svo_graft_report *report) {
+  CTX(ctx, "svo_graft_generate");
+  if (!scene || !in) return fail(SVO_ERR_INVALID_ARGUMENT, "svo_graft_generate: null argument");
+  if (in->tick < 1 || in->tick > 65533) return fail(SVO_ERR_INVALID_ARGUMENT, "svo_graft_generate: tick must be 1..65533");
+  svo::TerrainInfo ti;
+  if (!svo::scene_terrain_info(scene, &ti))
+    return fail(SVO_ERR_INVALID_ARGUMENT, "svo_graft_generate: device generation needs a terrain scene");
+  if (ti.base_depth != c.base_depth)
+    return fail(SVO_ERR_INVALID_ARGUMENT, "svo_graft_generate: scene and resident tree differ in base depth");
+  svo_status st = svo::ensure_tree_buffers(c);
+  if (st) return st;
+  svo::TreeView t = svo::view_of(c);
+  if (!c.free_valid) {  // no GC ran since the tree changed: build the free list now
+    uint64_t dummy = 0;
+    st = svo::sweep_and_free_list(c, t, &dummy);
+    if (st) return st;
+    c.n_freed = dummy;
+  }
+  if (report) std::memset(report, 0, sizeof(*report));
+  const uint32_t cap = c.request_cap;
+  if (cap == 0 || !c.requests.p) {
+    c.n_claimed = 0;
+    return SVO_OK;
+  }
+  // the scene's column pyramids, once per scene
+  svo::DevTerrain T{};
+  uint64_t total = 0;
+  for (int l = 0; l <= ti.leaf; l++) {
+    T.off[l] = total;
+    total += 1ull << (2 * l);
+  }
+  if (c.terrain_id != ti.id) {
+    c.terrain_id = 0;
+    if (c.terrain_lo.reserve(total) || c.terrain_hi.reserve(total))
+      return fail(SVO_ERR_OUT_OF_MEMORY, "svo_graft_generate: terrain allocation failed");
+    for (int l = 0; l <= ti.leaf; l++) {
+      size_t bytes = (1ull << (2 * l)) * sizeof(uint16_t);
+      SVO_CUDA(cudaMemcpyAsync(c.terrain_lo.p + T.off[l], ti.lo[l], bytes, cudaMemcpyHostToDevice, c.stream),
+               "svo_graft_generate: terrain");
+      SVO_CUDA(cudaMemcpyAsync(c.terrain_hi.p + T.off[l], ti.hi[l], bytes, cudaMemcpyHostToDevice, c.stream),
+               "svo_graft_generate: terrain");
+    }
+    SVO_CUDA(cudaStreamSynchronize(c.stream), "svo_graft_generate: terrain");
+    c.terrain_id = ti.id;
+  }
+  T.lo = c.terrain_lo.p;
+  T.hi = c.terrain_hi.p;
+  T.leaf = ti.leaf;
+  T.res = ti.res;
+  T.seed = ti.seed;
+  // marker (zero between calls), compaction counts, jobs
+  const uint32_t n_nodes = (uint32_t)(c.n_groups * 8);
+  if (c.gen_marker.n < n_nodes) {
+    if (c.gen_marker.reserve(n_nodes)) return fail(SVO_ERR_OUT_OF_MEMORY, "svo_graft_generate: allocation failed");
+    SVO_CUDA(cudaMemsetAsync(c.gen_marker.p, 0, (size_t)n_nodes * 4, c.stream), "svo_graft_generate: marker");
+  }
+  const uint32_t nb = (n_nodes + svo::kScanBlock - 1) / svo::kScanBlock;
+  if (c.gen_counts.reserve(nb + 1) || c.gen_addr.reserve(std::max(1u, std::min(n_nodes, cap))) ||
+      c.gen_scalars.reserve(4) || c.gen_jobs.reserve(sizeof(svo::GenJob) * (size_t)cap))
+    return fail(SVO_ERR_OUT_OF_MEMORY, "svo_graft_generate: allocation failed");
+  uint32_t *scalars = c.gen_scalars.p;  // [0] jobs, [1] applied, [2] claimed groups
+  svo::GenJob *jobs = reinterpret_cast<svo::GenJob *>(c.gen_jobs.p);
+  const uint32_t *n_req = c.counters.p + 1;  // the last trace's request count
+  svo::k_gen_mark<<<svo::grid_for(cap), 256, 0, c.stream>>>(c.requests.p, n_req, cap, c.gen_marker.p, n_nodes,
+                                                            ti.base_depth + 2, ti.scene_depth);
+  svo::k_count<<<nb, svo::kScanBlock, 0, c.stream>>>(c.gen_marker.p, n_nodes, c.gen_counts.p);
+  svo::k_scan_counts<<<1, svo::kScanBlock, 0, c.stream>>>(c.gen_counts.p, nb, scalars);
+  // marked nodes never exceed the stored requests (at most cap), the job buffer's size
+  svo::k_scatter<<<nb, svo::kScanBlock, 0, c.stream>>>(c.gen_marker.p, n_nodes, c.gen_counts.p, c.gen_addr.p);
+  svo::k_gen_size<<<svo::grid_for(cap), 256, 0, c.stream>>>(T, c.gen_addr.p, scalars, cap, c.gen_marker.p,
+                                                            c.requests.p, ti.scene_depth, jobs);
+  const uint64_t avail = c.n_free - c.free_used;
+  svo::k_gen_claim<<<1, 1024, 0, c.stream>>>(jobs, scalars, cap, avail, scalars);
+  svo::k_gen_write<<<svo::grid_for(8ull * cap), 256, 0, c.stream>>>(T, t, jobs, scalars, cap, c.free_list.p,
+                                                                    c.free_used, in->tick);
+  SVO_CUDA(cudaGetLastError(), "svo_graft_generate: kernels");
+  uint32_t sc[3] = {0, 0, 0};
+  SVO_CUDA(cudaMemcpyAsync(sc, scalars, sizeof(sc), cudaMemcpyDeviceToHost, c.stream), "svo_graft_generate: counts");
+  SVO_CUDA(cudaStreamSynchronize(c.stream), "svo_graft_generate: synchronize");
+  const uint64_t claimed = sc[2];
+  if (claimed) {
+    if (c.claimed_list.reserve(claimed)) return fail(SVO_ERR_OUT_OF_MEMORY, "svo_graft_generate: allocation failed");
+    SVO_CUDA(cudaMemcpyAsync(c.claimed_list.p, c.free_list.p + c.free_used, claimed * 4, cudaMemcpyDeviceToDevice,
+                             c.stream), "svo_graft_generate: claimed list");
+    SVO_CUDA(cudaStreamSynchronize(c.stream), "svo_graft_generate: synchronize");
+    c.tree_depth = SVO_MAX_TREE_DEPTH;  // grafted subtrees can reach below the deepest level seen at upload
+  }
+  c.n_claimed = claimed;
+  c.free_used += claimed;
+  if (report) {
+    report->applied = sc[1];
+    report->skipped = sc[0] - sc[1];
+    report->claimed = claimed;
+    report->free_left = c.n_free - c.free_used;
+  }
+  return SVO_OK;
+}

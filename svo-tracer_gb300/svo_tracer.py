@@ -154,6 +154,7 @@ def load_library(path: str | None = None) -> C.CDLL:
         "svo_tree_data": ([vp, C.POINTER(vp), C.POINTER(vp)], C.c_int32),
         "svo_tree_free": ([vp], C.c_int32),
         "svo_init_usage_tree": ([vp, C.c_uint16], C.c_int32),
+        "svo_graft_generate": ([vp, vp, C.POINTER(UpdateInputC), C.POINTER(GraftReportC)], C.c_int32),
         "svo_oct_write": ([C.c_char_p, C.c_uint8, C.c_uint32, vp, sz, vp, sz], C.c_int32),
         "svo_oct_read": ([C.c_char_p, C.POINTER(C.c_void_p)], C.c_int32),
         "svo_diff_set_params": ([vp, vp, sz, C.c_int32], C.c_int32),
@@ -755,6 +756,14 @@ class Tracer:
         rep = GraftReportC()
         _check("Graft", self._lib.svo_graft(self._ctx, C.byref(self._update(tick)), _ptr(rec), len(rec), _ptr(pay),
                                             len(pay), _ptr(loc), 0 if loc is None else loc.size, C.byref(rep)))
+        return {"applied": rep.applied, "skipped": rep.skipped, "claimed": rep.claimed, "free_left": rep.free_left}
+
+    def graft_generate(self, tick: int, scene: "Scene") -> dict:
+        """Answers the last trace's child requests on the device from a terrain
+        scene: what scene.graft_payload + graft do, without the host round trip."""
+        rep = GraftReportC()
+        _check("GraftGenerate", self._lib.svo_graft_generate(self._ctx, scene._h, C.byref(self._update(tick)),
+                                                             C.byref(rep)))
         return {"applied": rep.applied, "skipped": rep.skipped, "claimed": rep.claimed, "free_left": rep.free_left}
 
     def graft_claims(self, n: int) -> np.ndarray:

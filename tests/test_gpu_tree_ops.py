@@ -153,3 +153,51 @@ def test_graft_location_targets_and_budget(tracer):
     assert grep["applied"] == int(applied.sum()) > 0
     assert np.array_equal(tracer.graft_claims(grep["claimed"]), o_claims)
     assert_state(tracer, oracle, "graft")
+
+
+@pytest.mark.parametrize("initial,extra_groups", [(7, 1 << 14), (6, 40)], ids=["roomy", "budget_runs_out"])
+def test_graft_generate_matches_host_path(tracer, initial, extra_groups):
+    """Device-side generation (svo_graft_generate) against the host path of the
+    streaming workflow (read the requests back, generate the payload on the
+    host, svo_graft): same reports, same claimed groups, same tree, frame by
+    frame; with a small budget most jobs are skipped once it runs out."""
+    scene = st.Scene(st.SCENE_TERRAIN, seed=5, base_depth=3, depth=9)
+    tree = scene.build_tree(initial)
+    budget = len(tree.Blocks) // 8 + extra_groups
+    dev = st.Tracer(0)
+    try:
+        for tr in (tracer, dev):
+            tr.set_config(block_size=256, ctas_per_sm=0, ray_chunk=1, cadence=16, max_steps=1 << 16, collect_stats=0)
+            tr.upload(tree, block_budget=budget * 8)
+            tr.init_usage_tree(1)
+        cams = st.camera_path(seed=3, frames=8, width=160, height=90, MaxChildRequestId=1 << 16)
+        applied = skipped = 0
+        for f, cam in enumerate(cams):
+            tick = f + 1
+            tracer.trace(cam)
+            dev.trace(cam)
+            req, _ = tracer.read_child_requests()
+            rec, pay = scene.graft_payload(req)
+            assert tracer.gc(tick, 3) == dev.gc(tick, 3)
+            a = tracer.graft(tick, rec, pay)
+            b = dev.graft_generate(tick, scene)
+            assert a == b, "frame %d: %r vs %r" % (f, a, b)
+            assert np.array_equal(tracer.graft_claims(a["claimed"]), dev.graft_claims(b["claimed"]))
+            hb, hu = gpu_state(tracer, budget)
+            db, du = gpu_state(dev, budget)
+            assert hb.tobytes() == db.tobytes(), "frame %d: blocks differ" % f
+            assert hu.tobytes() == du.tobytes(), "frame %d: usage differs" % f
+            applied += a["applied"]
+            skipped += a["skipped"]
+        assert applied > 0
+        if extra_groups < 100:
+            assert skipped > 0
+    finally:
+        dev.close()
+
+
+def test_graft_generate_needs_terrain(tracer):
+    scene = st.Scene(st.SCENE_SPHERE, seed=1, base_depth=2, depth=6)
+    tracer.upload(scene.build_tree(5))
+    with pytest.raises(st.SvoError):
+        tracer.graft_generate(1, scene)
