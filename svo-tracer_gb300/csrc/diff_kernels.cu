@@ -161,6 +161,7 @@ __global__ void __launch_bounds__(256, kBackward ? SVO_DIFF_BWD_MIN_CTAS : SVO_D
     uint32_t *dst = reinterpret_cast<uint32_t *>(s_views);
     for (uint32_t i = threadIdx.x; i < a.n_views * sizeof(ViewParams) / 4; i += blockDim.x) dst[i] = src[i];
     for (uint32_t i = threadIdx.x; i < a.n_bases; i += blockDim.x) s_bases[i] = __ldg(a.bases + i);
+    fill_spread_table();
   }
   __syncthreads();
   __shared__ float4 s_agg[256];  // gradient slots of the warp aggregation, one per thread

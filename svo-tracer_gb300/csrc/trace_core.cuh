@@ -54,10 +54,20 @@ __device__ __forceinline__ uint32_t spread3(uint32_t v) {
   return v;
 }
 
-// baseLocation (wavefront.cl:405-411) for 1 <= depth <= 10.
+// spread3 of every 10-bit value, in shared memory: filled by each CTA of the
+// kernels that step rays (fill_spread_table before their first __syncthreads).
+__shared__ uint32_t s_spread3[1024];
+
+__device__ __forceinline__ void fill_spread_table() {
+  for (uint32_t i = threadIdx.x; i < 1024; i += blockDim.x) s_spread3[i] = spread3(i);
+}
+
+// baseLocation (wavefront.cl:405-411) for 1 <= depth <= 10: the Morton index of
+// the top `depth` bits of each coordinate (all within the high 32 bits).
 __device__ __forceinline__ uint32_t cell_index(int depth, uint64_t x, uint64_t y, uint64_t z) {
-  int s = 64 - depth;
-  return spread3((uint32_t)(x >> s)) | (spread3((uint32_t)(y >> s)) << 1) | (spread3((uint32_t)(z >> s)) << 2);
+  const uint32_t s = 32 - depth;
+  const uint32_t cx = (uint32_t)(x >> 32) >> s, cy = (uint32_t)(y >> 32) >> s, cz = (uint32_t)(z >> 32) >> s;
+  return s_spread3[cx] | (s_spread3[cy] << 1) | (s_spread3[cz] << 2);
 }
 
 // chunkPosition (wavefront.cl:428-430)
