@@ -19,8 +19,12 @@ namespace cg = cooperative_groups;
 constexpr unsigned kFull = 0xffffffffu;
 constexpr uint64_t kAll = ~0ull;
 
-__constant__ uint32_t c_pow_sum[12] = {0,      8,       72,       584,       4680,       37448,
-                                       299592, 2396744, 19173960, 153391688, 1227133512, 0};
+// powSum (wavefront.cl:224): base chunks of levels 1..depth, depth 0..10, by
+// the reference's shift of a repeating octal pattern (no table: lanes at
+// different depths would serialise on a constant-memory read).
+__device__ __forceinline__ uint32_t pow_sum(int depth) {
+  return (uint32_t)((0b1001001001001001001001001001001000ull >> ((11 - depth) * 3)) - 1);
+}
 
 // (float)x of a 64-bit fixed-point value (ulongToFloat, wavefront.cl:209,
 // without the 2^-64 scaling).
@@ -37,12 +41,14 @@ __device__ __forceinline__ uint64_t unit_to_ulong(float x) {
   return __float2ull_rz(v);
 }
 
-// roundUlong (wavefront.cl:211-221)
-__device__ __forceinline__ uint64_t round_ulong(uint64_t v, int d, bool up) {
-  uint64_t mask = ~(kAll >> (d + 1));
-  if (up) return ((v & mask) + (0x8000000000000000ull >> d)) - v;
-  uint64_t out = v - ((v & mask) - 1);
-  return out >= v ? v : out;
+// roundUlong (wavefront.cl:211-221) in closed form, `low` = the bits below
+// level d+1 (kAll >> (d + 1)): up, the distance to the next boundary is
+// (~v & low) + 1 (wrapping to 2^64 - v in the top cell like the reference's
+// sum); down, (v & low) + 1, or v itself in the lowest cell, where the
+// reference's subtraction wraps and its comparison returns v.
+__device__ __forceinline__ uint64_t round_ulong(uint64_t v, uint64_t low, bool up) {
+  if (up) return (~v & low) + 1;
+  return (v & ~low) ? (v & low) + 1 : v;
 }
 
 __device__ __forceinline__ uint32_t spread3(uint32_t v) {
@@ -103,9 +109,10 @@ __device__ __forceinline__ uint4 load_node(const uint4 *blocks, uint32_t n_block
 
 // traverseChunk (wavefront.cl:440-497) without the trailing setConeDepth.
 __device__ __forceinline__ void traverse(Ray &r, int depth) {
-  uint64_t d0 = round_ulong(r.lx, depth, r.sx);
-  uint64_t d1 = round_ulong(r.ly, depth, r.sy);
-  uint64_t d2 = round_ulong(r.lz, depth, r.sz);
+  const uint64_t low = kAll >> (depth + 1);
+  uint64_t d0 = round_ulong(r.lx, low, r.sx);
+  uint64_t d1 = round_ulong(r.ly, low, r.sy);
+  uint64_t d2 = round_ulong(r.lz, low, r.sz);
   const float f0 = ulong_to_float(d0), f1 = ulong_to_float(d1), f2 = ulong_to_float(d2);
   float a0 = fabsf(__fmul_rn(f0, r.ix));
   float a1 = fabsf(__fmul_rn(f1, r.iy));
@@ -256,7 +263,7 @@ __device__ __forceinline__ int step(const TraceLaunch &a, const ViewParams &v, c
   const int lvl = r.depth - (B + 2);
   uint32_t chunk;
   if (!block) {
-    uint32_t idx = c_pow_sum[r.depth - 1] + cell_index(r.depth, r.lx, r.ly, r.lz);
+    uint32_t idx = pow_sum(r.depth - 1) + cell_index(r.depth, r.lx, r.ly, r.lz);
     chunk = kSmemBases ? s_bases[idx] : __ldg(a.bases + idx);
     if (kStats) w.v_base++;
   } else {
