@@ -50,7 +50,8 @@ static uint32_t pow_sum(int depth) {
   return s;
 }
 
-// Deepest node level reachable from the dense level B+2 (host scan).
+// Deepest node level reachable from the dense level B+2 through child links
+// (host scan, bounded by SVO_MAX_TREE_DEPTH + 1).
 static int scan_tree_depth(const svo_block *blocks, size_t n_blocks, int B) {
   size_t dense = (size_t)1 << (3 * (B + 2));
   int threads = (int)std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
@@ -68,10 +69,10 @@ static int scan_tree_depth(const svo_block *blocks, size_t n_blocks, int B) {
           if (d > best[t]) best[t] = d;
           if (d >= SVO_MAX_TREE_DEPTH + 1) continue;
           uint32_t c = blocks[addr].child;
-          // only nodes the traversal can descend into: geometry octants
+          // every child group, as the reachability of the tree updates walks
+          // them (a tree may hang groups below octants without geometry)
           if (c == SVO_NO_CHILD || (size_t)c + 8 > n_blocks) continue;
-          for (uint32_t k = 0; k < 8; k++)
-            if ((blocks[addr].chunk >> (2 * k + 1)) & 1) stack.push_back({c + k, d + 1});
+          for (uint32_t k = 0; k < 8; k++) stack.push_back({c + k, d + 1});
         }
       }
     });

@@ -112,8 +112,16 @@ __global__ void k_stale_detach(TreeView t, uint16_t now, uint32_t threshold, uin
 }
 
 // Frees allocated groups that are no longer reachable; flags them.
-__global__ void k_sweep(TreeView t, const uint32_t *reach, uint8_t *flags) {
+// `unfinished`: the frontier left after the last breadth-first level; when it is
+// not empty the tree is deeper than the levels run, reachability is incomplete,
+// and nothing is freed (the host reports the error).
+__global__ void k_sweep(TreeView t, const uint32_t *reach, uint8_t *flags, const uint32_t *unfinished) {
+  const bool ok = *unfinished == 0;
   for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < t.n_groups; g += gridDim.x * blockDim.x) {
+    if (!ok) {
+      flags[g] = 0;
+      continue;
+    }
     uint8_t f = 0;
     uint32_t tk = t.usage[g].tick;
     if (tk >= 1 && tk <= 65533 && !reach[g] && !dense_real(t, g)) {
@@ -364,62 +372,85 @@ svo_status ensure_tree_buffers(Context &c) {
   size_t g = c.n_groups;
   size_t nb = (g + kScanBlock - 1) / kScanBlock + 1;
   if (c.reach.reserve(g) || c.parent_min.reserve(g) || c.frontier_a.reserve(g) || c.frontier_b.reserve(g) ||
-      c.flags.reserve(g) || c.scan_tmp.reserve(nb + 8) || c.free_list.reserve(g) || c.pruned_list.reserve(g) ||
+      c.flags.reserve(g) || c.scan_tmp.reserve(nb + 12) || c.free_list.reserve(g) || c.pruned_list.reserve(g) ||
       c.freed_list.reserve(g))
     return fail(SVO_ERR_OUT_OF_MEMORY, "tree update: device allocation failed");
   return SVO_OK;
 }
 
-// Breadth-first reachability from the dense-real groups (one launch per level).
-svo_status reachability(Context &c, const TreeView &t) {
-  // scan_tmp = [block counts | ... | n-8, n-7: frontier sizes | n-6: compact total | n-5: prune flag]
+// Breadth-first reachability from the dense-real groups, one launch per tree
+// level below B+2 without reading the frontier sizes back: each launch reads
+// its frontier size on the device (an empty frontier makes it a no-op). The
+// tree's nodes lie at depths <= c.tree_depth, so tree_depth - B - 1 levels end
+// with an empty frontier; the returned pointer holds the frontier left after
+// the last level (0 when reachability is complete).
+// scan_tmp = [block counts | ... | n-8, n-7: frontier sizes | n-6: compact total
+//             | n-5: prune flag | n-4..n-2: GC totals]
+uint32_t *reachability_async(Context &c, const TreeView &t) {
   uint32_t *cnt = c.scan_tmp.p + (c.scan_tmp.n - 8);
-  SVO_CUDA(cudaMemsetAsync(cnt, 0, 2 * sizeof(uint32_t), c.stream), "reachability: reset");
+  cudaMemsetAsync(cnt, 0, 2 * sizeof(uint32_t), c.stream);
   k_reach_seed<<<grid_for(t.n_groups), 256, 0, c.stream>>>(t, c.reach.p, c.parent_min.p, c.frontier_a.p, cnt);
   uint32_t *in = c.frontier_a.p, *out = c.frontier_b.p;
   uint32_t *n_in = cnt, *n_out = cnt + 1;
-  for (int level = 0; level < SVO_MAX_TREE_DEPTH + 2; level++) {
-    uint32_t n = 0;
-    SVO_CUDA(cudaMemcpyAsync(&n, n_in, 4, cudaMemcpyDeviceToHost, c.stream), "reachability: frontier size");
-    SVO_CUDA(cudaStreamSynchronize(c.stream), "reachability: synchronize");
-    if (n == 0) return SVO_OK;
-    SVO_CUDA(cudaMemsetAsync(n_out, 0, 4, c.stream), "reachability: reset");
-    k_reach_expand<<<grid_for(8ull * n), 256, 0, c.stream>>>(t, in, n_in, out, n_out, c.reach.p, c.parent_min.p);
-    SVO_CUDA(cudaGetLastError(), "reachability: expand");
+  const int levels = std::max(1, std::min(c.tree_depth, SVO_MAX_TREE_DEPTH) - (int)c.base_depth - 1);
+  for (int level = 0; level < levels; level++) {
+    cudaMemsetAsync(n_out, 0, 4, c.stream);
+    k_reach_expand<<<152 * 8, 256, 0, c.stream>>>(t, in, n_in, out, n_out, c.reach.p, c.parent_min.p);
     std::swap(in, out);
     std::swap(n_in, n_out);
   }
-  return fail(SVO_ERR_INTERNAL, "reachability: tree deeper than SVO_MAX_TREE_DEPTH");
+  return n_in;
 }
 
-// Ascending indices of flags[i] != 0 into out; returns the count.
-svo_status compact(Context &c, const uint8_t *flags, uint32_t n, uint32_t *out, uint64_t *count) {
-  uint32_t nb = (n + kScanBlock - 1) / kScanBlock;
-  uint32_t *counts = c.scan_tmp.p, *total = c.scan_tmp.p + (c.scan_tmp.n - 6);
-  if (nb == 0) {
-    *count = 0;
-    return SVO_OK;
-  }
-  k_count<<<nb, kScanBlock, 0, c.stream>>>(flags, n, counts);
-  k_scan_counts<<<1, kScanBlock, 0, c.stream>>>(counts, nb, total);
-  k_scatter<<<nb, kScanBlock, 0, c.stream>>>(flags, n, counts, out);
-  SVO_CUDA(cudaGetLastError(), "compact");
-  uint32_t t = 0;
-  SVO_CUDA(cudaMemcpyAsync(&t, total, 4, cudaMemcpyDeviceToHost, c.stream), "compact: total");
-  SVO_CUDA(cudaStreamSynchronize(c.stream), "compact: synchronize");
-  *count = t;
+svo_status reachability(Context &c, const TreeView &t) {
+  uint32_t *left = reachability_async(c, t);
+  SVO_CUDA(cudaGetLastError(), "reachability");
+  uint32_t n = 0;
+  SVO_CUDA(cudaMemcpyAsync(&n, left, 4, cudaMemcpyDeviceToHost, c.stream), "reachability: frontier size");
+  SVO_CUDA(cudaStreamSynchronize(c.stream), "reachability: synchronize");
+  if (n) return fail(SVO_ERR_INTERNAL, "reachability: tree deeper than its recorded depth");
   return SVO_OK;
 }
 
-svo_status sweep_and_free_list(Context &c, const TreeView &t, uint64_t *n_freed) {
-  svo_status st = reachability(c, t);
-  if (st) return st;
-  k_sweep<<<grid_for(t.n_groups), 256, 0, c.stream>>>(t, c.reach.p, c.flags.p);
-  st = compact(c, c.flags.p, t.n_groups, c.freed_list.p, n_freed);
-  if (st) return st;
+// Ascending indices of flags[i] != 0 into out; the count goes to *total on the device.
+void compact_async(Context &c, const uint8_t *flags, uint32_t n, uint32_t *out, uint32_t *total) {
+  uint32_t nb = (n + kScanBlock - 1) / kScanBlock;
+  if (nb == 0) {
+    cudaMemsetAsync(total, 0, 4, c.stream);
+    return;
+  }
+  uint32_t *counts = c.scan_tmp.p;
+  k_count<<<nb, kScanBlock, 0, c.stream>>>(flags, n, counts);
+  k_scan_counts<<<1, kScanBlock, 0, c.stream>>>(counts, nb, total);
+  k_scatter<<<nb, kScanBlock, 0, c.stream>>>(flags, n, counts, out);
+}
+
+
+// Reachability, the sweep of unreachable allocated groups and the free list,
+// then one read-back of the counts: the freed count, the free-list length and
+// (with `pruned_total`, a device slot already written) the pruned count.
+svo_status sweep_and_free_list(Context &c, const TreeView &t, uint64_t *n_freed, uint64_t *n_pruned = nullptr,
+                               const uint32_t *pruned_total = nullptr) {
+  uint32_t *left = reachability_async(c, t);
+  uint32_t *totals = c.scan_tmp.p + (c.scan_tmp.n - 4);  // [0] freed, [1] free, [2] frontier left
+  k_sweep<<<grid_for(t.n_groups), 256, 0, c.stream>>>(t, c.reach.p, c.flags.p, left);
+  compact_async(c, c.flags.p, t.n_groups, c.freed_list.p, totals);
   k_free_flags<<<grid_for(t.n_groups), 256, 0, c.stream>>>(t, c.flags.p);
-  st = compact(c, c.flags.p, t.n_groups, c.free_list.p, &c.n_free);
-  if (st) return st;
+  compact_async(c, c.flags.p, t.n_groups, c.free_list.p, totals + 1);
+  SVO_CUDA(cudaMemcpyAsync(totals + 2, left, 4, cudaMemcpyDeviceToDevice, c.stream), "tree update: frontier");
+  SVO_CUDA(cudaGetLastError(), "tree update: kernels");
+  uint32_t h[4] = {0, 0, 0, 0};
+  SVO_CUDA(cudaMemcpyAsync(h, totals, 3 * sizeof(uint32_t), cudaMemcpyDeviceToHost, c.stream), "tree update: counts");
+  if (pruned_total)
+    SVO_CUDA(cudaMemcpyAsync(h + 3, pruned_total, 4, cudaMemcpyDeviceToHost, c.stream), "tree update: counts");
+  SVO_CUDA(cudaStreamSynchronize(c.stream), "tree update: synchronize");
+  if (h[2]) {
+    c.free_valid = false;
+    return fail(SVO_ERR_INTERNAL, "tree update: tree deeper than its recorded depth; nothing was freed");
+  }
+  *n_freed = h[0];
+  if (n_pruned) *n_pruned = h[3];
+  c.n_free = h[1];
   c.free_used = 0;
   c.free_valid = true;
   return SVO_OK;
@@ -677,9 +708,9 @@ SVO_API svo_status svo_gc(void *ctx, const svo_update_input *in, svo_gc_report *
   if (st) return st;
   svo::TreeView t = svo::view_of(c);
   svo::k_stale_detach<<<svo::grid_for(t.n_groups), 256, 0, c.stream>>>(t, in->tick, in->offset, c.flags.p);
-  st = svo::compact(c, c.flags.p, t.n_groups, c.pruned_list.p, &c.n_pruned);
-  if (st) return st;
-  st = svo::sweep_and_free_list(c, t, &c.n_freed);
+  uint32_t *pruned_total = c.scan_tmp.p + (c.scan_tmp.n - 5 + 4);  // the slot after the GC totals
+  svo::compact_async(c, c.flags.p, t.n_groups, c.pruned_list.p, pruned_total);
+  st = svo::sweep_and_free_list(c, t, &c.n_freed, &c.n_pruned, pruned_total);
   if (st) return st;
   if (report) {
     report->pruned = c.n_pruned;
@@ -841,6 +872,8 @@ SVO_API svo_status svo_prune(void *ctx, const svo_update_input *in, const svo_pr
   SVO_CUDA(cudaMemcpyAsync(&was_culled, culled, 4, cudaMemcpyDeviceToHost, c.stream), "svo_prune: flag");
   SVO_CUDA(cudaMemcpyAsync(&after, c.counters.p + 1, 4, cudaMemcpyDeviceToHost, c.stream), "svo_prune: requests");
   SVO_CUDA(cudaStreamSynchronize(c.stream), "svo_prune: synchronize");
+  // CullChild can point a node at any group: the tree's depth is no longer known
+  c.tree_depth = SVO_MAX_TREE_DEPTH;
   uint64_t freed = 0;
   if (was_culled) {
     st = svo::sweep_and_free_list(c, t, &freed);
@@ -944,7 +977,8 @@ SVO_API svo_status svo_graft_generate(void *ctx, void *scene, const svo_update_i
     SVO_CUDA(cudaMemcpyAsync(c.claimed_list.p, c.free_list.p + c.free_used, claimed * 4, cudaMemcpyDeviceToDevice,
                              c.stream), "svo_graft_generate: claimed list");
     SVO_CUDA(cudaStreamSynchronize(c.stream), "svo_graft_generate: synchronize");
-    c.tree_depth = SVO_MAX_TREE_DEPTH;  // grafted subtrees can reach below the deepest level seen at upload
+    // generated nodes lie at most at the scene's depth
+    c.tree_depth = std::max(c.tree_depth, ti.scene_depth);
   }
   c.n_claimed = claimed;
   c.free_used += claimed;
