@@ -205,6 +205,8 @@ svo_status prepare_launch(Context &c, int32_t n_views, uint32_t total_rays, Trac
 constexpr int kMaxViews = 512;
 
 // Reads the kernel's error record (synchronises the stream).
+// Reads the kernel's error record together with whatever the stream already
+// holds (one synchronisation).
 static svo_status check_kernel_error(Context &c) {
   uint32_t e[6] = {0};
   SVO_CUDA(cudaMemcpyAsync(e, c.counters.p + 4, sizeof(e), cudaMemcpyDeviceToHost, c.stream), "svo_trace: error record");
@@ -223,10 +225,35 @@ static svo_status run_trace(Context &c, const svo_trace_input *in, int32_t n, co
   if (n <= 0 || !in || !out) return fail(SVO_ERR_INVALID_ARGUMENT, "svo_trace: bad view list");
   if (n > kMaxViews) return fail(SVO_ERR_INVALID_ARGUMENT, "svo_trace_batch: at most 512 views per call");
   SVO_CUDA(cudaSetDevice(c.device), "cudaSetDevice");
-  bool on_device = out[0].on_device != 0;
+  const bool host_outputs = out[0].on_device == 0;
   for (int i = 1; i < n; i++)
-    if ((out[i].on_device != 0) != on_device)
+    if ((out[i].on_device == 0) != host_outputs)
       return fail(SVO_ERR_INVALID_ARGUMENT, "svo_trace: outputs of one call must all be host or all device");
+  // Host outputs in pinned memory are written by the kernel itself (the GPU
+  // addresses pinned memory directly), so their transfer overlaps the trace;
+  // any other host output goes through device buffers and copies afterwards.
+  std::vector<svo_trace_output> mapped;
+  if (host_outputs) {
+    bool all_pinned = true;
+    mapped.assign(out, out + n);
+    for (int i = 0; i < n && all_pinned; i++) {
+      void **ptrs[4] = {reinterpret_cast<void **>(&mapped[i].hit_index), reinterpret_cast<void **>(&mapped[i].hit_depth),
+                        reinterpret_cast<void **>(&mapped[i].t), reinterpret_cast<void **>(&mapped[i].rgba)};
+      for (void **pp : ptrs) {
+        if (!*pp) continue;
+        cudaPointerAttributes at{};
+        if (cudaPointerGetAttributes(&at, *pp) != cudaSuccess || at.type != cudaMemoryTypeHost || !at.devicePointer) {
+          cudaGetLastError();  // an unregistered pointer is not an error here
+          all_pinned = false;
+          break;
+        }
+        *pp = at.devicePointer;
+      }
+      mapped[i].on_device = 1;
+    }
+    if (all_pinned) out = mapped.data();
+  }
+  const bool on_device = out[0].on_device != 0;  // device buffers, or pinned host memory the kernel writes
   size_t pixels = 0;
   uint32_t cap = 0;
   for (int i = 0; i < n; i++) {
@@ -325,9 +352,9 @@ static svo_status run_trace(Context &c, const svo_trace_input *in, int32_t n, co
         SVO_CUDA(cudaMemcpyAsync(out[i].rgba, c.o_rgba.p + 4 * off, np * 16, cudaMemcpyDeviceToHost, c.stream), "svo_trace: read rgba");
       off += np;
     }
-    SVO_CUDA(cudaStreamSynchronize(c.stream), "svo_trace: synchronize");
-    return check_kernel_error(c);
+    return check_kernel_error(c);  // synchronises after the copies
   }
+  if (host_outputs) return check_kernel_error(c);  // the kernel wrote pinned host memory: wait for it
   return SVO_OK;
 }
 

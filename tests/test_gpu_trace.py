@@ -252,3 +252,30 @@ def test_errors(tracer):
     with pytest.raises(st.SvoError):
         tracer.set_config(schedule=3)
     assert lib is not None
+
+
+def test_pinned_host_outputs_equal_staged_outputs(tracer):
+    """Host outputs in pinned memory are written by the kernel directly; pageable
+    host outputs go through device buffers. Both give the same results, on two
+    calls in a row and in a batch with one view's outputs partly absent."""
+    torch = pytest.importorskip("torch")
+    tree = st.TreeBuilder(st.SCENE_TERRAIN, seed=5).BuildTree(3, 8)
+    tracer.upload(tree)
+    tracer.init_usage()
+    cams = [st.look_at((0.1, 0.15, 0.55), (0.7, 0.7, 0.9), 123, 77, 60.0, Tick=3),
+            st.look_at((0.9, 0.2, 0.6), (0.3, 0.6, 0.9), 64, 48, 70.0, Tick=3)]
+
+    def pinned(w, h):
+        n = w * h
+        return st.TraceResult(torch.empty(n, dtype=torch.int32, pin_memory=True).numpy().view(np.uint32),
+                              torch.empty(n, dtype=torch.uint8, pin_memory=True).numpy(),
+                              torch.empty(n, dtype=torch.float32, pin_memory=True).numpy(),
+                              torch.empty(n * 4, dtype=torch.float32, pin_memory=True).numpy().reshape(n, 4))
+
+    for cam in cams:
+        for _ in range(2):
+            want = tracer.trace(cam)  # pageable numpy outputs: staged
+            got = tracer.trace(cam, out=pinned(*cam.ScreenSize))
+            for k in ("hit_index", "hit_depth", "t", "rgba"):
+                assert np.array_equal(getattr(got, k).reshape(-1), getattr(want, k).reshape(-1)), k
+    assert (want.hit_index != st.MISS).any()
