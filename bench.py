@@ -371,15 +371,20 @@ def _diff_timed(tr, torch, dev, stream, flush, args, tree, views, rays, nodes):
     bwd_recompute_ms = timed(lambda: tr.diff_backward_device(views, target.data_ptr()), steps)
     step_ms = timed(lambda: (tr.diff_forward_device(views, rgb.data_ptr()),
                              tr.diff_backward_device(views, target.data_ptr(), use_saved=True)), steps)
-    host_params = params.cpu().numpy()
-    host_target = target.cpu().numpy()
+    # host buffers in pinned memory, as a caller streaming through this API would hold them
+    host_params = torch.empty((nodes, 4), dtype=torch.float32, pin_memory=True).numpy()
+    host_params[:] = params.cpu().numpy()
+    host_target = torch.empty(rays * 3, dtype=torch.float32, pin_memory=True).numpy()
+    host_target[:] = target.cpu().numpy()
+    host_rgb = torch.empty(rays * 3, dtype=torch.float32, pin_memory=True).numpy()
+    host_grads = torch.empty((nodes, 4), dtype=torch.float32, pin_memory=True).numpy()
     loss0 = tr.diff_backward(views, host_target)
     t0 = time.perf_counter()
     for _ in range(steps):
         tr.diff_set_params(host_params)
-        tr.diff_forward(views)
+        tr.diff_forward(views, out=host_rgb)
         tr.diff_backward(views, host_target, use_saved=True)
-        tr.diff_grads(nodes)
+        tr.diff_grads(nodes, out=host_grads)
     e2e_s = (time.perf_counter() - t0) / steps
     tr.close()
     return {"workload": "depth-9 SDF sphere, %d views %dx%d, FP32 per-node RGBA, max 16 hits per ray"

@@ -186,6 +186,17 @@ struct Context {
 };
 
 
+// The device address of pinned (page-locked, registered) host memory, which
+// kernels can read and write directly; nullptr for any other pointer.
+inline void *pinned_device_ptr(const void *p) {
+  cudaPointerAttributes at{};
+  if (!p || cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+    cudaGetLastError();  // an unregistered pointer is not an error here
+    return nullptr;
+  }
+  return at.type == cudaMemoryTypeHost ? at.devicePointer : nullptr;
+}
+
 // Views, ray-setup tables and outputs of a batch into pinned staging. With
 // `tiled`, each view's ray slots cover whole 8x4 pixel tiles (total_rays then
 // exceeds total_pixels by the padding slots).

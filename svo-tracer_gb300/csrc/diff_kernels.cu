@@ -401,17 +401,21 @@ SVO_API svo_status svo_diff_forward(void *ctx, const svo_trace_input *views, int
   if (!rgb) return fail(SVO_ERR_INVALID_ARGUMENT, "svo_diff_forward: null output");
   uint64_t rays = svo::view_rays(views, n);
   float *dst = rgb;
-  if (!on_device) {
+  // a pinned host output is written by the kernel itself; other host memory
+  // through a device buffer and a copy
+  float *pinned = on_device ? nullptr : static_cast<float *>(svo::pinned_device_ptr(rgb));
+  if (pinned) {
+    dst = pinned;
+  } else if (!on_device) {
     if (c.diff_rgb.reserve(3 * rays)) return fail(SVO_ERR_OUT_OF_MEMORY, "svo_diff_forward: allocation failed");
     dst = c.diff_rgb.p;
   }
   svo_status st = svo::run_diff<false>(c, views, n, nullptr, dst, false, nullptr);
   if (st) return st;
-  if (!on_device) {
+  if (!on_device && !pinned)
     SVO_CUDA(cudaMemcpyAsync(rgb, dst, 3 * rays * sizeof(float), cudaMemcpyDeviceToHost, c.stream),
              "svo_diff_forward: read");
-    SVO_CUDA(cudaStreamSynchronize(c.stream), "svo_diff_forward: synchronize");
-  }
+  if (!on_device) SVO_CUDA(cudaStreamSynchronize(c.stream), "svo_diff_forward: synchronize");
   return SVO_OK;
 }
 
@@ -421,13 +425,21 @@ SVO_API svo_status svo_diff_backward(void *ctx, const svo_trace_input *views, in
   if (!target || !views || n <= 0) return fail(SVO_ERR_INVALID_ARGUMENT, "svo_diff_backward: null target or views");
   uint64_t rays = svo::view_rays(views, n);
   const float *src = target;
-  if (!on_device) {
+  // a pinned host target is read by the kernel itself; other host memory is copied
+  const float *pinned = on_device ? nullptr : static_cast<const float *>(svo::pinned_device_ptr(target));
+  if (pinned) {
+    src = pinned;
+  } else if (!on_device) {
     if (c.diff_target.reserve(3 * rays)) return fail(SVO_ERR_OUT_OF_MEMORY, "svo_diff_backward: allocation failed");
     SVO_CUDA(cudaMemcpyAsync(c.diff_target.p, target, 3 * rays * sizeof(float), cudaMemcpyHostToDevice, c.stream),
              "svo_diff_backward: target");
     src = c.diff_target.p;
   }
-  return svo::run_diff<true>(c, views, n, src, nullptr, use_saved != 0, loss);
+  svo_status st = svo::run_diff<true>(c, views, n, src, nullptr, use_saved != 0, loss);
+  if (st) return st;
+  // the caller may reuse a host target once the call returns
+  if (pinned && !loss) SVO_CUDA(cudaStreamSynchronize(c.stream), "svo_diff_backward: synchronize");
+  return SVO_OK;
 }
 
 }  // extern "C"

@@ -241,13 +241,12 @@ static svo_status run_trace(Context &c, const svo_trace_input *in, int32_t n, co
                         reinterpret_cast<void **>(&mapped[i].t), reinterpret_cast<void **>(&mapped[i].rgba)};
       for (void **pp : ptrs) {
         if (!*pp) continue;
-        cudaPointerAttributes at{};
-        if (cudaPointerGetAttributes(&at, *pp) != cudaSuccess || at.type != cudaMemoryTypeHost || !at.devicePointer) {
-          cudaGetLastError();  // an unregistered pointer is not an error here
+        void *d = pinned_device_ptr(*pp);
+        if (!d) {
           all_pinned = false;
           break;
         }
-        *pp = at.devicePointer;
+        *pp = d;
       }
       mapped[i].on_device = 1;
     }

@@ -693,14 +693,19 @@ class Tracer:
         p = np.ascontiguousarray(rgba, np.float32).reshape(-1, 4)
         _check("DiffSetParams", self._lib.svo_diff_set_params(self._ctx, _ptr(p), len(p), 0))
 
-    def diff_grads(self, n_nodes: int) -> np.ndarray:
-        g = np.zeros((n_nodes, 4), np.float32)
+    def diff_grads(self, n_nodes: int, out: np.ndarray | None = None) -> np.ndarray:
+        g = np.zeros((n_nodes, 4), np.float32) if out is None else out
+        assert g.dtype == np.float32 and g.flags.c_contiguous and g.size >= 4 * n_nodes
         _check("DiffGrads", self._lib.svo_diff_get_grads(self._ctx, _ptr(g), n_nodes, 0))
         return g
 
-    def diff_forward(self, views) -> np.ndarray:
+    def diff_forward(self, views, out: np.ndarray | None = None) -> np.ndarray:
+        """Composited colour, 3 floats per pixel; `out` (float32, C-contiguous) may
+        be a caller's buffer, written in place (by the kernel when it is pinned)."""
         n = sum(v.ScreenSize[0] * v.ScreenSize[1] for v in views)
-        out = np.zeros((n, 3), np.float32)
+        if out is None:
+            out = np.zeros((n, 3), np.float32)
+        assert out.dtype == np.float32 and out.flags.c_contiguous and out.size == 3 * n
         c_in = (TraceInputC * len(views))(*[v.to_c() for v in views])
         _check("DiffForward", self._lib.svo_diff_forward(self._ctx, c_in, len(views), _ptr(out), 0))
         return out

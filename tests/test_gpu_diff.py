@@ -169,3 +169,27 @@ def test_diff_without_params_fails(tracer):
     tracer.upload(tree)
     with pytest.raises(st.SvoError):
         tracer.diff_forward(st.orbit_views(n=1, width=8, height=8))
+
+
+def test_pinned_host_buffers_equal_pageable(tracer, fitting):
+    """A pinned host colour buffer is written by the forward kernel and a pinned
+    host target read by the backward kernel directly; the results are those of
+    pageable buffers, which go through device copies."""
+    torch = pytest.importorskip("torch")
+    tree, views, _, params, target = fitting
+    tracer.upload(tree)
+    tracer.diff_set_params(params)
+    n = sum(v.ScreenSize[0] * v.ScreenSize[1] for v in views)
+    rgb_pinned = torch.empty(3 * n, dtype=torch.float32, pin_memory=True).numpy()
+    tgt_pinned = torch.empty(3 * n, dtype=torch.float32, pin_memory=True).numpy()
+    tgt_pinned[:] = target.reshape(-1)
+    for _ in range(2):
+        want_rgb = tracer.diff_forward(views)
+        got_rgb = tracer.diff_forward(views, out=rgb_pinned)
+        assert np.array_equal(got_rgb.reshape(-1, 3), want_rgb)
+        want_loss = tracer.diff_backward(views, target)
+        want_grad = tracer.diff_grads(len(tree.Blocks))
+        got_loss = tracer.diff_backward(views, tgt_pinned)
+        got_grad = tracer.diff_grads(len(tree.Blocks))
+        assert abs(got_loss - want_loss) <= 1e-12 * want_loss
+        assert np.abs(got_grad - want_grad).max() <= 1e-6 * np.abs(want_grad).max()  # atomic order only
