@@ -401,6 +401,7 @@ def _diff_timed(tr, torch, dev, stream, flush, args, tree, views, rays, nodes):
 def run_ours(args, rank, world):
     import torch
 
+    import replicas
     import svo_tracer as st
 
     dev = int(os.environ.get("LOCAL_RANK", "0"))
@@ -474,10 +475,7 @@ def run_ours(args, rank, world):
         tr.trace(cam, out=res)  # uploads view + trig tables, traces, downloads all outputs, synchronises
     e2e_s = time.perf_counter() - t0
 
-    if dist:
-        t = torch.tensor([total_ms, e2e_s], dtype=torch.float64, device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms, e2e_s = float(t[0]), float(t[1])
+    total_ms, e2e_s = replicas.max_over_ranks([total_ms, e2e_s], dist, dev)
     if rank != 0:
         tr.close()
         if dist:
@@ -485,7 +483,7 @@ def run_ours(args, rank, world):
         return
 
     ms_per_step = total_ms / args.steps
-    value = world * n / (ms_per_step / 1000.0) / 1e6
+    value = replicas.replica_throughput(world, n, ms_per_step)
     peak, peak_kind = measured_peak()
     achieved = alg_bytes / (ms_per_step / 1000.0) / 1e9
     traffic = ncu_traffic()
@@ -498,7 +496,8 @@ def run_ours(args, rank, world):
         "config": config_dict(tree, {"parallelism": "replicas" if world > 1 else "single GPU",
                                      "step_ms_min": min(step_ms), "step_ms_max": max(step_ms),
                                      "wall_s_timed_loop": t_wall}),
-        "e2e": {"value": world * n * args.steps / e2e_s / 1e6, "unit": "Mrays/s", "h2d_bytes_per_step": h2d,
+        "e2e": {"value": replicas.replica_throughput(world, n, 1000.0 * e2e_s / args.steps), "unit": "Mrays/s",
+                "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},
         "gpu_launches": args.steps,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
