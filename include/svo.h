@@ -149,7 +149,11 @@ typedef struct svo_child_request {
 
 /* Per-pixel results of a trace. Pointers are host memory unless on_device is
  * non-zero, then they are device pointers the caller owns. Any pointer may be
- * NULL to skip that output. */
+ * NULL to skip that output. When every host output of a call is pinned
+ * (cudaMallocHost / cudaHostRegister), the kernel writes them directly and the
+ * transfer overlaps the trace; other host memory goes through device buffers
+ * and a copy after the trace. Either way the call returns with the outputs
+ * written. */
 typedef struct svo_trace_output {
   uint32_t *hit_index; /* node index of the hit, SVO_MISS for background */
   uint8_t *hit_depth;  /* level of the hit node, 0 for background */
@@ -320,7 +324,8 @@ SVO_API svo_status svo_prune(void *ctx, const svo_update_input *in, const svo_pr
 SVO_API svo_status svo_diff_set_params(void *ctx, const float *rgba, size_t n_nodes, int32_t on_device);
 /* Gradients of the last svo_diff_backward, 4 floats per node. */
 SVO_API svo_status svo_diff_get_grads(void *ctx, float *grad_rgba, size_t n_nodes, int32_t on_device);
-/* Composited colour, 3 floats per ray, views concatenated in order. */
+/* Composited colour, 3 floats per ray, views concatenated in order (a pinned
+ * host buffer is written by the kernel directly). */
 SVO_API svo_status svo_diff_forward(void *ctx, const svo_trace_input *views, int32_t n_views, float *rgb,
                                     int32_t on_device);
 /* L = sum over rays and channels of (C - target)^2 / rays; recomputes the
