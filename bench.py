@@ -52,6 +52,9 @@ def config_dict(tree, extra=None):
 
 
 class ClockSampler:
+    """nvidia-smi clock samples (every 100 ms) with the host time they arrived at.
+    Started before the warm-up so that the tool is already sampling when the timed
+    loops run; `summary(windows)` keeps the samples inside the timed windows."""
     FIELDS = "clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown," \
              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown," \
              "clocks_event_reasons.sw_power_cap"
@@ -72,7 +75,7 @@ class ClockSampler:
 
     def _read(self):
         for line in self.proc.stdout:
-            self.rows.append([x.strip() for x in line.split(",")])
+            self.rows.append((time.perf_counter(), [x.strip() for x in line.split(",")]))
 
     def __exit__(self, *exc):
         if self.proc:
@@ -82,15 +85,18 @@ class ClockSampler:
             except subprocess.TimeoutExpired:
                 self.proc.kill()
 
-    def summary(self):
-        if not self.rows:
-            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
-        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
-        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+    def summary(self, windows, margin_s=0.05):
+        rows = [r for t, r in self.rows if any(a - margin_s <= t <= b + margin_s for a, b in windows)]
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        sm = [float(r[0]) for r in rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({names[i] for r in self.rows for i in range(4) if len(r) > 4 + i and r[4 + i] == "Active"})
+        reasons = sorted({names[i] for r in rows for i in range(4) if len(r) > 4 + i and r[4 + i] == "Active"})
         return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": reasons, "samples": len(self.rows)}
+                "reasons": reasons, "samples": len(rows),
+                "timed_s": round(sum(b - a for a, b in windows), 3),
+                "windows": "headline frames, e2e calls, 64-view and colour-fitting sections"}
 
 
 def measured_peak():
@@ -168,7 +174,7 @@ def run_reference(args, rank, world):
     print(json.dumps(line))
 
 
-def multiview(tr, torch, dev, stream, flush, args):
+def multiview(tr, torch, dev, stream, flush, args, windows=None):
     """64 mixed-resolution views over the same tree: one autotuned, CUDA-graph-replayed
     persistent launch against 64 sequential plain launches, same device outputs."""
     import svo_tracer as st
@@ -192,6 +198,7 @@ def multiview(tr, torch, dev, stream, flush, args):
             for v, p in zip(views, plain_p):
                 tr.trace_device([v], [p])
         plain_ms = []
+        t_win = time.perf_counter()
         for _ in range(max(3, args.steps // 4)):
             flush.zero_()
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -201,11 +208,14 @@ def multiview(tr, torch, dev, stream, flush, args):
             e1.record(stream)
             plain_ms.append((e0, e1))
         torch.cuda.synchronize(dev)
+        if windows is not None:
+            windows.append((t_win, time.perf_counter()))
         plain = sorted(a.elapsed_time(b) for a, b in plain_ms)[len(plain_ms) // 2]
         tuned, tune_ms = tr.autotune(views, batched_p, repeats=2)
         for _ in range(2):
             tr.trace_device(views, batched_p, graph=True)
         batch_ms = []
+        t_win = time.perf_counter()
         for _ in range(max(3, args.steps // 4)):
             flush.zero_()
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -214,6 +224,8 @@ def multiview(tr, torch, dev, stream, flush, args):
             e1.record(stream)
             batch_ms.append((e0, e1))
         torch.cuda.synchronize(dev)
+        if windows is not None:
+            windows.append((t_win, time.perf_counter()))
         batched = sorted(a.elapsed_time(b) for a, b in batch_ms)[len(batch_ms) // 2]
     same = all(torch.equal(a[0], b[0]) and torch.equal(a[1], b[1]) and torch.equal(a[2], b[2])
                and torch.equal(a[3], b[3]) for a, b in zip(batched_t, plain_t))
@@ -314,7 +326,7 @@ def stream_workload(torch, dev, args):
     return out
 
 
-def diff_workload(torch, dev, flush, args):
+def diff_workload(torch, dev, flush, args, windows=None):
     """Differentiable colour fitting: the depth-9 SDF sphere (512^3 leaf grid), 16
     views of 512x512 around it, FP32 per-node RGBA initialised uniform in [0, 1],
     targets rendered from the seeded sinusoid ground-truth field (opacity 0.9).
@@ -335,10 +347,10 @@ def diff_workload(torch, dev, flush, args):
     tr.upload(tree)
     tr.set_config(max_hits=16)
     with torch.cuda.stream(stream):
-        return _diff_timed(tr, torch, dev, stream, flush, args, tree, views, rays, nodes)
+        return _diff_timed(tr, torch, dev, stream, flush, args, tree, views, rays, nodes, windows)
 
 
-def _diff_timed(tr, torch, dev, stream, flush, args, tree, views, rays, nodes):
+def _diff_timed(tr, torch, dev, stream, flush, args, tree, views, rays, nodes, windows=None):
     import svo_tracer as st
 
     gt = torch.from_numpy(st.sinusoid_field(tree, seed=9)).to(dev)
@@ -352,6 +364,7 @@ def _diff_timed(tr, torch, dev, stream, flush, args, tree, views, rays, nodes):
 
     def timed(fn, steps):
         ms = []
+        t_win = time.perf_counter()
         for _ in range(steps):
             flush.zero_()
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -360,6 +373,8 @@ def _diff_timed(tr, torch, dev, stream, flush, args, tree, views, rays, nodes):
             e1.record(stream)
             e1.synchronize()
             ms.append(e0.elapsed_time(e1))
+        if windows is not None:
+            windows.append((t_win, time.perf_counter()))
         return float(np.median(ms))
 
     steps = max(5, args.steps // 2)
@@ -436,6 +451,8 @@ def run_ours(args, rank, world):
     outs = [(o_idx.data_ptr(), o_dep.data_ptr(), o_t.data_ptr(), o_rgba.data_ptr())]
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
 
+    clk = ClockSampler(dev).__enter__()  # sampling from before the warm-up
+    windows = []  # host-time spans of the timed GPU work
     with torch.cuda.stream(stream):
         for _ in range(args.warmup):
             flush.zero_()
@@ -446,15 +463,15 @@ def run_ours(args, rank, world):
         if dist:
             dist.barrier()
         torch.cuda.synchronize(dev)
-        with ClockSampler(dev) as clk:
-            t_wall = time.perf_counter()
-            for i in range(args.steps):
-                flush.zero_()
-                starts[i].record(stream)
-                tr.trace_device([cam], outs)
-                ends[i].record(stream)
-            torch.cuda.synchronize(dev)
-            t_wall = time.perf_counter() - t_wall
+        t_start = time.perf_counter()
+        for i in range(args.steps):
+            flush.zero_()
+            starts[i].record(stream)
+            tr.trace_device([cam], outs)
+            ends[i].record(stream)
+        torch.cuda.synchronize(dev)
+        windows.append((t_start, time.perf_counter()))
+        t_wall = windows[-1][1] - t_start
         if dist:
             dist.barrier()
         torch.cuda.synchronize(dev)
@@ -474,9 +491,11 @@ def run_ours(args, rank, world):
     for _ in range(args.steps):
         tr.trace(cam, out=res)  # uploads view + trig tables, traces, downloads all outputs, synchronises
     e2e_s = time.perf_counter() - t0
+    windows.append((t0, t0 + e2e_s))
 
     total_ms, e2e_s = replicas.max_over_ranks([total_ms, e2e_s], dist, dev)
     if rank != 0:
+        clk.__exit__(None, None, None)
         tr.close()
         if dist:
             dist.destroy_process_group()
@@ -504,13 +523,14 @@ def run_ours(args, rank, world):
                      "traffic": traffic, "peak_kind": peak_kind,
                      "algorithmic_bytes_per_launch": int(alg_bytes),
                      "bytes_per_ray": alg_bytes / n},
-        "clocks": clk.summary(),
         "trace_stats": {k: int(v) for k, v in stats.items()},
     }
     if not args.no_multiview:
-        line["multiview"] = multiview(tr, torch, dev, stream, flush, args)
+        line["multiview"] = multiview(tr, torch, dev, stream, flush, args, windows)
     if not args.no_diff:
-        line["diff"] = diff_workload(torch, dev, flush, args)
+        line["diff"] = diff_workload(torch, dev, flush, args, windows)
+    clk.__exit__(None, None, None)
+    line["clocks"] = clk.summary(windows)
     if args.stream_frames > 0:
         line["stream"] = stream_workload(torch, dev, args)
     if not args.no_cpu_baseline:
