@@ -41,14 +41,33 @@ __device__ __forceinline__ uint64_t unit_to_ulong(float x) {
   return __float2ull_rz(v);
 }
 
-// roundUlong (wavefront.cl:211-221) in closed form, `low` = the bits below
-// level d+1 (kAll >> (d + 1)): up, the distance to the next boundary is
-// (~v & low) + 1 (wrapping to 2^64 - v in the top cell like the reference's
-// sum); down, (v & low) + 1, or v itself in the lowest cell, where the
-// reference's subtraction wraps and its comparison returns v.
-__device__ __forceinline__ uint64_t round_ulong(uint64_t v, uint64_t low, bool up) {
-  if (up) return (~v & low) + 1;
-  return (v & ~low) ? (v & low) + 1 : v;
+// Locations in travel space. A ray keeps each 64-bit fixed-point coordinate v
+// as w = v for a positive direction and w = ~v for a negative one, so that a
+// step in the travel direction always increases w. Then, with
+// low = kAll >> (d + 1) (the bits below level d+1), the reference's rules of
+// both directions become one:
+//   roundUlong (wavefront.cl:211-221): the distance to the next level-(d+1)
+//     boundary is (~w & low) + 1, except for a negative direction in the lowest
+//     cell ((w | low) == kAll), where the reference's subtraction wraps and its
+//     comparison returns v = ~w;
+//   traverseChunk's move and clamp (:440-497): w += d, and a wrap to 0 becomes
+//     kAll (v + d wrapping to 0 becomes ULONG_MAX; v - d wrapping to
+//     ULONG_MAX becomes 0);
+//   leaving (:433-437): some w == kAll;
+//   comparePositions (:413-426): the bits that flipped against the travel
+//     direction are w_before & ~w_after.
+// Real coordinates (octants, cell indices, float conversions, requests) are
+// w ^ dir_mask.
+__device__ __forceinline__ uint64_t dir_mask(bool positive) { return positive ? 0ull : kAll; }
+
+__device__ __forceinline__ uint64_t boundary_distance(uint64_t w, uint64_t low, bool positive) {
+  const uint64_t d = (~w & low) + 1;
+  return (!positive && (w | low) == kAll) ? ~w : d;
+}
+
+__device__ __forceinline__ uint64_t step_travel(uint64_t w, uint64_t d) {
+  const uint64_t n = w + d;
+  return n == 0 ? kAll : n;
 }
 
 __device__ __forceinline__ uint32_t spread3(uint32_t v) {
@@ -68,24 +87,27 @@ __device__ __forceinline__ void fill_spread_table() {
   for (uint32_t i = threadIdx.x; i < 1024; i += blockDim.x) s_spread3[i] = spread3(i);
 }
 
-// baseLocation (wavefront.cl:405-411) for 1 <= depth <= 10: the Morton index of
-// the top `depth` bits of each coordinate (all within the high 32 bits).
-__device__ __forceinline__ uint32_t cell_index(int depth, uint64_t x, uint64_t y, uint64_t z) {
+// baseLocation (wavefront.cl:405-411) for 1 <= depth <= 10 from travel-space
+// coordinates: the Morton index of the top `depth` bits of each real coordinate
+// (all within the high 32 bits; `flip` bit k set for a negative axis k).
+__device__ __forceinline__ uint32_t cell_index(int depth, uint64_t wx, uint64_t wy, uint64_t wz, uint32_t flip) {
   const uint32_t s = 32 - depth;
-  const uint32_t cx = (uint32_t)(x >> 32) >> s, cy = (uint32_t)(y >> 32) >> s, cz = (uint32_t)(z >> 32) >> s;
+  const uint32_t cx = ((uint32_t)(wx >> 32) ^ (0u - (flip & 1u))) >> s;
+  const uint32_t cy = ((uint32_t)(wy >> 32) ^ (0u - ((flip >> 1) & 1u))) >> s;
+  const uint32_t cz = ((uint32_t)(wz >> 32) ^ (0u - ((flip >> 2) & 1u))) >> s;
   return s_spread3[cx] | (s_spread3[cy] << 1) | (s_spread3[cz] << 2);
 }
 
-// chunkPosition (wavefront.cl:428-430)
-__device__ __forceinline__ uint32_t octant(int depth, uint64_t x, uint64_t y, uint64_t z) {
+// chunkPosition (wavefront.cl:428-430) from travel-space coordinates.
+__device__ __forceinline__ uint32_t octant(int depth, uint64_t wx, uint64_t wy, uint64_t wz, uint32_t flip) {
   int s = 63 - depth;
-  return (uint32_t)(((x >> s) & 1) | (((y >> s) & 1) << 1) | (((z >> s) & 1) << 2));
+  return (uint32_t)(((wx >> s) & 1) | (((wy >> s) & 1) << 1) | (((wz >> s) & 1) << 2)) ^ flip;
 }
 
 __device__ __forceinline__ float pow2_neg(int k) { return __int_as_float((127 - k) << 23); }
 
 struct Ray {
-  uint64_t lx, ly, lz;
+  uint64_t wx, wy, wz;  // location in travel space (see dir_mask)
   float dx, dy, dz;
   float ix, iy, iz;
   float ox, oy, oz;
@@ -95,7 +117,17 @@ struct Ray {
   int depth;
   int steps;
   bool sx, sy, sz;
+  uint32_t flip;  // bit k: axis k travels towards 0
 };
+
+__device__ __forceinline__ uint64_t loc_x(const Ray &r) { return r.wx ^ dir_mask(r.sx); }
+__device__ __forceinline__ uint64_t loc_y(const Ray &r) { return r.wy ^ dir_mask(r.sy); }
+__device__ __forceinline__ uint64_t loc_z(const Ray &r) { return r.wz ^ dir_mask(r.sz); }
+__device__ __forceinline__ void set_loc(Ray &r, uint64_t x, uint64_t y, uint64_t z) {
+  r.wx = x ^ dir_mask(r.sx);
+  r.wy = y ^ dir_mask(r.sy);
+  r.wz = z ^ dir_mask(r.sz);
+}
 
 struct Node {
   uint32_t child;
@@ -110,9 +142,9 @@ __device__ __forceinline__ uint4 load_node(const uint4 *blocks, uint32_t n_block
 // traverseChunk (wavefront.cl:440-497) without the trailing setConeDepth.
 __device__ __forceinline__ void traverse(Ray &r, int depth) {
   const uint64_t low = kAll >> (depth + 1);
-  uint64_t d0 = round_ulong(r.lx, low, r.sx);
-  uint64_t d1 = round_ulong(r.ly, low, r.sy);
-  uint64_t d2 = round_ulong(r.lz, low, r.sz);
+  uint64_t d0 = boundary_distance(r.wx, low, r.sx);
+  uint64_t d1 = boundary_distance(r.wy, low, r.sy);
+  uint64_t d2 = boundary_distance(r.wz, low, r.sz);
   const float f0 = ulong_to_float(d0), f1 = ulong_to_float(d1), f2 = ulong_to_float(d2);
   float a0 = fabsf(__fmul_rn(f0, r.ix));
   float a1 = fabsf(__fmul_rn(f1, r.iy));
@@ -124,38 +156,29 @@ __device__ __forceinline__ void traverse(Ray &r, int depth) {
   if (ax != 0) d0 = unit_to_ulong(__fmul_rn(__fmul_rn(r.dx, inv), u));
   if (ax != 1) d1 = unit_to_ulong(__fmul_rn(__fmul_rn(r.dy, inv), u));
   if (ax != 2) d2 = unit_to_ulong(__fmul_rn(__fmul_rn(r.dz, inv), u));
-  uint64_t x = r.sx ? r.lx + d0 : r.lx - d0;
-  uint64_t y = r.sy ? r.ly + d1 : r.ly - d1;
-  uint64_t z = r.sz ? r.lz + d2 : r.lz - d2;
-  if (r.sx && x == 0) x = kAll; else if (!r.sx && x == kAll) x = 0;
-  if (r.sy && y == 0) y = kAll; else if (!r.sy && y == kAll) y = 0;
-  if (r.sz && z == 0) z = kAll; else if (!r.sz && z == kAll) z = 0;
-  r.lx = x;
-  r.ly = y;
-  r.lz = z;
+  r.wx = step_travel(r.wx, d0);
+  r.wy = step_travel(r.wy, d1);
+  r.wz = step_travel(r.wz, d2);
 }
 
 // comparePositions (wavefront.cl:413-426): the loop pops one level for every
 // consecutive level, counted upwards from `depth`, whose octant bit flipped
 // against the travel direction on some axis; it stops at level 1.
+// px, py, pz: the travel-space location before the step.
 __device__ __forceinline__ int pop_depth(const Ray &r, int depth, uint64_t px, uint64_t py, uint64_t pz) {
-  uint64_t m = (r.sx ? (px & ~r.lx) : (~px & r.lx)) | (r.sy ? (py & ~r.ly) : (~py & r.ly)) |
-               (r.sz ? (pz & ~r.lz) : (~pz & r.lz));
+  uint64_t m = (px & ~r.wx) | (py & ~r.wy) | (pz & ~r.wz);
   uint64_t run = ~(m >> (63 - depth));
   int ones = __ffsll((long long)run) - 1;
   return ones < depth ? depth - ones : 1;
 }
 
-__device__ __forceinline__ bool leaving(const Ray &r) {
-  return (!r.sx && r.lx == 0) || (!r.sy && r.ly == 0) || (!r.sz && r.lz == 0) || (r.sx && r.lx == kAll) ||
-         (r.sy && r.ly == kAll) || (r.sz && r.lz == kAll);
-}
+__device__ __forceinline__ bool leaving(const Ray &r) { return r.wx == kAll || r.wy == kAll || r.wz == kAll; }
 
 // coneSize (wavefront.cl:387-391) at the distance setConeDepth uses (:394-399).
 __device__ __forceinline__ float cone_at(const Ray &r, float dof0, float dof1) {
-  float x = __fsub_rn(r.ox, ulong_to_unit(r.lx));
-  float y = __fsub_rn(r.oy, ulong_to_unit(r.ly));
-  float z = __fsub_rn(r.oz, ulong_to_unit(r.lz));
+  float x = __fsub_rn(r.ox, ulong_to_unit(loc_x(r)));
+  float y = __fsub_rn(r.oy, ulong_to_unit(loc_y(r)));
+  float z = __fsub_rn(r.oz, ulong_to_unit(loc_z(r)));
   float m = fabsf(__fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(x, x), __fmul_rn(y, y)), __fmul_rn(z, z))));
   float eye = __fmul_rn(r.fov, m);
   float f = fabsf(__fmul_rn(dof0, __fsub_rn(dof1, m)));
@@ -177,9 +200,7 @@ __device__ __forceinline__ bool enter_volume(Ray &r) {
     any |= lo[k] | hi[k];
   }
   if (!any) {
-    r.lx = unit_to_ulong(o[0]);
-    r.ly = unit_to_ulong(o[1]);
-    r.lz = unit_to_ulong(o[2]);
+    set_loc(r, unit_to_ulong(o[0]), unit_to_ulong(o[1]), unit_to_ulong(o[2]));
     return true;
   }
 #pragma unroll
@@ -209,9 +230,7 @@ __device__ __forceinline__ bool enter_volume(Ray &r) {
   float p[3];
 #pragma unroll
   for (int k = 0; k < 3; k++) p[k] = (k == axis) ? (hi[k] ? 1.0f : 0.0f) : __fadd_rn(o[k], __fmul_rn(d[k], m));
-  r.lx = unit_to_ulong(p[0]);
-  r.ly = unit_to_ulong(p[1]);
-  r.lz = unit_to_ulong(p[2]);
+  set_loc(r, unit_to_ulong(p[0]), unit_to_ulong(p[1]), unit_to_ulong(p[2]));
   // DoF of a fresh TraceData is zero (setupInitialTrace leaves it unset).
   float eye = __fmul_rn(r.fov, m);
   float f = fabsf(__fmul_rn(0.0f, __fsub_rn(0.0f, m)));
@@ -263,7 +282,7 @@ __device__ __forceinline__ int step(const TraceLaunch &a, const ViewParams &v, c
   const int lvl = r.depth - (B + 2);
   uint32_t chunk;
   if (!block) {
-    uint32_t idx = pow_sum(r.depth - 1) + cell_index(r.depth, r.lx, r.ly, r.lz);
+    uint32_t idx = pow_sum(r.depth - 1) + cell_index(r.depth, r.wx, r.wy, r.wz, r.flip);
     chunk = kSmemBases ? s_bases[idx] : __ldg(a.bases + idx);
     if (kStats) w.v_base++;
   } else {
@@ -288,19 +307,19 @@ __device__ __forceinline__ int step(const TraceLaunch &a, const ViewParams &v, c
       w.last_group = group;
     }
   }
-  if (((chunk >> (octant(r.depth, r.lx, r.ly, r.lz) * 2)) & 2) == 0) {
+  if (((chunk >> (octant(r.depth, r.wx, r.wy, r.wz, r.flip) * 2)) & 2) == 0) {
     // empty octant: step to the neighbouring cell and pop (traverseChunk, comparePositions)
-    uint64_t px = r.lx, py = r.ly, pz = r.lz;
+    uint64_t px = r.wx, py = r.wy, pz = r.wz;
     traverse(r, r.depth);
     if (leaving(r)) return kStepBackground;
     int nd = pop_depth(r, r.depth, px, py, pz);
-    if (block && nd >= B + 2 && (((px ^ r.lx) | (py ^ r.ly) | (pz ^ r.lz)) >> (64 - nd)) != 0) {
+    if (block && nd >= B + 2 && (((px ^ r.wx) | (py ^ r.wy) | (pz ^ r.wz)) >> (64 - nd)) != 0) {
       // an ancestor cell changed: rebuild the path like getBlockAddress
-      uint32_t n = cell_index(B + 2, r.lx, r.ly, r.lz);
+      uint32_t n = cell_index(B + 2, r.wx, r.wy, r.wz, r.flip);
       w.path[0] = n;
       for (int d = B + 2; d < nd; d++) {
         uint4 n2 = load_node(blocks, a.n_blocks, n);
-        n = n2.x + octant(d, r.lx, r.ly, r.lz);
+        n = n2.x + octant(d, r.wx, r.wy, r.wz, r.flip);
         w.path[(d - B - 1) * w.stride] = n;
       }
     }
@@ -313,7 +332,7 @@ __device__ __forceinline__ int step(const TraceLaunch &a, const ViewParams &v, c
       r.depth++;
     } else {
       r.depth = B + 2;
-      w.path[0] = cell_index(B + 2, r.lx, r.ly, r.lz);
+      w.path[0] = cell_index(B + 2, r.wx, r.wy, r.wz, r.flip);
     }
     return kStepOn;
   }
@@ -339,9 +358,9 @@ __device__ __forceinline__ int step(const TraceLaunch &a, const ViewParams &v, c
       q.tick = 0;  // TraceData.Tick is never set by resolveTrace
       q.depth = (uint8_t)r.depth;
       q._pad0 = 0;
-      q.location[0] = r.lx;
-      q.location[1] = r.ly;
-      q.location[2] = r.lz;
+      q.location[0] = loc_x(r);
+      q.location[1] = loc_y(r);
+      q.location[2] = loc_z(r);
       q.tree_size = c <= pow2_neg(r.depth + 1) ? 1 : 0;
       for (int k = 0; k < 7; k++) q._pad1[k] = 0;
       a.requests[slot] = q;
@@ -349,7 +368,7 @@ __device__ __forceinline__ int step(const TraceLaunch &a, const ViewParams &v, c
     return kStepHit;
   }
   if (c < pow2_neg(r.depth + 1) && lvl + 1 < a.path_levels) {
-    w.path[(lvl + 1) * w.stride] = w.cur_child + octant(r.depth, r.lx, r.ly, r.lz);
+    w.path[(lvl + 1) * w.stride] = w.cur_child + octant(r.depth, r.wx, r.wy, r.wz, r.flip);
     r.depth++;
     return kStepOn;
   }
@@ -411,6 +430,7 @@ __device__ __forceinline__ bool setup_ray(const TraceLaunch &a, const ViewParams
   r.sx = r.dx >= 0.0f;
   r.sy = r.dy >= 0.0f;
   r.sz = r.dz >= 0.0f;
+  r.flip = (r.sx ? 0u : 1u) | (r.sy ? 0u : 2u) | (r.sz ? 0u : 4u);
   r.ox = v.origin[0];
   r.oy = v.origin[1];
   r.oz = v.origin[2];
@@ -426,16 +446,16 @@ __device__ __forceinline__ bool setup_ray(const TraceLaunch &a, const ViewParams
 // ray leaves the cube.
 __device__ __forceinline__ int step_past(const TraceLaunch &a, const uint4 *blocks, int B, Ray &r, Walk &w) {
   const bool block = r.depth > B;
-  uint64_t px = r.lx, py = r.ly, pz = r.lz;
+  uint64_t px = r.wx, py = r.wy, pz = r.wz;
   traverse(r, r.depth);
   if (leaving(r)) return kStepBackground;
   int nd = pop_depth(r, r.depth, px, py, pz);
-  if (block && nd >= B + 2 && (((px ^ r.lx) | (py ^ r.ly) | (pz ^ r.lz)) >> (64 - nd)) != 0) {
-    uint32_t n = cell_index(B + 2, r.lx, r.ly, r.lz);
+  if (block && nd >= B + 2 && (((px ^ r.wx) | (py ^ r.wy) | (pz ^ r.wz)) >> (64 - nd)) != 0) {
+    uint32_t n = cell_index(B + 2, r.wx, r.wy, r.wz, r.flip);
     w.path[0] = n;
     for (int d = B + 2; d < nd; d++) {
       uint4 n2 = load_node(blocks, a.n_blocks, n);
-      n = n2.x + octant(d, r.lx, r.ly, r.lz);
+      n = n2.x + octant(d, r.wx, r.wy, r.wz, r.flip);
       w.path[(d - B - 1) * w.stride] = n;
     }
   }

@@ -125,9 +125,9 @@ __global__ void __launch_bounds__(256, SVO_TRACE_MIN_CTAS) trace_kernel(const Tr
       cr = (nd.z >> 16) & 0xffu;
       cg_ = nd.z >> 24;
       cb = nd.w & 0xffu;
-      float x = __fsub_rn(ulong_to_unit(r.lx), r.ox);
-      float y = __fsub_rn(ulong_to_unit(r.ly), r.oy);
-      float z = __fsub_rn(ulong_to_unit(r.lz), r.oz);
+      float x = __fsub_rn(ulong_to_unit(loc_x(r)), r.ox);
+      float y = __fsub_rn(ulong_to_unit(loc_y(r)), r.oy);
+      float z = __fsub_rn(ulong_to_unit(loc_z(r)), r.oz);
       t = __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(x, x), __fmul_rn(y, y)), __fmul_rn(z, z)));
       if (kStats) {
         w.v_block += (uint32_t)(r.depth - B - 1);
