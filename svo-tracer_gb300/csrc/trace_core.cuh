@@ -263,14 +263,16 @@ struct Walk {
   uint32_t v_block, v_base;                 // reference-walk counters (stats launches)
 };
 
-enum : int { kStepOn = 0, kStepBackground = 1, kStepHit = 2 };
+enum : int { kStepOn = 0, kStepBackground = 1, kStepHit = 2, kStepEmpty = 3 };
 
-// One runBaseTrace (wavefront.cl:1400-1463) or runBlockTrace (:1465-1566) step.
-// Both read a 2-bit octant pair from a chunk (a base chunk or the current
-// node's) and share the empty-octant stepping code, so lanes at base and block
-// levels run it together.
+// The first part of one runBaseTrace (wavefront.cl:1400-1463) or runBlockTrace
+// (:1465-1566) step: read the 2-bit octant pair from a chunk (a base chunk or
+// the current node's) and, when the octant holds geometry, descend or take the
+// cone LOD decision. An empty octant returns kStepEmpty: the step ends with
+// advance() (the traverseChunk / comparePositions part), which callers can run
+// for the lanes of a warp together.
 template <bool kStats, bool kSmemBases>
-__device__ __forceinline__ int step(const TraceLaunch &a, const ViewParams &v, const uint16_t *s_bases,
+__device__ __forceinline__ int probe(const TraceLaunch &a, const ViewParams &v, const uint16_t *s_bases,
                                     const uint4 *blocks, int B, Ray &r, Walk &w, Stats &st) {
   if (r.depth == 0) return kStepBackground;
   if (a.max_steps > 0 && r.steps >= a.max_steps) {
@@ -307,25 +309,7 @@ __device__ __forceinline__ int step(const TraceLaunch &a, const ViewParams &v, c
       w.last_group = group;
     }
   }
-  if (((chunk >> (octant(r.depth, r.wx, r.wy, r.wz, r.flip) * 2)) & 2) == 0) {
-    // empty octant: step to the neighbouring cell and pop (traverseChunk, comparePositions)
-    uint64_t px = r.wx, py = r.wy, pz = r.wz;
-    traverse(r, r.depth);
-    if (leaving(r)) return kStepBackground;
-    int nd = pop_depth(r, r.depth, px, py, pz);
-    if (block && nd >= B + 2 && (((px ^ r.wx) | (py ^ r.wy) | (pz ^ r.wz)) >> (64 - nd)) != 0) {
-      // an ancestor cell changed: rebuild the path like getBlockAddress
-      uint32_t n = cell_index(B + 2, r.wx, r.wy, r.wz, r.flip);
-      w.path[0] = n;
-      for (int d = B + 2; d < nd; d++) {
-        uint4 n2 = load_node(blocks, a.n_blocks, n);
-        n = n2.x + octant(d, r.wx, r.wy, r.wz, r.flip);
-        w.path[(d - B - 1) * w.stride] = n;
-      }
-    }
-    r.depth = nd == B + 1 ? B : nd;
-    return kStepOn;
-  }
+  if (((chunk >> (octant(r.depth, r.wx, r.wy, r.wz, r.flip) * 2)) & 2) == 0) return kStepEmpty;
   if (!block) {
     // geometry below a base cell: descend, jumping from level B to B+2
     if (r.depth < B) {
@@ -441,10 +425,11 @@ __device__ __forceinline__ bool setup_ray(const TraceLaunch &a, const ViewParams
   return true;
 }
 
-// Continues a ray past a hit as if the hit octant held no geometry (the
-// empty-octant branch of runBlockTrace). Returns kStepBackground when the
-// ray leaves the cube.
-__device__ __forceinline__ int step_past(const TraceLaunch &a, const uint4 *blocks, int B, Ray &r, Walk &w) {
+// The empty-octant part of a step (runBaseTrace / runBlockTrace): move to the
+// neighbouring cell (traverseChunk), pop (comparePositions) and rebuild the
+// cached path when an ancestor cell changed (getBlockAddress). Returns
+// kStepBackground when the ray leaves the cube.
+__device__ __forceinline__ int advance(const TraceLaunch &a, const uint4 *blocks, int B, Ray &r, Walk &w) {
   const bool block = r.depth > B;
   uint64_t px = r.wx, py = r.wy, pz = r.wz;
   traverse(r, r.depth);
@@ -461,6 +446,19 @@ __device__ __forceinline__ int step_past(const TraceLaunch &a, const uint4 *bloc
   }
   r.depth = nd == B + 1 ? B : nd;
   return kStepOn;
+}
+
+// One whole step.
+template <bool kStats, bool kSmemBases>
+__device__ __forceinline__ int step(const TraceLaunch &a, const ViewParams &v, const uint16_t *s_bases,
+                                    const uint4 *blocks, int B, Ray &r, Walk &w, Stats &st) {
+  const int f = probe<kStats, kSmemBases>(a, v, s_bases, blocks, B, r, w, st);
+  return f == kStepEmpty ? advance(a, blocks, B, r, w) : f;
+}
+
+// Continues a ray past a hit as if the hit octant held no geometry.
+__device__ __forceinline__ int step_past(const TraceLaunch &a, const uint4 *blocks, int B, Ray &r, Walk &w) {
+  return advance(a, blocks, B, r, w);
 }
 
 // Sky colour of evaluateBackground (wavefront.cl:1741-1797) for a primary ray.

@@ -170,7 +170,7 @@ __global__ void __launch_bounds__(256, SVO_TRACE_MIN_CTAS) trace_kernel(const Tr
       if (my < a.total_rays && !timed_out && start_ray(my)) {
         const ViewParams &v = s_views[r.view];
         int finish = kStepOn;
-        // step() ends a ray after max_steps steps, so a ray needing more
+        // a step ends a ray after max_steps steps, so a ray needing more
         // passes than that is a fault: record it and stop the warp
         const uint32_t ray_limit = (uint32_t)a.max_steps + 2u;
         uint32_t ray_iters = 0;

@@ -201,3 +201,23 @@ def test_graft_generate_needs_terrain(tracer):
     tracer.upload(scene.build_tree(5))
     with pytest.raises(st.SvoError):
         tracer.graft_generate(1, scene)
+
+
+def test_graft_generate_edge_cases(tracer):
+    """Without child requests there is nothing to graft; a tick outside 1..65533 is
+    refused."""
+    scene = st.Scene(st.SCENE_TERRAIN, seed=5, base_depth=2, depth=7)
+    tree = scene.build_tree(5)
+    with st.Tracer(0) as fresh:  # no trace yet: no request queue
+        fresh.upload(tree, block_budget=(len(tree.Blocks) // 8 + 64) * 8)
+        rep = fresh.graft_generate(1, scene)
+        assert rep["applied"] == 0 and rep["claimed"] == 0
+        with pytest.raises(st.SvoError):
+            fresh.graft_generate(0, scene)
+        with pytest.raises(st.SvoError):
+            fresh.graft_generate(65534, scene)
+        # a view of the sky only raises no requests
+        fresh.trace(st.look_at((0.5, 0.5, -2.0), (0.5, 0.5, -3.0), 16, 16, 30.0, MaxChildRequestId=64))
+        assert fresh.read_child_requests()[1] == 0
+        rep = fresh.graft_generate(2, scene)
+        assert rep["applied"] == 0 and rep["claimed"] == 0
