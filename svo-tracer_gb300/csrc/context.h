@@ -111,7 +111,7 @@ struct Context {
   // (kept zero between calls), compaction counts, jobs and counters
   DevBuf<uint16_t> terrain_lo, terrain_hi;
   uint64_t terrain_id = 0;
-  DevBuf<uint32_t> gen_marker, gen_counts, gen_addr, gen_scalars;
+  DevBuf<uint32_t> gen_marker, gen_bits, gen_counts, gen_addr, gen_groups, gen_scalars;
   DevBuf<uint8_t> gen_jobs;
 
   // differentiable colour fitting: per-node RGBA parameters and gradients
@@ -175,6 +175,8 @@ struct Context {
     terrain_lo.release();
     terrain_hi.release();
     gen_marker.release();
+    gen_bits.release();
+    gen_groups.release();
     gen_counts.release();
     gen_addr.release();
     gen_scalars.release();

@@ -152,7 +152,8 @@ __global__ void k_count(const T *flags, uint32_t n, uint32_t *block_counts) {
 }
 
 // Exclusive scan of n block counts (in place) by one CTA; writes the total.
-__global__ void k_scan_counts(uint32_t *counts, uint32_t n, uint32_t *total) {
+// Exclusive scan in place of n counts by one CTA of kScanBlock threads, total to *total.
+__device__ void scan_in_place(uint32_t *counts, uint32_t n, uint32_t *total) {
   __shared__ uint32_t part[kScanBlock];
   uint32_t per = (n + kScanBlock - 1) / kScanBlock;
   uint32_t b = threadIdx.x * per, e = min(n, b + per), s = 0;
@@ -173,6 +174,8 @@ __global__ void k_scan_counts(uint32_t *counts, uint32_t n, uint32_t *total) {
   }
   if (threadIdx.x == kScanBlock - 1) *total = part[kScanBlock - 1];
 }
+
+__global__ void k_scan_counts(uint32_t *counts, uint32_t n, uint32_t *total) { scan_in_place(counts, n, total); }
 
 template <class T>
 __global__ void k_scatter(const T *flags, uint32_t n, const uint32_t *offsets, uint32_t *out) {
@@ -516,13 +519,89 @@ __device__ __forceinline__ svo_block terrain_block(const DevTerrain &T, int leve
 
 // Marks every requesting node with (TreeSize != 0) << 31 | (request + 1),
 // keeping the largest: any request of a node gives its depth and cell.
+// The marked node's group also gets its bit in `group_bits` (one bit per group).
 __global__ void k_gen_mark(const svo_child_request *req, const uint32_t *n_req, uint32_t cap, uint32_t *marker,
-                           uint32_t n_nodes, int min_depth, int scene_depth) {
+                           uint32_t *group_bits, uint32_t n_nodes, int min_depth, int scene_depth) {
   const uint32_t n = min(*n_req, cap);
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const svo_child_request r = req[i];
-    if (r.depth >= min_depth && r.depth < scene_depth && r.address < n_nodes)
+    if (r.depth >= min_depth && r.depth < scene_depth && r.address < n_nodes) {
       atomicMax(&marker[r.address], ((r.tree_size ? 1u : 0u) << 31) | (i + 1));
+      atomicOr(&group_bits[r.address >> 8], 1u << ((r.address >> 3) & 31u));
+    }
+  }
+}
+
+// Stream compaction of a group bitmap into the ascending list of marked groups
+// (which clears the bitmap): set bits counted per CTA of 1024 words, then each
+// word's bits written at its exclusive offset.
+__global__ void k_bits_count(const uint32_t *bits, uint32_t n_words, uint32_t *block_counts) {
+  __shared__ uint32_t wsum[32];
+  const uint32_t i = blockIdx.x * kScanBlock + threadIdx.x;
+  uint32_t c = __reduce_add_sync(0xffffffffu, i < n_words ? (uint32_t)__popc(bits[i]) : 0u);
+  if ((threadIdx.x & 31u) == 0) wsum[threadIdx.x >> 5] = c;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    c = __reduce_add_sync(0xffffffffu, wsum[threadIdx.x]);
+    if (threadIdx.x == 0) block_counts[blockIdx.x] = c;
+  }
+}
+
+__global__ void k_bits_scatter(uint32_t *bits, uint32_t n_words, const uint32_t *offsets, uint32_t *out) {
+  __shared__ uint32_t wsum[32];
+  const uint32_t i = blockIdx.x * kScanBlock + threadIdx.x;
+  const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+  const uint32_t word = i < n_words ? bits[i] : 0u;
+  const uint32_t c = __popc(word);
+  uint32_t x = c;  // inclusive scan within the warp
+  for (int o = 1; o < 32; o <<= 1) {
+    uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= (uint32_t)o) x += y;
+  }
+  if (lane == 31) wsum[warp] = x;
+  __syncthreads();
+  if (warp == 0) {
+    const uint32_t own = wsum[lane];
+    uint32_t incl = own;
+    for (int o = 1; o < 32; o <<= 1) {
+      uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= (uint32_t)o) incl += y;
+    }
+    wsum[lane] = incl - own;  // exclusive prefix of the warps' counts
+  }
+  __syncthreads();
+  uint32_t off = offsets[blockIdx.x] + wsum[warp] + (x - c);
+  for (uint32_t m = word; m; m &= m - 1u) out[off++] = i * 32u + (uint32_t)(__ffs(m) - 1);
+  if (word) bits[i] = 0;
+}
+
+// Marked nodes of each listed group (counts[j] for group list entry j).
+__global__ void k_group_node_count(const uint32_t *groups, const uint32_t *n_groups, uint32_t cap,
+                                   const uint32_t *marker, uint32_t *counts) {
+  const uint32_t n = min(*n_groups, cap);
+  for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+    const uint32_t *m = marker + 8ull * groups[j];
+    uint32_t c = 0;
+    for (int k = 0; k < 8; k++) c += m[k] != 0;
+    counts[j] = c;
+  }
+}
+
+// The same scan of *n_ptr (read on the device, at most cap) counts.
+__global__ void __launch_bounds__(kScanBlock) k_scan_device_n(uint32_t *counts, const uint32_t *n_ptr, uint32_t cap,
+                                                              uint32_t *total) {
+  scan_in_place(counts, min(*n_ptr, cap), total);
+}
+
+// The marked nodes of the listed groups in ascending order.
+__global__ void k_group_node_emit(const uint32_t *groups, const uint32_t *n_groups, uint32_t cap,
+                                  const uint32_t *marker, const uint32_t *offsets, uint32_t *out) {
+  const uint32_t n = min(*n_groups, cap);
+  for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+    const uint32_t node0 = 8u * groups[j];
+    uint32_t off = offsets[j];
+    for (uint32_t k = 0; k < 8; k++)
+      if (marker[node0 + k]) out[off++] = node0 + k;
   }
 }
 
@@ -948,19 +1027,32 @@ SVO_API svo_status svo_graft_generate(void *ctx, void *scene, const svo_update_i
     if (c.gen_marker.reserve(n_nodes)) return fail(SVO_ERR_OUT_OF_MEMORY, "svo_graft_generate: allocation failed");
     SVO_CUDA(cudaMemsetAsync(c.gen_marker.p, 0, (size_t)n_nodes * 4, c.stream), "svo_graft_generate: marker");
   }
-  const uint32_t nb = (n_nodes + svo::kScanBlock - 1) / svo::kScanBlock;
-  if (c.gen_counts.reserve(nb + 1) || c.gen_addr.reserve(std::max(1u, std::min(n_nodes, cap))) ||
-      c.gen_scalars.reserve(4) || c.gen_jobs.reserve(sizeof(svo::GenJob) * (size_t)cap))
+  // the group bitmap (one bit per group, zero between calls)
+  const uint32_t n_words = (uint32_t)((c.n_groups + 31) / 32);
+  if (c.gen_bits.n < n_words) {
+    if (c.gen_bits.reserve(n_words)) return fail(SVO_ERR_OUT_OF_MEMORY, "svo_graft_generate: allocation failed");
+    SVO_CUDA(cudaMemsetAsync(c.gen_bits.p, 0, (size_t)n_words * 4, c.stream), "svo_graft_generate: bitmap");
+  }
+  const uint32_t nb = (n_words + svo::kScanBlock - 1) / svo::kScanBlock;
+  const uint32_t list_cap = std::max(1u, cap);  // marked groups and nodes never exceed the stored requests
+  if (c.gen_counts.reserve(std::max(nb + 1, list_cap)) || c.gen_addr.reserve(list_cap) ||
+      c.gen_groups.reserve(list_cap) || c.gen_scalars.reserve(4) ||
+      c.gen_jobs.reserve(sizeof(svo::GenJob) * (size_t)list_cap))
     return fail(SVO_ERR_OUT_OF_MEMORY, "svo_graft_generate: allocation failed");
-  uint32_t *scalars = c.gen_scalars.p;  // [0] jobs, [1] applied, [2] claimed groups
+  uint32_t *scalars = c.gen_scalars.p;  // [0] jobs, [1] applied, [2] claimed groups, [3] marked groups
   svo::GenJob *jobs = reinterpret_cast<svo::GenJob *>(c.gen_jobs.p);
   const uint32_t *n_req = c.counters.p + 1;  // the last trace's request count
-  svo::k_gen_mark<<<svo::grid_for(cap), 256, 0, c.stream>>>(c.requests.p, n_req, cap, c.gen_marker.p, n_nodes,
-                                                            ti.base_depth + 2, ti.scene_depth);
-  svo::k_count<<<nb, svo::kScanBlock, 0, c.stream>>>(c.gen_marker.p, n_nodes, c.gen_counts.p);
-  svo::k_scan_counts<<<1, svo::kScanBlock, 0, c.stream>>>(c.gen_counts.p, nb, scalars);
-  // marked nodes never exceed the stored requests (at most cap), the job buffer's size
-  svo::k_scatter<<<nb, svo::kScanBlock, 0, c.stream>>>(c.gen_marker.p, n_nodes, c.gen_counts.p, c.gen_addr.p);
+  svo::k_gen_mark<<<svo::grid_for(cap), 256, 0, c.stream>>>(c.requests.p, n_req, cap, c.gen_marker.p, c.gen_bits.p,
+                                                            n_nodes, ti.base_depth + 2, ti.scene_depth);
+  // marked groups (ascending), then their marked nodes (ascending): the jobs
+  svo::k_bits_count<<<nb, svo::kScanBlock, 0, c.stream>>>(c.gen_bits.p, n_words, c.gen_counts.p);
+  svo::k_scan_counts<<<1, svo::kScanBlock, 0, c.stream>>>(c.gen_counts.p, nb, scalars + 3);
+  svo::k_bits_scatter<<<nb, svo::kScanBlock, 0, c.stream>>>(c.gen_bits.p, n_words, c.gen_counts.p, c.gen_groups.p);
+  svo::k_group_node_count<<<svo::grid_for(cap), 256, 0, c.stream>>>(c.gen_groups.p, scalars + 3, list_cap,
+                                                                    c.gen_marker.p, c.gen_counts.p);
+  svo::k_scan_device_n<<<1, svo::kScanBlock, 0, c.stream>>>(c.gen_counts.p, scalars + 3, list_cap, scalars);
+  svo::k_group_node_emit<<<svo::grid_for(cap), 256, 0, c.stream>>>(c.gen_groups.p, scalars + 3, list_cap,
+                                                                   c.gen_marker.p, c.gen_counts.p, c.gen_addr.p);
   svo::k_gen_size<<<svo::grid_for(cap), 256, 0, c.stream>>>(T, c.gen_addr.p, scalars, cap, c.gen_marker.p,
                                                             c.requests.p, ti.scene_depth, jobs);
   const uint64_t avail = c.n_free - c.free_used;
