@@ -1,20 +1,27 @@
 """Build recipe for oracle/_ref: the reference's own OpenCL kernels compiled for the CPU.
 
-TEST INFRASTRUCTURE ONLY. Reads SvoTracer/SvoTracer.Kernel/wavefront.cl from the
-reference checkout, applies two mechanical syntax rewrites that C needs and writes
-the result to oracle/_ref/wavefront_ref.c:
+TEST INFRASTRUCTURE ONLY. Reads SvoTracer/SvoTracer.Kernel/wavefront.cl (and the
+megakernel SvoTracer/SvoTracer.Kernel/kernel.cl) from the reference checkout,
+applies mechanical syntax rewrites that C needs and writes the results to
+oracle/_ref/wavefront_ref.c (and oracle/_ref/kernel_ref.c):
 
 * OpenCL vector literals ``(float3)(a, b, c)`` become GCC compound literals
   ``((float3){a, b, c})``;
 * component access ``.x .y .z .w`` becomes ``[0] [1] [2] [3]`` (wavefront.cl has no
   swizzles and no struct member named x, y, z or w);
+* floatToUlong's ``(ulong)(fabs(x) * ULONG_MAX)`` becomes
+  ``ref_float_to_ulong(fabs(x) * ULONG_MAX)``: C leaves the conversion of NaN and
+  of values >= 2^64 undefined (x86 gives 2^63, GPUs and Arm saturate), and the
+  shim's function saturates (NaN -> 0), as the parity contract defines it;
 * the kernels' ``local uint localQueue[5];`` gets a zero initialiser. ``increment``
   (wavefront.cl:254-258) relies on work-items 0..4 of a group to clear the five
   entries; the harness runs one work-item per group, which would clear only entry 0.
 
 Nothing else in the kernel source changes. ref_shim.h supplies the OpenCL types and
 built-ins, ref_harness.c drives the kernels the way SvoTracer.Window/MainWindow.cs
-does, and gcc links the three into oracle/_ref/libsvo_ref.so.
+does, and gcc links the three into oracle/_ref/libsvo_ref.so. The megakernel gets
+its own library, oracle/_ref/libsvo_ref_mega.so (ref_mega_harness.c runs its
+`trace` kernel once per pixel), because both sources define the same helpers.
 
 The rewritten source stays in oracle/_ref/ (git-ignored), so a machine without the
 reference checkout can still compile it with ``compile_ref()``.
@@ -34,6 +41,12 @@ REF_SOURCE = os.environ.get(
 )
 REWRITTEN = os.path.join(REF_DIR, "wavefront_ref.c")
 REF_LIB = os.path.join(REF_DIR, "libsvo_ref.so")
+MEGA_SOURCE = os.environ.get(
+    "SVO_REFERENCE_MEGAKERNEL",
+    "/root/reference/SvoTracer/SvoTracer.Kernel/kernel.cl",
+)
+MEGA_REWRITTEN = os.path.join(REF_DIR, "kernel_ref.c")
+MEGA_LIB = os.path.join(REF_DIR, "libsvo_ref_mega.so")
 
 _VEC = re.compile(r"\((float|int|uint|ulong|uchar|ushort|long|short|char)([234])\)\(")
 
@@ -66,45 +79,61 @@ def _rewrite_literals(src: str) -> str:
 def rewrite(src: str) -> str:
     src = _rewrite_literals(src)
     src = src.replace("local uint localQueue[5];", "local uint localQueue[5] = {0, 0, 0, 0, 0};")
+    src = src.replace("return (ulong)(fabs(x) * ULONG_MAX);", "return ref_float_to_ulong(fabs(x) * ULONG_MAX);")
     src = re.sub(r"\.([xyzw])\b", lambda m: "[%d]" % "xyzw".index(m.group(1)), src)
     return src
 
 
-def generate() -> bool:
-    """Write oracle/_ref/wavefront_ref.c from the reference checkout, if present."""
-    if not os.path.exists(REF_SOURCE):
-        return os.path.exists(REWRITTEN)
+def _generate(source: str, rewritten: str, name: str) -> bool:
+    if not os.path.exists(source):
+        return os.path.exists(rewritten)
     os.makedirs(REF_DIR, exist_ok=True)
-    with open(REF_SOURCE, "r", encoding="utf-8-sig") as f:
+    with open(source, "r", encoding="utf-8-sig") as f:
         src = f.read()
     text = (
-        "/* Generated by oracle/build_ref.py from the reference's wavefront.cl: "
-        "vector literals and component access rewritten for C. */\n" + rewrite(src)
+        "/* Generated by oracle/build_ref.py from the reference's %s: "
+        "vector literals and component access rewritten for C. */\n" % name + rewrite(src)
     )
-    if not os.path.exists(REWRITTEN) or open(REWRITTEN).read() != text:
-        with open(REWRITTEN, "w") as f:
+    if not os.path.exists(rewritten) or open(rewritten).read() != text:
+        with open(rewritten, "w") as f:
             f.write(text)
     return True
+
+
+def generate() -> bool:
+    """Write oracle/_ref/wavefront_ref.c from the reference checkout, if present."""
+    return _generate(REF_SOURCE, REWRITTEN, "wavefront.cl")
+
+
+def _compile(rewritten: str, harness: str, lib: str, cc: str) -> str:
+    deps = [rewritten, os.path.join(HERE, harness), os.path.join(HERE, "ref_shim.h")]
+    if os.path.exists(lib) and all(os.path.getmtime(lib) >= os.path.getmtime(d) for d in deps):
+        return lib
+    cmd = [
+        cc, "-std=gnu11", "-O2", "-fPIC", "-shared", "-ffp-contract=off", "-fno-fast-math",
+        "-fopenmp", "-w", "-Wno-psabi", "-include", os.path.join(HERE, "ref_shim.h"),
+        os.path.join(HERE, harness), "-o", lib + ".tmp", "-lm",
+    ]
+    subprocess.run(cmd, check=True, cwd=REF_DIR)
+    os.replace(lib + ".tmp", lib)
+    return lib
 
 
 def compile_ref(cc: str = "gcc") -> str | None:
     """Compile libsvo_ref.so; returns its path or None when the source is absent."""
     if not generate():
         return None
-    deps = [REWRITTEN, os.path.join(HERE, "ref_harness.c"), os.path.join(HERE, "ref_shim.h")]
-    if os.path.exists(REF_LIB) and all(os.path.getmtime(REF_LIB) >= os.path.getmtime(d) for d in deps):
-        return REF_LIB
-    cmd = [
-        cc, "-std=gnu11", "-O2", "-fPIC", "-shared", "-ffp-contract=off", "-fno-fast-math",
-        "-fopenmp", "-w", "-Wno-psabi", "-include", os.path.join(HERE, "ref_shim.h"),
-        os.path.join(HERE, "ref_harness.c"), "-o", REF_LIB + ".tmp", "-lm",
-    ]
-    subprocess.run(cmd, check=True, cwd=REF_DIR)
-    os.replace(REF_LIB + ".tmp", REF_LIB)
-    return REF_LIB
+    return _compile(REWRITTEN, "ref_harness.c", REF_LIB, cc)
+
+
+def compile_ref_mega(cc: str = "gcc") -> str | None:
+    """Compile libsvo_ref_mega.so (kernel.cl); returns its path or None when the source is absent."""
+    if not _generate(MEGA_SOURCE, MEGA_REWRITTEN, "kernel.cl"):
+        return None
+    return _compile(MEGA_REWRITTEN, "ref_mega_harness.c", MEGA_LIB, cc)
 
 
 if __name__ == "__main__":
-    p = compile_ref()
-    print(p if p else "reference source not available")
+    for p in (compile_ref(), compile_ref_mega()):
+        print(p if p else "reference source not available")
     sys.exit(0)

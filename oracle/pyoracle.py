@@ -2,7 +2,9 @@
 
 ``trace_view`` runs the C restatement (libsvo_oracle.so); ``ref_trace_view`` runs the
 reference's own wavefront.cl kernels compiled for the CPU (oracle/_ref/libsvo_ref.so).
-Both take the same inputs as the CUDA path and return per-pixel results.
+``mega_trace_view`` and ``ref_mega_trace_view`` are the same pair for the megakernel
+(kernel.cl, oracle/_ref/libsvo_ref_mega.so). All take the same inputs as the CUDA
+path and return per-pixel results.
 """
 from __future__ import annotations
 
@@ -24,6 +26,7 @@ from svo_tracer import (BLOCK_DTYPE, CHILD_REQUEST_DTYPE, GRAFTING_DTYPE, PRUNIN
 _vp = C.c_void_p
 _oracle = None
 _ref = None
+_ref_mega = None
 
 
 class _ViewOut(C.Structure):
@@ -43,6 +46,10 @@ def oracle_lib() -> C.CDLL:
         lib.oracle_trace_view.restype = C.c_int64
         lib.oracle_trace_rows.argtypes = lib.oracle_trace_view.argtypes + [C.c_uint32, C.c_uint32]
         lib.oracle_trace_rows.restype = C.c_int64
+        lib.oracle_mega_trace_rows.argtypes = [_vp, C.c_uint8, _vp, C.c_size_t, _vp, C.c_size_t, C.c_char_p,
+                                               C.c_int32, C.c_int32, C.POINTER(_ViewOut), _vp, _vp, C.c_uint32,
+                                               C.POINTER(C.c_uint32), C.c_int32, C.c_uint32, C.c_uint32]
+        lib.oracle_mega_trace_rows.restype = C.c_int64
         lib.oracle_float_to_ulong.argtypes = [C.c_float]
         lib.oracle_float_to_ulong.restype = C.c_uint64
         lib.oracle_ulong_to_float.argtypes = [C.c_uint64]
@@ -96,6 +103,74 @@ def ref_lib() -> C.CDLL:
         lib.ref_trace_rows.restype = C.c_long
         _ref = lib
     return _ref
+
+
+def mega_trace_view(tree, inp: TraceInput, usage=None, max_steps: int = 1 << 16, threads: int = 0, rows=None,
+                    req_cap: int = 1 << 22, cone_limit: int = 1 << 16):
+    """The oracle's megakernel (kernel.cl's `trace`) on one view or rows [rows[0],
+    rows[1]) of it (per-pixel outputs then cover the band). usage is stamped in
+    place. Returns rgba, the primary's hit_index/hit_depth/t, per-pixel traversal
+    steps and secondary cone counts, and the child requests."""
+    lib = oracle_lib()
+    w, h = inp.ScreenSize
+    r0, r1 = (0, h) if rows is None else rows
+    n = w * (r1 - r0)
+    r = {"hit_index": np.empty(n, np.uint32), "hit_depth": np.empty(n, np.uint8), "t": np.empty(n, np.float32),
+         "rgba": np.zeros((n, 4), np.float32), "steps": np.empty(n, np.uint32), "cones": np.zeros(n, np.uint32)}
+    vo = _ViewOut(_p(r["hit_index"]), _p(r["hit_depth"]), _p(r["t"]), _p(r["rgba"]), None, None, None, _p(r["steps"]))
+    bases = np.ascontiguousarray(tree.BaseBlocks, np.uint16)
+    blocks = np.ascontiguousarray(tree.Blocks)
+    req = np.zeros(req_cap, CHILD_REQUEST_DTYPE)
+    nreq = C.c_uint32(0)
+    ng = 0 if usage is None else len(usage)
+    rc = lib.oracle_mega_trace_rows(_p(bases), tree.BaseDepth, _p(blocks), len(blocks), _p(usage), ng, inp.to_bytes(),
+                                    max_steps, cone_limit, C.byref(vo), _p(r["cones"]), _p(req), req_cap,
+                                    C.byref(nreq), threads, r0, r1)
+    if rc < 0:
+        raise ValueError("cone schedule does not end")
+    r["requests"] = req[: min(nreq.value, req_cap)]
+    r["n_requests"] = nreq.value
+    return r
+
+
+def ref_mega_available() -> bool:
+    try:
+        return build_ref.compile_ref_mega() is not None
+    except Exception:
+        return False
+
+
+def ref_mega_lib() -> C.CDLL:
+    global _ref_mega
+    if _ref_mega is None:
+        path = os.environ.get("SVO_REF_MEGA_LIB") or build_ref.compile_ref_mega()
+        if path is None:
+            raise RuntimeError("reference megakernel unavailable (no kernel.cl source)")
+        lib = C.CDLL(path)
+        lib.ref_mega_trace_rows.argtypes = [_vp, C.c_uint8, _vp, C.c_size_t, _vp, C.c_char_p, _vp, _vp, C.c_uint32,
+                                            C.c_int, C.c_uint, C.c_uint, C.c_long]
+        lib.ref_mega_trace_rows.restype = C.c_long
+        _ref_mega = lib
+    return _ref_mega
+
+
+def ref_mega_trace_view(tree, inp: TraceInput, usage=None, threads: int = 0, rows=None, req_cap: int = 1 << 22,
+                        cone_limit: int = 1 << 16):
+    """Runs the reference's megakernel (CPU build of kernel.cl's `trace`) on one view,
+    or on rows [rows[0], rows[1]) of it. usage is stamped in place. Returns rgba
+    (rows outside the band stay zero) and the child requests."""
+    lib = ref_mega_lib()
+    w, h = inp.ScreenSize
+    r0, r1 = (0, h) if rows is None else rows
+    rgba = np.zeros((w * h, 4), np.float32)
+    bases = np.ascontiguousarray(tree.BaseBlocks, np.uint16)
+    blocks = np.ascontiguousarray(tree.Blocks)
+    req = np.zeros(req_cap, CHILD_REQUEST_DTYPE)
+    n = lib.ref_mega_trace_rows(_p(bases), tree.BaseDepth, _p(blocks), len(blocks), _p(usage), inp.to_bytes()[:96],
+                                _p(rgba), _p(req), req_cap, threads, r0, r1, cone_limit)
+    if n < 0:
+        raise ValueError("cone schedule does not end")
+    return {"rgba": rgba, "requests": req[: min(n, req_cap)], "n_requests": int(n)}
 
 
 def _result(n, counts=True):

@@ -17,7 +17,11 @@
  * fast_length is sqrtf((x*x + y*y) + z*z), and half_log2 returns a value
  * whose comparisons with integers (the only way wavefront.cl reads
  * ConeDepth = -half_log2(c)) are exact: floor(log2 x) + 0.5 when x is not a
- * power of two, log2 x exactly when it is.
+ * power of two, log2 x exactly when it is. length and normalize (kernel.cl)
+ * use the same correctly rounded sqrtf((x*x + y*y) + z*z); normalize returns
+ * its argument when every element is zero, as the OpenCL C specification
+ * defines it. floatToUlong's out-of-range and NaN conversions saturate
+ * (NaN -> 0), as on the GPU.
  */
 #ifndef REF_SHIM_H
 #define REF_SHIM_H
@@ -84,6 +88,13 @@ static inline float nd_s(float a, float b) { return a / b; }
 static inline float3 nd_v3(float a, float3 b) { return a / b; }
 #define native_divide(a, b) _Generic((b), float3: nd_v3, default: nd_s)((a), (b))
 
+/* floatToUlong's conversion (rewritten by build_ref.py): saturating, NaN -> 0. */
+static inline ulong ref_float_to_ulong(double v) {
+  if (v != v || v <= 0.0) return 0;
+  if (v >= 18446744073709551616.0) return ULONG_MAX;
+  return (ulong)v;
+}
+
 static inline float native_sin(float x) { return (float)sin((double)x); }
 static inline float native_cos(float x) { return (float)cos((double)x); }
 
@@ -98,7 +109,9 @@ static inline float half_log2(float x) {
 
 static inline float fast_length(float3 v) { return sqrtf(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]); }
 static inline float dot(float3 a, float3 b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
+static inline float length(float3 v) { return sqrtf(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]); }
 static inline float3 normalize(float3 v) {
+  if (v[0] == 0.0f && v[1] == 0.0f && v[2] == 0.0f) return v;
   float l = sqrtf(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
   return v / l;
 }

@@ -729,3 +729,448 @@ void oracle_diff_fd(const uint32_t *hits, const uint8_t *n_hits, const uint8_t *
     }
   }
 }
+
+
+/* ---- megakernel: kernel.cl's `trace` (kernel.cl:1531-1558) ----------------
+ *
+ * One work-item per pixel: the primary cone (the same fixed-point traversal as
+ * the wavefront, with kernel.cl's differences noted below), then spawnRays's
+ * fan of secondary cones from the hit (kernel.cl:1115-1253), each traced to
+ * the sky or to a surface, their light accumulated in generation order, and
+ * draw (kernel.cl:1264-1275). Extra parity-contract rules: length and
+ * normalize use sqrtf((x*x + y*y) + z*z); normalize of a zero vector is that
+ * vector (OpenCL C); the double literal of `dotprod > 0.8` is compared in
+ * double; native_sin/cos of the spine and ring angles and of normalVector are
+ * (float)sin((double)x), like the ray-setup tables. */
+
+#define MEGA_PI_F 3.14159274101257324219f
+#define MEGA_PI_2_F 1.57079637050628662109f
+
+/* The cone fan's per-launch constants: spawnRays's spine and ring loops depend
+ * only on TraceInput (FovMultiplier/Constant, WeightingMultiplier/Constant). */
+typedef struct {
+  float fov, weighting, c, s, one_minus_c; /* spine: cone FoV, weighting, cos/sin(-spineAngle), 1 - cos */
+  int ring_begin, n_rings;
+} mega_spine;
+typedef struct {
+  float c, s, one_minus_c; /* cos/sin(-ringAngle), 1 - cos */
+} mega_ring;
+typedef struct {
+  int n_spines, n_rings;
+  mega_spine *spine;
+  mega_ring *ring;
+} mega_schedule;
+
+/* Returns 0 when the loops would not end within `limit` cones per pixel. */
+static int mega_build_schedule(const svo_trace_input *in, int limit, mega_schedule *S) {
+  S->n_spines = S->n_rings = 0;
+  S->spine = NULL;
+  S->ring = NULL;
+  int cap_s = 16, cap_r = 64, cones = 1;
+  S->spine = (mega_spine *)malloc(sizeof(mega_spine) * cap_s);
+  S->ring = (mega_ring *)malloc(sizeof(mega_ring) * cap_r);
+  float fov = in->fov_constant, oldfov = fov, spine = 0.0f;
+  const float FM = in->fov_multiplier, FC = in->fov_constant;
+  while (spine < MEGA_PI_F) {
+    fov = (FM * (spine + fov) + FC) / (1 - FM);
+    spine = (1 + FM) * (spine + oldfov) / (1 - FM);
+    oldfov = fov;
+    if (S->n_spines == cap_s) S->spine = (mega_spine *)realloc(S->spine, sizeof(mega_spine) * (cap_s *= 2));
+    mega_spine *sp = &S->spine[S->n_spines++];
+    sp->fov = fov;
+    sp->weighting = spine * in->weighting_multiplier + in->weighting_constant;
+    sp->c = (float)cos((double)(-spine));
+    sp->s = (float)sin((double)(-spine));
+    sp->one_minus_c = 1.0f - sp->c;
+    sp->ring_begin = S->n_rings;
+    sp->n_rings = 0;
+    cones += 1;
+    for (int j = 1; (float)j * fov < MEGA_PI_2_F; j++) {
+      if (cones + 2 > limit) return 0;
+      if (S->n_rings == cap_r) S->ring = (mega_ring *)realloc(S->ring, sizeof(mega_ring) * (cap_r *= 2));
+      mega_ring *rg = &S->ring[S->n_rings++];
+      float angle = (float)(j * 2) * fov;
+      rg->c = (float)cos((double)(-angle));
+      rg->s = (float)sin((double)(-angle));
+      rg->one_minus_c = 1.0f - rg->c;
+      sp->n_rings++;
+      cones += 2;
+    }
+    if (cones > limit) return 0;
+  }
+  return 1;
+}
+
+static float dot3(const float a[3], const float b[3]) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
+
+static void normalize3(float v[3]) {
+  if (v[0] == 0.0f && v[1] == 0.0f && v[2] == 0.0f) return;
+  float l = sqrtf(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+  v[0] = v[0] / l;
+  v[1] = v[1] / l;
+  v[2] = v[2] / l;
+}
+
+/* Rodrigues rotation of v about the unit axis a by the angle whose cos, sin
+ * and 1 - cos are (c, s, k), in kernel.cl's product order (spineRotation /
+ * ringRotation, :1142-1166, :1181-1206); transpose = 1 gives the rotation by
+ * the opposite angle (the second ring vector, :1217-1222). */
+static void rotate3(const float a[3], float c, float s, float k, const float v[3], int transpose, float out[3]) {
+  float r3 = k * a[0] * a[0], r4 = k * a[0] * a[1], r5 = k * a[0] * a[2];
+  float r6 = k * a[1] * a[1], r7 = k * a[1] * a[2], r8 = k * a[2] * a[2];
+  float r9 = s * a[0], r10 = s * a[1], r11 = s * a[2];
+  if (!transpose) {
+    out[0] = (r3 + c) * v[0] + (r4 - r11) * v[1] + (r5 + r10) * v[2];
+    out[1] = (r4 + r11) * v[0] + (r6 + c) * v[1] + (r7 - r9) * v[2];
+    out[2] = (r5 - r10) * v[0] + (r7 + r9) * v[1] + (r8 + c) * v[2];
+  } else {
+    out[0] = (r3 + c) * v[0] + (r4 + r11) * v[1] + (r5 - r10) * v[2];
+    out[1] = (r4 - r11) * v[0] + (r6 + c) * v[1] + (r7 + r9) * v[2];
+    out[2] = (r5 + r10) * v[0] + (r7 - r9) * v[1] + (r8 + c) * v[2];
+  }
+}
+
+typedef struct {
+  float origin[3], dir[3], inv[3], dof[2], fov;
+  int sign[3];
+  int cone_set; /* ConeDepth is 0 until a traverse sets it (setupInitialTrace leaves it unset) */
+  uint64_t loc[3];
+  uint8_t depth;
+} mega_ray;
+
+/* traceVoxel (kernel.cl:1075-1089) with traceBase (:1058-1073) and traceBlock
+ * (:1002-1056). Returns 1 at a surface (*node: the block resolveRayData reads),
+ * 0 in the sky (including a trace stopped by max_steps). */
+static int mega_trace_voxel(const uint16_t *bases, uint8_t B, const svo_block *blocks, size_t n_blocks,
+                            svo_usage *usage, size_t n_groups, uint16_t tick, int32_t max_steps, mega_ray *r,
+                            uint32_t *node, uint32_t *steps, svo_child_request *req, uint32_t req_cap,
+                            uint32_t *n_req) {
+  uint32_t heap[64];
+  heap[B + 1] = SVO_NO_CHILD;
+  int32_t n = 0;
+  for (;;) {
+    if (r->depth == B + 1) {
+      r->depth = B;
+      continue;
+    }
+    if (max_steps > 0 && n >= max_steps) return 0;
+    n++;
+    (*steps)++;
+    if (r->depth <= B) {
+      uint16_t chunk = bases[oracle_pow_sum((uint8_t)(r->depth - 1)) + oracle_base_location(r->depth, r->loc)];
+      if (((chunk >> (oracle_chunk_position(r->depth, r->loc) * 2)) & 2) != 2) {
+        uint64_t prev[3] = {r->loc[0], r->loc[1], r->loc[2]};
+        oracle_traverse_chunk(r->depth, r->dir, r->inv, r->sign, r->loc);
+        r->cone_set = 1;
+        if (leaving(r->loc, r->sign)) return 0;
+        r->depth = oracle_compare_positions(r->depth, prev, r->loc, r->sign);
+      } else {
+        r->depth = r->depth < B ? (uint8_t)(r->depth + 1) : (uint8_t)(B + 2);
+      }
+      continue;
+    }
+    uint32_t addr = r->depth == B + 2
+                        ? oracle_base_location((uint8_t)(B + 2), r->loc)
+                        : node_at(blocks, n_blocks, heap[r->depth - 1])->child +
+                              oracle_chunk_position((uint8_t)(r->depth - 1), r->loc);
+    heap[r->depth] = addr;
+    if (usage && (addr >> 3) < n_groups) {
+      svo_usage *u = &usage[addr >> 3];
+      if (u->tick < 65534 && u->tick != tick) u->tick = tick;
+    }
+    const svo_block *blk = node_at(blocks, n_blocks, addr);
+    if (((blk->chunk >> (oracle_chunk_position(r->depth, r->loc) * 2)) & 2) != 2) {
+      uint64_t prev[3] = {r->loc[0], r->loc[1], r->loc[2]};
+      oracle_traverse_chunk(r->depth, r->dir, r->inv, r->sign, r->loc);
+      r->cone_set = 1;
+      if (leaving(r->loc, r->sign)) return 0;
+      r->depth = oracle_compare_positions(r->depth, prev, r->loc, r->sign);
+      continue;
+    }
+    /* ConeDepth = -half_log2(c) compared exactly; an unset ConeDepth (0) is
+     * below B+2, so the first branch takes it. */
+    float c = r->cone_set ? cone_size(cone_distance(r->origin, r->loc), r->fov, r->dof) : 1.0f;
+    if (c > pow2_neg(B + 2)) {
+      r->depth = (uint8_t)(B + 2);
+      *node = heap[B + 2];
+      return 1;
+    }
+    if (c > pow2_neg(r->depth)) {
+      r->depth--;
+      continue;
+    }
+    if (blk->child == SVO_NO_CHILD) {
+      /* requestChild with buildChildRequest(localAddress, Depth, Tick, 1, Location) */
+      uint32_t slot;
+#ifdef _OPENMP
+#pragma omp atomic capture
+#endif
+      slot = (*n_req)++;
+      if (req && slot < req_cap) {
+        svo_child_request *q = &req[slot];
+        memset(q, 0, sizeof(*q));
+        q->address = addr;
+        q->tick = tick;
+        q->depth = r->depth;
+        q->location[0] = r->loc[0];
+        q->location[1] = r->loc[1];
+        q->location[2] = r->loc[2];
+        q->tree_size = 1;
+      }
+      *node = addr;
+      return 1;
+    }
+    if (c < pow2_neg(r->depth + 1)) {
+      r->depth++;
+      continue;
+    }
+    *node = addr; /* average() returns the block itself */
+    return 1;
+  }
+}
+
+/* resolveBackgroundRayData (kernel.cl:1225-1240): colour and luminosity of the sky. */
+static void mega_sky(const float dir[3], uint8_t rgb[3], float *lum) {
+  float dotp = dir[0] * 0.0f + dir[1] * 0.0f + dir[2] * -1.0f;
+  if ((double)dotp > 0.8) {
+    rgb[0] = rgb[1] = rgb[2] = 255;
+    *lum = dotp * 150.0f;
+  } else {
+    rgb[0] = 135;
+    rgb[1] = 206;
+    rgb[2] = 235;
+    *lum = 10.0f;
+  }
+}
+
+/* normalVector (kernel.cl:264-275). */
+static void mega_normal(int16_t pitch, int16_t yaw, float n[3]) {
+  float fy = (float)yaw * MEGA_PI_F / 32767.0f, fp = (float)pitch * MEGA_PI_F / 32767.0f;
+  float sy = (float)sin((double)fy), cy = (float)cos((double)fy);
+  float sp = (float)sin((double)fp), cp = (float)cos((double)fp);
+  n[0] = cy * cp;
+  n[1] = sy * cp;
+  n[2] = sp;
+}
+
+/* traverseChunkNormal (kernel.cl:428-489): the cone's start, one level-`depth`
+ * cell along the normal, choosing the axis of the largest distance. */
+static void mega_step_normal(uint8_t depth, const float nrm[3], uint64_t loc[3]) {
+  int s[3];
+  float inv[3], a[3];
+  uint64_t d[3];
+  for (int k = 0; k < 3; k++) {
+    s[k] = nrm[k] >= 0;
+    inv[k] = 1.0f / nrm[k];
+    d[k] = oracle_round_ulong(loc[k], depth, s[k]);
+    a[k] = fabsf((float)d[k] * inv[k]);
+  }
+  if (a[0] >= a[1] && a[0] >= a[2]) {
+    float u = oracle_ulong_to_float(d[0]);
+    d[1] = oracle_float_to_ulong(nrm[1] * inv[0] * u);
+    d[2] = oracle_float_to_ulong(nrm[2] * inv[0] * u);
+  } else if (a[1] >= a[0] && a[1] >= a[2]) {
+    float u = oracle_ulong_to_float(d[1]);
+    d[0] = oracle_float_to_ulong(nrm[0] * inv[1] * u);
+    d[2] = oracle_float_to_ulong(nrm[2] * inv[1] * u);
+  } else {
+    float u = oracle_ulong_to_float(d[2]);
+    d[0] = oracle_float_to_ulong(nrm[0] * inv[2] * u);
+    d[1] = oracle_float_to_ulong(nrm[1] * inv[2] * u);
+  }
+  for (int k = 0; k < 3; k++) loc[k] = s[k] ? loc[k] + d[k] : loc[k] - d[k];
+  for (int k = 0; k < 3; k++) {
+    if (s[k] && loc[k] == 0)
+      loc[k] = ULMAX;
+    else if (!s[k] && loc[k] == ULMAX)
+      loc[k] = 0;
+  }
+}
+
+typedef struct {
+  float weight, r, g, b; /* RayAccumulator: TotalWeighting, ColourR/G/B */
+} mega_acc;
+
+/* accumulateRay (kernel.cl:1110-1113): setupTrace (:524-544), traceRay and
+ * writeToAccumulator (:1255-1262) for one cone. */
+static void mega_cone(const uint16_t *bases, uint8_t B, const svo_block *blocks, size_t n_blocks, svo_usage *usage,
+                      size_t n_groups, uint16_t tick, int32_t max_steps, const uint64_t hit_loc[3], uint8_t hit_depth,
+                      const float nrm[3], const float dir[3], float fov, float weighting, mega_acc *acc,
+                      uint32_t *steps, svo_child_request *req, uint32_t req_cap, uint32_t *n_req) {
+  mega_ray c;
+  for (int k = 0; k < 3; k++) {
+    c.origin[k] = oracle_ulong_to_float(hit_loc[k]);
+    c.dir[k] = dir[k];
+    c.inv[k] = 1.0f / dir[k];
+    c.sign[k] = dir[k] >= 0;
+    c.loc[k] = hit_loc[k];
+  }
+  c.dof[0] = c.dof[1] = 0.0f;
+  c.fov = fov;
+  c.depth = 1;
+  mega_step_normal(hit_depth, nrm, c.loc);
+  c.cone_set = 1;
+  uint32_t node;
+  int surface = mega_trace_voxel(bases, B, blocks, n_blocks, usage, n_groups, tick, max_steps, &c, &node, steps, req,
+                                 req_cap, n_req);
+  acc->weight += weighting;
+  if (surface) return; /* Luminosity 0 */
+  uint8_t rgb[3];
+  float lum;
+  mega_sky(dir, rgb, &lum);
+  acc->r += ((float)rgb[0] / 255.0f) * weighting * lum;
+  acc->g += ((float)rgb[1] / 255.0f) * weighting * lum;
+  acc->b += ((float)rgb[2] / 255.0f) * weighting * lum;
+}
+
+int64_t oracle_mega_trace_rows(const uint16_t *bases, uint8_t base_depth, const svo_block *blocks, size_t n_blocks,
+                               svo_usage *usage, size_t n_groups, const svo_trace_input *in, int32_t max_steps,
+                               int32_t cone_limit, const oracle_view_out *out, uint32_t *n_cones,
+                               svo_child_request *req, uint32_t req_cap, uint32_t *n_req, int32_t threads,
+                               uint32_t row_begin, uint32_t row_end) {
+  /* kernel.cl:1533-1534: nothing is drawn for an unusable cone schedule */
+  if (in->fov_constant <= 0 || in->fov_multiplier >= 1 || in->fov_multiplier <= -1) return 0;
+  mega_schedule S;
+  if (!mega_build_schedule(in, cone_limit, &S)) {
+    free(S.spine);
+    free(S.ring);
+    return -1;
+  }
+  uint32_t W = in->screen_size[0], H = in->screen_size[1];
+  if (row_end > H) row_end = H;
+  if (row_begin > row_end) row_begin = row_end;
+  const uint8_t B = base_depth;
+  float *su = (float *)malloc(sizeof(float) * (W + 1));
+  float *cu = (float *)malloc(sizeof(float) * (W + 1));
+  float *sv = (float *)malloc(sizeof(float) * (H + 1));
+  float *cv = (float *)malloc(sizeof(float) * (H + 1));
+  oracle_view_tables(in, su, cu, sv, cv);
+  int64_t n = (int64_t)W * (row_end - row_begin);
+#ifdef _OPENMP
+  int nt = threads > 0 ? threads : omp_get_max_threads();
+#pragma omp parallel for schedule(dynamic, 16) num_threads(nt)
+#endif
+  for (int64_t id = 0; id < n; id++) {
+    uint32_t px = (uint32_t)(id % W), py = row_begin + (uint32_t)(id / W);
+    /* setupInitialTrace (kernel.cl:491-522): DoF and Tick come from the input */
+    float m0 = cu[px] * cv[py], m1 = (0.0f - su[px]) * cv[py], m2 = sv[py];
+    const float *F = in->facing;
+    mega_ray p;
+    p.dir[0] = F[0] * m0 + F[3] * m1 + F[6] * m2;
+    p.dir[1] = F[1] * m0 + F[4] * m1 + F[7] * m2;
+    p.dir[2] = F[2] * m0 + F[5] * m1 + F[8] * m2;
+    for (int k = 0; k < 3; k++) {
+      p.inv[k] = 1.0f / p.dir[k];
+      p.sign[k] = p.dir[k] >= 0;
+      p.origin[k] = in->origin[k];
+    }
+    p.dof[0] = in->dof[0];
+    p.dof[1] = in->dof[1];
+    p.fov = in->fov[0] / (float)W;
+    p.cone_set = 0;
+    p.depth = 1;
+    uint32_t steps = 0, cones = 0, hit_index = SVO_MISS;
+    uint8_t hit_depth = 0;
+    float t = INFINITY;
+    uint8_t rgb[3];
+    mega_acc acc = {0.0f, 0.0f, 0.0f, 0.0f};
+    if (!oracle_trace_into_volume(p.origin, p.dir, p.inv, p.fov, p.dof, p.loc)) {
+      float lum;
+      mega_sky(p.dir, rgb, &lum);
+    } else {
+      uint32_t node = 0;
+      int surface = mega_trace_voxel(bases, B, blocks, n_blocks, usage, n_groups, in->tick, max_steps, &p, &node,
+                                     &steps, req, req_cap, n_req);
+      float nrm[3] = {0.0f, 0.0f, 0.0f};
+      uint8_t depth = 1; /* RayData.Depth of a sky ray */
+      if (surface) {
+        /* resolveRayData (kernel.cl:1242-1253) */
+        const svo_block *blk = node_at(blocks, n_blocks, node);
+        rgb[0] = blk->colour_r;
+        rgb[1] = blk->colour_g;
+        rgb[2] = blk->colour_b;
+        mega_normal(blk->normal_pitch, blk->normal_yaw, nrm);
+        depth = p.depth;
+        hit_index = node;
+        hit_depth = p.depth;
+        float x = oracle_ulong_to_float(p.loc[0]) - p.origin[0];
+        float y = oracle_ulong_to_float(p.loc[1]) - p.origin[1];
+        float z = oracle_ulong_to_float(p.loc[2]) - p.origin[2];
+        t = sqrtf(x * x + y * y + z * z);
+      } else {
+        float lum;
+        mega_sky(p.dir, rgb, &lum);
+      }
+      /* spawnRays (kernel.cl:1115-1253) with baseWeighting 1 */
+      const float *D = p.dir;
+      float axis[3] = {D[1] * nrm[2] - D[2] * nrm[1], D[2] * nrm[0] - D[0] * nrm[2], D[0] * nrm[1] - D[1] * nrm[0]};
+      normalize3(axis);
+      float d2 = 2.0f * dot3(D, nrm);
+      float refl[3] = {D[0] - d2 * nrm[0], D[1] - d2 * nrm[1], D[2] - d2 * nrm[2]};
+      float fov = in->fov_constant, weighting = in->weighting_constant, rw = weighting;
+      float dp = dot3(refl, nrm);
+      if (dp < fov) rw = weighting * dp / fov;
+      mega_cone(bases, B, blocks, n_blocks, usage, n_groups, in->tick, max_steps, p.loc, depth, nrm, refl, fov,
+                rw * 1.0f, &acc, &steps, req, req_cap, n_req);
+      cones++;
+      for (int s = 0; s < S.n_spines; s++) {
+        const mega_spine *sp = &S.spine[s];
+        fov = sp->fov;
+        weighting = sp->weighting;
+        rw = weighting;
+        float seed[3];
+        rotate3(axis, sp->c, sp->s, sp->one_minus_c, refl, 0, seed);
+        normalize3(seed);
+        dp = dot3(seed, nrm);
+        if (dp < 0) break;
+        if (dp < fov) rw = weighting * dp / fov;
+        mega_cone(bases, B, blocks, n_blocks, usage, n_groups, in->tick, max_steps, p.loc, depth, nrm, seed, fov,
+                  rw * 1.0f, &acc, &steps, req, req_cap, n_req);
+        cones++;
+        for (int j = 0; j < sp->n_rings; j++) {
+          const mega_ring *rg = &S.ring[sp->ring_begin + j];
+          rw = weighting;
+          float v[3];
+          rotate3(refl, rg->c, rg->s, rg->one_minus_c, seed, 0, v);
+          normalize3(v);
+          dp = dot3(v, nrm);
+          if (dp < 0) break;
+          if (dp < fov) rw = weighting * dp / fov;
+          mega_cone(bases, B, blocks, n_blocks, usage, n_groups, in->tick, max_steps, p.loc, depth, nrm, v, fov,
+                    rw * 1.0f, &acc, &steps, req, req_cap, n_req);
+          rotate3(refl, rg->c, rg->s, rg->one_minus_c, seed, 1, v);
+          normalize3(v);
+          mega_cone(bases, B, blocks, n_blocks, usage, n_groups, in->tick, max_steps, p.loc, depth, nrm, v, fov,
+                    rw * 1.0f, &acc, &steps, req, req_cap, n_req);
+          cones += 2;
+        }
+      }
+    }
+    if (out->hit_index) out->hit_index[id] = hit_index;
+    if (out->hit_depth) out->hit_depth[id] = hit_depth;
+    if (out->t) out->t[id] = t;
+    if (out->steps) out->steps[id] = steps;
+    if (n_cones) n_cones[id] = cones;
+    if (out->rgba) {
+      /* draw (kernel.cl:1264-1275) */
+      float *o = &out->rgba[4 * id];
+      if (acc.weight > 0.01f) {
+        o[0] = fminf(((float)rgb[0] + acc.r / acc.weight) / 255.0f, 1.0f);
+        o[1] = fminf(((float)rgb[1] + acc.g / acc.weight) / 255.0f, 1.0f);
+        o[2] = fminf(((float)rgb[2] + acc.b / acc.weight) / 255.0f, 1.0f);
+      } else {
+        o[0] = (float)rgb[0] / 255.0f;
+        o[1] = (float)rgb[1] / 255.0f;
+        o[2] = (float)rgb[2] / 255.0f;
+      }
+      o[3] = 1.0f;
+    }
+  }
+  free(su);
+  free(cu);
+  free(sv);
+  free(cv);
+  free(S.spine);
+  free(S.ring);
+  return 0;
+}

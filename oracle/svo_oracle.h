@@ -63,6 +63,20 @@ uint8_t oracle_compare_positions(uint8_t depth, const uint64_t prev[3], const ui
 int oracle_trace_into_volume(const float origin[3], const float dir[3], const float inv[3], float fov,
                              const float dof[2], uint64_t loc[3]);
 
+/* The megakernel (kernel.cl's `trace`) over rows [row_begin, row_end): per pixel
+ * the primary cone, the spawnRays fan of secondary cones and draw's colour.
+ * out->hit_index/hit_depth/t describe the primary's surface block, out->steps
+ * counts the traversal steps of all the pixel's traces and n_cones its
+ * secondary cones (either may be NULL). Returns -1 (nothing traced) when the
+ * cone schedule has more than cone_limit cones per pixel, else 0; an unusable
+ * schedule (FovConstant <= 0, |FovMultiplier| >= 1) draws nothing, as the
+ * kernel does. */
+int64_t oracle_mega_trace_rows(const uint16_t *bases, uint8_t base_depth, const svo_block *blocks, size_t n_blocks,
+                               svo_usage *usage, size_t n_groups, const svo_trace_input *in, int32_t max_steps,
+                               int32_t cone_limit, const oracle_view_out *out, uint32_t *n_cones,
+                               svo_child_request *req, uint32_t req_cap, uint32_t *n_req, int32_t threads,
+                               uint32_t row_begin, uint32_t row_end);
+
 /* Usage initialisation rule of MainWindow.cs:129-141. */
 void oracle_init_usage(const uint16_t *bases, uint8_t base_depth, svo_usage *usage, size_t n_groups);
 
