@@ -184,6 +184,8 @@ typedef struct svo_trace_config {
   int32_t collect_stats; /* 0 none, 1 totals (svo_last_trace_stats), 2 totals and per-ray counts */
   int32_t max_hits;     /* differentiable forward: LOD hits composited per ray (1..1024) */
   int32_t schedule;     /* SVO_SCHEDULE_LANE or SVO_SCHEDULE_WARP */
+  int32_t mega_band_tiles; /* megakernel: 8x4 tiles per cone band (0: as many as 2^26 cone slots hold) */
+  int32_t _pad;
 } svo_trace_config;
 
 /* Ray scheduling of the persistent trace kernel. LANE: each thread claims rays
@@ -191,6 +193,18 @@ typedef struct svo_trace_config {
  * warp claims 32 consecutive rays, runs them to the end and regroups before the
  * next claim (ray_chunk and cadence unused). Results are identical. */
 enum { SVO_SCHEDULE_LANE = 1, SVO_SCHEDULE_WARP = 2 };
+
+/* Counters of the last svo_mega_trace. */
+typedef struct svo_mega_stats {
+  uint64_t pixels;     /* primary cones */
+  uint64_t surfaces;   /* primary cones that ended at a surface */
+  uint64_t cones;      /* secondary cones traced (spawnRays's fans) */
+  uint64_t cone_slots; /* cone slots laid out: tiles x cones of each tile's fullest pixel x 32 */
+} svo_mega_stats;
+
+/* Cones per pixel the megakernel accepts in one fan (spawnRays's loops end
+ * after at most this many cones, or the call is refused). */
+#define SVO_MEGA_MAX_CONES 4096
 
 /* ---- context ------------------------------------------------------------ */
 
@@ -249,6 +263,22 @@ SVO_API svo_status svo_autotune(void *ctx, const svo_trace_input *inputs, int32_
 SVO_API svo_status svo_read_ray_counts(void *ctx, uint32_t *v_block, uint32_t *v_base, size_t n);
 /* Child requests of the last trace. *n = requests raised (may exceed cap). */
 SVO_API svo_status svo_read_child_requests(void *ctx, svo_child_request *out, uint32_t cap, uint32_t *n);
+
+/* ---- megakernel ------------------------------------------------------------ */
+
+/* Replaces an Enqueue of kernel.cl's `trace` over ScreenSize (kernel.cl:1531-1558,
+ * the kernel.cl build of MainWindow.cs:45): per pixel the primary cone, the
+ * spawnRays fan of secondary cones from where it ends (kernel.cl:1115-1253), and
+ * draw's colour (kernel.cl:1264-1275) into out->rgba. Reads the first 96 bytes of
+ * `input` (kernel.cl's TraceInput, which has no AmbientLightLevel).
+ * out->hit_index / hit_depth / t describe the primary cone's surface block
+ * (SVO_MISS / 0 / +inf in the sky). Usage ticks are stamped and child requests
+ * (Tick = input->tick, TreeSize 1) queued as by svo_trace. FovConstant <= 0 or
+ * |FovMultiplier| >= 1 draws nothing, as the kernel returns; a cone schedule
+ * whose loops would run past SVO_MEGA_MAX_CONES cones per pixel (the kernel's
+ * would not end) returns SVO_ERR_INVALID_ARGUMENT. */
+SVO_API svo_status svo_mega_trace(void *ctx, const svo_trace_input *input, const svo_trace_output *out);
+SVO_API svo_status svo_last_mega_stats(void *ctx, svo_mega_stats *stats);
 
 /* ---- tree updates: usage, block GC, grafting, pruning --------------------- */
 

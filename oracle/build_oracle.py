@@ -2,8 +2,8 @@
 
 Compiles oracle/svo_oracle.c (the C restatement of the reference's wavefront hot
 path) into oracle/libsvo_oracle.so, and, through build_ref.py, the reference's own
-wavefront.cl kernels into oracle/_ref/libsvo_ref.so where their rewritten source is
-available. Only tests, __graft_entry__.smoke() and bench.py's CPU legs load these.
+wavefront.cl kernels into oracle/_ref/libsvo_ref.so and its megakernel kernel.cl into
+oracle/_ref/libsvo_ref_mega.so where their rewritten sources are available. Only tests, __graft_entry__.smoke() and bench.py's CPU legs load these.
 """
 from __future__ import annotations
 
@@ -33,11 +33,12 @@ def build_oracle(cc: str = "gcc") -> str:
 
 def build_all() -> dict:
     out = {"oracle": build_oracle()}
-    try:
-        out["ref"] = build_ref.compile_ref()
-    except subprocess.CalledProcessError as e:  # the reference harness is optional
-        out["ref"] = None
-        out["ref_error"] = str(e)
+    for key, fn in (("ref", build_ref.compile_ref), ("ref_mega", build_ref.compile_ref_mega)):
+        try:
+            out[key] = fn()
+        except subprocess.CalledProcessError as e:  # the reference harnesses are optional
+            out[key] = None
+            out[key + "_error"] = str(e)
     return out
 
 

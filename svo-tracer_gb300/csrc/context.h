@@ -10,6 +10,7 @@
 #include <string>
 #include <vector>
 
+#include "mega_internal.h"
 #include "svo_internal.h"
 
 namespace svo {
@@ -125,6 +126,22 @@ struct Context {
   uint64_t saved_params_gen = 0;
   int32_t saved_max_hits = 0;
   bool saved_valid = false;
+  // megakernel: per-slot pixel records, one band's cone slots, normalVector's
+  // table of the int16 angles, the cone schedule of the last input (by the bits
+  // of FovMultiplier, FovConstant, WeightingMultiplier, WeightingConstant)
+  DevBuf<MegaPixel> mega_pix;
+  DevBuf<float4> mega_cone_dw;
+  DevBuf<uint16_t> mega_cone_s, mega_tile_k;
+  DevBuf<uint8_t> mega_cone_sky;
+  DevBuf<float2> mega_normal_sc;
+  DevBuf<MegaSpine> mega_spine;
+  DevBuf<MegaRing> mega_ring;
+  DevBuf<unsigned long long> mega_totals;
+  PinBuf<unsigned long long> h_mega_totals;
+  std::array<uint32_t, 4> mega_sched_key{};
+  bool mega_sched_valid = false;
+  int32_t mega_n_spines = 0, mega_k_max = 0;
+  svo_mega_stats last_mega{};
   uint64_t n_free = 0, free_used = 0, n_pruned = 0, n_freed = 0, n_claimed = 0;
   bool free_valid = false;
   // graph cache for svo_trace_batch_graph
@@ -183,6 +200,16 @@ struct Context {
     gen_jobs.release();
     diff_saved.release();
     diff_loss.release();
+    mega_pix.release();
+    mega_cone_dw.release();
+    mega_cone_s.release();
+    mega_tile_k.release();
+    mega_cone_sky.release();
+    mega_normal_sc.release();
+    mega_spine.release();
+    mega_ring.release();
+    mega_totals.release();
+    h_mega_totals.release();
     if (own_stream) cudaStreamDestroy(own_stream);
   }
 };

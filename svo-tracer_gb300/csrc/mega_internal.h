@@ -1,0 +1,60 @@
+// Internal declarations of the megakernel path (kernel.cl's `trace`), shared by
+// mega_kernels.cu and the C ABI in svo_api.cu.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "svo_internal.h"
+
+namespace svo {
+
+// Per pixel slot (the view's 8x4 tiles, 32 slots per tile) between the kernels.
+enum : uint8_t { kMegaPad = 0, kMegaMiss = 1, kMegaSky = 2, kMegaSurface = 3 };
+struct MegaPixel {
+  uint64_t loc[3];   // primary's end location; after the fan kernel, the cones' start
+  float origin[3];   // cones' Origin: ulongToFloat of the primary's end location
+  float dir[3];      // primary direction
+  uint32_t node;     // surface block, SVO_MISS for the sky
+  uint32_t id;       // pixel index in the view
+  uint16_t n_cones;  // cones of this pixel's fan
+  uint8_t kind;      // kMega*
+  uint8_t depth;     // RayData.Depth: the surface's level, 1 for the sky
+  uint32_t _pad;
+};
+static_assert(sizeof(MegaPixel) == 64, "MegaPixel layout");
+
+// spawnRays's per-launch constants (kernel.cl:1115-1253): one spine step of the
+// fan (its cones' FoV and weighting, cos/sin(-spineAngle), 1 - cos) and its
+// ring rotations (cos/sin(-ringAngle), 1 - cos).
+struct MegaSpine {
+  float fov, weighting, c, s, k;
+  uint32_t ring_begin, n_rings, _pad;
+};
+struct MegaRing {
+  float c, s, k, _pad;
+};
+
+struct MegaLaunch {
+  TraceLaunch t;            // tree, queue, view and table of the primary cones
+  MegaPixel *pix;           // per slot of the view
+  float4 *cone_dw;          // per cone slot of the band: direction, weighting
+  uint16_t *cone_s;         // per cone slot: spine step + 1 (0: the reflection cone)
+  uint8_t *cone_sky;        // per cone slot: 1 when the cone reached the sky
+  uint16_t *tile_k;         // per tile of the band: cones of its fullest pixel
+  const float2 *normal_sc;  // normalVector's (sin, cos) of each int16 angle, index angle + 32768
+  const MegaSpine *spine;
+  const MegaRing *ring;
+  uint32_t *unit_counter;       // cone kernel's (tile, k) queue head
+  unsigned long long *totals;   // [0] cones of the fans, [1] primary surfaces
+  int32_t n_spines;
+  int32_t k_max;                // cones per pixel at most: the cone slot stride
+  float fov_c, weighting_c;     // FovConstant, WeightingConstant: the reflection cone's
+  uint32_t band_tile0, band_tiles, n_units;  // tiles [band_tile0, +band_tiles), units band_tiles * k_max
+  int32_t grid_cones;           // persistent grid of the cone kernel
+};
+
+svo_status launch_mega_primary(const MegaLaunch &m, void *stream);
+svo_status launch_mega_band(const MegaLaunch &m, void *stream);
+int mega_occupancy(const MegaLaunch &m);
+
+}  // namespace svo

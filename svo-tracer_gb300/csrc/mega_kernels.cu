@@ -1,0 +1,522 @@
+// The megakernel path for sm_103a: kernel.cl's `trace` (SvoTracer.Kernel/
+// kernel.cl:1531-1558), which runs per pixel a primary cone, spawnRays's fan of
+// secondary cones from its end point (:1115-1253) and draw (:1264-1275).
+//
+// One OpenCL work-item per pixel runs ~20 dependent traces in a row; here the
+// pixel's work is split into four kernels over the view's 8x4 pixel tiles, so
+// that a warp always steps 32 cones that start close together and point the
+// same way:
+//  1. mega_primary_kernel: the primary cone of every pixel, the persistent
+//     warp-batch traversal of trace_kernels.cu with kernel.cl's differences
+//     (DoF at the volume entry, ConeDepth 0 until the first move, requests with
+//     the frame's Tick and TreeSize 1), ending in a MegaPixel record.
+//  2. mega_fan_kernel: spawnRays for each pixel: cone directions and
+//     weightings in generation order, stored [tile][cone k][lane], and the
+//     cones' common start (traverseChunkNormal, the same for every cone of a
+//     pixel).
+//  3. mega_cone_kernel: every cone traced to a surface or the sky; a warp
+//     claims one (tile, k) unit, cone k of the tile's 32 pixels.
+//  4. mega_resolve_kernel: writeToAccumulator in generation order, then draw.
+// The cone slots of a frame are processed in bands of tiles so that their
+// memory stays bounded for any cone schedule.
+//
+// Every float operation is one IEEE round-to-nearest operation in kernel.cl's
+// order (no contraction). The trigonometry of the fan is per-launch constants
+// and a table over the 65536 int16 normal angles, (float)sin((double)x) on the
+// host like the ray-setup tables; normalize of a zero vector is that vector.
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "mega_internal.h"
+#include "trace_core.cuh"
+
+namespace svo {
+namespace {
+
+#ifndef SVO_MEGA_MIN_CTAS
+#define SVO_MEGA_MIN_CTAS 4
+#endif
+
+__device__ __forceinline__ size_t cone_slot(const MegaLaunch &m, uint32_t tile_in_band, uint32_t k, uint32_t lane) {
+  return ((size_t)tile_in_band * (uint32_t)m.k_max + k) * 32u + lane;
+}
+
+__device__ __forceinline__ float dot3(float ax, float ay, float az, float bx, float by, float bz) {
+  return __fadd_rn(__fadd_rn(__fmul_rn(ax, bx), __fmul_rn(ay, by)), __fmul_rn(az, bz));
+}
+
+// normalize (OpenCL C): v / sqrt(x*x + y*y + z*z); a zero vector stays zero.
+__device__ __forceinline__ void normalize3(float &x, float &y, float &z) {
+  if (x == 0.0f && y == 0.0f && z == 0.0f) return;
+  const float l = __fsqrt_rn(dot3(x, y, z, x, y, z));
+  x = __fdiv_rn(x, l);
+  y = __fdiv_rn(y, l);
+  z = __fdiv_rn(z, l);
+}
+
+// Rotation of v about the unit axis a (cos c, sin s, k = 1 - c) in kernel.cl's
+// product order (spineRotation / ringRotation); `transpose` rotates by the
+// opposite angle (the second vector of a ring pair).
+__device__ __forceinline__ void rotate3(float ax, float ay, float az, float c, float s, float k, float vx, float vy,
+                                        float vz, bool transpose, float &ox, float &oy, float &oz) {
+  const float r3 = __fmul_rn(__fmul_rn(k, ax), ax), r4 = __fmul_rn(__fmul_rn(k, ax), ay);
+  const float r5 = __fmul_rn(__fmul_rn(k, ax), az), r6 = __fmul_rn(__fmul_rn(k, ay), ay);
+  const float r7 = __fmul_rn(__fmul_rn(k, ay), az), r8 = __fmul_rn(__fmul_rn(k, az), az);
+  const float r9 = __fmul_rn(s, ax), r10 = __fmul_rn(s, ay), r11 = __fmul_rn(s, az);
+  const float sg = transpose ? -1.0f : 1.0f;  // exact: flips the sign of the sine terms
+  const float q9 = __fmul_rn(sg, r9), q10 = __fmul_rn(sg, r10), q11 = __fmul_rn(sg, r11);
+  ox = __fadd_rn(__fadd_rn(__fmul_rn(__fadd_rn(r3, c), vx), __fmul_rn(__fsub_rn(r4, q11), vy)),
+                 __fmul_rn(__fadd_rn(r5, q10), vz));
+  oy = __fadd_rn(__fadd_rn(__fmul_rn(__fadd_rn(r4, q11), vx), __fmul_rn(__fadd_rn(r6, c), vy)),
+                 __fmul_rn(__fsub_rn(r7, q9), vz));
+  oz = __fadd_rn(__fadd_rn(__fmul_rn(__fsub_rn(r5, q10), vx), __fmul_rn(__fadd_rn(r7, q9), vy)),
+                 __fmul_rn(__fadd_rn(r8, c), vz));
+}
+
+// roundUlong (kernel.cl:240-251) in real coordinates.
+__device__ __forceinline__ uint64_t round_ulong(uint64_t v, int depth, bool up) {
+  const uint64_t keep = kAll - (kAll >> (depth + 1));
+  if (up) return ((v & keep) + ((kAll - (kAll >> 1)) >> depth)) - v;
+  const uint64_t out = v - ((v & keep) - 1);
+  return out >= v ? v : out;
+}
+
+// traverseChunkNormal (kernel.cl:428-489): one level-`depth` cell along the
+// normal, the axis of the largest distance chosen.
+__device__ __forceinline__ void step_normal(int depth, const float n[3], uint64_t loc[3]) {
+  bool s[3];
+  float inv[3], a[3];
+  uint64_t d[3];
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    s[k] = n[k] >= 0.0f;
+    inv[k] = __frcp_rn(n[k]);
+    d[k] = round_ulong(loc[k], depth, s[k]);
+    a[k] = fabsf(__fmul_rn(ulong_to_float(d[k]), inv[k]));
+  }
+  const int ax = (a[0] >= a[1] && a[0] >= a[2]) ? 0 : ((a[1] >= a[0] && a[1] >= a[2]) ? 1 : 2);
+  const float u = __fmul_rn(ulong_to_float(d[ax]), 0x1p-64f);
+#pragma unroll
+  for (int k = 0; k < 3; k++)
+    if (k != ax) d[k] = unit_to_ulong(__fmul_rn(__fmul_rn(n[k], inv[ax]), u));
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    uint64_t v = s[k] ? loc[k] + d[k] : loc[k] - d[k];
+    if (s[k] && v == 0)
+      v = kAll;
+    else if (!s[k] && v == kAll)
+      v = 0;
+    loc[k] = v;
+  }
+}
+
+// resolveBackgroundRayData (kernel.cl:1225-1240). `dotprod > 0.8` compares with
+// a double constant; the smallest float above 0.8 is 0.8f.
+__device__ __forceinline__ void sky_light(float dx, float dy, float dz, uint32_t &r, uint32_t &g, uint32_t &b,
+                                          float &lum) {
+  const float dotp = dot3(dx, dy, dz, 0.0f, 0.0f, -1.0f);
+  if (dotp >= 0.8f) {
+    r = g = b = 255;
+    lum = __fmul_rn(dotp, 150.0f);
+  } else {
+    r = 135;
+    g = 206;
+    b = 235;
+    lum = 10.0f;
+  }
+}
+
+// Shared-memory prologue of the tracing kernels (view, base chunks, path
+// cache, Morton table); zero_dof clears the view's DoF (setupTrace's cones).
+template <bool kSmemBases>
+__device__ __forceinline__ void stage_shared(const TraceLaunch &a, uint8_t *smem, ViewParams *&s_views,
+                                             uint16_t *&s_bases, uint32_t *&s_path, bool zero_dof) {
+  s_views = reinterpret_cast<ViewParams *>(smem);
+  s_bases = reinterpret_cast<uint16_t *>(smem + a.n_views * sizeof(ViewParams));
+  const size_t bases_bytes = kSmemBases ? ((a.n_bases * 2 + 15) & ~15u) : 0;
+  s_path = reinterpret_cast<uint32_t *>(smem + a.n_views * sizeof(ViewParams) + bases_bytes);
+  const uint32_t *src = reinterpret_cast<const uint32_t *>(a.views);
+  uint32_t *dst = reinterpret_cast<uint32_t *>(s_views);
+  for (uint32_t i = threadIdx.x; i < a.n_views * sizeof(ViewParams) / 4; i += blockDim.x) dst[i] = src[i];
+  if (kSmemBases)
+    for (uint32_t i = threadIdx.x; i < a.n_bases; i += blockDim.x) s_bases[i] = __ldg(a.bases + i);
+  fill_spread_table();
+  __syncthreads();
+  if (zero_dof && threadIdx.x == 0) {
+    s_views[0].dof[0] = 0.0f;
+    s_views[0].dof[1] = 0.0f;
+  }
+  __syncthreads();
+}
+
+__device__ __forceinline__ void reset_walk(Walk &w) {
+  w.cur_addr = kFull;
+  w.cur_child = 0;
+  w.cur_chunk = 0;
+  w.last_group = kFull;
+  w.v_block = 0;
+  w.v_base = 0;
+}
+
+__device__ __forceinline__ void record_timeout(const TraceLaunch &a, uint32_t item, const Ray &r) {
+  if (a.error && atomicCAS(a.error, 0u, (unsigned)SVO_ERR_TIMEOUT) == 0u) {
+    a.error[1] = blockIdx.x;
+    a.error[2] = threadIdx.x;
+    a.error[3] = item;
+    a.error[4] = (uint32_t)r.depth;
+    a.error[5] = (uint32_t)r.steps;
+  }
+}
+
+// Runs a cone to its end: kStepHit at a surface, kStepBackground in the sky;
+// false when it needed more passes than max_steps allows (a fault).
+template <bool kSmemBases>
+__device__ __forceinline__ bool run_cone(const TraceLaunch &a, const ViewParams &v, const uint16_t *s_bases,
+                                         const uint4 *blocks, int B, Ray &r, Walk &w, int &finish) {
+  Stats st;
+  const uint32_t limit = (uint32_t)a.max_steps + 2u;
+  uint32_t n = 0;
+  finish = kStepOn;
+  while (finish == kStepOn) {
+    if (++n > limit) return false;
+    finish = probe<false, kSmemBases, true>(a, v, s_bases, blocks, B, r, w, st);
+    if (finish == kStepEmpty) {
+      finish = advance(a, blocks, B, r, w);
+      r.fresh = false;
+    }
+  }
+  return true;
+}
+
+template <bool kSmemBases>
+__global__ void __launch_bounds__(256, SVO_MEGA_MIN_CTAS) mega_primary_kernel(const MegaLaunch m) {
+  extern __shared__ __align__(16) uint8_t smem[];
+  const TraceLaunch &a = m.t;
+  ViewParams *s_views;
+  uint16_t *s_bases;
+  uint32_t *s_path;
+  stage_shared<kSmemBases>(a, smem, s_views, s_bases, s_path, false);
+  const int B = a.base_depth;
+  const uint4 *blocks = reinterpret_cast<const uint4 *>(a.blocks);
+  const ViewParams &v = s_views[0];
+  Walk w;
+  w.path = s_path + threadIdx.x;
+  w.stride = blockDim.x;
+  Ray r;
+  const uint32_t lane = threadIdx.x & 31u;
+  bool timed_out = false;
+  unsigned long long surfaces = 0;
+  for (;;) {
+    uint32_t base = 0;
+    if (lane == 0) base = atomicAdd(a.ray_counter, 32u);
+    base = __shfl_sync(kFull, base, 0);
+    if (base >= a.total_rays) break;
+    const uint32_t my = base + lane;
+    if (my < a.total_rays && !timed_out) {
+      MegaPixel P;
+      P.n_cones = 0;
+      P._pad = 0;
+      P.node = SVO_MISS;
+      if (!setup_ray(a, s_views, my, r, true)) {
+        P.kind = kMegaPad;
+        P.id = 0;
+        P.depth = 0;
+      } else {
+        reset_walk(w);
+        r.fresh = true;
+        const bool entered = r.depth != 0;
+        int finish;
+        if (!run_cone<kSmemBases>(a, v, s_bases, blocks, B, r, w, finish)) {
+          record_timeout(a, my, r);
+          timed_out = true;
+        }
+        P.id = r.id;
+        P.dir[0] = r.dx;
+        P.dir[1] = r.dy;
+        P.dir[2] = r.dz;
+        P.loc[0] = loc_x(r);
+        P.loc[1] = loc_y(r);
+        P.loc[2] = loc_z(r);
+        uint32_t hit_index = SVO_MISS;
+        uint8_t hit_depth = 0;
+        float t = __int_as_float(0x7f800000);
+        if (!entered) {
+          P.kind = kMegaMiss;
+          P.depth = 1;
+        } else if (finish == kStepHit) {
+          // resolveRayData: the block, RayLength = length(Location - Origin)
+          P.kind = kMegaSurface;
+          P.depth = (uint8_t)r.depth;
+          P.node = w.path[(r.depth - B - 2) * w.stride];
+          hit_index = P.node;
+          hit_depth = (uint8_t)r.depth;
+          const float x = __fsub_rn(ulong_to_unit(P.loc[0]), r.ox);
+          const float y = __fsub_rn(ulong_to_unit(P.loc[1]), r.oy);
+          const float z = __fsub_rn(ulong_to_unit(P.loc[2]), r.oz);
+          t = __fsqrt_rn(dot3(x, y, z, x, y, z));
+          surfaces++;
+        } else {
+          P.kind = kMegaSky;
+          P.depth = 1;
+        }
+        if (v.hit_index) v.hit_index[r.id] = hit_index;
+        if (v.hit_depth) v.hit_depth[r.id] = hit_depth;
+        if (v.t) v.t[r.id] = t;
+      }
+      m.pix[my] = P;
+    }
+    if (__any_sync(kFull, timed_out)) break;
+  }
+  surfaces = __reduce_add_sync(kFull, (unsigned)surfaces);
+  if (lane == 0 && surfaces) atomicAdd(m.totals + 1, surfaces);
+}
+
+// spawnRays for one slot of the band; one warp per tile.
+__global__ void __launch_bounds__(256) mega_fan_kernel(const MegaLaunch m) {
+  const uint32_t gid = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t tile = gid >> 5, lane = gid & 31u;
+  uint32_t count = 0;
+  if (tile < m.band_tiles) {
+    const size_t slot = ((size_t)m.band_tile0 + tile) * 32u + lane;
+    MegaPixel P = m.pix[slot];
+    if (P.kind == kMegaSky || P.kind == kMegaSurface) {
+      float n[3] = {0.0f, 0.0f, 0.0f};
+      if (P.kind == kMegaSurface) {
+        // normalVector (kernel.cl:264-275) of the block's NormalPitch/NormalYaw
+        const uint4 nd = load_node(reinterpret_cast<const uint4 *>(m.t.blocks), m.t.n_blocks, P.node);
+        const int16_t pitch = (int16_t)(nd.y >> 16), yaw = (int16_t)(nd.z & 0xffffu);
+        const float2 sp = __ldg(m.normal_sc + (pitch + 32768)), sy = __ldg(m.normal_sc + (yaw + 32768));
+        n[0] = __fmul_rn(sy.y, sp.y);
+        n[1] = __fmul_rn(sy.x, sp.y);
+        n[2] = sp.x;
+      }
+      const float Dx = P.dir[0], Dy = P.dir[1], Dz = P.dir[2];
+      float axx = __fsub_rn(__fmul_rn(Dy, n[2]), __fmul_rn(Dz, n[1]));
+      float axy = __fsub_rn(__fmul_rn(Dz, n[0]), __fmul_rn(Dx, n[2]));
+      float axz = __fsub_rn(__fmul_rn(Dx, n[1]), __fmul_rn(Dy, n[0]));
+      normalize3(axx, axy, axz);
+      const float d2 = __fmul_rn(2.0f, dot3(Dx, Dy, Dz, n[0], n[1], n[2]));
+      const float rx = __fsub_rn(Dx, __fmul_rn(d2, n[0]));
+      const float ry = __fsub_rn(Dy, __fmul_rn(d2, n[1]));
+      const float rz = __fsub_rn(Dz, __fmul_rn(d2, n[2]));
+      auto emit = [&](float x, float y, float z, float wgt, uint32_t s) {
+        const size_t i = cone_slot(m, tile, count, lane);
+        m.cone_dw[i] = make_float4(x, y, z, __fmul_rn(wgt, 1.0f));  // ringWeighting * baseWeighting
+        m.cone_s[i] = (uint16_t)s;
+        count++;
+      };
+      float fov = m.fov_c, weighting = m.weighting_c, rw = weighting;
+      float dp = dot3(rx, ry, rz, n[0], n[1], n[2]);
+      if (dp < fov) rw = __fdiv_rn(__fmul_rn(weighting, dp), fov);
+      emit(rx, ry, rz, rw, 0);
+      for (int s = 0; s < m.n_spines; s++) {
+        const MegaSpine sp = m.spine[s];
+        fov = sp.fov;
+        weighting = sp.weighting;
+        rw = weighting;
+        float sx, sy, sz;
+        rotate3(axx, axy, axz, sp.c, sp.s, sp.k, rx, ry, rz, false, sx, sy, sz);
+        normalize3(sx, sy, sz);
+        dp = dot3(sx, sy, sz, n[0], n[1], n[2]);
+        if (dp < 0.0f) break;
+        if (dp < fov) rw = __fdiv_rn(__fmul_rn(weighting, dp), fov);
+        emit(sx, sy, sz, rw, s + 1);
+        for (uint32_t j = 0; j < sp.n_rings; j++) {
+          const MegaRing rg = m.ring[sp.ring_begin + j];
+          rw = weighting;
+          float vx, vy, vz;
+          rotate3(rx, ry, rz, rg.c, rg.s, rg.k, sx, sy, sz, false, vx, vy, vz);
+          normalize3(vx, vy, vz);
+          dp = dot3(vx, vy, vz, n[0], n[1], n[2]);
+          if (dp < 0.0f) break;
+          if (dp < fov) rw = __fdiv_rn(__fmul_rn(weighting, dp), fov);
+          emit(vx, vy, vz, rw, s + 1);
+          rotate3(rx, ry, rz, rg.c, rg.s, rg.k, sx, sy, sz, true, vx, vy, vz);
+          normalize3(vx, vy, vz);
+          emit(vx, vy, vz, rw, s + 1);
+        }
+      }
+      // setupTrace (kernel.cl:524-544): Origin from the end location, then one
+      // cell along the normal
+#pragma unroll
+      for (int k = 0; k < 3; k++) P.origin[k] = ulong_to_unit(P.loc[k]);
+      step_normal(P.depth, n, P.loc);
+      P.n_cones = (uint16_t)count;
+      MegaPixel *dst = m.pix + slot;
+      dst->loc[0] = P.loc[0];
+      dst->loc[1] = P.loc[1];
+      dst->loc[2] = P.loc[2];
+      dst->origin[0] = P.origin[0];
+      dst->origin[1] = P.origin[1];
+      dst->origin[2] = P.origin[2];
+      dst->n_cones = P.n_cones;
+    }
+  }
+  const uint32_t kmax = __reduce_max_sync(kFull, count);
+  const uint32_t total = __reduce_add_sync(kFull, count);
+  if (lane == 0 && tile < m.band_tiles) {
+    m.tile_k[tile] = (uint16_t)kmax;
+    if (total) atomicAdd(m.totals, (unsigned long long)total);
+  }
+}
+
+// accumulateRay for every cone: a warp takes cone k of one tile's 32 pixels.
+template <bool kSmemBases>
+__global__ void __launch_bounds__(256, SVO_MEGA_MIN_CTAS) mega_cone_kernel(const MegaLaunch m) {
+  extern __shared__ __align__(16) uint8_t smem[];
+  const TraceLaunch &a = m.t;
+  ViewParams *s_views;
+  uint16_t *s_bases;
+  uint32_t *s_path;
+  stage_shared<kSmemBases>(a, smem, s_views, s_bases, s_path, true);
+  const int B = a.base_depth;
+  const uint4 *blocks = reinterpret_cast<const uint4 *>(a.blocks);
+  const ViewParams &v = s_views[0];
+  Walk w;
+  w.path = s_path + threadIdx.x;
+  w.stride = blockDim.x;
+  Ray r;
+  r.view = 0;
+  r.fresh = false;
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t K = (uint32_t)m.k_max;
+  bool timed_out = false;
+  for (;;) {
+    uint32_t u = 0;
+    if (lane == 0) u = atomicAdd(m.unit_counter, 1u);
+    u = __shfl_sync(kFull, u, 0);
+    if (u >= m.n_units) break;
+    const uint32_t tile = u / K, k = u - tile * K;
+    if (k >= m.tile_k[tile]) continue;  // uniform: no pixel of the tile has cone k
+    const size_t slot = ((size_t)m.band_tile0 + tile) * 32u + lane;
+    const MegaPixel *P = m.pix + slot;
+    if (!timed_out && k < P->n_cones) {
+      const size_t i = cone_slot(m, tile, k, lane);
+      const float4 dw = m.cone_dw[i];
+      const uint32_t s = m.cone_s[i];
+      // setupTrace (kernel.cl:524-544)
+      r.dx = dw.x;
+      r.dy = dw.y;
+      r.dz = dw.z;
+      r.ix = __frcp_rn(r.dx);
+      r.iy = __frcp_rn(r.dy);
+      r.iz = __frcp_rn(r.dz);
+      r.sx = r.dx >= 0.0f;
+      r.sy = r.dy >= 0.0f;
+      r.sz = r.dz >= 0.0f;
+      r.flip = (r.sx ? 0u : 1u) | (r.sy ? 0u : 2u) | (r.sz ? 0u : 4u);
+      set_loc(r, P->loc[0], P->loc[1], P->loc[2]);
+      r.ox = P->origin[0];
+      r.oy = P->origin[1];
+      r.oz = P->origin[2];
+      r.fov = s ? m.spine[s - 1].fov : m.fov_c;
+      r.id = P->id;
+      r.depth = 1;
+      r.steps = 0;
+      reset_walk(w);
+      int finish;
+      if (!run_cone<kSmemBases>(a, v, s_bases, blocks, B, r, w, finish)) {
+        record_timeout(a, u, r);
+        timed_out = true;
+      }
+      m.cone_sky[i] = finish == kStepBackground ? 1 : 0;
+    }
+    if (__any_sync(kFull, timed_out)) break;
+  }
+}
+
+// writeToAccumulator over the pixel's cones in generation order, then draw.
+__global__ void __launch_bounds__(256) mega_resolve_kernel(const MegaLaunch m) {
+  const uint32_t gid = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t tile = gid >> 5, lane = gid & 31u;
+  if (tile >= m.band_tiles) return;
+  const MegaPixel P = m.pix[((size_t)m.band_tile0 + tile) * 32u + lane];
+  if (P.kind == kMegaPad) return;
+  const ViewParams &v = m.t.views[0];
+  if (!v.rgba || P.id >= v.width * v.height) return;
+  uint32_t cr, cg_, cb;
+  if (P.kind == kMegaSurface) {
+    const uint4 nd = load_node(reinterpret_cast<const uint4 *>(m.t.blocks), m.t.n_blocks, P.node);
+    cr = (nd.z >> 16) & 0xffu;
+    cg_ = nd.z >> 24;
+    cb = nd.w & 0xffu;
+  } else {
+    float lum;
+    sky_light(P.dir[0], P.dir[1], P.dir[2], cr, cg_, cb, lum);
+  }
+  float tw = 0.0f, ar = 0.0f, ag = 0.0f, ab = 0.0f;
+  for (uint32_t k = 0; k < P.n_cones; k++) {
+    const size_t i = cone_slot(m, tile, k, lane);
+    const float4 dw = m.cone_dw[i];
+    tw = __fadd_rn(tw, dw.w);
+    if (!m.cone_sky[i]) continue;  // a surface has Luminosity 0
+    uint32_t r, g, b;
+    float lum;
+    sky_light(dw.x, dw.y, dw.z, r, g, b, lum);
+    ar = __fadd_rn(ar, __fmul_rn(__fmul_rn(__fdiv_rn(__uint2float_rn(r), 255.0f), dw.w), lum));
+    ag = __fadd_rn(ag, __fmul_rn(__fmul_rn(__fdiv_rn(__uint2float_rn(g), 255.0f), dw.w), lum));
+    ab = __fadd_rn(ab, __fmul_rn(__fmul_rn(__fdiv_rn(__uint2float_rn(b), 255.0f), dw.w), lum));
+  }
+  float4 px;
+  if (tw > 0.01f) {
+    px.x = fminf(__fdiv_rn(__fadd_rn(__uint2float_rn(cr), __fdiv_rn(ar, tw)), 255.0f), 1.0f);
+    px.y = fminf(__fdiv_rn(__fadd_rn(__uint2float_rn(cg_), __fdiv_rn(ag, tw)), 255.0f), 1.0f);
+    px.z = fminf(__fdiv_rn(__fadd_rn(__uint2float_rn(cb), __fdiv_rn(ab, tw)), 255.0f), 1.0f);
+  } else {
+    px.x = __fdiv_rn(__uint2float_rn(cr), 255.0f);
+    px.y = __fdiv_rn(__uint2float_rn(cg_), 255.0f);
+    px.z = __fdiv_rn(__uint2float_rn(cb), 255.0f);
+  }
+  px.w = 1.0f;
+  reinterpret_cast<float4 *>(v.rgba)[P.id] = px;
+}
+
+bool bases_in_smem(const TraceLaunch &a) { return (size_t)a.n_bases * 2 <= 96 * 1024; }
+
+template <class K>
+cudaError_t launch_traversal(K kernel, const MegaLaunch &m, int grid, cudaStream_t s) {
+  const size_t smem = trace_smem_bytes(m.t, bases_in_smem(m.t));
+  cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  kernel<<<grid, m.t.block_size, smem, s>>>(m);
+  return cudaGetLastError();
+}
+
+}  // namespace
+
+int mega_occupancy(const MegaLaunch &m) {
+  const bool sb = bases_in_smem(m.t);
+  const size_t smem = trace_smem_bytes(m.t, sb);
+  const void *k = sb ? (const void *)mega_cone_kernel<true> : (const void *)mega_cone_kernel<false>;
+  cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  int n = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, m.t.block_size, smem) != cudaSuccess) return 0;
+  return n;
+}
+
+svo_status launch_mega_primary(const MegaLaunch &m, void *stream) {
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  cudaError_t e = bases_in_smem(m.t) ? launch_traversal(mega_primary_kernel<true>, m, m.t.grid, s)
+                                     : launch_traversal(mega_primary_kernel<false>, m, m.t.grid, s);
+  if (e != cudaSuccess) return fail(SVO_ERR_CUDA, std::string("megakernel primary launch: ") + cudaGetErrorString(e));
+  return SVO_OK;
+}
+
+svo_status launch_mega_band(const MegaLaunch &m, void *stream) {
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const uint32_t blocks = (m.band_tiles * 32u + 255u) / 256u;
+  mega_fan_kernel<<<blocks, 256, 0, s>>>(m);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess)
+    e = bases_in_smem(m.t) ? launch_traversal(mega_cone_kernel<true>, m, m.grid_cones, s)
+                           : launch_traversal(mega_cone_kernel<false>, m, m.grid_cones, s);
+  if (e == cudaSuccess) {
+    mega_resolve_kernel<<<blocks, 256, 0, s>>>(m);
+    e = cudaGetLastError();
+  }
+  if (e != cudaSuccess) return fail(SVO_ERR_CUDA, std::string("megakernel band launch: ") + cudaGetErrorString(e));
+  return SVO_OK;
+}
+
+}  // namespace svo

@@ -439,7 +439,7 @@ SVO_API svo_status svo_set_trace_config(void *ctx, const svo_trace_config *cfg) 
   if (n.block_size % 32 || n.block_size < 32 || n.block_size > 256)
     return fail(SVO_ERR_INVALID_ARGUMENT, "svo_set_trace_config: block_size must be a multiple of 32 in 32..256");
   if (n.ray_chunk < 1 || n.ray_chunk > 64 || n.cadence < 1 || n.cadence > 1024 || n.max_steps < 1 || n.ctas_per_sm < 0 ||
-      n.collect_stats < 0 || n.collect_stats > 2 || n.max_hits < 1 || n.max_hits > 1024 ||
+      n.collect_stats < 0 || n.collect_stats > 2 || n.max_hits < 1 || n.max_hits > 1024 || n.mega_band_tiles < 0 ||
       (n.schedule != SVO_SCHEDULE_LANE && n.schedule != SVO_SCHEDULE_WARP))
     return fail(SVO_ERR_INVALID_ARGUMENT, "svo_set_trace_config: value out of range");
   c.cfg = n;

@@ -118,6 +118,7 @@ struct Ray {
   int steps;
   bool sx, sy, sz;
   uint32_t flip;  // bit k: axis k travels towards 0
+  bool fresh;     // megakernel primary: no move yet, so kernel.cl's ConeDepth is still 0
 };
 
 __device__ __forceinline__ uint64_t loc_x(const Ray &r) { return r.wx ^ dir_mask(r.sx); }
@@ -185,10 +186,12 @@ __device__ __forceinline__ float cone_at(const Ray &r, float dof0, float dof1) {
   return eye < f ? f : eye;
 }
 
-// traceIntoVolume (wavefront.cl:639-1088): enter the unit cube on the face of
-// the outside slab with the largest entry distance (ties x, then y); reject
-// when the entry point is outside the cube grown by the cone size.
-__device__ __forceinline__ bool enter_volume(Ray &r) {
+// traceIntoVolume (wavefront.cl:639-1088, kernel.cl:546-995): enter the unit
+// cube on the face of the outside slab with the largest entry distance (ties x,
+// then y); reject when the entry point is outside the cube grown by the cone
+// size. The DoF of the cone size is the TraceData's: zero for the wavefront's
+// fresh TraceData, the input's for kernel.cl's setupInitialTrace.
+__device__ __forceinline__ bool enter_volume(Ray &r, float dof0 = 0.0f, float dof1 = 0.0f) {
   const float o[3] = {r.ox, r.oy, r.oz};
   const float d[3] = {r.dx, r.dy, r.dz};
   const float iv[3] = {r.ix, r.iy, r.iz};
@@ -231,9 +234,8 @@ __device__ __forceinline__ bool enter_volume(Ray &r) {
 #pragma unroll
   for (int k = 0; k < 3; k++) p[k] = (k == axis) ? (hi[k] ? 1.0f : 0.0f) : __fadd_rn(o[k], __fmul_rn(d[k], m));
   set_loc(r, unit_to_ulong(p[0]), unit_to_ulong(p[1]), unit_to_ulong(p[2]));
-  // DoF of a fresh TraceData is zero (setupInitialTrace leaves it unset).
   float eye = __fmul_rn(r.fov, m);
-  float f = fabsf(__fmul_rn(0.0f, __fsub_rn(0.0f, m)));
+  float f = fabsf(__fmul_rn(dof0, __fsub_rn(dof1, m)));
   float c = eye < f ? f : eye;
 #pragma unroll
   for (int k = 0; k < 3; k++)
@@ -271,7 +273,10 @@ enum : int { kStepOn = 0, kStepBackground = 1, kStepHit = 2, kStepEmpty = 3 };
 // cone LOD decision. An empty octant returns kStepEmpty: the step ends with
 // advance() (the traverseChunk / comparePositions part), which callers can run
 // for the lanes of a warp together.
-template <bool kStats, bool kSmemBases>
+// kMega: kernel.cl's traceBase/traceBlock (kernel.cl:1002-1073), which differ
+// in two points: ConeDepth keeps its initial 0 until the first move (r.fresh),
+// and a request carries the frame's Tick and TreeSize 1.
+template <bool kStats, bool kSmemBases, bool kMega = false>
 __device__ __forceinline__ int probe(const TraceLaunch &a, const ViewParams &v, const uint16_t *s_bases,
                                     const uint4 *blocks, int B, Ray &r, Walk &w, Stats &st) {
   if (r.depth == 0) return kStepBackground;
@@ -320,8 +325,9 @@ __device__ __forceinline__ int probe(const TraceLaunch &a, const ViewParams &v, 
     }
     return kStepOn;
   }
-  // geometry below a node: the cone LOD decision (ConeDepth = -half_log2(c))
-  float c = cone_at(r, v.dof[0], v.dof[1]);
+  // geometry below a node: the cone LOD decision (ConeDepth = -half_log2(c));
+  // ConeDepth 0 compares like c = 1
+  float c = (kMega && r.fresh) ? 1.0f : cone_at(r, v.dof[0], v.dof[1]);
   if (c > pow2_neg(B + 2)) {
     r.depth = B + 2;
     return kStepHit;
@@ -339,13 +345,13 @@ __device__ __forceinline__ int probe(const TraceLaunch &a, const ViewParams &v, 
     if (slot < a.request_cap && a.requests) {
       svo_child_request q;
       q.address = w.cur_addr;
-      q.tick = 0;  // TraceData.Tick is never set by resolveTrace
+      q.tick = kMega ? v.tick : 0;  // TraceData.Tick is never set by the wavefront's resolveTrace
       q.depth = (uint8_t)r.depth;
       q._pad0 = 0;
       q.location[0] = loc_x(r);
       q.location[1] = loc_y(r);
       q.location[2] = loc_z(r);
-      q.tree_size = c <= pow2_neg(r.depth + 1) ? 1 : 0;
+      q.tree_size = kMega ? 1 : (c <= pow2_neg(r.depth + 1) ? 1 : 0);
       for (int k = 0; k < 7; k++) q._pad1[k] = 0;
       a.requests[slot] = q;
     }
@@ -390,8 +396,10 @@ __device__ __forceinline__ bool ray_slot(const TraceLaunch &a, const ViewParams 
 
 // setupInitialTrace (wavefront.cl:563-595) for ray slot `my` of the batch,
 // then traceIntoVolume; a ray that misses the cube gets depth 0 (background).
-// Returns false (and sets nothing else) for a padding slot.
-__device__ __forceinline__ bool setup_ray(const TraceLaunch &a, const ViewParams *s_views, uint32_t my, Ray &r) {
+// Returns false (and sets nothing else) for a padding slot. kernel.cl's
+// setupInitialTrace (kernel.cl:491-522) also takes the view's DoF (use_dof).
+__device__ __forceinline__ bool setup_ray(const TraceLaunch &a, const ViewParams *s_views, uint32_t my, Ray &r,
+                                          bool use_dof = false) {
   int view;
   uint32_t px, py;
   if (!ray_slot(a, s_views, my, view, px, py)) return false;
@@ -421,7 +429,7 @@ __device__ __forceinline__ bool setup_ray(const TraceLaunch &a, const ViewParams
   r.fov = v.fov_px;
   r.depth = 1;
   r.steps = 0;
-  if (!enter_volume(r)) r.depth = 0;
+  if (!(use_dof ? enter_volume(r, v.dof[0], v.dof[1]) : enter_volume(r))) r.depth = 0;
   return true;
 }
 

@@ -84,7 +84,7 @@ class TraceStatsC(C.Structure):
 
 class TraceConfigC(C.Structure):
     _fields_ = [(n, C.c_int32) for n in ("block_size", "ctas_per_sm", "ray_chunk", "cadence", "max_steps",
-                                          "collect_stats", "max_hits", "schedule")]
+                                          "collect_stats", "max_hits", "schedule", "mega_band_tiles", "_pad")]
 
 
 class SceneParamsC(C.Structure):
@@ -104,6 +104,10 @@ class GcReportC(C.Structure):
 
 class GraftReportC(C.Structure):
     _fields_ = [("applied", C.c_uint32), ("skipped", C.c_uint32), ("claimed", C.c_uint64), ("free_left", C.c_uint64)]
+
+
+class MegaStatsC(C.Structure):
+    _fields_ = [("pixels", C.c_uint64), ("surfaces", C.c_uint64), ("cones", C.c_uint64), ("cone_slots", C.c_uint64)]
 
 
 class PruneReportC(C.Structure):
@@ -145,6 +149,8 @@ def load_library(path: str | None = None) -> C.CDLL:
         "svo_trace_batch": ([vp, C.POINTER(TraceInputC), C.c_int32, C.POINTER(TraceOutputC)], C.c_int32),
         "svo_trace_batch_graph": ([vp, C.POINTER(TraceInputC), C.c_int32, C.POINTER(TraceOutputC)], C.c_int32),
         "svo_last_trace_stats": ([vp, C.POINTER(TraceStatsC)], C.c_int32),
+        "svo_mega_trace": ([vp, C.POINTER(TraceInputC), C.POINTER(TraceOutputC)], C.c_int32),
+        "svo_last_mega_stats": ([vp, C.POINTER(MegaStatsC)], C.c_int32),
         "svo_autotune": ([vp, C.POINTER(TraceInputC), C.c_int32, C.POINTER(TraceOutputC), C.c_int32,
                           C.POINTER(TraceConfigC), C.POINTER(C.c_float)], C.c_int32),
         "svo_read_ray_counts": ([vp, vp, vp, sz], C.c_int32),
@@ -645,6 +651,26 @@ class Tracer:
         self._req_cap = inp.MaxChildRequestId
         _check("RunWavefront", self._lib.svo_trace(self._ctx, C.byref(c_in), C.byref(c_out)))
         return r
+
+    def mega_trace(self, inp: TraceInput, out: TraceResult | None = None) -> TraceResult:
+        """kernel.cl's `trace` (the megakernel): the primary cone, spawnRays's cone
+        fan and draw's colour. hit_index/hit_depth/t describe the primary cone."""
+        r = out if out is not None else self._alloc(*inp.ScreenSize)
+        c_in, c_out = inp.to_c(), self._out(r)
+        self._req_cap = inp.MaxChildRequestId
+        _check("RunMegakernel", self._lib.svo_mega_trace(self._ctx, C.byref(c_in), C.byref(c_out)))
+        return r
+
+    def mega_trace_device(self, inp: TraceInput, hit_index=0, hit_depth=0, t=0, rgba=0) -> None:
+        """The megakernel into caller-owned device buffers (addresses, 0 = skip)."""
+        c_out = TraceOutputC(hit_index or None, hit_depth or None, t or None, rgba or None, 1, 0)
+        self._req_cap = inp.MaxChildRequestId
+        _check("RunMegakernelDevice", self._lib.svo_mega_trace(self._ctx, C.byref(inp.to_c()), C.byref(c_out)))
+
+    def mega_stats(self) -> dict:
+        s = MegaStatsC()
+        _check("MegaStats", self._lib.svo_last_mega_stats(self._ctx, C.byref(s)))
+        return {n: getattr(s, n) for n, _ in MegaStatsC._fields_}
 
     def trace_batch(self, inputs, graph: bool = False):
         res = [self._alloc(*i.ScreenSize) for i in inputs]

@@ -1,0 +1,130 @@
+"""svo_mega_trace (kernel.cl's `trace`: primary cone, spawnRays's cone fan, draw)
+against the megakernel oracle: bit-exact image, primary hit outputs, child
+requests and usage ticks."""
+import dataclasses
+
+import numpy as np
+import pytest
+
+import pyoracle as po
+import svo_tracer as st
+
+pytestmark = pytest.mark.gpu
+
+
+def with_random_normals(tree, seed):
+    rng = np.random.default_rng(seed)
+    blocks = tree.Blocks.copy()
+    blocks["normal_pitch"] = rng.integers(-32768, 32768, len(blocks), dtype=np.int16)
+    blocks["normal_yaw"] = rng.integers(-32768, 32768, len(blocks), dtype=np.int16)
+    return dataclasses.replace(tree, Blocks=blocks)
+
+
+@pytest.fixture(scope="module")
+def sphere():
+    return st.TreeBuilder(st.SCENE_SPHERE, seed=1).BuildTree(3, 8)
+
+
+@pytest.fixture(scope="module")
+def terrain():
+    return with_random_normals(st.TreeBuilder(st.SCENE_TERRAIN, seed=2).BuildTree(3, 8), 21)
+
+
+@pytest.fixture(scope="module")
+def tracer():
+    t = st.Tracer(0)
+    yield t
+    t.close()
+
+
+def run_both(tracer, tree, view, **cfg):
+    tracer.upload(tree)
+    tracer.init_usage()
+    if cfg:
+        tracer.set_config(**cfg)
+    try:
+        got = tracer.mega_trace(view)
+        stats = tracer.mega_stats()
+        gpu_req, n_req = tracer.read_child_requests()
+        gpu_usage = tracer.read_usage()
+    finally:
+        if cfg:
+            tracer.set_config(**{k: 0 for k in cfg})
+    usage = po.init_usage(tree)
+    ref = po.mega_trace_view(tree, view, usage=usage)
+    assert n_req == len(gpu_req)
+    return got, stats, gpu_req, gpu_usage, ref, usage
+
+
+def check(tracer, tree, view, **cfg):
+    view = dataclasses.replace(view, MaxChildRequestId=1 << 20)
+    got, stats, gpu_req, gpu_usage, ref, usage = run_both(tracer, tree, view, **cfg)
+    n = view.ScreenSize[0] * view.ScreenSize[1]
+    assert np.array_equal(got.rgba.reshape(n, 4).view(np.uint32), ref["rgba"].view(np.uint32))
+    assert np.array_equal(got.hit_index.reshape(-1), ref["hit_index"])
+    assert np.array_equal(got.hit_depth.reshape(-1), ref["hit_depth"])
+    assert np.array_equal(got.t.reshape(-1).view(np.uint32), ref["t"].view(np.uint32))
+    assert len(gpu_req) == ref["n_requests"]
+    a, b = po.sort_requests(gpu_req), po.sort_requests(ref["requests"])
+    for f in ("address", "tick", "depth", "location", "tree_size"):
+        assert np.array_equal(a[f], b[f]), f
+    assert np.array_equal(gpu_usage["tick"][: len(usage)], usage["tick"])
+    assert stats["pixels"] == n
+    assert stats["cones"] == int(ref["cones"].sum())
+    assert stats["surfaces"] == int((ref["hit_index"] != st.MISS).sum())
+    return got, stats, ref
+
+
+@pytest.mark.parametrize("k", range(3))
+def test_sphere_orbit_views(tracer, sphere, k):
+    v = st.orbit_views(seed=5, n=3, width=64, height=48)[k]
+    check(tracer, sphere, v)
+
+
+@pytest.mark.parametrize("k", range(3))
+def test_terrain_random_normals(tracer, terrain, k):
+    v = st.orbit_views(seed=7, n=3, width=67, height=45, distance=1.2)[k]  # ragged tiles
+    got, stats, ref = check(tracer, terrain, v)
+    assert ref["n_requests"] > 0 and stats["cones"] > 0
+
+
+def test_inside_cube_with_dof(tracer, sphere):
+    v = st.look_at((0.5, 0.5, 0.12), (0.5, 0.55, 0.6), 48, 40, 70.0, DoF=(0.02, 0.3), Tick=9)
+    check(tracer, with_random_normals(sphere, 3), v)
+
+
+def test_other_cone_schedule_and_bands(tracer, terrain):
+    v = st.look_at((0.2, 0.1, 0.05), (0.5, 0.5, 0.8), 40, 32, 75.0, FovMultiplier=0.1, FovConstant=0.08,
+                   WeightingMultiplier=0.1, WeightingConstant=0.3, Tick=3)
+    # 3 tiles per band: the fan, cone and resolve kernels run band after band
+    got, stats, ref = check(tracer, terrain, v, mega_band_tiles=3)
+    assert ref["cones"].max() > 40
+
+
+def test_request_cap(tracer, terrain):
+    v = dataclasses.replace(st.orbit_views(seed=7, n=1, width=64, height=48, distance=1.2)[0], MaxChildRequestId=50)
+    tracer.upload(terrain)
+    tracer.init_usage()
+    tracer.mega_trace(v)
+    req, n = tracer.read_child_requests()
+    ref = po.mega_trace_view(terrain, v)
+    assert ref["n_requests"] > 50 and len(req) == 50 and n == ref["n_requests"]
+    assert tracer.stats()["child_requests"] == ref["n_requests"]
+
+
+def test_unusable_schedule_draws_nothing(tracer, sphere):
+    v = st.orbit_views(seed=5, n=1, width=16, height=12)[0]
+    tracer.upload(sphere)
+    for kw in ({"FovConstant": 0.0}, {"FovMultiplier": 1.0}, {"FovMultiplier": -1.0}):
+        r = st.TraceResult(np.full((12, 16), 7, np.uint32), np.full((12, 16), 7, np.uint8),
+                           np.full((12, 16), 7.0, np.float32), np.full((12, 16, 4), 7.0, np.float32))
+        tracer.mega_trace(dataclasses.replace(v, **kw), out=r)
+        assert (r.hit_index == 7).all() and (r.rgba == 7.0).all()
+        assert tracer.mega_stats()["pixels"] == 0
+
+
+def test_endless_schedule_is_refused(tracer, sphere):
+    v = dataclasses.replace(st.orbit_views(seed=5, n=1, width=8, height=8)[0], FovMultiplier=-0.9, FovConstant=0.01)
+    tracer.upload(sphere)
+    with pytest.raises(st.SvoError):
+        tracer.mega_trace(v)
