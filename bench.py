@@ -237,6 +237,87 @@ def multiview(tr, torch, dev, stream, flush, args, windows=None):
             "plain": "64 sequential single-view launches, same stream, default configuration"}
 
 
+def mega_workload(tr, torch, dev, stream, flush, args, tree, cam, windows=None):
+    """The megakernel (kernel.cl's `trace`: primary cone, spawnRays's fan of
+    secondary cones, draw) on the same 1080p terrain frame, with the reference's
+    default cone parameters (FovMultiplier 0.2, FovConstant 0.2, WeightingMultiplier
+    -0.05, WeightingConstant 0.5). Rays = primary + secondary cones."""
+    import svo_tracer as st
+
+    n = WIDTH * HEIGHT
+    o = [torch.empty(n, dtype=torch.int32, device=dev), torch.empty(n, dtype=torch.uint8, device=dev),
+         torch.empty(n, dtype=torch.float32, device=dev), torch.empty(4 * n, dtype=torch.float32, device=dev)]
+    ptrs = [x.data_ptr() for x in o]
+    steps = max(3, args.steps // 4)
+    with torch.cuda.stream(stream):
+        for _ in range(2):
+            flush.zero_()
+            tr.mega_trace_device(cam, *ptrs)
+        stats = tr.mega_stats()
+        ev = []
+        torch.cuda.synchronize(dev)
+        t_win = time.perf_counter()
+        for _ in range(steps):
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            tr.mega_trace_device(cam, *ptrs)
+            e1.record(stream)
+            ev.append((e0, e1))
+        torch.cuda.synchronize(dev)
+        if windows is not None:
+            windows.append((t_win, time.perf_counter()))
+    ms = sorted(a.elapsed_time(b) for a, b in ev)
+    frame_ms = sum(ms) / len(ms)
+    rays = stats["pixels"] + stats["cones"]
+    # end to end through the public API with pinned host outputs
+    h = st.TraceResult(torch.empty(n, dtype=torch.int32, pin_memory=True).numpy().view(np.uint32),
+                       torch.empty(n, dtype=torch.uint8, pin_memory=True).numpy(),
+                       torch.empty(n, dtype=torch.float32, pin_memory=True).numpy(),
+                       torch.empty(n * 4, dtype=torch.float32, pin_memory=True).numpy().reshape(n, 4))
+    tr.mega_trace(cam, out=h)
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        tr.mega_trace(cam, out=h)
+    e2e_s = (time.perf_counter() - t0) / steps
+    if windows is not None:
+        windows.append((t0, time.perf_counter()))
+    return {"frame_ms": frame_ms, "frame_ms_min": ms[0], "frames_per_s": 1000.0 / frame_ms,
+            "mrays_s": rays / frame_ms / 1e3, "primary_rays": stats["pixels"], "cones": stats["cones"],
+            "cones_per_pixel": stats["cones"] / max(1, stats["pixels"]), "surfaces": stats["surfaces"],
+            "cone_slots": stats["cone_slots"], "steps": steps,
+            "e2e": {"frame_ms": 1000.0 * e2e_s, "mrays_s": rays / e2e_s / 1e6,
+                    "d2h_bytes_per_step": n * OUT_BYTES},
+            "workload": "kernel.cl trace over the 1080p terrain frame, reference default cone parameters"}
+
+
+def mega_cpu_sample(tree, cam, budget_s=8.0):
+    """The reference's megakernel (kernel.cl built for the host CPU) over row bands
+    of the same frame until ~budget_s; rays = primary + secondary cones, the cone
+    count taken from the oracle over the same rows."""
+    import pyoracle as po
+
+    if not po.ref_mega_available():
+        return None
+    threads = os.cpu_count() or 1
+    rows, band, px, t_ref = 4, 0, 0, 0.0
+    cones = 0
+    while t_ref < budget_s and band * rows < HEIGHT:
+        r0 = (HEIGHT // 2 + band * rows) % HEIGHT
+        r1 = min(HEIGHT, r0 + rows)
+        t0 = time.perf_counter()
+        po.ref_mega_trace_view(tree, cam, threads=threads, rows=(r0, r1), req_cap=1 << 16)
+        t_ref += time.perf_counter() - t0
+        cones += int(po.mega_trace_view(tree, cam, threads=threads, rows=(r0, r1), req_cap=1)["cones"].sum())
+        px += (r1 - r0) * WIDTH
+        band += 1
+    return {"value": (px + cones) / t_ref / 1e6, "unit": "Mrays/s", "cores": threads, "kind": "reference",
+            "frames_per_s": px / (WIDTH * HEIGHT) / t_ref,
+            "sample": "%d pixels (%d cones) in %d bands of %d rows through the frame's middle, %.1f s" %
+                      (px, cones, band, rows, t_ref)}
+
+
 def _stream_run(st, scene, tree, cams, dev, device_generate):
     """One pass of the stream: per frame trace (usage stamps, child requests),
     graft payloads (on the device, or generated on the host and uploaded), GC of
@@ -529,6 +610,8 @@ def run_ours(args, rank, world):
         line["multiview"] = multiview(tr, torch, dev, stream, flush, args, windows)
     if not args.no_diff:
         line["diff"] = diff_workload(torch, dev, flush, args, windows)
+    if not args.no_mega:
+        line["megakernel"] = mega_workload(tr, torch, dev, stream, flush, args, tree, cam, windows)
     clk.__exit__(None, None, None)
     line["clocks"] = clk.summary(windows)
     if args.stream_frames > 0:
@@ -538,6 +621,8 @@ def run_ours(args, rank, world):
 
         kind = "reference" if po.ref_available() else "port"
         line["cpu_baseline"] = cpu_sample(tree, cam, kind)
+        if "megakernel" in line:
+            line["megakernel"]["cpu_baseline"] = mega_cpu_sample(tree, cam)
     print(json.dumps(line))
     tr.close()
     if dist:
@@ -554,6 +639,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-multiview", action="store_true")
     ap.add_argument("--no-diff", action="store_true")
+    ap.add_argument("--no-mega", action="store_true")
     ap.add_argument("--schedule", choices=["lane", "warp"], default=None)
     ap.add_argument("--diff-views", type=int, default=16)
     ap.add_argument("--diff-size", type=int, default=512)

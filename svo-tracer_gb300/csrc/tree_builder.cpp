@@ -73,6 +73,8 @@ struct Scene {
   virtual ~Scene() = default;
   virtual void classify(int level, uint32_t cx, uint32_t cy, uint32_t cz, bool &geo, bool &air) const = 0;
   virtual void colour(int level, uint32_t cx, uint32_t cy, uint32_t cz, uint8_t rgb[3]) const = 0;
+  // GetNormal (TreeBuilder.cs:46-55): the encoded surface normal of a cell
+  virtual void normal(int level, uint32_t cx, uint32_t cy, uint32_t cz, int16_t &pitch, int16_t &yaw) const = 0;
 };
 
 // Sphere of radius 0.2 (0.4 of the [-1,1] world) at the cube centre, displaced
@@ -136,6 +138,11 @@ struct SphereScene final : Scene {
     }
     for (int k = 0; k < 8 && !(geo && air); k++)
       classify_rec(level + 1, 2 * x + (k & 1), 2 * y + ((k >> 1) & 1), 2 * z + ((k >> 2) & 1), geo, air);
+  }
+  // radial, like SphereDefinition.Normal
+  void normal(int level, uint32_t x, uint32_t y, uint32_t z, int16_t &pitch, int16_t &yaw) const override {
+    const double s = std::ldexp(1.0, -level);
+    scene::normal_angles((x + 0.5) * s - cx, (y + 0.5) * s - cy, (z + 0.5) * s - cz, pitch, yaw);
   }
   void colour(int level, uint32_t x, uint32_t y, uint32_t z, uint8_t rgb[3]) const override {
     uint32_t h = hash4(seed ^ 0x51ed270bU, (uint32_t)level, x, y, z);
@@ -226,6 +233,9 @@ struct TerrainScene final : Scene {
   void colour(int level, uint32_t x, uint32_t y, uint32_t z, uint8_t rgb[3]) const override {
     scene::terrain_colour(seed, level, x, y, z, rgb);
   }
+  void normal(int level, uint32_t x, uint32_t y, uint32_t, int16_t &pitch, int16_t &yaw) const override {
+    scene::terrain_normal(hi[level].data(), level, leaf, x, y, pitch, yaw);
+  }
 };
 
 using scene::can_have_children;
@@ -248,6 +258,7 @@ svo_block make_block(const Scene &sc, int level, uint32_t x, uint32_t y, uint32_
   b.child = SVO_NO_CHILD;
   b.chunk = make_chunk(sc, level, x, y, z);
   b.opacity = 255;
+  sc.normal(level, x, y, z, b.normal_pitch, b.normal_yaw);
   uint8_t rgb[3];
   sc.colour(level, x, y, z, rgb);
   b.colour_r = rgb[0];

@@ -504,8 +504,7 @@ __device__ __forceinline__ svo_block terrain_block(const DevTerrain &T, int leve
   svo_block b;
   b.child = kNone;
   b.chunk = terrain_chunk(T, level, x, y, z);
-  b.normal_pitch = 0;
-  b.normal_yaw = 0;
+  scene::terrain_normal(T.hi + T.off[level], level, T.leaf, x, y, b.normal_pitch, b.normal_yaw);
   uint8_t rgb[3];
   scene::terrain_colour(T.seed, level, x, y, z, rgb);
   b.colour_r = rgb[0];
