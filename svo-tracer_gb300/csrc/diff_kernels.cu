@@ -50,6 +50,7 @@
 #include <vector>
 
 #include "context.h"
+#define SVO_CVT_INTEGER 1  // integer ulong_to_float: faster in this kernel mix
 #include "trace_core.cuh"
 
 // Resident CTAs of 256 threads per SM the kernels are compiled for (4 and 4

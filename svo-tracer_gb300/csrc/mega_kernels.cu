@@ -29,6 +29,7 @@
 #include <cstdint>
 
 #include "mega_internal.h"
+#define SVO_CVT_INTEGER 1  // integer ulong_to_float: faster in this kernel mix
 #include "trace_core.cuh"
 
 namespace svo {

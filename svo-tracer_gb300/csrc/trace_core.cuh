@@ -26,11 +26,35 @@ __device__ __forceinline__ uint32_t pow_sum(int depth) {
   return (uint32_t)((0b1001001001001001001001001001001000ull >> ((11 - depth) * 3)) - 1);
 }
 
-// (float)x of a 64-bit fixed-point value (ulongToFloat, wavefront.cl:209,
-// without the 2^-64 scaling).
-__device__ __forceinline__ float ulong_to_float(uint64_t x) { return __ull2float_rn(x); }
+// The fixed-point conversions exist in two exact forms: the 64-bit conversion
+// instructions, which run on this GPU's FP64 pipe at 1/64 of the FP32 rate, and
+// an integer form around the 32-bit conversion (more instructions, no FP64
+// pipe). Which is faster depends on the kernel's instruction mix: a
+// translation unit defines SVO_CVT_INTEGER to 1 before including this header
+// to take the integer form of ulong_to_float (the colour-fitting backward:
+// 1.15 -> 1.04 ms; the megakernel's cones: 19.03 -> 18.91 ms per frame; the
+// primary trace: 1.80 -> 1.83 ms, so it keeps the instruction). unit_to_ulong
+// keeps the instruction everywhere.
+#ifndef SVO_CVT_INTEGER
+#define SVO_CVT_INTEGER 0
+#endif
+
+// (float)x of a 64-bit fixed-point value, rounded to nearest even
+// (ulongToFloat, wavefront.cl:209, without the 2^-64 scaling). Integer form:
+// the top 32 significant bits of x with every lower bit folded into a sticky
+// LSB (which leaves the rounding decision unchanged), the 32-bit conversion,
+// and the scale 2^(32 - n) added to the exponent field; x = 0 gives 0.
+__device__ __forceinline__ float ulong_to_float(uint64_t x) {
+  if (!SVO_CVT_INTEGER) return __ull2float_rn(x);
+  const uint32_t hi = (uint32_t)(x >> 32), lo = (uint32_t)x;
+  const uint32_t n = __clz(hi);                       // 32 when hi == 0
+  const uint32_t top = __funnelshift_lc(lo, hi, n);   // bits 63..32 of x << n
+  const uint32_t rest = __funnelshift_lc(0u, lo, n);  // bits 31..0 of x << n
+  const float f = __uint2float_rn(top | (rest != 0u ? 1u : 0u));
+  return __int_as_float(__float_as_int(f) + (int)((32u - n) << 23));
+}
 // ulongToFloat (wavefront.cl:209): (float)x * 2^-64, the scaling exact.
-__device__ __forceinline__ float ulong_to_unit(uint64_t x) { return __fmul_rn(__ull2float_rn(x), 0x1p-64f); }
+__device__ __forceinline__ float ulong_to_unit(uint64_t x) { return __fmul_rn(ulong_to_float(x), 0x1p-64f); }
 
 // floatToUlong (wavefront.cl:200-207); out-of-range products saturate, NaN -> 0.
 __device__ __forceinline__ uint64_t unit_to_ulong(float x) {
