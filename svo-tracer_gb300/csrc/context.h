@@ -131,7 +131,8 @@ struct Context {
   // of FovMultiplier, FovConstant, WeightingMultiplier, WeightingConstant)
   DevBuf<MegaPixel> mega_pix;
   DevBuf<float4> mega_cone_dw;
-  DevBuf<uint16_t> mega_cone_s, mega_tile_k;
+  DevBuf<uint16_t> mega_cone_s;
+  DevBuf<uint32_t> mega_tile_cones, mega_entries, mega_queue;
   DevBuf<uint8_t> mega_cone_sky;
   DevBuf<float2> mega_normal_sc;
   DevBuf<MegaSpine> mega_spine;
@@ -203,7 +204,9 @@ struct Context {
     mega_pix.release();
     mega_cone_dw.release();
     mega_cone_s.release();
-    mega_tile_k.release();
+    mega_tile_cones.release();
+    mega_entries.release();
+    mega_queue.release();
     mega_cone_sky.release();
     mega_normal_sc.release();
     mega_spine.release();

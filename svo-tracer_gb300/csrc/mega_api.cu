@@ -166,7 +166,8 @@ svo_status run_mega(Context &c, const svo_trace_input *in, const svo_trace_outpu
   const size_t band_slots = (size_t)band_tiles * K * 32;
   if (c.views.reserve(1) || c.tables.reserve(table_floats) || c.mega_pix.reserve(total_rays) ||
       c.mega_cone_dw.reserve(band_slots) || c.mega_cone_s.reserve(band_slots) || c.mega_cone_sky.reserve(band_slots) ||
-      c.mega_tile_k.reserve(band_tiles) || c.mega_totals.reserve(2) || c.h_mega_totals.reserve(2))
+      c.mega_tile_cones.reserve(band_tiles) || c.mega_entries.reserve(band_slots) || c.mega_queue.reserve(2) ||
+      c.mega_totals.reserve(2) || c.h_mega_totals.reserve(2))
     return fail(SVO_ERR_OUT_OF_MEMORY, "svo_mega_trace: allocation failed");
 
   MegaLaunch m{};
@@ -176,11 +177,14 @@ svo_status run_mega(Context &c, const svo_trace_input *in, const svo_trace_outpu
   m.cone_dw = c.mega_cone_dw.p;
   m.cone_s = c.mega_cone_s.p;
   m.cone_sky = c.mega_cone_sky.p;
-  m.tile_k = c.mega_tile_k.p;
+  m.tile_cones = c.mega_tile_cones.p;
+  m.entries = c.mega_entries.p;
+  m.queue = c.mega_queue.p;
+  m.max_entries = (uint32_t)band_slots;
+  m.cone_schedule = c.cfg.schedule;
   m.normal_sc = c.mega_normal_sc.p;
   m.spine = c.mega_spine.p;
   m.ring = c.mega_ring.p;
-  m.unit_counter = c.counters.p + 2;
   m.totals = c.mega_totals.p;
   m.n_spines = c.mega_n_spines;
   m.k_max = K;
@@ -203,10 +207,9 @@ svo_status run_mega(Context &c, const svo_trace_input *in, const svo_trace_outpu
   for (uint32_t t0 = 0; t0 < n_tiles; t0 += band_tiles) {
     m.band_tile0 = t0;
     m.band_tiles = std::min(band_tiles, n_tiles - t0);
-    m.n_units = m.band_tiles * (uint32_t)K;
-    m.grid_cones = (int)std::max(1L, std::min(persistent, ((long)m.n_units * 32 + m.t.block_size - 1) / m.t.block_size));
-    slots += (uint64_t)m.n_units * 32;
-    SVO_CUDA(cudaMemsetAsync(m.unit_counter, 0, sizeof(uint32_t), c.stream), fn);
+    const uint64_t band_cone_slots = (uint64_t)m.band_tiles * (uint32_t)K * 32;
+    m.grid_cones = (int)std::max(1L, std::min(persistent, (long)((band_cone_slots + m.t.block_size - 1) / m.t.block_size)));
+    slots += band_cone_slots;
     st = launch_mega_band(m, c.stream);
     if (st) return st;
   }

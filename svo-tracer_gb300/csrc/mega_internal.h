@@ -40,17 +40,20 @@ struct MegaLaunch {
   float4 *cone_dw;          // per cone slot of the band: direction, weighting
   uint16_t *cone_s;         // per cone slot: spine step + 1 (0: the reflection cone)
   uint8_t *cone_sky;        // per cone slot: 1 when the cone reached the sky
-  uint16_t *tile_k;         // per tile of the band: cones of its fullest pixel
+  uint32_t *tile_cones;     // per tile of the band: its cones, then (scanned) its first entry
+  uint32_t *entries;        // the band's cones compacted: cone slots by tile, cone k, lane
+  uint32_t *queue;          // [0] entry queue head of the cone kernel, [1] entries of the band
   const float2 *normal_sc;  // normalVector's (sin, cos) of each int16 angle, index angle + 32768
   const MegaSpine *spine;
   const MegaRing *ring;
-  uint32_t *unit_counter;       // cone kernel's (tile, k) queue head
   unsigned long long *totals;   // [0] cones of the fans, [1] primary surfaces
   int32_t n_spines;
   int32_t k_max;                // cones per pixel at most: the cone slot stride
   float fov_c, weighting_c;     // FovConstant, WeightingConstant: the reflection cone's
-  uint32_t band_tile0, band_tiles, n_units;  // tiles [band_tile0, +band_tiles), units band_tiles * k_max
+  uint32_t band_tile0, band_tiles;  // tiles [band_tile0, band_tile0 + band_tiles)
+  uint32_t max_entries;         // cone slots of a band (bounds the entry count)
   int32_t grid_cones;           // persistent grid of the cone kernel
+  int32_t cone_schedule;        // SVO_SCHEDULE_WARP: 32 entries per warp claim; LANE: lanes refill
 };
 
 svo_status launch_mega_primary(const MegaLaunch &m, void *stream);

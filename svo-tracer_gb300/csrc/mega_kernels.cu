@@ -14,8 +14,10 @@
 //     weightings in generation order, stored [tile][cone k][lane], and the
 //     cones' common start (traverseChunkNormal, the same for every cone of a
 //     pixel).
-//  3. mega_cone_kernel: every cone traced to a surface or the sky; a warp
-//     claims one (tile, k) unit, cone k of the tile's 32 pixels.
+//  3. mega_scan_kernel / mega_emit_kernel: the band's cones compacted into one
+//     list, tile by tile, cone k of the tile's pixels before cone k + 1; then
+//     mega_cone_kernel: every cone traced to a surface or the sky, a warp
+//     taking 32 consecutive entries of the list.
 //  4. mega_resolve_kernel: writeToAccumulator in generation order, then draw.
 // The cone slots of a frame are processed in bands of tiles so that their
 // memory stays bounded for any cone schedule.
@@ -354,16 +356,90 @@ __global__ void __launch_bounds__(256) mega_fan_kernel(const MegaLaunch m) {
       dst->n_cones = P.n_cones;
     }
   }
-  const uint32_t kmax = __reduce_max_sync(kFull, count);
   const uint32_t total = __reduce_add_sync(kFull, count);
   if (lane == 0 && tile < m.band_tiles) {
-    m.tile_k[tile] = (uint16_t)kmax;
+    m.tile_cones[tile] = total;
     if (total) atomicAdd(m.totals, (unsigned long long)total);
   }
 }
 
-// accumulateRay for every cone: a warp takes cone k of one tile's 32 pixels.
-template <bool kSmemBases>
+// Exclusive scan of the band's per-tile cone counts (one CTA), total to queue[1].
+__global__ void __launch_bounds__(1024) mega_scan_kernel(const MegaLaunch m) {
+  __shared__ uint32_t part[1024];
+  const uint32_t n = m.band_tiles;
+  const uint32_t per = (n + 1023u) / 1024u, b = threadIdx.x * per, e = min(n, b + per);
+  uint32_t s = 0;
+  for (uint32_t i = b; i < e; i++) s += m.tile_cones[i];
+  part[threadIdx.x] = s;
+  __syncthreads();
+  for (uint32_t off = 1; off < 1024u; off <<= 1) {
+    const uint32_t v = threadIdx.x >= off ? part[threadIdx.x - off] : 0u;
+    __syncthreads();
+    part[threadIdx.x] += v;
+    __syncthreads();
+  }
+  uint32_t run = part[threadIdx.x] - s;
+  for (uint32_t i = b; i < e; i++) {
+    const uint32_t c = m.tile_cones[i];
+    m.tile_cones[i] = run;
+    run += c;
+  }
+  if (threadIdx.x == 1023) {
+    m.queue[0] = 0;
+    m.queue[1] = min(part[1023], m.max_entries);
+  }
+}
+
+// The compacted cone list: per tile (one warp), cone k of every pixel that has
+// one, k = 0, 1, ... (neighbouring entries start close together and point alike).
+__global__ void __launch_bounds__(256) mega_emit_kernel(const MegaLaunch m) {
+  const uint32_t gid = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t tile = gid >> 5, lane = gid & 31u;
+  if (tile >= m.band_tiles) return;  // whole warps
+  const uint32_t count = m.pix[((size_t)m.band_tile0 + tile) * 32u + lane].n_cones;
+  const uint32_t kmax = __reduce_max_sync(kFull, count);
+  uint32_t base = m.tile_cones[tile];
+  const uint32_t below = (1u << lane) - 1u;
+  for (uint32_t k = 0; k < kmax; k++) {
+    const uint32_t b = __ballot_sync(kFull, k < count);
+    const uint32_t at = base + __popc(b & below);
+    if (k < count && at < m.max_entries) m.entries[at] = (uint32_t)cone_slot(m, tile, k, lane);
+    base += __popc(b);
+  }
+}
+
+// setupTrace (kernel.cl:524-544) of the cone in slot `e` of the band.
+__device__ __forceinline__ void start_cone(const MegaLaunch &m, uint32_t e, Ray &r, Walk &w) {
+  const uint32_t lane = e & 31u, tk = e >> 5, K = (uint32_t)m.k_max;
+  const uint32_t tile = tk / K;
+  const MegaPixel *P = m.pix + ((size_t)m.band_tile0 + tile) * 32u + lane;
+  const float4 dw = m.cone_dw[e];
+  const uint32_t s = m.cone_s[e];
+  r.dx = dw.x;
+  r.dy = dw.y;
+  r.dz = dw.z;
+  r.ix = __frcp_rn(r.dx);
+  r.iy = __frcp_rn(r.dy);
+  r.iz = __frcp_rn(r.dz);
+  r.sx = r.dx >= 0.0f;
+  r.sy = r.dy >= 0.0f;
+  r.sz = r.dz >= 0.0f;
+  r.flip = (r.sx ? 0u : 1u) | (r.sy ? 0u : 2u) | (r.sz ? 0u : 4u);
+  set_loc(r, P->loc[0], P->loc[1], P->loc[2]);
+  r.ox = P->origin[0];
+  r.oy = P->origin[1];
+  r.oz = P->origin[2];
+  r.fov = s ? m.spine[s - 1].fov : m.fov_c;
+  r.id = P->id;
+  r.depth = 1;
+  r.steps = 0;
+  reset_walk(w);
+}
+
+// accumulateRay's trace for every cone of the band's compacted list: warps
+// claim 32 consecutive entries (kLane false) or lanes refill from the list
+// every `cadence` steps (kLane true).
+template <bool kSmemBases, bool kLane>
 __global__ void __launch_bounds__(256, SVO_MEGA_MIN_CTAS) mega_cone_kernel(const MegaLaunch m) {
   extern __shared__ __align__(16) uint8_t smem[];
   const TraceLaunch &a = m.t;
@@ -380,50 +456,59 @@ __global__ void __launch_bounds__(256, SVO_MEGA_MIN_CTAS) mega_cone_kernel(const
   Ray r;
   r.view = 0;
   r.fresh = false;
-  const uint32_t lane = threadIdx.x & 31u;
-  const uint32_t K = (uint32_t)m.k_max;
-  bool timed_out = false;
-  for (;;) {
-    uint32_t u = 0;
-    if (lane == 0) u = atomicAdd(m.unit_counter, 1u);
-    u = __shfl_sync(kFull, u, 0);
-    if (u >= m.n_units) break;
-    const uint32_t tile = u / K, k = u - tile * K;
-    if (k >= m.tile_k[tile]) continue;  // uniform: no pixel of the tile has cone k
-    const size_t slot = ((size_t)m.band_tile0 + tile) * 32u + lane;
-    const MegaPixel *P = m.pix + slot;
-    if (!timed_out && k < P->n_cones) {
-      const size_t i = cone_slot(m, tile, k, lane);
-      const float4 dw = m.cone_dw[i];
-      const uint32_t s = m.cone_s[i];
-      // setupTrace (kernel.cl:524-544)
-      r.dx = dw.x;
-      r.dy = dw.y;
-      r.dz = dw.z;
-      r.ix = __frcp_rn(r.dx);
-      r.iy = __frcp_rn(r.dy);
-      r.iz = __frcp_rn(r.dz);
-      r.sx = r.dx >= 0.0f;
-      r.sy = r.dy >= 0.0f;
-      r.sz = r.dz >= 0.0f;
-      r.flip = (r.sx ? 0u : 1u) | (r.sy ? 0u : 2u) | (r.sz ? 0u : 4u);
-      set_loc(r, P->loc[0], P->loc[1], P->loc[2]);
-      r.ox = P->origin[0];
-      r.oy = P->origin[1];
-      r.oz = P->origin[2];
-      r.fov = s ? m.spine[s - 1].fov : m.fov_c;
-      r.id = P->id;
-      r.depth = 1;
-      r.steps = 0;
-      reset_walk(w);
-      int finish;
-      if (!run_cone<kSmemBases>(a, v, s_bases, blocks, B, r, w, finish)) {
-        record_timeout(a, u, r);
-        timed_out = true;
+  const uint32_t n = m.queue[1];
+  if (!kLane) {
+    const uint32_t lane = threadIdx.x & 31u;
+    bool timed_out = false;
+    for (;;) {
+      uint32_t base = 0;
+      if (lane == 0) base = atomicAdd(m.queue, 32u);
+      base = __shfl_sync(kFull, base, 0);
+      if (base >= n) break;
+      const uint32_t i = base + lane;
+      if (i < n && !timed_out) {
+        const uint32_t e = m.entries[i];
+        start_cone(m, e, r, w);
+        int finish;
+        if (!run_cone<kSmemBases>(a, v, s_bases, blocks, B, r, w, finish)) {
+          record_timeout(a, e, r);
+          timed_out = true;
+        }
+        m.cone_sky[e] = finish == kStepBackground ? 1 : 0;
       }
-      m.cone_sky[i] = finish == kStepBackground ? 1 : 0;
+      if (__any_sync(kFull, timed_out)) break;
     }
-    if (__any_sync(kFull, timed_out)) break;
+  } else {
+    // every pass starts a cone or steps one, so a thread runs at most
+    // n * (max_steps + 2) + 64 passes; past that it records its state and stops
+    const unsigned long long iter_limit = (unsigned long long)n * (unsigned long long)(a.max_steps + 2) + 64;
+    unsigned long long iters = 0;
+    const int cadence = a.cadence;
+    bool have = false;
+    uint32_t e = 0;
+    Stats st;
+    for (;;) {
+      if (++iters > iter_limit) {
+        record_timeout(a, e, r);
+        break;
+      }
+      if (!have) {
+        cg::coalesced_group g = cg::coalesced_threads();
+        const uint32_t my = claim(g, m.queue, 1);
+        if (my >= n) break;
+        e = m.entries[my];
+        start_cone(m, e, r, w);
+        have = true;
+      }
+      int finish = kStepOn;
+      for (int k = 0; k < cadence && finish == kStepOn; k++) {
+        finish = probe<false, kSmemBases, true>(a, v, s_bases, blocks, B, r, w, st);
+        if (finish == kStepEmpty) finish = advance(a, blocks, B, r, w);
+      }
+      if (finish == kStepOn) continue;
+      m.cone_sky[e] = finish == kStepBackground ? 1 : 0;
+      have = false;
+    }
   }
 }
 
@@ -489,7 +574,7 @@ cudaError_t launch_traversal(K kernel, const MegaLaunch &m, int grid, cudaStream
 int mega_occupancy(const MegaLaunch &m) {
   const bool sb = bases_in_smem(m.t);
   const size_t smem = trace_smem_bytes(m.t, sb);
-  const void *k = sb ? (const void *)mega_cone_kernel<true> : (const void *)mega_cone_kernel<false>;
+  const void *k = sb ? (const void *)mega_cone_kernel<true, false> : (const void *)mega_cone_kernel<false, false>;
   cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   int n = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, m.t.block_size, smem) != cudaSuccess) return 0;
@@ -508,10 +593,16 @@ svo_status launch_mega_band(const MegaLaunch &m, void *stream) {
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   const uint32_t blocks = (m.band_tiles * 32u + 255u) / 256u;
   mega_fan_kernel<<<blocks, 256, 0, s>>>(m);
+  mega_scan_kernel<<<1, 1024, 0, s>>>(m);
+  mega_emit_kernel<<<blocks, 256, 0, s>>>(m);
   cudaError_t e = cudaGetLastError();
-  if (e == cudaSuccess)
-    e = bases_in_smem(m.t) ? launch_traversal(mega_cone_kernel<true>, m, m.grid_cones, s)
-                           : launch_traversal(mega_cone_kernel<false>, m, m.grid_cones, s);
+  if (e == cudaSuccess) {
+    const bool sb = bases_in_smem(m.t), lane = m.cone_schedule == SVO_SCHEDULE_LANE;
+    e = sb ? (lane ? launch_traversal(mega_cone_kernel<true, true>, m, m.grid_cones, s)
+                   : launch_traversal(mega_cone_kernel<true, false>, m, m.grid_cones, s))
+           : (lane ? launch_traversal(mega_cone_kernel<false, true>, m, m.grid_cones, s)
+                   : launch_traversal(mega_cone_kernel<false, false>, m, m.grid_cones, s));
+  }
   if (e == cudaSuccess) {
     mega_resolve_kernel<<<blocks, 256, 0, s>>>(m);
     e = cudaGetLastError();

@@ -88,6 +88,15 @@ def test_terrain_random_normals(tracer, terrain, k):
     assert ref["n_requests"] > 0 and stats["cones"] > 0
 
 
+@pytest.mark.parametrize("schedule", ["lane", "warp"])
+def test_cone_schedules(tracer, terrain, schedule):
+    """Both cone-kernel schedules (warp batches of 32 list entries, lanes refilled
+    every `cadence` steps) give the same frame."""
+    v = st.orbit_views(seed=11, n=1, width=56, height=40, distance=1.25)[0]
+    sched = {"lane": st.SCHEDULE_LANE, "warp": st.SCHEDULE_WARP}[schedule]
+    check(tracer, terrain, v, schedule=sched, cadence=5)
+
+
 def test_inside_cube_with_dof(tracer, sphere):
     v = st.look_at((0.5, 0.5, 0.12), (0.5, 0.55, 0.6), 48, 40, 70.0, DoF=(0.02, 0.3), Tick=9)
     check(tracer, with_random_normals(sphere, 3), v)
