@@ -154,12 +154,16 @@ def run_reference(args, rank, world):
         return
     tree, cam = workload(st)
     threads = os.cpu_count() or 1
-    rows = 24
+    # each step: 2 bands of 20 rows; the bands of all steps spread evenly over the
+    # frame (its top rows are mostly sky, its bottom rows terrain)
+    rows, bands = 40, 2
+    n = args.warmup + args.steps
     times = []
-    for i in range(args.warmup + args.steps):
-        r0 = (i * rows) % HEIGHT
+    for i in range(n):
         t0 = time.perf_counter()
-        po.ref_trace_rows(tree, cam, r0, r0 + rows, threads=threads)
+        for j in range(bands):
+            r0 = min(HEIGHT - rows // bands, int((i * bands + j + 0.5) / (n * bands) * HEIGHT))
+            po.ref_trace_rows(tree, cam, r0, r0 + rows // bands, threads=threads)
         if i >= args.warmup:
             times.append(time.perf_counter() - t0)
     total = sum(times)
@@ -169,7 +173,8 @@ def run_reference(args, rank, world):
             "scaling": "weak", "vs_baseline": None, "dtype": "f32+u64", "data": "synthetic",
             "config": config_dict(tree, {"sample_rows_per_step": rows}), "impl": "reference",
             "cpu_baseline": {"value": value, "unit": "Mrays/s", "cores": threads, "kind": "reference",
-                             "sample": "%d rows (%d rays) of the 1080p frame per step" % (rows, rows * WIDTH)},
+                             "sample": "%d rows (%d rays) of the 1080p frame per step, in %d bands spread over the "
+                                       "frame across the steps" % (rows, rows * WIDTH, bands)},
             "e2e": {"value": value, "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 

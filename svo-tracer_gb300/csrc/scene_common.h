@@ -68,26 +68,27 @@ SVO_SCENE_FN void terrain_colour(uint32_t seed, int level, uint32_t x, uint32_t 
   }
 }
 
-// atan2(y, x) from the basic double operations only (two half-angle
-// reductions atan t = 2 atan(t / (1 + sqrt(1 + t^2))) to |t| <= tan(pi/16),
-// then the Taylor series of atan to t^23), so that the host builder and the
-// device generator round every step alike.
-SVO_SCENE_FN double atan2_basic(double y, double x) {
-  const double pi = 3.14159265358979323846;
-  if (x == 0.0 && y == 0.0) return 0.0;
-  const double ax = x < 0.0 ? -x : x, ay = y < 0.0 ? -y : y;
-  double t = ay <= ax ? ay / ax : ax / ay;
-  for (int i = 0; i < 2; i++) t = t / (1.0 + sqrt(1.0 + t * t));
-  const double t2 = t * t;
-  double term = t, sum = t;
-  for (int k = 1; k <= 11; k++) {
+// atan2(y, x) from basic float operations only (two half-angle reductions
+// atan t = 2 atan(t / (1 + sqrt(1 + t^2))) to |t| <= tan(pi/16), then the
+// Taylor series of atan to t^11), so that the host builder and the device
+// generator round every step alike. Single precision: the device's FP64 pipe is
+// slow, and the result is truncated to 1/32767 of pi anyway.
+SVO_SCENE_FN float atan2_basic(float y, float x) {
+  const float pi = 3.14159265358979f;
+  if (x == 0.0f && y == 0.0f) return 0.0f;
+  const float ax = x < 0.0f ? -x : x, ay = y < 0.0f ? -y : y;
+  float t = ay <= ax ? ay / ax : ax / ay;
+  for (int i = 0; i < 2; i++) t = t / (1.0f + sqrtf(1.0f + t * t));
+  const float t2 = t * t;
+  float term = t, sum = t;
+  for (int k = 1; k <= 5; k++) {
     term = -term * t2;
-    sum = sum + term / (double)(2 * k + 1);
+    sum = sum + term / (float)(2 * k + 1);
   }
-  double a = 4.0 * sum;
-  if (ay > ax) a = pi / 2.0 - a;
-  if (x < 0.0) a = pi - a;
-  return y < 0.0 ? -a : a;
+  float a = 4.0f * sum;
+  if (ay > ax) a = pi / 2.0f - a;
+  if (x < 0.0f) a = pi - a;
+  return y < 0.0f ? -a : a;
 }
 
 // NormalAngle (TreeBuilder.cs:328-334) of the surface normal n. The
@@ -95,19 +96,19 @@ SVO_SCENE_FN double atan2_basic(double y, double x) {
 // (SphereDefinition.Normal), which normalVector (kernel.cl:264-275) decodes
 // back to n: pitch = asin(n.z) / pi, yaw = atan2(n.y, n.x) / pi, each times
 // 32767 and truncated. A zero vector gives (0, 0).
-SVO_SCENE_FN void normal_angles(double nx, double ny, double nz, int16_t &pitch, int16_t &yaw) {
-  const double pi = 3.14159265358979323846;
-  const double l = sqrt(nx * nx + ny * ny + nz * nz);
-  if (!(l > 0.0)) {
+SVO_SCENE_FN void normal_angles(float nx, float ny, float nz, int16_t &pitch, int16_t &yaw) {
+  const float pi = 3.14159265358979f;
+  const float l = sqrtf(nx * nx + ny * ny + nz * nz);
+  if (!(l > 0.0f)) {
     pitch = yaw = 0;
     return;
   }
   nx = nx / l;
   ny = ny / l;
   nz = nz / l;
-  const double c = 1.0 - nz * nz;
-  pitch = (int16_t)(32767.0 * (atan2_basic(nz, sqrt(c > 0.0 ? c : 0.0)) / pi));
-  yaw = (int16_t)(32767.0 * (atan2_basic(ny, nx) / pi));
+  const float c = 1.0f - nz * nz;
+  pitch = (int16_t)(32767.0f * (atan2_basic(nz, sqrtf(c > 0.0f ? c : 0.0f)) / pi));
+  yaw = (int16_t)(32767.0f * (atan2_basic(ny, nx) / pi));
 }
 
 // The terrain's surface normal at column (x, y) of `level` (up = -z), from
@@ -117,14 +118,14 @@ SVO_SCENE_FN void terrain_normal(const uint16_t *hi_level, int level, int leaf, 
   const uint32_t n = 1u << level;
   const uint32_t x0 = x ? x - 1 : x, x1 = x + 1 < n ? x + 1 : x;
   const uint32_t y0 = y ? y - 1 : y, y1 = y + 1 < n ? y + 1 : y;
-  const double s = (double)(1u << (leaf - level));  // leaf cells per column side
-  const double hx = x1 > x0 ? ((double)hi_level[(size_t)y * n + x1] - (double)hi_level[(size_t)y * n + x0]) /
-                                  ((double)(x1 - x0) * s)
-                            : 0.0;
-  const double hy = y1 > y0 ? ((double)hi_level[(size_t)y1 * n + x] - (double)hi_level[(size_t)y0 * n + x]) /
-                                  ((double)(y1 - y0) * s)
-                            : 0.0;
-  normal_angles(-hx, -hy, -1.0, pitch, yaw);
+  const float s = (float)(1u << (leaf - level));  // leaf cells per column side
+  const float hx = x1 > x0 ? ((float)hi_level[(size_t)y * n + x1] - (float)hi_level[(size_t)y * n + x0]) /
+                                 ((float)(x1 - x0) * s)
+                           : 0.0f;
+  const float hy = y1 > y0 ? ((float)hi_level[(size_t)y1 * n + x] - (float)hi_level[(size_t)y0 * n + x]) /
+                                 ((float)(y1 - y0) * s)
+                           : 0.0f;
+  normal_angles(-hx, -hy, -1.0f, pitch, yaw);
 }
 
 // CanHaveChildren (TreeBuilder.cs): some octant holds both air and geometry.

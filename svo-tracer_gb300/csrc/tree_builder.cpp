@@ -142,7 +142,8 @@ struct SphereScene final : Scene {
   // radial, like SphereDefinition.Normal
   void normal(int level, uint32_t x, uint32_t y, uint32_t z, int16_t &pitch, int16_t &yaw) const override {
     const double s = std::ldexp(1.0, -level);
-    scene::normal_angles((x + 0.5) * s - cx, (y + 0.5) * s - cy, (z + 0.5) * s - cz, pitch, yaw);
+    scene::normal_angles((float)((x + 0.5) * s - cx), (float)((y + 0.5) * s - cy), (float)((z + 0.5) * s - cz), pitch,
+                         yaw);
   }
   void colour(int level, uint32_t x, uint32_t y, uint32_t z, uint8_t rgb[3]) const override {
     uint32_t h = hash4(seed ^ 0x51ed270bU, (uint32_t)level, x, y, z);
