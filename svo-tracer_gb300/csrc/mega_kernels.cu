@@ -396,7 +396,10 @@ __global__ void __launch_bounds__(256) mega_emit_kernel(const MegaLaunch m) {
   const uint32_t gid = blockIdx.x * blockDim.x + threadIdx.x;
   const uint32_t tile = gid >> 5, lane = gid & 31u;
   if (tile >= m.band_tiles) return;  // whole warps
-  const uint32_t count = m.pix[((size_t)m.band_tile0 + tile) * 32u + lane].n_cones;
+  const MegaPixel &P = m.pix[((size_t)m.band_tile0 + tile) * 32u + lane];
+  // only fans of this call count (bounded by the slot stride)
+  const uint32_t count =
+      (P.kind == kMegaSky || P.kind == kMegaSurface) ? min((uint32_t)P.n_cones, (uint32_t)m.k_max) : 0u;
   const uint32_t kmax = __reduce_max_sync(kFull, count);
   uint32_t base = m.tile_cones[tile];
   const uint32_t below = (1u << lane) - 1u;
@@ -532,7 +535,8 @@ __global__ void __launch_bounds__(256) mega_resolve_kernel(const MegaLaunch m) {
     sky_light(P.dir[0], P.dir[1], P.dir[2], cr, cg_, cb, lum);
   }
   float tw = 0.0f, ar = 0.0f, ag = 0.0f, ab = 0.0f;
-  for (uint32_t k = 0; k < P.n_cones; k++) {
+  const uint32_t n_cones = P.kind == kMegaMiss ? 0u : min((uint32_t)P.n_cones, (uint32_t)m.k_max);
+  for (uint32_t k = 0; k < n_cones; k++) {
     const size_t i = cone_slot(m, tile, k, lane);
     const float4 dw = m.cone_dw[i];
     tw = __fadd_rn(tw, dw.w);
