@@ -242,6 +242,59 @@ def multiview(tr, torch, dev, stream, flush, args, windows=None):
             "plain": "64 sequential single-view launches, same stream, default configuration"}
 
 
+def sphere_workload(torch, dev, flush, args, windows=None):
+    """The CPU-runnable case: one 640x480 view (FoV 60 degrees, camera at world
+    distance 1.5 on a seeded direction, i.e. 0.75 in the unit cube that the [-1,1]
+    world maps onto) of the depth-8 SDF sphere, traced by the plain path, with the
+    reference's CPU build timed on the same whole frame."""
+    import pyoracle as po
+    import svo_tracer as st
+
+    tree = st.TreeBuilder(st.SCENE_SPHERE, seed=SEED).BuildTree(BASE_DEPTH, 8)
+    cam = st.orbit_views(seed=SEED, n=1, width=640, height=480, distance=0.75, Tick=7, MaxChildRequestId=1 << 16)[0]
+    n = 640 * 480
+    tr = st.Tracer(dev)
+    stream = torch.cuda.Stream(device=dev)
+    tr.set_stream(stream.cuda_stream)
+    tr.upload(tree)
+    tr.init_usage()
+    tr.set_config(collect_stats=1)
+    tr.trace(cam)
+    stats = tr.stats()
+    tr.set_config(collect_stats=0)
+    o = [torch.empty(n, dtype=torch.int32, device=dev), torch.empty(n, dtype=torch.uint8, device=dev),
+         torch.empty(n, dtype=torch.float32, device=dev), torch.empty(4 * n, dtype=torch.float32, device=dev)]
+    outs = [tuple(x.data_ptr() for x in o)]
+    with torch.cuda.stream(stream):
+        for _ in range(3):
+            tr.trace_device([cam], outs)
+        ev = []
+        t_win = time.perf_counter()
+        for _ in range(max(5, args.steps)):
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            tr.trace_device([cam], outs)
+            e1.record(stream)
+            ev.append((e0, e1))
+        torch.cuda.synchronize(dev)
+        if windows is not None:
+            windows.append((t_win, time.perf_counter()))
+    ms = sum(a.elapsed_time(b) for a, b in ev) / len(ev)
+    tr.close()
+    alg = 16 * stats["block_node_reads"] + 2 * stats["base_steps"] + OUT_BYTES * n
+    out = {"workload": "640x480 view of the depth-8 SDF sphere (%d nodes)" % len(tree.Blocks), "ms": ms,
+           "mrays_s": n / ms / 1e3, "algorithmic_gb_s": alg / ms / 1e6, "hits": int(stats["hits"])}
+    if not args.no_cpu_baseline and po.ref_available():
+        threads = os.cpu_count() or 1
+        t0 = time.perf_counter()
+        po.ref_trace_view(tree, cam, threads=threads)
+        el = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": n / el / 1e6, "unit": "Mrays/s", "cores": threads, "kind": "reference",
+                               "sample": "the whole 640x480 frame, %.2f s" % el}
+    return out
+
+
 def mega_workload(tr, torch, dev, stream, flush, args, tree, cam, windows=None):
     """The megakernel (kernel.cl's `trace`: primary cone, spawnRays's fan of
     secondary cones, draw) on the same 1080p terrain frame, with the reference's
@@ -617,6 +670,8 @@ def run_ours(args, rank, world):
         line["diff"] = diff_workload(torch, dev, flush, args, windows)
     if not args.no_mega:
         line["megakernel"] = mega_workload(tr, torch, dev, stream, flush, args, tree, cam, windows)
+    if not args.no_sphere:
+        line["sphere_640x480"] = sphere_workload(torch, dev, flush, args, windows)
     clk.__exit__(None, None, None)
     line["clocks"] = clk.summary(windows)
     if args.stream_frames > 0:
@@ -645,6 +700,7 @@ def main():
     ap.add_argument("--no-multiview", action="store_true")
     ap.add_argument("--no-diff", action="store_true")
     ap.add_argument("--no-mega", action="store_true")
+    ap.add_argument("--no-sphere", action="store_true")
     ap.add_argument("--schedule", choices=["lane", "warp"], default=None)
     ap.add_argument("--diff-views", type=int, default=16)
     ap.add_argument("--diff-size", type=int, default=512)
