@@ -467,7 +467,8 @@ def stream_workload(torch, dev, args):
 
 def diff_workload(torch, dev, flush, args, windows=None):
     """Differentiable colour fitting: the depth-9 SDF sphere (512^3 leaf grid), 16
-    views of 512x512 around it, FP32 per-node RGBA initialised uniform in [0, 1],
+    views of 512x512 around it at the sphere case's camera distance (world 1.5, 0.75
+    in the unit cube), FP32 per-node RGBA initialised uniform in [0, 1],
     targets rendered from the seeded sinusoid ground-truth field (opacity 0.9).
     One step = forward colour + backward (loss and dL/dRGBA per node, traversal
     recomputed once, the forward's colour reused), device-resident; L2 flushed
@@ -477,7 +478,7 @@ def diff_workload(torch, dev, flush, args, windows=None):
     import svo_tracer as st
 
     tree = st.TreeBuilder(st.SCENE_SPHERE, seed=1).BuildTree(4, 9)
-    views = st.orbit_views(seed=7, n=args.diff_views, width=args.diff_size, height=args.diff_size)
+    views = st.orbit_views(seed=7, n=args.diff_views, width=args.diff_size, height=args.diff_size, distance=0.75)
     rays = sum(v.ScreenSize[0] * v.ScreenSize[1] for v in views)
     nodes = len(tree.Blocks)
     tr = st.Tracer(dev)

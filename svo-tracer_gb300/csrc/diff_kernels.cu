@@ -50,7 +50,9 @@
 #include <vector>
 
 #include "context.h"
+#ifndef SVO_CVT_INTEGER
 #define SVO_CVT_INTEGER 1  // integer ulong_to_float: faster in this kernel mix
+#endif
 #include "trace_core.cuh"
 
 // Resident CTAs of 256 threads per SM the kernels are compiled for (4 and 4
