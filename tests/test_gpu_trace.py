@@ -21,7 +21,7 @@ def default_config(tracer):
                       schedule=st.SCHEDULE_LANE)
     yield
 
-T_RTOL = 1e-5  # the benchmark spec's tolerance for t and RGBA; the checks below are tighter (exact)
+T_RTOL = 1e-5  # the required tolerance for t and RGBA (relative); the checks below are tighter (exact)
 
 
 def assert_same(got, want, label=""):
