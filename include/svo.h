@@ -184,7 +184,7 @@ typedef struct svo_trace_config {
   int32_t collect_stats; /* 0 none, 1 totals (svo_last_trace_stats), 2 totals and per-ray counts */
   int32_t max_hits;     /* differentiable forward: LOD hits composited per ray (1..1024) */
   int32_t schedule;     /* SVO_SCHEDULE_LANE or SVO_SCHEDULE_WARP */
-  int32_t mega_band_tiles; /* megakernel: 8x4 tiles per cone band (0: as many as 2^26 cone slots hold) */
+  int32_t mega_band_tiles; /* megakernel: pixel tiles of 32 per cone band (0: as many as 2^26 cone slots hold) */
   int32_t _pad;
 } svo_trace_config;
 

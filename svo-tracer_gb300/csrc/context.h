@@ -229,11 +229,11 @@ inline void *pinned_device_ptr(const void *p) {
   return at.type == cudaMemoryTypeHost ? at.devicePointer : nullptr;
 }
 
-// Views, ray-setup tables and outputs of a batch into pinned staging. With
-// `tiled`, each view's ray slots cover whole 8x4 pixel tiles (total_rays then
-// exceeds total_pixels by the padding slots).
+// Views, ray-setup tables and outputs of a batch into pinned staging. With a
+// tile width, each view's ray slots cover whole tile_w x (32 / tile_w) pixel
+// tiles (total_rays then exceeds total_pixels by the padding slots); 0 = rows.
 svo_status stage_views(Context &c, const svo_trace_input *in, int32_t n, const svo_trace_output *out,
-                       bool outputs_on_device, bool tiled, uint32_t &total_rays, uint32_t &total_pixels,
+                       bool outputs_on_device, uint32_t tile_w, uint32_t &total_rays, uint32_t &total_pixels,
                        size_t &table_floats);
 svo_status prepare_launch(Context &c, int32_t n_views, uint32_t total_rays, TraceLaunch &a, bool stats);
 

@@ -292,7 +292,7 @@ svo_status run_diff(Context &c, const svo_trace_input *views, int32_t n, const f
   SVO_CUDA(cudaEventSynchronize(c.staged), "svo_diff: staging");
   uint32_t total = 0, pixels = 0;
   size_t table_floats = 0;
-  svo_status st = stage_views(c, views, n, outs.data(), true, /*tiled=*/true, total, pixels, table_floats);
+  svo_status st = stage_views(c, views, n, outs.data(), true, kDiffTileW, total, pixels, table_floats);
   if (st) return st;
   if (kBackward && use_saved &&
       !(c.saved_valid && c.saved_params_gen == c.params_gen && c.saved_max_hits == c.cfg.max_hits &&

@@ -157,7 +157,7 @@ svo_status run_mega(Context &c, const svo_trace_input *in, const svo_trace_outpu
   SVO_CUDA(cudaEventSynchronize(c.staged), "svo_mega_trace: staging");
   uint32_t total_rays = 0, total_pixels = 0;
   size_t table_floats = 0;
-  st = stage_views(c, in, 1, &out, direct, /*tiled=*/true, total_rays, total_pixels, table_floats);
+  st = stage_views(c, in, 1, &out, direct, kTraceTileW, total_rays, total_pixels, table_floats);
   if (st) return st;
   const uint32_t n_tiles = total_rays / 32;
   const int32_t K = c.mega_k_max;

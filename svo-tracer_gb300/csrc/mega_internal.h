@@ -8,7 +8,7 @@
 
 namespace svo {
 
-// Per pixel slot (the view's 8x4 tiles, 32 slots per tile) between the kernels.
+// Per pixel slot (the view's warp tiles, 32 slots per tile) between the kernels.
 enum : uint8_t { kMegaPad = 0, kMegaMiss = 1, kMegaSky = 2, kMegaSurface = 3 };
 struct MegaPixel {
   uint64_t loc[3];   // primary's end location; after the fan kernel, the cones' start

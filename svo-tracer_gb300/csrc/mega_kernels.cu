@@ -3,7 +3,7 @@
 // secondary cones from its end point (:1115-1253) and draw (:1264-1275).
 //
 // One OpenCL work-item per pixel runs ~20 dependent traces in a row; here the
-// pixel's work is split into four kernels over the view's 8x4 pixel tiles, so
+// pixel's work is split into kernels over the view's 4x8 pixel tiles, so
 // that a warp always steps 32 cones that start close together and point the
 // same way:
 //  1. mega_primary_kernel: the primary cone of every pixel, the persistent

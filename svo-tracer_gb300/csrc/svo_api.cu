@@ -83,8 +83,9 @@ static int scan_tree_depth(const svo_block *blocks, size_t n_blocks, int B) {
 
 // Builds the view table and trig tables for `n` views in pinned staging.
 svo_status stage_views(Context &c, const svo_trace_input *in, int32_t n, const svo_trace_output *out,
-                       bool outputs_on_device, bool tiled, uint32_t &total_rays, uint32_t &total_pixels,
+                       bool outputs_on_device, uint32_t tile_w, uint32_t &total_rays, uint32_t &total_pixels,
                        size_t &table_floats) {
+  const uint32_t tile_h = tile_w ? 32 / tile_w : 0;
   total_rays = 0;
   total_pixels = 0;
   table_floats = 0;
@@ -94,7 +95,7 @@ svo_status stage_views(Context &c, const svo_trace_input *in, int32_t n, const s
       return fail(SVO_ERR_INVALID_ARGUMENT, "svo_trace: screen_size must be 1..65536 per axis");
     if (in[i].base_depth != 0 && in[i].base_depth != c.base_depth)
       return fail(SVO_ERR_INVALID_ARGUMENT, "svo_trace: input base_depth differs from the resident tree's");
-    uint64_t slots = tiled ? ((w + kTileW - 1) / kTileW) * ((h + kTileH - 1) / kTileH) * 32 : w * h;
+    uint64_t slots = tile_w ? ((w + tile_w - 1) / tile_w) * ((h + tile_h - 1) / tile_h) * 32 : w * h;
     if ((uint64_t)total_rays + slots > 0xF0000000ull)
       return fail(SVO_ERR_INVALID_ARGUMENT, "svo_trace: too many rays in one call");
     total_rays += (uint32_t)slots;
@@ -120,7 +121,7 @@ svo_status stage_views(Context &c, const svo_trace_input *in, int32_t n, const s
     v.height = H;
     v.ray_begin = ray;
     v.pixel_begin = (uint32_t)out_off;
-    v.tile = tiled ? 1 : 0;
+    v.tile = (uint16_t)tile_w;
     v.table_off = (uint32_t)toff;
     v.tick = t.tick;
     if (outputs_on_device) {
@@ -161,7 +162,7 @@ svo_status stage_views(Context &c, const svo_trace_input *in, int32_t n, const s
     std::memcpy(tb, it->second.data(), it->second.size() * sizeof(float));
     toff += 2 * ((size_t)W + H);
     out_off += (size_t)W * H;
-    ray += tiled ? ((W + kTileW - 1) / kTileW) * ((H + kTileH - 1) / kTileH) * 32 : W * H;
+    ray += tile_w ? ((W + tile_w - 1) / tile_w) * ((H + tile_h - 1) / tile_h) * 32 : W * H;
   }
   return SVO_OK;
 }
@@ -270,8 +271,10 @@ static svo_status run_trace(Context &c, const svo_trace_input *in, int32_t n, co
   size_t table_floats;
   // the previous call's uploads must have read the pinned staging before it is rewritten
   SVO_CUDA(cudaEventSynchronize(c.staged), "svo_trace: staging");
-  // warp batches take 8x4 pixel tiles
-  svo_status st = stage_views(c, in, n, out, on_device, c.cfg.schedule == SVO_SCHEDULE_WARP, total_rays,
+  // warp batches take pixel tiles: wider ones when the kernel writes host memory
+  const uint32_t tile_w =
+      c.cfg.schedule != SVO_SCHEDULE_WARP ? 0 : (host_outputs && on_device ? kTraceHostTileW : kTraceTileW);
+  svo_status st = stage_views(c, in, n, out, on_device, tile_w, total_rays,
                               total_pixels, table_floats);
   if (st) return st;
   bool stats = c.cfg.collect_stats > 0;
@@ -299,6 +302,7 @@ static svo_status run_trace(Context &c, const svo_trace_input *in, int32_t n, co
     std::vector<uint32_t> key;
     key.push_back((uint32_t)n);
     key.push_back(on_device ? 1u : 0u);
+    key.push_back(tile_w);  // the launch's ray count depends on it
     for (int i = 0; i < n; i++) {
       key.push_back(in[i].screen_size[0]);
       key.push_back(in[i].screen_size[1]);

@@ -13,13 +13,29 @@ svo_status fail(svo_status status, const std::string &message);
 
 struct TreeHost;
 
-// Per-view constants of one trace, as the kernel reads them.
-// Pixel tile of a warp batch (kTileW x kTileH = 32 rays).
-#ifndef SVO_TILE_W
-#define SVO_TILE_W 8
+// Pixel tile of a warp batch: tile_w x (32 / tile_w) pixels, tile_w a power of
+// two; results do not depend on it. Measured on GB300: 4x8 tiles for the trace
+// and the megakernel (1080p frame 1.80 -> 1.78 ms, megakernel 18.39 -> 17.73 ms
+// against 8x4), but 8x4 for a trace whose kernel writes pinned host outputs
+// directly (its stores leave the GPU in row segments of the tile width: e2e 1041
+// Mrays/s with 4x8 against 1100 with 8x4), and 8x4 for the colour-fitting kernels
+// (2.21 / 2.43 ms against 2.24 / 2.46 ms with 4x8).
+#ifndef SVO_TRACE_TILE_W
+#define SVO_TRACE_TILE_W 4
 #endif
-constexpr uint32_t kTileW = SVO_TILE_W, kTileH = 32 / SVO_TILE_W;
-static_assert(kTileW * kTileH == 32, "a tile is one warp of rays");
+#ifndef SVO_TRACE_HOST_TILE_W
+#define SVO_TRACE_HOST_TILE_W 8
+#endif
+#ifndef SVO_DIFF_TILE_W
+#define SVO_DIFF_TILE_W 8
+#endif
+constexpr uint32_t kTraceTileW = SVO_TRACE_TILE_W, kTraceHostTileW = SVO_TRACE_HOST_TILE_W,
+                   kDiffTileW = SVO_DIFF_TILE_W;
+static_assert((kTraceTileW & (kTraceTileW - 1)) == 0 && kTraceTileW <= 32, "tile width: a power of two up to 32");
+static_assert((kDiffTileW & (kDiffTileW - 1)) == 0 && kDiffTileW <= 32, "tile width: a power of two up to 32");
+static_assert((kTraceHostTileW & (kTraceHostTileW - 1)) == 0 && kTraceHostTileW <= 32, "tile width");
+
+// Per-view constants of one trace, as the kernel reads them.
 
 struct ViewParams {
   float origin[3];
@@ -31,7 +47,7 @@ struct ViewParams {
   uint32_t ray_begin;  // first ray of this view in the batch's ray index space
   uint32_t table_off;  // sinU, cosU at [off, off+W); sinV, cosV at [off+2W, off+2W+2H)
   uint16_t tick;
-  uint16_t tile;         // 1: the view's rays are claimed in 8x4 pixel tiles (ray slots padded to whole tiles)
+  uint16_t tile;         // tile width: rays are claimed in tile x (32 / tile) pixel tiles (slots padded to whole tiles); 0: rows
   uint32_t pixel_begin;  // first pixel of this view in the batch's concatenated pixel space
   uint32_t *hit_index;
   uint8_t *hit_depth;

@@ -391,9 +391,10 @@ __device__ __forceinline__ int probe(const TraceLaunch &a, const ViewParams &v, 
 
 
 // Slot `my` of the batch's ray index space: its view and pixel. Views are
-// sorted by ray_begin. A tiled view's slots run over 8x4 pixel tiles, row of
-// tiles by row of tiles, so the 32 slots a warp takes form one tile; the slots
-// of a tile that fall outside the image are padding (returns false).
+// sorted by ray_begin. A tiled view's slots run over pixel tiles of 32 (tile
+// width v.tile, a power of two), row of tiles by row of tiles, so the 32 slots a
+// warp takes form one tile; the slots of a tile that fall outside the image are
+// padding (returns false).
 __device__ __forceinline__ bool ray_slot(const TraceLaunch &a, const ViewParams *s_views, uint32_t my, int &view,
                                          uint32_t &px, uint32_t &py) {
   int lo = 0, hi = a.n_views - 1;
@@ -408,9 +409,10 @@ __device__ __forceinline__ bool ray_slot(const TraceLaunch &a, const ViewParams 
   view = lo;
   const uint32_t rel = my - v.ray_begin;
   if (v.tile) {
-    const uint32_t tiles_x = (v.width + kTileW - 1) / kTileW, t = rel >> 5, l = rel & 31u;
-    py = (t / tiles_x) * kTileH + l / kTileW;
-    px = (t % tiles_x) * kTileW + l % kTileW;
+    const uint32_t tw = v.tile, lg = (uint32_t)(__ffs((int)tw) - 1);
+    const uint32_t tiles_x = (v.width + tw - 1) >> lg, t = rel >> 5, l = rel & 31u;
+    py = (t / tiles_x) * (32u >> lg) + (l >> lg);
+    px = (t % tiles_x) * tw + (l & (tw - 1));
     return px < v.width && py < v.height;
   }
   px = rel % v.width;

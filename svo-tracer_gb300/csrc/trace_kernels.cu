@@ -157,7 +157,7 @@ __global__ void __launch_bounds__(256, SVO_TRACE_MIN_CTAS) trace_kernel(const Tr
   };
 
   if (kWarpBatch) {
-    // ---- warp batches: 32 consecutive ray slots (one 8x4 pixel tile of a tiled
+    // ---- warp batches: 32 consecutive ray slots (one pixel tile of a tiled
     // view) per warp, regrouped between batches
     const uint32_t lane = threadIdx.x & 31u;
     bool timed_out = false;
