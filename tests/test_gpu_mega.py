@@ -137,3 +137,28 @@ def test_endless_schedule_is_refused(tracer, sphere):
     tracer.upload(sphere)
     with pytest.raises(st.SvoError):
         tracer.mega_trace(v)
+
+
+def test_output_kinds_agree(tracer, terrain):
+    """Pageable host outputs (staged through device buffers), pinned host outputs
+    (written by the kernels) and device outputs give the same frame."""
+    torch = pytest.importorskip("torch")
+    v = dataclasses.replace(st.orbit_views(seed=12, n=1, width=61, height=37, distance=1.2)[0], Tick=4)
+    tracer.upload(terrain)
+    tracer.init_usage()
+    want = tracer.mega_trace(v)
+    n = 61 * 37
+    pinned = st.TraceResult(torch.empty(n, dtype=torch.int32, pin_memory=True).numpy().view(np.uint32),
+                            torch.empty(n, dtype=torch.uint8, pin_memory=True).numpy(),
+                            torch.empty(n, dtype=torch.float32, pin_memory=True).numpy(),
+                            torch.empty(n * 4, dtype=torch.float32, pin_memory=True).numpy().reshape(n, 4))
+    got = tracer.mega_trace(v, out=pinned)
+    dev = [torch.empty(n, dtype=torch.int32, device="cuda"), torch.empty(n, dtype=torch.uint8, device="cuda"),
+           torch.empty(n, dtype=torch.float32, device="cuda"), torch.empty(4 * n, dtype=torch.float32, device="cuda")]
+    tracer.mega_trace_device(v, *[x.data_ptr() for x in dev])
+    tracer.synchronize()
+    on_dev = [x.cpu().numpy() for x in dev]
+    for k, d in zip(("hit_index", "hit_depth", "t", "rgba"), on_dev):
+        a = getattr(want, k).reshape(-1)
+        assert np.array_equal(getattr(got, k).reshape(-1).view(np.uint8), a.view(np.uint8)), k
+        assert np.array_equal(d.reshape(-1).view(np.uint8), a.view(np.uint8)), k
