@@ -162,3 +162,24 @@ def test_output_kinds_agree(tracer, terrain):
         a = getattr(want, k).reshape(-1)
         assert np.array_equal(getattr(got, k).reshape(-1).view(np.uint8), a.view(np.uint8)), k
         assert np.array_equal(d.reshape(-1).view(np.uint8), a.view(np.uint8)), k
+
+
+def test_step_limit_matches_oracle(tracer, terrain):
+    """A primary cone or secondary cone stopped by max_steps ends as sky, on the GPU
+    and in the oracle alike."""
+    v = dataclasses.replace(st.orbit_views(seed=13, n=1, width=48, height=32, distance=1.2)[0], Tick=2,
+                            MaxChildRequestId=1 << 20)
+    tracer.upload(terrain)
+    tracer.init_usage()
+    tracer.set_config(max_steps=24)
+    try:
+        got = tracer.mega_trace(v)
+        req, n = tracer.read_child_requests()
+    finally:
+        tracer.set_config(max_steps=0)
+    ref = po.mega_trace_view(terrain, v, max_steps=24)
+    full = po.mega_trace_view(terrain, v)
+    assert not np.array_equal(ref["rgba"], full["rgba"])  # the limit changes the frame
+    assert np.array_equal(got.rgba.reshape(-1, 4).view(np.uint32), ref["rgba"].view(np.uint32))
+    assert np.array_equal(got.hit_index.reshape(-1), ref["hit_index"])
+    assert n == ref["n_requests"]
