@@ -17,6 +17,7 @@
 // reference serialises its dereferencing through a global spin lock
 // (wavefront.cl:226-231); here reachability is recomputed breadth-first with
 // one pass per tree level, so no thread ever waits on another.
+#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -31,6 +32,7 @@
 #include "scene_common.h"
 
 namespace svo {
+namespace cg = cooperative_groups;
 namespace {
 
 constexpr uint32_t kNone = 0xFFFFFFFFu;
@@ -55,12 +57,21 @@ __device__ __forceinline__ uint32_t tick_age(uint32_t t, uint32_t now) {
   return now >= t ? now - t : now + 65533u - t;
 }
 
+// Appends v to a list at *count with one atomic per group of the warp's lanes
+// that append at the same time (the list's order is not significant).
+__device__ __forceinline__ void append(uint32_t *list, uint32_t *count, uint32_t v) {
+  cg::coalesced_group g = cg::coalesced_threads();
+  uint32_t base = 0;
+  if (g.thread_rank() == 0) base = atomicAdd(count, g.size());
+  list[g.shfl(base, 0) + g.thread_rank()] = v;
+}
+
 __global__ void k_reach_seed(TreeView t, uint32_t *reach, uint32_t *parent_min, uint32_t *frontier,
                              uint32_t *count) {
   for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < t.n_groups; g += gridDim.x * blockDim.x) {
     reach[g] = 0;
-    parent_min[g] = kNone;
-    if (dense_real(t, g)) frontier[atomicAdd(count, 1u)] = g;
+    if (parent_min) parent_min[g] = kNone;
+    if (dense_real(t, g)) append(frontier, count, g);
   }
 }
 
@@ -74,8 +85,8 @@ __global__ void k_reach_expand(TreeView t, const uint32_t *frontier, const uint3
     if (c == kNone || (c & 7u)) continue;
     uint32_t h = c >> 3;
     if (h >= t.n_groups || dense_real(t, h)) continue;
-    atomicMin(parent_min + h, node);
-    if (atomicExch(reach + h, 1u) == 0u) next[atomicAdd(n_out, 1u)] = h;
+    if (parent_min) atomicMin(parent_min + h, node);
+    if (atomicExch(reach + h, 1u) == 0u) append(next, n_out, h);
   }
 }
 
@@ -389,16 +400,19 @@ svo_status ensure_tree_buffers(Context &c) {
 // the last level (0 when reachability is complete).
 // scan_tmp = [block counts | ... | n-8, n-7: frontier sizes | n-6: compact total
 //             | n-5: prune flag | n-4..n-2: GC totals]
-uint32_t *reachability_async(Context &c, const TreeView &t) {
+uint32_t *reachability_async(Context &c, const TreeView &t, bool with_parents) {
   uint32_t *cnt = c.scan_tmp.p + (c.scan_tmp.n - 8);
+  // the smallest parent node of each group is needed only for the usage
+  // initialisation; without it the walk takes one scattered atomic per group, not two
+  uint32_t *parents = with_parents ? c.parent_min.p : nullptr;
   cudaMemsetAsync(cnt, 0, 2 * sizeof(uint32_t), c.stream);
-  k_reach_seed<<<grid_for(t.n_groups), 256, 0, c.stream>>>(t, c.reach.p, c.parent_min.p, c.frontier_a.p, cnt);
+  k_reach_seed<<<grid_for(t.n_groups), 256, 0, c.stream>>>(t, c.reach.p, parents, c.frontier_a.p, cnt);
   uint32_t *in = c.frontier_a.p, *out = c.frontier_b.p;
   uint32_t *n_in = cnt, *n_out = cnt + 1;
   const int levels = std::max(1, std::min(c.tree_depth, SVO_MAX_TREE_DEPTH) - (int)c.base_depth - 1);
   for (int level = 0; level < levels; level++) {
     cudaMemsetAsync(n_out, 0, 4, c.stream);
-    k_reach_expand<<<152 * 8, 256, 0, c.stream>>>(t, in, n_in, out, n_out, c.reach.p, c.parent_min.p);
+    k_reach_expand<<<152 * 8, 256, 0, c.stream>>>(t, in, n_in, out, n_out, c.reach.p, parents);
     std::swap(in, out);
     std::swap(n_in, n_out);
   }
@@ -406,7 +420,7 @@ uint32_t *reachability_async(Context &c, const TreeView &t) {
 }
 
 svo_status reachability(Context &c, const TreeView &t) {
-  uint32_t *left = reachability_async(c, t);
+  uint32_t *left = reachability_async(c, t, true);
   SVO_CUDA(cudaGetLastError(), "reachability");
   uint32_t n = 0;
   SVO_CUDA(cudaMemcpyAsync(&n, left, 4, cudaMemcpyDeviceToHost, c.stream), "reachability: frontier size");
@@ -434,7 +448,7 @@ void compact_async(Context &c, const uint8_t *flags, uint32_t n, uint32_t *out, 
 // (with `pruned_total`, a device slot already written) the pruned count.
 svo_status sweep_and_free_list(Context &c, const TreeView &t, uint64_t *n_freed, uint64_t *n_pruned = nullptr,
                                const uint32_t *pruned_total = nullptr) {
-  uint32_t *left = reachability_async(c, t);
+  uint32_t *left = reachability_async(c, t, false);
   uint32_t *totals = c.scan_tmp.p + (c.scan_tmp.n - 4);  // [0] freed, [1] free, [2] frontier left
   k_sweep<<<grid_for(t.n_groups), 256, 0, c.stream>>>(t, c.reach.p, c.flags.p, left);
   compact_async(c, c.flags.p, t.n_groups, c.freed_list.p, totals);
