@@ -381,11 +381,13 @@ def _stream_run(st, scene, tree, cams, dev, device_generate):
     graft payloads (on the device, or generated on the host and uploaded), GC of
     groups unused for more than 30 frames, grafts into the freed groups."""
     budget = 1 << 22
+    import torch
     tr = st.Tracer(dev)
+    stream = torch.cuda.Stream(device=dev)  # GPU time of each phase by events on the context's stream
+    tr.set_stream(stream.cuda_stream)
     tr.upload(tree, block_budget=budget * 8)
     tr.init_usage_tree(1)
     n = WIDTH * HEIGHT
-    import torch
     o = [torch.empty(n, dtype=torch.int32, device=dev), torch.empty(n, dtype=torch.uint8, device=dev),
          torch.empty(n, dtype=torch.float32, device=dev), torch.empty(4 * n, dtype=torch.float32, device=dev)]
     outs = [tuple(x.data_ptr() for x in o)]
@@ -396,11 +398,16 @@ def _stream_run(st, scene, tree, cams, dev, device_generate):
         tr.graft_generate(1, scene)
         tr.upload(tree, block_budget=budget * 8)
         tr.init_usage_tree(1)
+    ev = []
     t_loop = time.perf_counter()
     for f, cam in enumerate(cams):
         tick = f + 1
+        marks = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+        ev.append(marks)
         a = time.perf_counter()
+        marks[0].record(stream)
         tr.trace_device([cam], outs)
+        marks[1].record(stream)
         if device_generate:
             rec = pay = None
         else:
@@ -410,8 +417,10 @@ def _stream_run(st, scene, tree, cams, dev, device_generate):
             rec, pay = scene.graft_payload(req)
         c = time.perf_counter()
         rep = tr.gc(tick, 30)
+        marks[2].record(stream)
         d = time.perf_counter()
         grep = tr.graft_generate(tick, scene) if device_generate else tr.graft(tick, rec, pay)
+        marks[3].record(stream)
         e = time.perf_counter()
         if device_generate:
             n_req = tr.stats()["child_requests"]  # the trace's request count (kept until the next trace)
@@ -427,6 +436,12 @@ def _stream_run(st, scene, tree, cams, dev, device_generate):
         totals["pruned_groups"] += rep["pruned"]
         totals["freed_groups"] += rep["freed"]
     loop_s = time.perf_counter() - t_loop
+    torch.cuda.synchronize(dev)
+    gpu = {"trace": 0.0, "gc": 0.0, "graft": 0.0}
+    for m in ev:
+        gpu["trace"] += m[0].elapsed_time(m[1])
+        gpu["gc"] += m[1].elapsed_time(m[2])
+        gpu["graft"] += m[2].elapsed_time(m[3])
     usage = tr.read_usage(budget)
     resident = int(((usage["tick"] >= 1) & (usage["tick"] <= 65533)).sum())
     tr.close()
@@ -434,6 +449,7 @@ def _stream_run(st, scene, tree, cams, dev, device_generate):
     return {"frames_per_s": frames / loop_s, "ms_per_frame": 1000 * loop_s / frames,
             "mrays_s_with_updates": frames * n / loop_s / 1e6,
             "ms_per_frame_by_phase": {k: 1000 * v / frames for k, v in phase.items()},
+            "gpu_ms_per_frame_by_phase": {k: v / frames for k, v in gpu.items()},
             "totals": totals, "resident_groups_end": resident}
 
 
@@ -457,7 +473,8 @@ def stream_workload(torch, dev, args):
            "budget_groups": 1 << 22, "stale_frames": 30, "request_cap": 1 << 16, "setup_s": setup_s,
            "graft_generation": "device (svo_graft_generate)"}
     out.update(on_device)
-    out["host_generation"] = {k: on_host[k] for k in ("ms_per_frame", "ms_per_frame_by_phase", "totals")}
+    out["host_generation"] = {k: on_host[k] for k in ("ms_per_frame", "ms_per_frame_by_phase",
+                                                       "gpu_ms_per_frame_by_phase", "totals")}
     # A 1080p frame raises ~2M child requests against the 65,536-entry queue; which
     # of them are stored depends on the order of the queue's atomics, so two runs
     # of either path diverge (below the cap both paths give the same tree).
