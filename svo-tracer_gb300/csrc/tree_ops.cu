@@ -76,17 +76,41 @@ __global__ void k_reach_seed(TreeView t, uint32_t *reach, uint32_t *parent_min, 
 }
 
 // One breadth-first level: every node of every frontier group marks its child group.
+// Visits one child link of the walk: marks the child group reached and appends
+// it to the next frontier the first time.
+__device__ __forceinline__ uint32_t reach_child(const TreeView &t, uint32_t node, uint32_t c, uint32_t *parent_min) {
+  if (c == kNone || (c & 7u)) return kNone;
+  const uint32_t h = c >> 3;
+  if (h >= t.n_groups || dense_real(t, h)) return kNone;
+  if (parent_min) atomicMin(parent_min + h, node);
+  return h;
+}
+
+// One level of the walk: one node per thread (loads coalesced across the warp),
+// each thread taking up to four nodes a grid apart whose loads and atomics are
+// issued together (the walk is bound by the latency of these dependent loads
+// and atomics, not by bandwidth).
 __global__ void k_reach_expand(TreeView t, const uint32_t *frontier, const uint32_t *n_in, uint32_t *next,
                                uint32_t *n_out, uint32_t *reach, uint32_t *parent_min) {
-  uint64_t total = 8ull * *n_in;
-  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < total; i += (uint64_t)gridDim.x * blockDim.x) {
-    uint32_t node = frontier[i >> 3] * 8u + (uint32_t)(i & 7);
-    uint32_t c = t.blocks[node].child;
-    if (c == kNone || (c & 7u)) continue;
-    uint32_t h = c >> 3;
-    if (h >= t.n_groups || dense_real(t, h)) continue;
-    if (parent_min) atomicMin(parent_min + h, node);
-    if (atomicExch(reach + h, 1u) == 0u) append(next, n_out, h);
+  constexpr int kU = 4;
+  const uint64_t total = 8ull * *n_in;
+  const uint64_t threads = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t base = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; base < total; base += kU * threads) {
+    uint32_t node[kU], h[kU], first[kU];
+#pragma unroll
+    for (int u = 0; u < kU; u++) {
+      const uint64_t i = base + u * threads;
+      node[u] = i < total ? frontier[i >> 3] * 8u + (uint32_t)(i & 7) : kNone;
+    }
+#pragma unroll
+    for (int u = 0; u < kU; u++) h[u] = node[u] != kNone ? t.blocks[node[u]].child : kNone;
+#pragma unroll
+    for (int u = 0; u < kU; u++) h[u] = node[u] != kNone ? reach_child(t, node[u], h[u], parent_min) : kNone;
+#pragma unroll
+    for (int u = 0; u < kU; u++) first[u] = h[u] != kNone ? atomicExch(reach + h[u], 1u) : 1u;
+#pragma unroll
+    for (int u = 0; u < kU; u++)
+      if (first[u] == 0u) append(next, n_out, h[u]);
   }
 }
 
