@@ -8,15 +8,16 @@
 // persistent launch:
 //
 //  * The ray queue is the batch's ray index space with a device-side head
-//    counter. A persistent grid of threads takes rays from it: whenever a
+//    counter, and a persistent grid takes rays from it. Warp batches (the
+//    default): a warp claims 32 consecutive slots, one pixel tile of a tiled
+//    view, traces them to the end and claims again; the coherence of a tile
+//    is worth more than keeping every lane busy. Lane refills: whenever a
 //    thread finishes a ray it claims the next one, the threads of a warp that
 //    need rays at the same moment sharing one atomicAdd (coalesced group,
-//    `ray_chunk` rays per thread). A thread runs up to `cadence` steps of its
-//    ray per pass, so the rays of a warp that finish within the same window are
-//    retired and replaced together. No step depends on the warp staying
-//    converged, so a lane leaves the loop as soon as the queue is drained.
-//    Ray state stays in registers, so the reference's per-step reload of
-//    ~74 B of SoA state disappears.
+//    `ray_chunk` rays per thread), and rays are retired and replaced every
+//    `cadence` steps. No step depends on the warp staying converged. Ray
+//    state stays in registers, so the reference's per-step reload of ~74 B of
+//    SoA state disappears.
 //  * Each step is runBaseTrace or runBlockTrace for one ray. The reference
 //    re-walks the block tree from level B+2 at every block step
 //    (getBlockAddress, wavefront.cl:296-304); here each lane keeps the node
