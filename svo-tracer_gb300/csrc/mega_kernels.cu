@@ -31,7 +31,9 @@
 #include <cstdint>
 
 #include "mega_internal.h"
+#ifndef SVO_CVT_INTEGER
 #define SVO_CVT_INTEGER 1  // integer ulong_to_float: faster in this kernel mix
+#endif
 #include "trace_core.cuh"
 
 namespace svo {
