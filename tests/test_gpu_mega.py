@@ -183,3 +183,20 @@ def test_step_limit_matches_oracle(tracer, terrain):
     assert np.array_equal(got.rgba.reshape(-1, 4).view(np.uint32), ref["rgba"].view(np.uint32))
     assert np.array_equal(got.hit_index.reshape(-1), ref["hit_index"])
     assert n == ref["n_requests"]
+
+
+@pytest.mark.parametrize("size", [(1, 1), (1, 37), (37, 1), (5, 3), (130, 2)])
+def test_degenerate_view_sizes(tracer, terrain, size):
+    """Single pixels, single rows and columns, and views narrower than one warp tile:
+    the padded lanes of each tile draw nothing and the real pixels match the oracle."""
+    w, h = size
+    v = st.look_at((0.15, 0.2, 0.1), (0.55, 0.5, 0.8), w, h, 50.0, Tick=6)
+    check(tracer, terrain, v)
+
+
+def test_view_away_from_the_cube(tracer, sphere):
+    """Every primary cone misses the volume: nothing is requested, no cone fan is
+    spawned, and every pixel is what the oracle draws for a miss."""
+    v = st.look_at((1.6, 0.5, 0.5), (3.0, 0.5, 0.5), 24, 16, 40.0, Tick=5)
+    got, stats, ref = check(tracer, sphere, v)
+    assert stats["surfaces"] == 0 and stats["cones"] == 0 and ref["n_requests"] == 0

@@ -151,7 +151,7 @@ def test_batch_equals_single_views_and_graph(tracer):
             assert np.array_equal(getattr(s, k), getattr(b, k))
             assert np.array_equal(getattr(s, k), getattr(g1, k))
             assert np.array_equal(getattr(s, k), getattr(g2, k))
-    for c, s in zip(cams[:3], singles[:3]):
+    for c, s in zip(cams, singles):  # includes the 1x1 and 200x3 views
         want = po.trace_view(tree, c)
         assert_same(s, want)
 
