@@ -185,7 +185,8 @@ typedef struct svo_trace_config {
   int32_t max_hits;     /* differentiable forward: LOD hits composited per ray (1..1024) */
   int32_t schedule;     /* SVO_SCHEDULE_LANE or SVO_SCHEDULE_WARP */
   int32_t mega_band_tiles; /* megakernel: pixel tiles of 32 per cone band (0: as many as 2^26 cone slots hold) */
-  int32_t _pad;
+  int32_t l2_window;    /* 1: the trace kernel reads the dense level-(B+2) nodes through an L2 persisting
+                           access-policy window, -1: no window */
 } svo_trace_config;
 
 /* Ray scheduling of the persistent trace kernel. LANE: each thread claims rays

@@ -145,6 +145,16 @@ struct Context {
   svo_mega_stats last_mega{};
   uint64_t n_free = 0, free_used = 0, n_pruned = 0, n_freed = 0, n_claimed = 0;
   bool free_valid = false;
+  // L2 set-aside for persisting accesses taken by this context (restored on release)
+  bool l2_limit_set = false;
+  size_t l2_limit_prev = 0;
+  void release_l2_set_aside() {
+    if (!l2_limit_set) return;
+    cudaCtxResetPersistingL2Cache();
+    cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, l2_limit_prev);
+    cudaGetLastError();
+    l2_limit_set = false;
+  }
   // graph cache for svo_trace_batch_graph
   cudaGraphExec_t graph_exec = nullptr;
   std::vector<uint32_t> graph_key;
@@ -152,6 +162,7 @@ struct Context {
   ~Context() {
     if (device >= 0) cudaSetDevice(device);
     if (graph_exec) cudaGraphExecDestroy(graph_exec);
+    release_l2_set_aside();
     if (staged) cudaEventDestroy(staged);
     bases.release();
     blocks.release();

@@ -38,6 +38,7 @@ static svo_trace_config default_config() {
   c.collect_stats = 0;
   c.max_hits = 16;
   c.schedule = SVO_SCHEDULE_WARP;  // 13% faster than lane refills on the 1080p terrain frame
+  c.l2_window = -1;
   return c;
 }
 
@@ -167,6 +168,36 @@ svo_status stage_views(Context &c, const svo_trace_input *in, int32_t n, const s
   return SVO_OK;
 }
 
+// The L2 persisting window of a trace launch: the dense level-(B+2) nodes at the
+// head of the node array, which every ray entering a block reads first. The
+// context's persisting set-aside is raised to the window's size the first time
+// (within the device's limits) and given back when the window is switched off
+// or the context is destroyed.
+static void plan_l2_window(Context &c, TraceLaunch &a) {
+  if (c.cfg.l2_window <= 0 || !c.blocks.p || !c.n_blocks) return;
+  int max_persist = 0, max_window = 0;
+  if (cudaDeviceGetAttribute(&max_persist, cudaDevAttrMaxPersistingL2CacheSize, c.device) != cudaSuccess ||
+      cudaDeviceGetAttribute(&max_window, cudaDevAttrMaxAccessPolicyWindowSize, c.device) != cudaSuccess) {
+    cudaGetLastError();
+    return;
+  }
+  const size_t dense = std::min(c.n_blocks, (size_t)1 << (3 * (c.base_depth + 2))) * sizeof(svo_block);
+  const size_t bytes = std::min(dense, (size_t)std::min(max_persist, max_window));
+  if (!bytes) return;
+  if (!c.l2_limit_set) {
+    size_t prev = 0;
+    if (cudaDeviceGetLimit(&prev, cudaLimitPersistingL2CacheSize) != cudaSuccess ||
+        (prev < bytes && cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, bytes) != cudaSuccess)) {
+      cudaGetLastError();
+      return;
+    }
+    c.l2_limit_prev = prev;
+    c.l2_limit_set = true;
+  }
+  a.l2_base = c.blocks.p;
+  a.l2_bytes = bytes;
+}
+
 svo_status prepare_launch(Context &c, int32_t n_views, uint32_t total_rays, TraceLaunch &a, bool stats) {
   a = TraceLaunch{};
   a.bases = c.bases.p;
@@ -194,6 +225,7 @@ svo_status prepare_launch(Context &c, int32_t n_views, uint32_t total_rays, Trac
   a.block_size = c.cfg.block_size;
   a.schedule = c.cfg.schedule;
   a.path_levels = std::max(1, c.tree_depth - (int)c.base_depth - 1);
+  plan_l2_window(c, a);
   int occ = c.cfg.ctas_per_sm > 0 ? c.cfg.ctas_per_sm : trace_occupancy(a, stats);
   if (occ <= 0) return fail(SVO_ERR_NO_DEVICE, "svo_trace: the trace kernel cannot be resident (no sm_103a image?)");
   long want = (long)occ * c.sm_count;
@@ -440,12 +472,14 @@ SVO_API svo_status svo_set_trace_config(void *ctx, const svo_trace_config *cfg) 
   if (n.max_steps == 0) n.max_steps = d.max_steps;
   if (n.max_hits == 0) n.max_hits = d.max_hits;
   if (n.schedule == 0) n.schedule = d.schedule;
+  if (n.l2_window == 0) n.l2_window = d.l2_window;
   if (n.block_size % 32 || n.block_size < 32 || n.block_size > 256)
     return fail(SVO_ERR_INVALID_ARGUMENT, "svo_set_trace_config: block_size must be a multiple of 32 in 32..256");
   if (n.ray_chunk < 1 || n.ray_chunk > 64 || n.cadence < 1 || n.cadence > 1024 || n.max_steps < 1 || n.ctas_per_sm < 0 ||
       n.collect_stats < 0 || n.collect_stats > 2 || n.max_hits < 1 || n.max_hits > 1024 || n.mega_band_tiles < 0 ||
-      (n.schedule != SVO_SCHEDULE_LANE && n.schedule != SVO_SCHEDULE_WARP))
+      (n.schedule != SVO_SCHEDULE_LANE && n.schedule != SVO_SCHEDULE_WARP) || (n.l2_window != 1 && n.l2_window != -1))
     return fail(SVO_ERR_INVALID_ARGUMENT, "svo_set_trace_config: value out of range");
+  if (n.l2_window < 0) c.release_l2_set_aside();
   c.cfg = n;
   if (c.graph_exec) cudaGraphExecDestroy(c.graph_exec);
   c.graph_exec = nullptr;

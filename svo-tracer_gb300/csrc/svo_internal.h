@@ -83,6 +83,9 @@ struct TraceLaunch {
   int32_t schedule;  // SVO_SCHEDULE_LANE / SVO_SCHEDULE_WARP
   int32_t grid;
   int32_t path_levels;
+  // L2 persisting access-policy window of the launch (host side only; 0 bytes: none)
+  const void *l2_base;
+  size_t l2_bytes;
 };
 
 // Launches the persistent trace kernel on `stream`.

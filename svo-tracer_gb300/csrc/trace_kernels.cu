@@ -261,8 +261,26 @@ static cudaError_t launch_one(const TraceLaunch &a, size_t smem, cudaStream_t st
   auto k = trace_kernel<S, M, W>;
   cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  k<<<a.grid, a.block_size, smem, stream>>>(a);
-  return cudaGetLastError();
+  if (!a.l2_bytes) {
+    k<<<a.grid, a.block_size, smem, stream>>>(a);
+    return cudaGetLastError();
+  }
+  // the launch's node reads in [l2_base, l2_base + l2_bytes) persist in L2
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeAccessPolicyWindow;
+  attr[0].val.accessPolicyWindow.base_ptr = const_cast<void *>(a.l2_base);
+  attr[0].val.accessPolicyWindow.num_bytes = a.l2_bytes;
+  attr[0].val.accessPolicyWindow.hitRatio = 1.0f;
+  attr[0].val.accessPolicyWindow.hitProp = cudaAccessPropertyPersisting;
+  attr[0].val.accessPolicyWindow.missProp = cudaAccessPropertyStreaming;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)a.grid);
+  cfg.blockDim = dim3((unsigned)a.block_size);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = stream;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, k, a);
 }
 
 template <bool W>

@@ -160,7 +160,8 @@ def test_batch_equals_single_views_and_graph(tracer):
                                  dict(block_size=256, ray_chunk=8, cadence=32),
                                  dict(block_size=64, ray_chunk=3, cadence=5, ctas_per_sm=1),
                                  dict(block_size=128, schedule=st.SCHEDULE_WARP),
-                                 dict(block_size=64, schedule=st.SCHEDULE_WARP, ctas_per_sm=1)])
+                                 dict(block_size=64, schedule=st.SCHEDULE_WARP, ctas_per_sm=1),
+                                 dict(schedule=st.SCHEDULE_WARP, l2_window=1)])
 def test_launch_shapes_do_not_change_results(tracer, cfg):
     tree = st.TreeBuilder(st.SCENE_SPHERE, seed=6).BuildTree(4, 8)
     cam = st.look_at((1.1, 0.2, 0.9), (0.5, 0.5, 0.5), 120, 90, 60.0)
@@ -169,7 +170,8 @@ def test_launch_shapes_do_not_change_results(tracer, cfg):
         tracer.upload(tree)
         got = tracer.trace(cam)
     finally:
-        tracer.set_config(block_size=256, ray_chunk=1, cadence=16, ctas_per_sm=0, schedule=st.SCHEDULE_LANE)
+        tracer.set_config(block_size=256, ray_chunk=1, cadence=16, ctas_per_sm=0, schedule=st.SCHEDULE_LANE,
+                          l2_window=-1)
     assert_same(got, po.trace_view(tree, cam))
 
 
@@ -251,6 +253,8 @@ def test_errors(tracer):
         tracer.set_config(block_size=100)
     with pytest.raises(st.SvoError):
         tracer.set_config(schedule=3)
+    with pytest.raises(st.SvoError):
+        tracer.set_config(l2_window=2)
     assert lib is not None
 
 
