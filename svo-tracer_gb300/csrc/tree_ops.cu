@@ -849,6 +849,30 @@ SVO_API svo_status svo_read_gc_lists(void *ctx, uint32_t *pruned, size_t cap_pru
   return SVO_OK;
 }
 
+// Node levels that a graft record's payload hangs below its target: the longest
+// chain of child groups from the record's group 0 (links outside the record's
+// groups are dropped, as k_graft_nodes drops them); -1 when the links form a cycle.
+static int payload_levels(const svo_block *payload, uint32_t P, uint32_t G) {
+  std::vector<uint32_t> frontier{0}, next, mark(G, 0);
+  for (uint32_t level = 1; level <= G; level++) {
+    next.clear();
+    for (uint32_t g : frontier)
+      for (uint32_t i = 0; i < 8; i++) {
+        const uint32_t c = payload[P + 8ull * g + i].child;
+        if (c == SVO_NO_CHILD || c < P) continue;
+        const uint32_t rel = c - P;
+        if ((rel & 7u) || rel / 8u >= G) continue;
+        if (mark[rel / 8u] != level + 1) {
+          mark[rel / 8u] = level + 1;
+          next.push_back(rel / 8u);
+        }
+      }
+    if (next.empty()) return (int)level;
+    frontier.swap(next);
+  }
+  return -1;  // a group is still reached after G levels
+}
+
 SVO_API svo_status svo_graft(void *ctx, const svo_update_input *in, const svo_grafting *records, uint32_t n_records,
                              const svo_block *payload, size_t n_payload, const uint64_t *locations,
                              size_t n_locations, svo_graft_report *report) {
@@ -889,6 +913,7 @@ SVO_API svo_status svo_graft(void *ctx, const svo_update_input *in, const svo_gr
   std::set<uint32_t> seen;
   uint64_t q = c.free_used;
   uint64_t n_blocks = (uint64_t)c.n_groups * 8;
+  int deepest = c.tree_depth;  // deepest node level once the applied records are grafted
   for (uint32_t r = 0; r < n_records; r++) {
     uint32_t G = records[r].graft_total_size, P = records[r].graft_data_address;
     if (G == 0 || (P & 7u) || (uint64_t)P + 8ull * G > n_payload) continue;
@@ -898,6 +923,11 @@ SVO_API svo_status svo_graft(void *ctx, const svo_update_input *in, const svo_gr
     if (!seen.insert(target).second)
       return fail(SVO_ERR_INVALID_ARGUMENT, "svo_graft: two records graft onto node " + std::to_string(target));
     svo::GraftRec gr{P, G, (uint32_t)q, target};
+    // the target of a Location record is the node at level max(depth, B+2); a
+    // target given as a node index has no known level
+    const int levels = records[r].depth == 255 ? -1 : payload_levels(payload, P, G);
+    deepest = levels < 0 ? SVO_MAX_TREE_DEPTH
+                         : std::max(deepest, std::max<int>(records[r].depth, c.base_depth + 2) + levels);
     uint32_t rec_index = (uint32_t)recs.size();
     recs.push_back(gr);
     for (uint32_t k = 0; k < G; k++) jobs.push_back(svo::GraftJob{P + 8 * k, rec_index, k});
@@ -932,8 +962,8 @@ SVO_API svo_status svo_graft(void *ctx, const svo_update_input *in, const svo_gr
   }
   c.n_claimed = claimed;
   c.free_used = q;
-  // grafted subtrees can reach below the deepest level seen at upload
-  if (claimed) c.tree_depth = SVO_MAX_TREE_DEPTH;
+  // grafted subtrees can reach below the deepest level seen so far
+  if (claimed) c.tree_depth = std::min(SVO_MAX_TREE_DEPTH, std::max(c.tree_depth, deepest));
   if (report) {
     report->applied = (uint32_t)recs.size();
     report->skipped = n_records - (uint32_t)recs.size();
