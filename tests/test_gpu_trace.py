@@ -156,6 +156,24 @@ def test_batch_equals_single_views_and_graph(tracer):
         assert_same(s, want)
 
 
+def test_l2_window_in_graph_replay(tracer):
+    """A graph captured with the L2 persisting window on replays the same frames."""
+    tree = st.TreeBuilder(st.SCENE_TERRAIN, seed=3).BuildTree(3, 8)
+    cams = [st.look_at((0.2, 0.3, 0.4), (0.5, 0.5, 0.85), w, h, 60.0, Tick=2) for w, h in ((64, 48), (37, 19))]
+    tracer.set_config(collect_stats=0, schedule=st.SCHEDULE_WARP)
+    tracer.upload(tree)
+    want = tracer.trace_batch(cams)
+    tracer.set_config(l2_window=1)
+    try:
+        got = [tracer.trace_batch(cams, graph=True) for _ in range(2)]
+    finally:
+        tracer.set_config(l2_window=-1)
+    for g in got:
+        for a, b in zip(want, g):
+            for k in ("hit_index", "hit_depth", "t", "rgba"):
+                assert np.array_equal(getattr(a, k), getattr(b, k))
+
+
 @pytest.mark.parametrize("cfg", [dict(block_size=128, ray_chunk=1, cadence=1),
                                  dict(block_size=256, ray_chunk=8, cadence=32),
                                  dict(block_size=64, ray_chunk=3, cadence=5, ctas_per_sm=1),
