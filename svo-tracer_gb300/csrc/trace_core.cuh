@@ -74,10 +74,9 @@ __device__ __forceinline__ uint64_t unit_to_ulong(float x) {
 //     boundary is (~w & low) + 1, except for a negative direction in the lowest
 //     cell ((w | low) == kAll), where the reference's subtraction wraps and its
 //     comparison returns v = ~w;
-//   traverseChunk's move and clamp (:440-497): w += d, and a wrap to 0 becomes
-//     kAll (v + d wrapping to 0 becomes ULONG_MAX; v - d wrapping to
-//     ULONG_MAX becomes 0);
-//   leaving (:433-437): some w == kAll;
+//   traverseChunk's move and clamp (:440-497): w += d, and a sum of 0 becomes
+//     kAll (v + d giving 0 becomes ULONG_MAX; v - d giving ULONG_MAX becomes 0);
+//   leaving (:433-437): some w == kAll, so after a move: some sum is 0 or kAll;
 //   comparePositions (:413-426): the bits that flipped against the travel
 //     direction are w_before & ~w_after.
 // Real coordinates (octants, cell indices, float conversions, requests) are
@@ -89,9 +88,11 @@ __device__ __forceinline__ uint64_t boundary_distance(uint64_t w, uint64_t low, 
   return (!positive && (w | low) == kAll) ? ~w : d;
 }
 
-__device__ __forceinline__ uint64_t step_travel(uint64_t w, uint64_t d) {
-  const uint64_t n = w + d;
-  return n == 0 ? kAll : n;
+// A coordinate after a move that leaves the cube: w == 0 (the reference clamps it
+// to kAll) or w == kAll.
+__device__ __forceinline__ bool leaves_cube(uint64_t w) {
+  const uint32_t lo = (uint32_t)w, hi = (uint32_t)(w >> 32);
+  return lo == hi && hi + 1u <= 1u;
 }
 
 __device__ __forceinline__ uint32_t spread3(uint32_t v) {
@@ -164,8 +165,11 @@ __device__ __forceinline__ uint4 load_node(const uint4 *blocks, uint32_t n_block
   return __ldg(blocks + addr);
 }
 
-// traverseChunk (wavefront.cl:440-497) without the trailing setConeDepth.
-__device__ __forceinline__ void traverse(Ray &r, int depth) {
+// traverseChunk (wavefront.cl:440-497) without the trailing setConeDepth,
+// returning leaving (:433-437) of the new location. A sum that the reference
+// clamps (0 to kAll) always leaves, so the clamp is left to the caller's
+// leaving branch.
+__device__ __forceinline__ bool traverse(Ray &r, int depth) {
   const uint64_t low = kAll >> (depth + 1);
   uint64_t d0 = boundary_distance(r.wx, low, r.sx);
   uint64_t d1 = boundary_distance(r.wy, low, r.sy);
@@ -181,9 +185,10 @@ __device__ __forceinline__ void traverse(Ray &r, int depth) {
   if (ax != 0) d0 = unit_to_ulong(__fmul_rn(__fmul_rn(r.dx, inv), u));
   if (ax != 1) d1 = unit_to_ulong(__fmul_rn(__fmul_rn(r.dy, inv), u));
   if (ax != 2) d2 = unit_to_ulong(__fmul_rn(__fmul_rn(r.dz, inv), u));
-  r.wx = step_travel(r.wx, d0);
-  r.wy = step_travel(r.wy, d1);
-  r.wz = step_travel(r.wz, d2);
+  r.wx += d0;
+  r.wy += d1;
+  r.wz += d2;
+  return leaves_cube(r.wx) | leaves_cube(r.wy) | leaves_cube(r.wz);
 }
 
 // comparePositions (wavefront.cl:413-426): the loop pops one level for every
@@ -196,8 +201,6 @@ __device__ __forceinline__ int pop_depth(const Ray &r, int depth, uint64_t px, u
   int ones = __ffsll((long long)run) - 1;
   return ones < depth ? depth - ones : 1;
 }
-
-__device__ __forceinline__ bool leaving(const Ray &r) { return r.wx == kAll || r.wy == kAll || r.wz == kAll; }
 
 // coneSize (wavefront.cl:387-391) at the distance setConeDepth uses (:394-399).
 __device__ __forceinline__ float cone_at(const Ray &r, float dof0, float dof1) {
@@ -466,8 +469,13 @@ __device__ __forceinline__ bool setup_ray(const TraceLaunch &a, const ViewParams
 __device__ __forceinline__ int advance(const TraceLaunch &a, const uint4 *blocks, int B, Ray &r, Walk &w) {
   const bool block = r.depth > B;
   uint64_t px = r.wx, py = r.wy, pz = r.wz;
-  traverse(r, r.depth);
-  if (leaving(r)) return kStepBackground;
+  if (traverse(r, r.depth)) {
+    // traverseChunk's clamp; the megakernel starts cones at a sky primary's exit
+    if (r.wx == 0) r.wx = kAll;
+    if (r.wy == 0) r.wy = kAll;
+    if (r.wz == 0) r.wz = kAll;
+    return kStepBackground;
+  }
   int nd = pop_depth(r, r.depth, px, py, pz);
   if (block && nd >= B + 2 && (((px ^ r.wx) | (py ^ r.wy) | (pz ^ r.wz)) >> (64 - nd)) != 0) {
     uint32_t n = cell_index(B + 2, r.wx, r.wy, r.wz, r.flip);
