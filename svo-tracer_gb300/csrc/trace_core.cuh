@@ -182,9 +182,14 @@ __device__ __forceinline__ bool traverse(Ray &r, int depth) {
   float inv = ax == 0 ? r.ix : (ax == 1 ? r.iy : r.iz);
   // ulongToFloat of the chosen distance: its float conversion times 2^-64 (exact)
   float u = __fmul_rn(ax == 0 ? f0 : (ax == 1 ? f1 : f2), 0x1p-64f);
-  if (ax != 0) d0 = unit_to_ulong(__fmul_rn(__fmul_rn(r.dx, inv), u));
-  if (ax != 1) d1 = unit_to_ulong(__fmul_rn(__fmul_rn(r.dy, inv), u));
-  if (ax != 2) d2 = unit_to_ulong(__fmul_rn(__fmul_rn(r.dz, inv), u));
+  // the two other axes' moves, exactly two conversions per lane: A is x unless x
+  // was chosen (then y), B is z unless z was chosen (then y)
+  const bool c0 = ax == 0, c2 = ax == 2;
+  const uint64_t eA = unit_to_ulong(__fmul_rn(__fmul_rn(c0 ? r.dy : r.dx, inv), u));
+  const uint64_t eB = unit_to_ulong(__fmul_rn(__fmul_rn(c2 ? r.dy : r.dz, inv), u));
+  d1 = c0 ? eA : (c2 ? eB : d1);
+  if (!c0) d0 = eA;
+  if (!c2) d2 = eB;
   r.wx += d0;
   r.wy += d1;
   r.wz += d2;
