@@ -59,10 +59,9 @@ __device__ __forceinline__ float ulong_to_unit(uint64_t x) { return __fmul_rn(ul
 // floatToUlong (wavefront.cl:200-207); out-of-range products saturate, NaN -> 0.
 __device__ __forceinline__ uint64_t unit_to_ulong(float x) {
   if (x >= 0.999999911f) return kAll;
-  float v = __fmul_rn(fabsf(x), 0x1p64f);
-  if (v != v) return 0;
-  if (!(v < 0x1p64f)) return kAll;
-  return __float2ull_rz(v);
+  const float v = __fmul_rn(fabsf(x), 0x1p64f);
+  // the conversion clamps v >= 2^64 to kAll, but turns NaN into 2^63
+  return v != v ? 0 : __float2ull_rz(v);
 }
 
 // Locations in travel space. A ray keeps each 64-bit fixed-point coordinate v
@@ -123,10 +122,14 @@ __device__ __forceinline__ uint32_t cell_index(int depth, uint64_t wx, uint64_t 
   return s_spread3[cx] | (s_spread3[cy] << 1) | (s_spread3[cz] << 2);
 }
 
-// chunkPosition (wavefront.cl:428-430) from travel-space coordinates.
+// Levels 1..31 are bits 63..32 of a coordinate, so the stepping helpers below
+// read only the high words (trees are at most SVO_MAX_TREE_DEPTH = 24 deep).
+__device__ __forceinline__ uint32_t hi32(uint64_t w) { return (uint32_t)(w >> 32); }
+
+// chunkPosition (wavefront.cl:428-430) from travel-space coordinates, depth 0..31.
 __device__ __forceinline__ uint32_t octant(int depth, uint64_t wx, uint64_t wy, uint64_t wz, uint32_t flip) {
-  int s = 63 - depth;
-  return (uint32_t)(((wx >> s) & 1) | (((wy >> s) & 1) << 1) | (((wz >> s) & 1) << 2)) ^ flip;
+  const uint32_t s = 31u - (uint32_t)depth;
+  return (((hi32(wx) >> s) & 1u) | (((hi32(wy) >> s) & 1u) << 1) | (((hi32(wz) >> s) & 1u) << 2)) ^ flip;
 }
 
 __device__ __forceinline__ float pow2_neg(int k) { return __int_as_float((127 - k) << 23); }
@@ -201,9 +204,9 @@ __device__ __forceinline__ bool traverse(Ray &r, int depth) {
 // against the travel direction on some axis; it stops at level 1.
 // px, py, pz: the travel-space location before the step.
 __device__ __forceinline__ int pop_depth(const Ray &r, int depth, uint64_t px, uint64_t py, uint64_t pz) {
-  uint64_t m = (px & ~r.wx) | (py & ~r.wy) | (pz & ~r.wz);
-  uint64_t run = ~(m >> (63 - depth));
-  int ones = __ffsll((long long)run) - 1;
+  const uint32_t m = (hi32(px) & ~hi32(r.wx)) | (hi32(py) & ~hi32(r.wy)) | (hi32(pz) & ~hi32(r.wz));
+  const uint32_t run = ~(m >> (31 - depth));  // bit k: level depth - k kept its octant bit
+  const int ones = run ? __ffs((int)run) - 1 : 32;
   return ones < depth ? depth - ones : 1;
 }
 
@@ -482,7 +485,7 @@ __device__ __forceinline__ int advance(const TraceLaunch &a, const uint4 *blocks
     return kStepBackground;
   }
   int nd = pop_depth(r, r.depth, px, py, pz);
-  if (block && nd >= B + 2 && (((px ^ r.wx) | (py ^ r.wy) | (pz ^ r.wz)) >> (64 - nd)) != 0) {
+  if (block && nd >= B + 2 && (((hi32(px) ^ hi32(r.wx)) | (hi32(py) ^ hi32(r.wy)) | (hi32(pz) ^ hi32(r.wz))) >> (32 - nd)) != 0) {
     uint32_t n = cell_index(B + 2, r.wx, r.wy, r.wz, r.flip);
     w.path[0] = n;
     for (int d = B + 2; d < nd; d++) {
