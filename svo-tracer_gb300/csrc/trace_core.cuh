@@ -82,9 +82,13 @@ __device__ __forceinline__ uint64_t unit_to_ulong(float x) {
 // w ^ dir_mask.
 __device__ __forceinline__ uint64_t dir_mask(bool positive) { return positive ? 0ull : kAll; }
 
-__device__ __forceinline__ uint64_t boundary_distance(uint64_t w, uint64_t low, bool positive) {
-  const uint64_t d = (~w & low) + 1;
-  return (!positive && (w | low) == kAll) ? ~w : d;
+// low = kAll >> (d + 1) for a level d below 32: its low word is all ones, so
+// only its high word low_hi is passed. In the negative-direction case ~w has no
+// bit above low, so ~w & low is ~w itself.
+__device__ __forceinline__ uint64_t boundary_distance(uint64_t w, uint32_t low_hi, bool positive) {
+  const uint32_t wh = (uint32_t)(w >> 32);
+  const uint64_t t = ((uint64_t)(~wh & low_hi) << 32) | (uint32_t)~(uint32_t)w;  // ~w & low
+  return t + ((!positive && (wh | low_hi) == ~0u) ? 0u : 1u);
 }
 
 // A coordinate after a move that leaves the cube: w == 0 (the reference clamps it
@@ -173,10 +177,10 @@ __device__ __forceinline__ uint4 load_node(const uint4 *blocks, uint32_t n_block
 // clamps (0 to kAll) always leaves, so the clamp is left to the caller's
 // leaving branch.
 __device__ __forceinline__ bool traverse(Ray &r, int depth) {
-  const uint64_t low = kAll >> (depth + 1);
-  uint64_t d0 = boundary_distance(r.wx, low, r.sx);
-  uint64_t d1 = boundary_distance(r.wy, low, r.sy);
-  uint64_t d2 = boundary_distance(r.wz, low, r.sz);
+  const uint32_t low_hi = 0xffffffffu >> (depth + 1);  // kAll >> (depth + 1), depth < 31
+  uint64_t d0 = boundary_distance(r.wx, low_hi, r.sx);
+  uint64_t d1 = boundary_distance(r.wy, low_hi, r.sy);
+  uint64_t d2 = boundary_distance(r.wz, low_hi, r.sz);
   const float f0 = ulong_to_float(d0), f1 = ulong_to_float(d1), f2 = ulong_to_float(d2);
   float a0 = fabsf(__fmul_rn(f0, r.ix));
   float a1 = fabsf(__fmul_rn(f1, r.iy));
