@@ -50,7 +50,7 @@ namespace svo {
 namespace {
 
 #ifndef SVO_TRACE_MIN_CTAS
-#define SVO_TRACE_MIN_CTAS 5  // 48 registers, no spills (4: 1% slower on the 1080p frame, 6: spills)
+#define SVO_TRACE_MIN_CTAS 4  // 57 registers, no spills (5: 48 registers with a spill, 1.4% slower on the 1080p frame)
 #endif
 template <bool kStats, bool kSmemBases, bool kWarpBatch>
 __global__ void __launch_bounds__(256, SVO_TRACE_MIN_CTAS) trace_kernel(const TraceLaunch a) {
