@@ -151,6 +151,7 @@ struct Ray {
   bool sx, sy, sz;
   uint32_t flip;  // bit k: axis k travels towards 0
   bool fresh;     // megakernel primary: no move yet, so kernel.cl's ConeDepth is still 0
+  float cone;     // coneSize at the current location, < 0 until computed there
 };
 
 __device__ __forceinline__ uint64_t loc_x(const Ray &r) { return r.wx ^ dir_mask(r.sx); }
@@ -160,6 +161,7 @@ __device__ __forceinline__ void set_loc(Ray &r, uint64_t x, uint64_t y, uint64_t
   r.wx = x ^ dir_mask(r.sx);
   r.wy = y ^ dir_mask(r.sy);
   r.wz = z ^ dir_mask(r.sz);
+  r.cone = -1.0f;
 }
 
 struct Node {
@@ -365,8 +367,13 @@ __device__ __forceinline__ int probe(const TraceLaunch &a, const ViewParams &v, 
     return kStepOn;
   }
   // geometry below a node: the cone LOD decision (ConeDepth = -half_log2(c));
-  // ConeDepth 0 compares like c = 1
-  float c = (kMega && r.fresh) ? 1.0f : cone_at(r, v.dof[0], v.dof[1]);
+  // ConeDepth 0 compares like c = 1. Descents and ascents keep the location, so
+  // the cone size computed there is reused until the next move.
+  float c = 1.0f;
+  if (!(kMega && r.fresh)) {
+    if (r.cone < 0.0f) r.cone = cone_at(r, v.dof[0], v.dof[1]);
+    c = r.cone;
+  }
   if (c > pow2_neg(B + 2)) {
     r.depth = B + 2;
     return kStepHit;
@@ -481,6 +488,7 @@ __device__ __forceinline__ bool setup_ray(const TraceLaunch &a, const ViewParams
 __device__ __forceinline__ int advance(const TraceLaunch &a, const uint4 *blocks, int B, Ray &r, Walk &w) {
   const bool block = r.depth > B;
   uint64_t px = r.wx, py = r.wy, pz = r.wz;
+  r.cone = -1.0f;
   if (traverse(r, r.depth)) {
     // traverseChunk's clamp; the megakernel starts cones at a sky primary's exit
     if (r.wx == 0) r.wx = kAll;
