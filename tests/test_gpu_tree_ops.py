@@ -1,6 +1,8 @@
 """Tree-update kernels (usage initialisation, block GC, grafting, pruning) against the
 oracle, through the C ABI. Every set the specification defines (pruned, freed,
 free-list and claimed groups) and the whole block and usage arrays must be bit-exact."""
+import dataclasses
+
 import numpy as np
 import pytest
 
@@ -153,6 +155,53 @@ def test_graft_location_targets_and_budget(tracer):
     assert grep["applied"] == int(applied.sum()) > 0
     assert np.array_equal(tracer.graft_claims(grep["claimed"]), o_claims)
     assert_state(tracer, oracle, "graft")
+
+
+def test_location_grafts_deepen_the_tree_for_trace_and_gc(tracer):
+    """Grafts addressed only by Location: the library records the tree's new depth
+    from the records' levels and payloads, and the next trace and GC reach the
+    grafted levels exactly as the oracle does."""
+    scene = st.Scene(st.SCENE_TERRAIN, seed=5, base_depth=3, depth=9)
+    tree = scene.build_tree(7)
+    budget = (len(tree.Blocks) + 7) // 8 + (1 << 14)
+    tracer.upload(tree, block_budget=budget * 8)
+    tracer.init_usage_tree(1)
+    oracle = po.TreeState(tree, budget)
+    oracle.init_usage_tree(1)
+    # close enough to the terrain that the cones want two levels below the tree
+    cam = st.look_at((0.4, 0.4, 0.7), (0.6, 0.6, 0.9), 96, 54, 40.0, Tick=1, MaxChildRequestId=1 << 16)
+    tracer.trace(cam)
+    req, n = tracer.read_child_requests()
+    assert 0 < n <= 1 << 16
+    rec, pay = scene.graft_payload(req)
+    uniq = {}
+    for r in po.sort_requests(req):
+        uniq.setdefault(int(r["address"]), r)
+    locs = []
+    for r in rec:
+        q = uniq[int(r["graft_address"])]
+        r["depth"] = q["depth"]
+        r["graft_address"] = len(locs) // 3
+        locs.extend(int(v) for v in q["location"])
+    locs = np.array(locs, np.uint64)
+    tracer.gc(2, 100)
+    oracle.gc(2, 100)
+    grep = tracer.graft(2, rec, pay, locs)
+    o_claims, applied = oracle.graft(2, rec, pay, locs)
+    assert grep["applied"] == int(applied.sum()) > 0
+    assert np.array_equal(tracer.graft_claims(grep["claimed"]), o_claims)
+    assert_state(tracer, oracle, "graft")
+    cam3 = dataclasses.replace(cam, Tick=3)
+    got = tracer.trace(cam3)
+    want = po.trace_view(oracle.as_octree(), cam3, usage=oracle.usage)
+    assert int(want["hit_depth"].max()) == 9  # the grafted grandchildren are hit
+    for k in ("hit_index", "hit_depth", "t", "rgba"):
+        assert np.array_equal(getattr(got, k), want[k]), k
+    rep = tracer.gc(3, 100)
+    g_pruned, g_freed, g_free = tracer.gc_lists(rep["pruned"], rep["freed"], rep["free"])
+    o_pruned, o_freed, o_free = oracle.gc(3, 100)
+    assert np.array_equal(g_freed, o_freed) and np.array_equal(g_free, o_free)
+    assert_state(tracer, oracle, "gc after the grafts")
 
 
 @pytest.mark.parametrize("initial,extra_groups", [(7, 1 << 14), (6, 40)], ids=["roomy", "budget_runs_out"])
