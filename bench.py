@@ -15,6 +15,7 @@ getBlockAddress + 2 B per base chunk read + 25 B of per-pixel output).
 from __future__ import annotations
 
 import argparse
+import hashlib
 import json
 import os
 import subprocess
@@ -385,6 +386,7 @@ def _stream_run(st, scene, tree, cams, dev, device_generate):
     tr = st.Tracer(dev)
     stream = torch.cuda.Stream(device=dev)  # GPU time of each phase by events on the context's stream
     tr.set_stream(stream.cuda_stream)
+    tr.set_config(request_order=st.REQUESTS_PIXEL)  # the kept requests do not depend on timing
     tr.upload(tree, block_budget=budget * 8)
     tr.init_usage_tree(1)
     n = WIDTH * HEIGHT
@@ -444,9 +446,12 @@ def _stream_run(st, scene, tree, cams, dev, device_generate):
         gpu["graft"] += m[2].elapsed_time(m[3])
     usage = tr.read_usage(budget)
     resident = int(((usage["tick"] >= 1) & (usage["tick"] <= 65533)).sum())
+    digest = hashlib.sha256()
+    digest.update(tr.read_blocks(0, budget * 8).tobytes())
+    digest.update(usage.tobytes())
     tr.close()
     frames = len(cams)
-    return {"frames_per_s": frames / loop_s, "ms_per_frame": 1000 * loop_s / frames,
+    return {"frames_per_s": frames / loop_s, "ms_per_frame": 1000 * loop_s / frames, "state_sha256": digest.hexdigest(),
             "mrays_s_with_updates": frames * n / loop_s / 1e6,
             "ms_per_frame_by_phase": {k: 1000 * v / frames for k, v in phase.items()},
             "gpu_ms_per_frame_by_phase": {k: v / frames for k, v in gpu.items()},
@@ -474,10 +479,14 @@ def stream_workload(torch, dev, args):
            "graft_generation": "device (svo_graft_generate)"}
     out.update(on_device)
     out["host_generation"] = {k: on_host[k] for k in ("ms_per_frame", "ms_per_frame_by_phase",
-                                                       "gpu_ms_per_frame_by_phase", "totals")}
-    # A 1080p frame raises ~2M child requests against the 65,536-entry queue; which
-    # of them are stored depends on the order of the queue's atomics, so two runs
-    # of either path diverge (below the cap both paths give the same tree).
+                                                       "gpu_ms_per_frame_by_phase", "totals", "state_sha256")}
+    # A 1080p frame raises ~2M child requests against the 65,536-entry queue; the
+    # pixel-order rule keeps those of the lowest pixels, so both generation paths
+    # (and every run) reach the same tree: same totals and the same final blocks
+    # and usage arrays.
+    out["request_order"] = "pixel (the requests of the lowest pixel indices up to the cap)"
+    out["generation_paths_agree"] = bool(on_device["state_sha256"] == on_host["state_sha256"]
+                                         and on_device["totals"] == on_host["totals"])
     out["timing"] = "host wall clock per frame, synchronous pipeline"
     return out
 

@@ -187,7 +187,23 @@ typedef struct svo_trace_config {
   int32_t mega_band_tiles; /* megakernel: pixel tiles of 32 per cone band (0: as many as 2^26 cone slots hold) */
   int32_t l2_window;    /* 1: the trace kernel reads the dense level-(B+2) nodes through an L2 persisting
                            access-policy window, -1: no window */
+  int32_t pass_limit;   /* per-ray pass bound of the trace, megakernel and colour-fitting loops (0: max_steps + 2,
+                           which only a fault reaches); a smaller value stops the kernels with SVO_ERR_TIMEOUT, a
+                           test of that path. A stopped kernel is reported by the next call that synchronises
+                           with the device (svo_synchronize included) and then cleared. */
+  int32_t request_order; /* SVO_REQUESTS_ARRIVAL (default) or SVO_REQUESTS_PIXEL, see below */
 } svo_trace_config;
+
+/* Child requests of svo_trace / svo_trace_batch past the queue's cap
+ * (max_child_request_id). ARRIVAL: the queue keeps the first requests to
+ * arrive, in arrival order, as the reference's requestChild does
+ * (wavefront.cl:362-375); which requests those are depends on the timing of
+ * the device's atomics. PIXEL: the queue holds the requests of the lowest
+ * pixel indices (views in call order, pixels row-major) in that order, so the
+ * queue, and every graft decision taken from it, is the same on every run.
+ * Below the cap both hold the same requests. A ray raises at most one request,
+ * when it stops. */
+enum { SVO_REQUESTS_ARRIVAL = 1, SVO_REQUESTS_PIXEL = 2 };
 
 /* Ray scheduling of the persistent trace kernel. LANE: each thread claims rays
  * on its own and finished rays are replaced every `cadence` steps. WARP: each

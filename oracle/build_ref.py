@@ -35,15 +35,20 @@ import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REF_DIR = os.path.join(HERE, "_ref")
+# The reference checkout: $SVO_REFERENCE_ROOT, else a directory named
+# "reference" beside this repository. SVO_REFERENCE_WAVEFRONT and
+# SVO_REFERENCE_MEGAKERNEL name the two kernel files directly.
+REF_ROOT = os.environ.get("SVO_REFERENCE_ROOT",
+                          os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference"))
 REF_SOURCE = os.environ.get(
     "SVO_REFERENCE_WAVEFRONT",
-    "/root/reference/SvoTracer/SvoTracer.Kernel/wavefront.cl",
+    os.path.join(REF_ROOT, "SvoTracer", "SvoTracer.Kernel", "wavefront.cl"),
 )
 REWRITTEN = os.path.join(REF_DIR, "wavefront_ref.c")
 REF_LIB = os.path.join(REF_DIR, "libsvo_ref.so")
 MEGA_SOURCE = os.environ.get(
     "SVO_REFERENCE_MEGAKERNEL",
-    "/root/reference/SvoTracer/SvoTracer.Kernel/kernel.cl",
+    os.path.join(REF_ROOT, "SvoTracer", "SvoTracer.Kernel", "kernel.cl"),
 )
 MEGA_REWRITTEN = os.path.join(REF_DIR, "kernel_ref.c")
 MEGA_LIB = os.path.join(REF_DIR, "libsvo_ref_mega.so")

@@ -30,7 +30,8 @@ _ref_mega = None
 
 
 class _ViewOut(C.Structure):
-    _fields_ = [(n, _vp) for n in ("hit_index", "hit_depth", "t", "rgba", "acc", "v_block", "v_base", "steps")]
+    _fields_ = [(n, _vp) for n in ("hit_index", "hit_depth", "t", "rgba", "acc", "v_block", "v_base", "steps",
+                                   "requested", "pixel_request")]
 
 
 def _p(a):
@@ -101,6 +102,9 @@ def ref_lib() -> C.CDLL:
         lib.ref_trace_view.restype = C.c_long
         lib.ref_trace_rows.argtypes = lib.ref_trace_view.argtypes + [C.c_uint, C.c_uint]
         lib.ref_trace_rows.restype = C.c_long
+        lib.ref_prune.argtypes = [_vp, C.c_uint8, _vp, C.c_size_t, _vp, C.c_size_t, _vp, C.c_uint, _vp, C.c_size_t,
+                                  _vp, C.c_size_t, C.c_uint16]
+        lib.ref_prune.restype = C.c_long
         _ref = lib
     return _ref
 
@@ -184,12 +188,18 @@ def _result(n, counts=True):
 
 
 def trace_view(tree, inp: TraceInput, usage=None, max_steps: int = 1 << 16, threads: int = 0, req_cap: int = 1 << 20):
-    """Runs the oracle on one view. usage (USAGE_DTYPE array) is stamped in place."""
+    """Runs the oracle on one view. usage (USAGE_DTYPE array) is stamped in place.
+    ``requests`` holds the queue in arrival order (capped at req_cap);
+    ``pixel_requests`` every raised request in pixel order, whose first
+    MaxChildRequestId entries are the queue of the pixel-order rule."""
     lib = oracle_lib()
     w, h = inp.ScreenSize
     n = w * h
     r = _result(n)
-    vo = _ViewOut(*[_p(r[k]) for k in ("hit_index", "hit_depth", "t", "rgba", "acc", "v_block", "v_base", "steps")])
+    requested = np.zeros(n, np.uint8)
+    per_pixel = np.zeros(n, CHILD_REQUEST_DTYPE)
+    vo = _ViewOut(*[_p(r[k]) for k in ("hit_index", "hit_depth", "t", "rgba", "acc", "v_block", "v_base", "steps")],
+                  _p(requested), _p(per_pixel))
     bases = np.ascontiguousarray(tree.BaseBlocks, np.uint16)
     blocks = np.ascontiguousarray(tree.Blocks)
     req = np.zeros(min(req_cap, n), CHILD_REQUEST_DTYPE)
@@ -200,7 +210,16 @@ def trace_view(tree, inp: TraceInput, usage=None, max_steps: int = 1 << 16, thre
     r["step_limited"] = int(limited)
     r["requests"] = req[: min(nreq.value, len(req))]
     r["n_requests"] = nreq.value
+    r["pixel_requests"] = per_pixel[requested != 0]
     return r
+
+
+def pixel_order_queue(per_view_requests, cap: int) -> np.ndarray:
+    """The child-request queue of the pixel-order rule for a call over several
+    views: the views' pixel-ordered requests concatenated in call order, the
+    first ``cap`` kept."""
+    allq = np.concatenate(per_view_requests) if per_view_requests else np.zeros(0, CHILD_REQUEST_DTYPE)
+    return allq[:cap]
 
 
 def ref_trace_view(tree, inp: TraceInput, usage=None, threads: int = 0, max_passes: int = 1 << 20):
@@ -221,6 +240,22 @@ def ref_trace_view(tree, inp: TraceInput, usage=None, threads: int = 0, max_pass
     r["requests"] = req[: min(nreq.value, len(req))]
     r["n_requests"] = nreq.value
     return r
+
+
+def ref_prune(bases, base_depth, blocks, usage, records, surface=None, locations=None, tick=1):
+    """The reference's own prune kernel (CPU build of wavefront.cl) over the records,
+    one work-item at a time in record order, editing bases, blocks and usage in
+    place. Returns the number of records run; a negative value -(x + 1) names the
+    first record the kernel cannot run faithfully (see ref_prune in
+    ref_harness.c), which is not run, nor anything after it."""
+    lib = ref_lib()
+    rec = np.ascontiguousarray(records, PRUNING_DTYPE)
+    sur = None if surface is None else np.ascontiguousarray(surface, BLOCK_DTYPE)
+    loc = None if locations is None else np.ascontiguousarray(locations, np.uint64)
+    for a in (bases, blocks, usage):
+        assert a.flags.c_contiguous
+    return int(lib.ref_prune(_p(bases), base_depth, _p(blocks), len(blocks), _p(usage), len(usage), _p(rec), len(rec),
+                             _p(sur), 0 if sur is None else len(sur), _p(loc), 0 if loc is None else loc.size, tick))
 
 
 def init_usage(tree) -> np.ndarray:

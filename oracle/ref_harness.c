@@ -21,6 +21,8 @@ _Static_assert(sizeof(TraceInput) == 104, "TraceInput layout");
 _Static_assert(sizeof(Block) == 16, "Block layout");
 _Static_assert(sizeof(Usage) == 8, "Usage layout");
 _Static_assert(sizeof(ChildRequest) == 40, "ChildRequest layout");
+_Static_assert(sizeof(Pruning) == 20, "Pruning layout");
+_Static_assert(sizeof(UpdateInputData) == 20, "UpdateInputData layout");
 
 _Thread_local size_t ref_gid[2];
 size_t ref_gsize[2];
@@ -199,4 +201,110 @@ long ref_trace_view(const ushort *bases, uchar base_depth, const Block *blocks_i
                     uint *acc, ChildRequest *req_out, uint req_cap, uint *n_req, int threads, long max_passes) {
   return ref_trace_rows(bases, base_depth, blocks_in, n_blocks, usage, n_groups, in, hit_index, hit_depth, t, rgba, acc,
                         req_out, req_cap, n_req, threads, max_passes, 0, in->ScreenSize[1]);
+}
+
+/* ---- prune (wavefront.cl:1215-1266) ------------------------------------------
+ *
+ * Runs the reference's own prune kernel over n records in record order, one
+ * work-item at a time (x = record index), on a single-parent tree (no usage
+ * tick 65534, so the Parent list is never read; the parent arrays passed are
+ * dummies).
+ *
+ * The kernel can only run faithfully where its dereference queue stays empty
+ * and findAddress meets no missing child:
+ *  - helpDereference pops with atomic_dec's old value, one slot past the last
+ *    push (push writes slot n and increments; pop reads slot n and decrements),
+ *    so any push is followed by a pop of an unwritten slot. With the queue count
+ *    at -1 before a record (the host initialises it to 0, MainWindow.cs:86, which
+ *    makes even an empty queue pop slot 0), a record that pushes nothing leaves
+ *    the queue untouched. A CullChild whose grandchild groups would be queued is
+ *    therefore refused here.
+ *  - findAddress's requestChild writes through an uninitialised Buffers
+ *    (wavefront.cl:1203-1204), so a Location record whose walk meets a missing
+ *    child is refused too.
+ * The producer (WorldManager.UpdatePruning, WorldManager.cs:66-82) stores
+ * ColourAddress as an index into the surface blocks and Address as a Location
+ * index; the kernel reads pruningSurfaceData[x] and addresses[Address + k]
+ * (ulongs). Each record is run with arrays arranged so that those reads return
+ * the producer's entries: a surface array whose entry x is
+ * surface[ColourAddress], and a ulong array whose entries Address..Address+2 are
+ * Location Address. A refused record is not run, and nothing after it.
+ * Returns n, or -(x + 1) for the first refused record x. */
+long ref_prune(ushort *bases, uchar base_depth, Block *blocks, size_t n_blocks, Usage *usage, size_t n_groups,
+               const Pruning *records, uint n, const Block *surface, size_t n_surface, const ulong *locations,
+               size_t n_locations, ushort tick) {
+  uint child_request_id = 0;
+  ChildRequest request_sink[4];
+  uint parent_size[1] = {0};
+  bool parent_residency[1] = {false};
+  Parent parents[1] = {{UINT_MAX, UINT_MAX}};
+  uint2 queue[8];
+  int semaphor = 0;
+  UpdateInputData in;
+  memset(&in, 0, sizeof(in));
+  in.BaseDepth = base_depth;
+  in.Tick = tick;
+  Block *surf_by_x = zalloc(sizeof(Block) * (n ? n : 1));
+  long result = n;
+  for (uint x = 0; x < n; x++) {
+    const Pruning *p = &records[x];
+    if (((p->Properties >> 3) & 1) && p->ColourAddress < n_surface) surf_by_x[x] = surface[p->ColourAddress];
+    ulong *loc_words = NULL;
+    uint target = p->Address;
+    if (!((p->Properties >> 4) & 1)) {
+      if (p->Depth != UCHAR_MAX) {
+        if ((size_t)p->Address * 3 + 3 > n_locations) {
+          result = -(long)x - 1;
+          break;
+        }
+        loc_words = zalloc(sizeof(ulong) * ((size_t)p->Address + 3));
+        for (int k = 0; k < 3; k++) loc_words[p->Address + k] = locations[3 * (size_t)p->Address + k];
+        ulong3 location = {loc_words[p->Address], loc_words[p->Address + 1], loc_words[p->Address + 2], 0};
+        uint a = baseLocation(base_depth + 2, location);
+        int missing = 0;
+        for (uchar i = base_depth + 2; i < p->Depth; i++) {
+          if (a >= n_blocks || blocks[a].Child == UINT_MAX) {
+            missing = 1;
+            break;
+          }
+          a = blocks[a].Child + chunkPosition(i, location);
+        }
+        if (missing || a >= n_blocks) {
+          free(loc_words);
+          result = -(long)x - 1;
+          break;
+        }
+        target = a;
+      } else if (target >= n_blocks || (size_t)(target >> 3) >= n_groups) {
+        result = -(long)x - 1;
+        break;
+      }
+      int live = p->Depth != UCHAR_MAX || usage[target >> 3].Tick != 0;
+      if (live && (p->Properties & 1) && blocks[target].Child != UINT_MAX) {
+        uint c0 = blocks[target].Child;
+        int pushes = 0;
+        for (uint i = 0; i < 8; i++) {
+          uint c = c0 + i < n_blocks ? blocks[c0 + i].Child : UINT_MAX;
+          if (c != UINT_MAX && usage[c >> 3].Tick < USHRT_MAX) pushes = 1;
+        }
+        if (pushes) {
+          free(loc_words);
+          result = -(long)x - 1;
+          break;
+        }
+      }
+    }
+    int remaining = -1;
+    ref_gid[0] = x;
+    ref_gid[1] = 0;
+    prune(bases, blocks, usage, &child_request_id, request_sink, parent_size, parent_residency, parents, queue,
+          &remaining, &semaphor, (Pruning *)records, surf_by_x, loc_words ? loc_words : (ulong *)locations, in);
+    free(loc_words);
+    if (remaining != -2 || semaphor != 0) { /* the queue was used after all */
+      result = -(long)x - 1;
+      break;
+    }
+  }
+  free(surf_by_x);
+  return result;
 }

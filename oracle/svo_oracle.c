@@ -280,6 +280,8 @@ typedef struct ray_result {
   uint32_t acc[4];
   uint32_t v_block, v_base, steps;
   int step_limited;
+  int requested; /* the ray stopped with a child request (at most one per ray) */
+  svo_child_request request;
 } ray_result;
 
 static void trace_ray(const uint16_t *bases, uint8_t B, const svo_block *blocks, size_t n_blocks, svo_usage *usage,
@@ -367,22 +369,22 @@ static void trace_ray(const uint16_t *bases, uint8_t B, const svo_block *blocks,
           /* requestChild, wavefront.cl:362-375 with the call of :1539.
            * TreeSize = min(1, (uchar)ConeDepth - Depth) is 1 exactly when
            * ConeDepth >= Depth + 1; Tick is the unset TraceData.Tick (0). */
+          svo_child_request *q = &r->request;
+          memset(q, 0, sizeof(*q));
+          q->address = addr;
+          q->tick = 0;
+          q->depth = depth;
+          q->location[0] = loc[0];
+          q->location[1] = loc[1];
+          q->location[2] = loc[2];
+          q->tree_size = c <= pow2_neg(depth + 1) ? 1 : 0;
+          r->requested = 1;
           uint32_t slot;
 #ifdef _OPENMP
 #pragma omp atomic capture
 #endif
           slot = (*n_req)++;
-          if (req && slot < req_cap) {
-            svo_child_request *q = &req[slot];
-            memset(q, 0, sizeof(*q));
-            q->address = addr;
-            q->tick = 0;
-            q->depth = depth;
-            q->location[0] = loc[0];
-            q->location[1] = loc[1];
-            q->location[2] = loc[2];
-            q->tree_size = c <= pow2_neg(depth + 1) ? 1 : 0;
-          }
+          if (req && slot < req_cap) req[slot] = *q;
           complete = 1;
         } else if (c < pow2_neg(depth + 1)) {
           depth++;
@@ -475,6 +477,8 @@ int64_t oracle_trace_rows(const uint16_t *bases, uint8_t base_depth, const svo_b
     if (out->v_block) out->v_block[id] = r.v_block;
     if (out->v_base) out->v_base[id] = r.v_base;
     if (out->steps) out->steps[id] = r.steps;
+    if (out->requested) out->requested[id] = (uint8_t)r.requested;
+    if (out->pixel_request && r.requested) out->pixel_request[id] = r.request;
     if (out->rgba) {
       /* drawTrace, wavefront.cl:1835-1850 */
       float *px = &out->rgba[4 * id];

@@ -28,6 +28,12 @@ typedef struct oracle_view_out {
   uint32_t *v_block; /* node reads of the reference's getBlockAddress walks */
   uint32_t *v_base;  /* base chunk reads */
   uint32_t *steps;   /* traversal steps (base + block) */
+  /* The request each ray raised, by pixel: requested[pixel] = 1 and
+   * pixel_request[pixel] = the record when the ray stopped with a child
+   * request, requested[pixel] = 0 otherwise. The queue of the pixel-order rule
+   * (SVO_REQUESTS_PIXEL) is the flagged records in pixel order, capped. */
+  uint8_t *requested;
+  svo_child_request *pixel_request;
 } oracle_view_out;
 
 /* Traces one view. usage (n_groups entries) is stamped like runBlockTrace;

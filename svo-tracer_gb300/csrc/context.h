@@ -75,9 +75,17 @@ struct Context {
   DevBuf<svo_block> blocks;
   DevBuf<svo_usage> usage;
   // trace scratch
-  DevBuf<uint32_t> counters;  // [0] ray queue head, [1] child requests raised, [4..9] kernel error record
+  // kCounterWords: [0] ray queue head, [1] child requests raised, then the
+  // kernel error record at kErrorOffset. Launches reset the words before the
+  // record; the record keeps a stopped kernel's report until a synchronising
+  // call returns it (report_kernel_error), which clears it.
+  DevBuf<uint32_t> counters;
   DevBuf<unsigned long long> stats;
   DevBuf<svo_child_request> requests;
+  // pixel-order requests: the staged record and flag per pixel, chunk offsets
+  DevBuf<svo_child_request> req_stage;
+  DevBuf<uint8_t> req_flag;
+  DevBuf<uint32_t> req_chunks;
   DevBuf<ViewParams> views;
   DevBuf<float> tables;
   DevBuf<uint32_t> ray_v_block, ray_v_base;
@@ -167,6 +175,9 @@ struct Context {
     bases.release();
     blocks.release();
     usage.release();
+    req_stage.release();
+    req_flag.release();
+    req_chunks.release();
     counters.release();
     stats.release();
     requests.release();
@@ -247,5 +258,9 @@ svo_status stage_views(Context &c, const svo_trace_input *in, int32_t n, const s
                        bool outputs_on_device, uint32_t tile_w, uint32_t &total_rays, uint32_t &total_pixels,
                        size_t &table_floats);
 svo_status prepare_launch(Context &c, int32_t n_views, uint32_t total_rays, TraceLaunch &a, bool stats);
+// Synchronises the context's stream and returns the error a kernel recorded
+// since the last report (SVO_ERR_TIMEOUT with the stopped thread's ray, depth
+// and steps), clearing the record; SVO_OK when none did.
+svo_status report_kernel_error(Context &c, const char *fn);
 
 }  // namespace svo

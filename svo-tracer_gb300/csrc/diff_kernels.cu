@@ -37,7 +37,7 @@
 // Scheduling: a persistent grid whose warps claim 32 consecutive ray slots at
 // a time from a device counter (one 8x4 pixel tile: the views are staged
 // tiled, outputs stay indexed by pixel); lane i takes slot base + i, and the warp regroups
-// with __syncwarp() between the walks of a ray and before the next claim, so
+// with a warp vote (a regrouping point) between the walks of a ray and before the next claim, so
 // lanes do not drift apart over rays and phases (measured 2-3x faster than a
 // free per-thread grid-stride loop).
 #include <cooperative_groups.h>
@@ -121,9 +121,13 @@ __device__ __forceinline__ float3 sky_rgb(const Ray &r) {
 }
 
 // Visits the hits of one ray in order: visit(node, is_background) with
-// is_background = true once for the sky contribution (node unused).
+// is_background = true once for the sky contribution (node unused). Each pass
+// of the loop probes (and counts) a step, and a probe past max_steps ends the
+// ray in the sky, so a walk takes at most max_steps + 1 passes. A walk that
+// needs more than its bound (max_steps + 2, or the launch's pass_limit) records
+// the timeout in the error record and returns false without finishing.
 template <class Visit>
-__device__ __forceinline__ void walk_hits(const DiffLaunch &d, const ViewParams *s_views, const uint16_t *s_bases,
+__device__ __forceinline__ bool walk_hits(const DiffLaunch &d, const ViewParams *s_views, const uint16_t *s_bases,
                                           uint32_t ray, Walk &w, Visit &&visit) {
   const TraceLaunch &a = d.t;
   const int B = a.base_depth;
@@ -135,18 +139,29 @@ __device__ __forceinline__ void walk_hits(const DiffLaunch &d, const ViewParams 
   Stats st;
   const ViewParams &v = s_views[r.view];
   int hits = 0;
-  for (;;) {
+  const uint32_t limit = a.pass_limit ? a.pass_limit : (uint32_t)a.max_steps + 2u;
+  for (uint32_t pass = 1;; pass++) {
+    if (pass > limit) {
+      if (a.error && atomicCAS(a.error, 0u, (unsigned)SVO_ERR_TIMEOUT) == 0u) {
+        a.error[1] = blockIdx.x;
+        a.error[2] = threadIdx.x;
+        a.error[3] = ray;
+        a.error[4] = (uint32_t)r.depth;
+        a.error[5] = (uint32_t)r.steps;
+      }
+      return false;
+    }
     int f = step<false, true>(a, v, s_bases, blocks, B, r, w, st);
     if (f == kStepOn) continue;
     if (f == kStepBackground) {
       visit(0u, true, r);
-      return;
+      return true;
     }
     visit(w.path[(r.depth - B - 2) * w.stride], false, r);
-    if (++hits >= d.max_hits) return;
+    if (++hits >= d.max_hits) return true;
     if (step_past(a, blocks, B, r, w) == kStepBackground) {
       visit(0u, true, r);
-      return;
+      return true;
     }
   }
 }
@@ -172,10 +187,11 @@ __global__ void __launch_bounds__(256, kBackward ? SVO_DIFF_BWD_MIN_CTAS : SVO_D
   w.path = s_path + threadIdx.x;
   w.stride = blockDim.x;
   double loss_part = 0.0;
-  // Warp-uniform loop over rays (lane i of a warp takes ray base + i) with
-  // __syncwarp() between the phases, which every lane of the warp reaches on
-  // every iteration: the lanes regroup before each walk instead of drifting
-  // apart over rays and phases.
+  // Warp-uniform loop over rays (lane i of a warp takes ray base + i) with a
+  // warp vote (__any_sync, which also regroups the lanes) after each phase,
+  // which every lane of the warp reaches on every iteration: the lanes regroup
+  // before each walk instead of drifting apart over rays and phases, and the
+  // whole warp leaves the loop when one of its walks ran past its pass bound.
   const uint32_t lane = threadIdx.x & 31u;
   for (;;) {
     // the warp claims the next 32 rays (persistent grid, dynamic balance)
@@ -190,15 +206,16 @@ __global__ void __launch_bounds__(256, kBackward ? SVO_DIFF_BWD_MIN_CTAS : SVO_D
     const uint32_t pixel = live ? s_views[view].pixel_begin + py * s_views[view].width + px : 0;
     Composite full;
     full.init();
+    bool stopped = false;  // a walk ran past its pass bound: the warp leaves the loop
     if (live && (!kBackward || !d.use_saved)) {
-      walk_hits(d, s_views, s_bases, ray, w, [&](uint32_t node, bool bg, const Ray &r) {
+      stopped = !walk_hits(d, s_views, s_bases, ray, w, [&](uint32_t node, bool bg, const Ray &r) {
         if (bg)
           full.sky(sky_rgb(r));
         else
           full.hit(__ldg(d.params + node));
       });
     }
-    __syncwarp();
+    if (__any_sync(kFull, stopped)) break;
     if (!kBackward) {
       if (live && d.rgb)
         for (int k = 0; k < 3; k++) d.rgb[3ull * pixel + k] = __fadd_rn(full.hi[k], full.lo[k]);
@@ -225,7 +242,7 @@ __global__ void __launch_bounds__(256, kBackward ? SVO_DIFF_BWD_MIN_CTAS : SVO_D
       // the gradient walk: replay the prefix sums, one contribution at a time
       Composite pre;
       pre.init();
-      walk_hits(d, s_views, s_bases, ray, w, [&](uint32_t node, bool bg, const Ray &) {
+      stopped = !walk_hits(d, s_views, s_bases, ray, w, [&](uint32_t node, bool bg, const Ray &) {
         if (bg) return;
         float4 p = __ldg(d.params + node);
         float T = pre.T, ta = __fmul_rn(T, p.w);
@@ -270,7 +287,7 @@ __global__ void __launch_bounds__(256, kBackward ? SVO_DIFF_BWD_MIN_CTAS : SVO_D
         }
       });
     }
-    __syncwarp();
+    if (__any_sync(kFull, stopped)) break;
   }
   if (kBackward) {
     cooperative_groups::coalesced_group g = cooperative_groups::coalesced_threads();
@@ -331,7 +348,7 @@ svo_status run_diff(Context &c, const svo_trace_input *views, int32_t n, const f
   SVO_CUDA(cudaMemcpyAsync(c.tables.p, c.h_tables.p, sizeof(float) * table_floats, cudaMemcpyHostToDevice, c.stream),
            "svo_diff: tables");
   SVO_CUDA(cudaEventRecord(c.staged, c.stream), "svo_diff: staging event");
-  SVO_CUDA(cudaMemsetAsync(c.counters.p, 0, 12 * sizeof(uint32_t), c.stream), "svo_diff: counters");
+  SVO_CUDA(cudaMemsetAsync(c.counters.p, 0, kErrorOffset * sizeof(uint32_t), c.stream), "svo_diff: counters");
   if (kBackward) {
     SVO_CUDA(cudaMemsetAsync(c.grads.p, 0, c.grads.n * sizeof(float), c.stream), "svo_diff: grads");
     SVO_CUDA(cudaMemsetAsync(c.diff_loss.p, 0, sizeof(double), c.stream), "svo_diff: loss");
@@ -341,7 +358,8 @@ svo_status run_diff(Context &c, const svo_trace_input *views, int32_t n, const f
   if (kBackward && loss_host) {
     SVO_CUDA(cudaMemcpyAsync(loss_host, c.diff_loss.p, sizeof(double), cudaMemcpyDeviceToHost, c.stream),
              "svo_diff: loss");
-    SVO_CUDA(cudaStreamSynchronize(c.stream), "svo_diff: synchronize");
+    svo_status es = report_kernel_error(c, "svo_diff_backward");  // synchronises
+    if (es) return es;
   }
   if (!kBackward) {
     c.saved_views.assign(views, views + n);
@@ -418,7 +436,7 @@ SVO_API svo_status svo_diff_forward(void *ctx, const svo_trace_input *views, int
   if (!on_device && !pinned)
     SVO_CUDA(cudaMemcpyAsync(rgb, dst, 3 * rays * sizeof(float), cudaMemcpyDeviceToHost, c.stream),
              "svo_diff_forward: read");
-  if (!on_device) SVO_CUDA(cudaStreamSynchronize(c.stream), "svo_diff_forward: synchronize");
+  if (!on_device) return svo::report_kernel_error(c, "svo_diff_forward");  // synchronises
   return SVO_OK;
 }
 
@@ -441,7 +459,7 @@ SVO_API svo_status svo_diff_backward(void *ctx, const svo_trace_input *views, in
   svo_status st = svo::run_diff<true>(c, views, n, src, nullptr, use_saved != 0, loss);
   if (st) return st;
   // the caller may reuse a host target once the call returns
-  if (pinned && !loss) SVO_CUDA(cudaStreamSynchronize(c.stream), "svo_diff_backward: synchronize");
+  if (pinned && !loss) return svo::report_kernel_error(c, "svo_diff_backward");  // synchronises
   return SVO_OK;
 }
 

@@ -72,16 +72,7 @@ svo_status ensure_normal_table(Context &c) {
   return SVO_OK;
 }
 
-svo_status read_error(Context &c, const char *fn) {
-  uint32_t e[6] = {0};
-  SVO_CUDA(cudaMemcpyAsync(e, c.counters.p + 4, sizeof(e), cudaMemcpyDeviceToHost, c.stream), fn);
-  SVO_CUDA(cudaStreamSynchronize(c.stream), fn);
-  if (e[0] == SVO_ERR_TIMEOUT)
-    return fail(SVO_ERR_TIMEOUT, std::string(fn) + ": thread " + std::to_string(e[2]) + " of block " +
-                                     std::to_string(e[1]) + " exceeded its step bound on item " + std::to_string(e[3]));
-  if (e[0]) return fail((svo_status)e[0], std::string(fn) + ": kernel reported an error");
-  return SVO_OK;
-}
+svo_status read_error(Context &c, const char *fn) { return report_kernel_error(c, fn); }
 
 svo_status run_mega(Context &c, const svo_trace_input *in, const svo_trace_output *out_in) {
   const char *fn = "svo_mega_trace";
@@ -199,7 +190,7 @@ svo_status run_mega(Context &c, const svo_trace_input *in, const svo_trace_outpu
   SVO_CUDA(cudaMemcpyAsync(c.tables.p, c.h_tables.p, sizeof(float) * table_floats, cudaMemcpyHostToDevice, c.stream),
            fn);
   SVO_CUDA(cudaEventRecord(c.staged, c.stream), fn);
-  SVO_CUDA(cudaMemsetAsync(c.counters.p, 0, 12 * sizeof(uint32_t), c.stream), fn);
+  SVO_CUDA(cudaMemsetAsync(c.counters.p, 0, kErrorOffset * sizeof(uint32_t), c.stream), fn);
   SVO_CUDA(cudaMemsetAsync(c.mega_totals.p, 0, 2 * sizeof(unsigned long long), c.stream), fn);
   st = launch_mega_primary(m, c.stream);
   if (st) return st;

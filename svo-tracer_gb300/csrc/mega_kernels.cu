@@ -164,6 +164,16 @@ __device__ __forceinline__ void reset_walk(Walk &w) {
   w.v_base = 0;
 }
 
+// True once a kernel of this call (or an earlier unreported one) recorded an
+// error: the kernels after the primary one then return at entry, so none of them
+// reads the pixel records of warps that stopped early. Nothing writes the record
+// while the fan, scan, emit and resolve kernels run, so every thread of one of
+// those launches reads the same value (the scan kernel's __syncthreads stay
+// uniform).
+__device__ __forceinline__ bool call_stopped(const MegaLaunch &m) {
+  return m.t.error && *reinterpret_cast<const volatile uint32_t *>(m.t.error) != 0u;
+}
+
 __device__ __forceinline__ void record_timeout(const TraceLaunch &a, uint32_t item, const Ray &r) {
   if (a.error && atomicCAS(a.error, 0u, (unsigned)SVO_ERR_TIMEOUT) == 0u) {
     a.error[1] = blockIdx.x;
@@ -180,7 +190,7 @@ template <bool kSmemBases>
 __device__ __forceinline__ bool run_cone(const TraceLaunch &a, const ViewParams &v, const uint16_t *s_bases,
                                          const uint4 *blocks, int B, Ray &r, Walk &w, int &finish) {
   Stats st;
-  const uint32_t limit = (uint32_t)a.max_steps + 2u;
+  const uint32_t limit = a.pass_limit ? a.pass_limit : (uint32_t)a.max_steps + 2u;
   uint32_t n = 0;
   finish = kStepOn;
   while (finish == kStepOn) {
@@ -279,6 +289,7 @@ __global__ void __launch_bounds__(256, SVO_MEGA_MIN_CTAS) mega_primary_kernel(co
 
 // spawnRays for one slot of the band; one warp per tile.
 __global__ void __launch_bounds__(256) mega_fan_kernel(const MegaLaunch m) {
+  if (call_stopped(m)) return;
   const uint32_t gid = blockIdx.x * blockDim.x + threadIdx.x;
   const uint32_t tile = gid >> 5, lane = gid & 31u;
   uint32_t count = 0;
@@ -368,6 +379,7 @@ __global__ void __launch_bounds__(256) mega_fan_kernel(const MegaLaunch m) {
 // Exclusive scan of the band's per-tile cone counts (one CTA), total to queue[1].
 __global__ void __launch_bounds__(1024) mega_scan_kernel(const MegaLaunch m) {
   __shared__ uint32_t part[1024];
+  if (call_stopped(m)) return;
   const uint32_t n = m.band_tiles;
   const uint32_t per = (n + 1023u) / 1024u, b = threadIdx.x * per, e = min(n, b + per);
   uint32_t s = 0;
@@ -395,6 +407,7 @@ __global__ void __launch_bounds__(1024) mega_scan_kernel(const MegaLaunch m) {
 // The compacted cone list: per tile (one warp), cone k of every pixel that has
 // one, k = 0, 1, ... (neighbouring entries start close together and point alike).
 __global__ void __launch_bounds__(256) mega_emit_kernel(const MegaLaunch m) {
+  if (call_stopped(m)) return;
   const uint32_t gid = blockIdx.x * blockDim.x + threadIdx.x;
   const uint32_t tile = gid >> 5, lane = gid & 31u;
   if (tile >= m.band_tiles) return;  // whole warps
@@ -447,6 +460,12 @@ __device__ __forceinline__ void start_cone(const MegaLaunch &m, uint32_t e, Ray 
 template <bool kSmemBases, bool kLane>
 __global__ void __launch_bounds__(256, SVO_MEGA_MIN_CTAS) mega_cone_kernel(const MegaLaunch m) {
   extern __shared__ __align__(16) uint8_t smem[];
+  // a block that starts after some cone stopped takes no work (the whole block
+  // returns together, before the __syncthreads of the staging)
+  __shared__ uint32_t s_stop;
+  if (threadIdx.x == 0) s_stop = call_stopped(m) ? 1u : 0u;
+  __syncthreads();
+  if (s_stop) return;
   const TraceLaunch &a = m.t;
   ViewParams *s_views;
   uint16_t *s_bases;
@@ -486,7 +505,9 @@ __global__ void __launch_bounds__(256, SVO_MEGA_MIN_CTAS) mega_cone_kernel(const
   } else {
     // every pass starts a cone or steps one, so a thread runs at most
     // n * (max_steps + 2) + 64 passes; past that it records its state and stops
-    const unsigned long long iter_limit = (unsigned long long)n * (unsigned long long)(a.max_steps + 2) + 64;
+    const unsigned long long iter_limit =
+        a.pass_limit ? (unsigned long long)a.pass_limit
+                     : (unsigned long long)n * (unsigned long long)(a.max_steps + 2) + 64;
     unsigned long long iters = 0;
     const int cadence = a.cadence;
     bool have = false;
@@ -519,6 +540,7 @@ __global__ void __launch_bounds__(256, SVO_MEGA_MIN_CTAS) mega_cone_kernel(const
 
 // writeToAccumulator over the pixel's cones in generation order, then draw.
 __global__ void __launch_bounds__(256) mega_resolve_kernel(const MegaLaunch m) {
+  if (call_stopped(m)) return;
   const uint32_t gid = blockIdx.x * blockDim.x + threadIdx.x;
   const uint32_t tile = gid >> 5, lane = gid & 31u;
   if (tile >= m.band_tiles) return;

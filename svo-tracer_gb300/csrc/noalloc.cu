@@ -10,7 +10,8 @@
 // kernel needs (ray queue head, child-request counter, error record, the view
 // record and the ray-setup sine/cosine tables) lives in a file-scope device
 // array of fixed size, so the call performs no cudaMalloc/cudaFree and creates
-// no context-owned buffer.
+// no context-owned buffer. It runs the library's default schedule (warp
+// batches over 4x8 pixel tiles), so its results are those of svo_trace.
 //
 // Limits and sharing rules:
 //  * the static scratch holds 132 KiB; it allows views with
@@ -19,10 +20,15 @@
 //  * every process that loads libsvo keeps those 132 KiB on every GPU it uses
 //    until it exits;
 //  * every call uses the same scratch, which keeps the previous call's
-//    contents; the call clears the counters it needs at the start. Calls whose
-//    work overlaps on the GPU (different streams, or different host threads)
-//    race on the scratch and must not be issued; calls on one stream are
-//    ordered and safe;
+//    contents; the call clears the counters it needs at the start. Two calls
+//    whose work overlapped on the GPU would race on it, so a process-wide lock
+//    is held from the staging of a call until its trace has completed: calls
+//    from different host threads run one after another, and a call blocks
+//    while another thread's call is tracing. What the lock cannot order is the
+//    caller's own work on the outputs, the usage array or the request array
+//    (on other streams): that must not run while a call traces;
+//  * the call switches to `device` for its work and restores the calling
+//    thread's current device before it returns;
 //  * the first call on a device looks up the scratch's device address on that
 //    device (cudaGetSymbolAddress) and caches it; make that first call before
 //    any stream capture on the device.
@@ -55,6 +61,20 @@ ViewParams g_host_view;
 float g_host_tables[2 * kMaxWidthPlusHeight];
 std::mutex g_lock;
 unsigned char *g_scratch_ptr[kMaxDevices];
+
+// Restores the calling thread's current device when a call returns.
+struct DeviceRestore {
+  int prev = -1;
+  DeviceRestore() {
+    if (cudaGetDevice(&prev) != cudaSuccess) {
+      prev = -1;
+      cudaGetLastError();
+    }
+  }
+  ~DeviceRestore() {
+    if (prev >= 0) cudaSetDevice(prev);
+  }
+};
 
 svo_status scratch_address(int device, unsigned char **out) {
   if (device < 0 || device >= kMaxDevices) return fail(SVO_ERR_INVALID_ARGUMENT, "svo_trace_noalloc: device index");
@@ -101,6 +121,7 @@ extern "C" SVO_API svo_status svo_trace_noalloc(int32_t device, void *stream, ui
     return fail(SVO_ERR_INVALID_ARGUMENT, "svo_trace_noalloc: max_node_depth must be base_depth+2..SVO_MAX_TREE_DEPTH");
 
   std::lock_guard<std::mutex> guard(g_lock);
+  DeviceRestore restore;
   cudaError_t e = cudaSetDevice(device);
   if (e != cudaSuccess) return fail(SVO_ERR_NO_DEVICE, std::string("svo_trace_noalloc: ") + cudaGetErrorString(e));
   unsigned char *scratch = nullptr;
@@ -122,8 +143,10 @@ extern "C" SVO_API svo_status svo_trace_noalloc(int32_t device, void *stream, ui
   v.width = W;
   v.height = H;
   v.ray_begin = 0;
+  v.pixel_begin = 0;
   v.table_off = 0;
   v.tick = input->tick;
+  v.tile = (uint16_t)kTraceTileW;  // warp batches over kTraceTileW x (32 / kTraceTileW) pixel tiles
   v.hit_index = out->hit_index;
   v.hit_depth = out->hit_depth;
   v.t = out->t;
@@ -163,18 +186,22 @@ extern "C" SVO_API svo_status svo_trace_noalloc(int32_t device, void *stream, ui
   a.n_bases = (uint32_t)n_bases;
   a.n_blocks = (uint32_t)n_blocks;
   a.n_groups = usage ? (uint32_t)n_groups : 0;
-  a.total_rays = W * H;
+  // ray slots: whole 32-pixel tiles (the padding slots of edge tiles are skipped)
+  const uint32_t tile_h = 32u / kTraceTileW;
+  a.total_rays = ((W + kTraceTileW - 1) / kTraceTileW) * ((H + tile_h - 1) / tile_h) * 32u;
   a.n_views = 1;
   a.base_depth = base_depth;
   a.max_steps = 1 << 16;
   a.ray_chunk = 1;
   a.cadence = 16;
   a.block_size = 256;
+  a.schedule = SVO_SCHEDULE_WARP;
   a.path_levels = depth - base_depth - 1;
   int occ = trace_occupancy(a, false);
   if (occ <= 0) return fail(SVO_ERR_NO_DEVICE, "svo_trace_noalloc: the trace kernel cannot be resident");
-  long need = ((long)a.total_rays + 255) / 256;
-  a.grid = (int)std::min<long>((long)occ * sm_count, need);
+  // the persistent grid of svo_trace: every resident CTA, or one per 32-slot tile when fewer
+  long need = ((long)a.total_rays + 31) / 32 * 32 / a.block_size + 1;
+  a.grid = (int)std::max(1L, std::min<long>((long)occ * sm_count, need));
   st = launch_trace(a, false, stream);
   if (st) return st;
 

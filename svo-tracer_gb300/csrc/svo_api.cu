@@ -39,6 +39,8 @@ static svo_trace_config default_config() {
   c.max_hits = 16;
   c.schedule = SVO_SCHEDULE_WARP;  // 13% faster than lane refills on the 1080p terrain frame
   c.l2_window = -1;
+  c.pass_limit = 0;
+  c.request_order = SVO_REQUESTS_ARRIVAL;
   return c;
 }
 
@@ -206,7 +208,7 @@ svo_status prepare_launch(Context &c, int32_t n_views, uint32_t total_rays, Trac
   a.requests = c.requests.p;
   a.request_cap = c.request_cap;
   a.ray_counter = c.counters.p;
-  a.error = c.counters.p + 4;
+  a.error = c.counters.p + kErrorOffset;
   a.request_count = c.counters.p + 1;
   a.stats = stats ? c.stats.p : nullptr;
   a.ray_v_block = (stats && c.cfg.collect_stats >= 2) ? c.ray_v_block.p : nullptr;
@@ -225,6 +227,7 @@ svo_status prepare_launch(Context &c, int32_t n_views, uint32_t total_rays, Trac
   a.block_size = c.cfg.block_size;
   a.schedule = c.cfg.schedule;
   a.path_levels = std::max(1, c.tree_depth - (int)c.base_depth - 1);
+  a.pass_limit = (uint32_t)c.cfg.pass_limit;
   plan_l2_window(c, a);
   int occ = c.cfg.ctas_per_sm > 0 ? c.cfg.ctas_per_sm : trace_occupancy(a, stats);
   if (occ <= 0) return fail(SVO_ERR_NO_DEVICE, "svo_trace: the trace kernel cannot be resident (no sm_103a image?)");
@@ -237,20 +240,23 @@ svo_status prepare_launch(Context &c, int32_t n_views, uint32_t total_rays, Trac
 // The view table lives in shared memory (120 B per view).
 constexpr int kMaxViews = 512;
 
-// Reads the kernel's error record (synchronises the stream).
-// Reads the kernel's error record together with whatever the stream already
-// holds (one synchronisation).
-static svo_status check_kernel_error(Context &c) {
-  uint32_t e[6] = {0};
-  SVO_CUDA(cudaMemcpyAsync(e, c.counters.p + 4, sizeof(e), cudaMemcpyDeviceToHost, c.stream), "svo_trace: error record");
-  SVO_CUDA(cudaStreamSynchronize(c.stream), "svo_trace: synchronize");
+svo_status report_kernel_error(Context &c, const char *fn) {
+  uint32_t e[kErrorWords] = {0};
+  SVO_CUDA(cudaMemcpyAsync(e, c.counters.p + kErrorOffset, sizeof(e), cudaMemcpyDeviceToHost, c.stream),
+           std::string(fn) + ": error record");
+  SVO_CUDA(cudaStreamSynchronize(c.stream), std::string(fn) + ": synchronize");
+  if (!e[0]) return SVO_OK;
+  // reported once: the next launches start with a clear record
+  SVO_CUDA(cudaMemsetAsync(c.counters.p + kErrorOffset, 0, sizeof(e), c.stream), std::string(fn) + ": error record");
+  SVO_CUDA(cudaStreamSynchronize(c.stream), std::string(fn) + ": synchronize");
   if (e[0] == SVO_ERR_TIMEOUT)
-    return fail(SVO_ERR_TIMEOUT, "svo_trace: thread " + std::to_string(e[2]) + " of block " + std::to_string(e[1]) +
-                                     " exceeded its iteration bound on ray " + std::to_string(e[3]) + " (depth " +
-                                     std::to_string(e[4]) + ", steps " + std::to_string(e[5]) + ")");
-  if (e[0]) return fail((svo_status)e[0], "svo_trace: kernel reported an error");
-  return SVO_OK;
+    return fail(SVO_ERR_TIMEOUT, std::string(fn) + ": thread " + std::to_string(e[2]) + " of block " +
+                                     std::to_string(e[1]) + " exceeded its pass bound on ray " + std::to_string(e[3]) +
+                                     " (depth " + std::to_string(e[4]) + ", steps " + std::to_string(e[5]) + ")");
+  return fail((svo_status)e[0], std::string(fn) + ": kernel reported error " + std::to_string(e[0]));
 }
+
+static svo_status check_kernel_error(Context &c) { return report_kernel_error(c, "svo_trace"); }
 
 static svo_status run_trace(Context &c, const svo_trace_input *in, int32_t n, const svo_trace_output *out,
                             bool use_graph) {
@@ -317,6 +323,16 @@ static svo_status run_trace(Context &c, const svo_trace_input *in, int32_t n, co
   TraceLaunch a;
   st = prepare_launch(c, n, total_rays, a, stats);
   if (st) return st;
+  // pixel-order child requests: staged per pixel, the queue built after the trace
+  const bool pixel_order = c.cfg.request_order == SVO_REQUESTS_PIXEL;
+  const size_t flag_bytes = ((size_t)total_pixels + kRequestChunk - 1) / kRequestChunk * kRequestChunk;
+  if (pixel_order) {
+    if (c.req_stage.reserve(total_pixels) || c.req_flag.reserve(flag_bytes) ||
+        c.req_chunks.reserve(flag_bytes / kRequestChunk))
+      return fail(SVO_ERR_OUT_OF_MEMORY, "svo_trace: pixel-order request staging allocation failed");
+    a.req_stage = c.req_stage.p;
+    a.req_flag = c.req_flag.p;
+  }
 
   auto enqueue = [&](bool capturing) -> svo_status {
     SVO_CUDA(cudaMemcpyAsync(c.views.p, c.h_views.p, sizeof(ViewParams) * n, cudaMemcpyHostToDevice, c.stream),
@@ -325,9 +341,12 @@ static svo_status run_trace(Context &c, const svo_trace_input *in, int32_t n, co
              "svo_trace: table upload");
     SVO_CUDA(cudaEventRecordWithFlags(c.staged, c.stream, capturing ? cudaEventRecordExternal : cudaEventRecordDefault),
              "svo_trace: staging event");
-    SVO_CUDA(cudaMemsetAsync(c.counters.p, 0, (4 + 8) * sizeof(uint32_t), c.stream), "svo_trace: counter reset");
+    SVO_CUDA(cudaMemsetAsync(c.counters.p, 0, kErrorOffset * sizeof(uint32_t), c.stream), "svo_trace: counter reset");
     if (stats) SVO_CUDA(cudaMemsetAsync(c.stats.p, 0, 8 * sizeof(unsigned long long), c.stream), "svo_trace: stats reset");
-    return launch_trace(a, stats, c.stream);
+    if (pixel_order) SVO_CUDA(cudaMemsetAsync(a.req_flag, 0, flag_bytes, c.stream), "svo_trace: request flags");
+    svo_status lst = launch_trace(a, stats, c.stream);
+    if (lst || !pixel_order) return lst;
+    return launch_request_compaction(a, total_pixels, c.req_chunks.p, c.stream);
   };
 
   if (use_graph && !stats) {
@@ -344,6 +363,10 @@ static svo_status run_trace(Context &c, const svo_trace_input *in, int32_t n, co
     key.push_back((uint32_t)(uintptr_t)c.views.p);
     key.push_back((uint32_t)(uintptr_t)c.tables.p);
     key.push_back((uint32_t)a.grid);
+    key.push_back(pixel_order ? 1u : 0u);
+    key.push_back((uint32_t)(uintptr_t)c.req_stage.p);
+    key.push_back((uint32_t)(uintptr_t)c.requests.p);
+    key.push_back(c.request_cap);
     if (!c.graph_exec || key != c.graph_key) {
       if (c.graph_exec) cudaGraphExecDestroy(c.graph_exec);
       c.graph_exec = nullptr;
@@ -434,7 +457,8 @@ SVO_API svo_status svo_create(int32_t device, void **ctx) {
   SVO_CUDA(cudaEventCreateWithFlags(&c->staged, cudaEventDisableTiming), "svo_create: event");
   c->stream = c->own_stream;
   c->cfg = svo::default_config();
-  SVO_CUDA(c->counters.reserve(4 + 8), "svo_create: counters");
+  SVO_CUDA(c->counters.reserve(svo::kCounterWords), "svo_create: counters");
+  SVO_CUDA(cudaMemset(c->counters.p, 0, svo::kCounterWords * sizeof(uint32_t)), "svo_create: counters");
   SVO_CUDA(c->stats.reserve(8), "svo_create: stats");
   SVO_CUDA(c->h_counters.reserve(4), "svo_create: pinned counters");
   *ctx = c.release();
@@ -459,7 +483,7 @@ SVO_API svo_status svo_set_stream(void *ctx, void *stream) {
 SVO_API svo_status svo_synchronize(void *ctx) {
   CTX_OR_FAIL(ctx, "svo_synchronize");
   SVO_CUDA(cudaStreamSynchronize(c.stream), "svo_synchronize");
-  return SVO_OK;
+  return svo::report_kernel_error(c, "svo_synchronize");
 }
 
 SVO_API svo_status svo_set_trace_config(void *ctx, const svo_trace_config *cfg) {
@@ -473,6 +497,10 @@ SVO_API svo_status svo_set_trace_config(void *ctx, const svo_trace_config *cfg) 
   if (n.max_hits == 0) n.max_hits = d.max_hits;
   if (n.schedule == 0) n.schedule = d.schedule;
   if (n.l2_window == 0) n.l2_window = d.l2_window;
+  if (n.request_order == 0) n.request_order = d.request_order;
+  if (n.request_order != SVO_REQUESTS_ARRIVAL && n.request_order != SVO_REQUESTS_PIXEL)
+    return fail(SVO_ERR_INVALID_ARGUMENT, "svo_set_trace_config: request_order must be SVO_REQUESTS_ARRIVAL or _PIXEL");
+  if (n.pass_limit < 0) return fail(SVO_ERR_INVALID_ARGUMENT, "svo_set_trace_config: pass_limit must be >= 0");
   if (n.block_size % 32 || n.block_size < 32 || n.block_size > 256)
     return fail(SVO_ERR_INVALID_ARGUMENT, "svo_set_trace_config: block_size must be a multiple of 32 in 32..256");
   if (n.ray_chunk < 1 || n.ray_chunk > 64 || n.cadence < 1 || n.cadence > 1024 || n.max_steps < 1 || n.ctas_per_sm < 0 ||

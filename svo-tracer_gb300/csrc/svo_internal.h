@@ -35,6 +35,15 @@ static_assert((kTraceTileW & (kTraceTileW - 1)) == 0 && kTraceTileW <= 32, "tile
 static_assert((kDiffTileW & (kDiffTileW - 1)) == 0 && kDiffTileW <= 32, "tile width: a power of two up to 32");
 static_assert((kTraceHostTileW & (kTraceHostTileW - 1)) == 0 && kTraceHostTileW <= 32, "tile width");
 
+// The device counter words of a trace launch: [0] ray queue head, [1] child
+// requests raised, [2..3] spare, [4 .. 4 + kErrorWords) the kernel error record
+// ([0] status, then block, thread, ray, depth and steps of the first thread that
+// stopped), the rest spare.
+constexpr int kCounterWords = 12;
+constexpr int kErrorOffset = 4;
+constexpr int kErrorWords = 6;
+static_assert(kErrorOffset + kErrorWords <= kCounterWords, "the counter area holds the error record");
+
 // Per-view constants of one trace, as the kernel reads them.
 
 struct ViewParams {
@@ -63,7 +72,7 @@ struct TraceLaunch {
   svo_child_request *requests;
   uint32_t *request_count;
   uint32_t *ray_counter;
-  uint32_t *error;            // [0] status, [1..3] diagnostics of a stopped warp
+  uint32_t *error;            // kErrorWords: [0] status, [1..5] block, thread, ray, depth, steps of a stopped thread
   unsigned long long *stats;  // 7 counters in svo_trace_stats order, or null
   uint32_t *ray_v_block;      // per-ray V_block (stats launches only), or null
   uint32_t *ray_v_base;
@@ -83,6 +92,16 @@ struct TraceLaunch {
   int32_t schedule;  // SVO_SCHEDULE_LANE / SVO_SCHEDULE_WARP
   int32_t grid;
   int32_t path_levels;
+  // per-ray pass bound of the device loops; 0: max_steps + 2 (a step ends a ray
+  // after max_steps steps, so only a fault can reach it). Lower values make the
+  // kernels stop with SVO_ERR_TIMEOUT, which tests that path.
+  uint32_t pass_limit;
+  // SVO_REQUESTS_PIXEL: a ray's child request goes to req_stage[pixel] with
+  // req_flag[pixel] = 1 (pixel in the batch's pixel space; the flags are
+  // cleared before the launch), and launch_request_compaction builds the queue
+  // afterwards. Null: requests are queued in arrival order.
+  svo_child_request *req_stage;
+  uint8_t *req_flag;
   // L2 persisting access-policy window of the launch (host side only; 0 bytes: none)
   const void *l2_base;
   size_t l2_bytes;
@@ -90,6 +109,14 @@ struct TraceLaunch {
 
 // Launches the persistent trace kernel on `stream`.
 svo_status launch_trace(const TraceLaunch &a, bool with_stats, void *stream);
+// The child-request queue of the pixel-order rule from a launch's staged
+// requests: a.request_count = requests raised, a.requests[0 .. min(raised,
+// request_cap)) = the staged records of the lowest pixels, in pixel order.
+// total_pixels flags are read (the flag array is padded with zeros to whole
+// chunks of kRequestChunk); chunk_offsets holds one word per chunk.
+constexpr uint32_t kRequestChunk = 4096;
+svo_status launch_request_compaction(const TraceLaunch &a, uint32_t total_pixels, uint32_t *chunk_offsets,
+                                     void *stream);
 // Dynamic shared memory the launch needs.
 size_t trace_smem_bytes(const TraceLaunch &a, bool bases_in_smem);
 int trace_occupancy(const TraceLaunch &a, bool with_stats);

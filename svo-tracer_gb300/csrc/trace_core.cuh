@@ -385,11 +385,22 @@ __device__ __forceinline__ int probe(const TraceLaunch &a, const ViewParams &v, 
     return kStepOn;
   }
   if (w.cur_child == SVO_NO_CHILD) {
-    // requestChild (wavefront.cl:362-375): one atomic per group of requesting lanes
-    cg::coalesced_group g = cg::coalesced_threads();
-    uint32_t slot = claim(g, a.request_count, 1);
+    // requestChild (wavefront.cl:362-375). Pixel order: the record goes to the
+    // ray's pixel slot and the queue is built after the trace. Arrival order:
+    // one atomic per group of requesting lanes.
     if (kStats) st.requests++;
-    if (slot < a.request_cap && a.requests) {
+    uint32_t slot = 0;
+    svo_child_request *dst = nullptr;
+    if (!kMega && a.req_stage) {
+      const uint32_t pixel = v.pixel_begin + r.id;
+      dst = a.req_stage + pixel;
+      a.req_flag[pixel] = 1;
+    } else {
+      cg::coalesced_group g = cg::coalesced_threads();
+      slot = claim(g, a.request_count, 1);
+      if (slot < a.request_cap && a.requests) dst = a.requests + slot;
+    }
+    if (dst) {
       svo_child_request q;
       q.address = w.cur_addr;
       q.tick = kMega ? v.tick : 0;  // TraceData.Tick is never set by the wavefront's resolveTrace
@@ -400,7 +411,7 @@ __device__ __forceinline__ int probe(const TraceLaunch &a, const ViewParams &v, 
       q.location[2] = loc_z(r);
       q.tree_size = kMega ? 1 : (c <= pow2_neg(r.depth + 1) ? 1 : 0);
       for (int k = 0; k < 7; k++) q._pad1[k] = 0;
-      a.requests[slot] = q;
+      *dst = q;
     }
     return kStepHit;
   }

@@ -91,8 +91,10 @@ __global__ void __launch_bounds__(256, SVO_TRACE_MIN_CTAS) trace_kernel(const Tr
   // Every pass either starts a ray or advances it by at least one step, so a
   // thread runs at most total_rays * (max_steps + 2) + 64 passes; past that
   // bound it records its state and stops instead of spinning.
+  // (a.pass_limit, when set, replaces that bound: a test of the timeout path)
   const unsigned long long iter_limit =
-      (unsigned long long)a.total_rays * (unsigned long long)(a.max_steps + 2) + 64;
+      a.pass_limit ? (unsigned long long)a.pass_limit
+                   : (unsigned long long)a.total_rays * (unsigned long long)(a.max_steps + 2) + 64;
   unsigned long long iters = 0;
   auto record_timeout = [&]() {
     if (a.error && atomicCAS(a.error, 0u, (unsigned)SVO_ERR_TIMEOUT) == 0u) {
@@ -173,7 +175,7 @@ __global__ void __launch_bounds__(256, SVO_TRACE_MIN_CTAS) trace_kernel(const Tr
         int finish = kStepOn;
         // a step ends a ray after max_steps steps, so a ray needing more
         // passes than that is a fault: record it and stop the warp
-        const uint32_t ray_limit = (uint32_t)a.max_steps + 2u;
+        const uint32_t ray_limit = a.pass_limit ? a.pass_limit : (uint32_t)a.max_steps + 2u;
         uint32_t ray_iters = 0;
         while (finish == kStepOn) {
           if (++ray_iters > ray_limit) {
@@ -245,7 +247,105 @@ __global__ void __launch_bounds__(256, SVO_TRACE_MIN_CTAS) trace_kernel(const Tr
   }
 }
 
+// ---- the child-request queue of the pixel-order rule ---------------------------
+// A chunk of kRequestChunk pixel flags is one CTA of 256 threads, 16 flags (one
+// 16-byte load) per thread; flags are 0 or 1 bytes, so a word's population
+// count is the number of its flagged pixels.
+constexpr int kReqThreads = 256;
+static_assert(kRequestChunk == kReqThreads * 16, "one 16-byte load of flags per thread");
+
+__device__ __forceinline__ uint32_t flag_count(uint4 f) { return __popc(f.x) + __popc(f.y) + __popc(f.z) + __popc(f.w); }
+
+// Exclusive prefix of `x` over the CTA (256 threads) and the CTA's total.
+__device__ __forceinline__ uint32_t cta_exclusive(uint32_t x, uint32_t &total) {
+  __shared__ uint32_t s_warp[kReqThreads / 32];
+  const uint32_t lane = threadIdx.x & 31u, wid = threadIdx.x >> 5;
+  uint32_t inc = x;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(kFull, inc, o);
+    if (lane >= (uint32_t)o) inc += y;
+  }
+  if (lane == 31) s_warp[wid] = inc;
+  __syncthreads();
+  uint32_t before = 0;
+  total = 0;
+#pragma unroll
+  for (int k = 0; k < kReqThreads / 32; k++) {
+    const uint32_t c = s_warp[k];
+    if ((uint32_t)k < wid) before += c;
+    total += c;
+  }
+  return before + inc - x;
+}
+
+__global__ void __launch_bounds__(kReqThreads) k_req_count(const uint8_t *flags, uint32_t *chunk_counts) {
+  const uint4 f = reinterpret_cast<const uint4 *>(flags)[(size_t)blockIdx.x * kReqThreads + threadIdx.x];
+  uint32_t total;
+  cta_exclusive(flag_count(f), total);
+  if (threadIdx.x == 0) chunk_counts[blockIdx.x] = total;
+}
+
+// One CTA of 1024 threads: chunk counts -> exclusive chunk offsets (in place);
+// *raised = the total.
+__global__ void __launch_bounds__(1024) k_req_scan(uint32_t *chunk, uint32_t n, uint32_t *raised) {
+  __shared__ uint32_t part[1024];
+  const uint32_t per = (n + 1023u) / 1024u, b = threadIdx.x * per, e = min(n, b + per);
+  uint32_t s = 0;
+  for (uint32_t i = b; i < e; i++) s += chunk[i];
+  part[threadIdx.x] = s;
+  __syncthreads();
+  for (uint32_t off = 1; off < 1024u; off <<= 1) {
+    const uint32_t v = threadIdx.x >= off ? part[threadIdx.x - off] : 0u;
+    __syncthreads();
+    part[threadIdx.x] += v;
+    __syncthreads();
+  }
+  uint32_t run = part[threadIdx.x] - s;
+  for (uint32_t i = b; i < e; i++) {
+    const uint32_t c = chunk[i];
+    chunk[i] = run;
+    run += c;
+  }
+  if (threadIdx.x == 1023) *raised = part[1023];
+}
+
+// Each flagged pixel's staged record goes to queue slot (its rank in pixel
+// order) while that rank is below the cap.
+__global__ void __launch_bounds__(kReqThreads) k_req_scatter(const uint8_t *flags, const uint32_t *chunk_offsets,
+                                                             const svo_child_request *stage, svo_child_request *queue,
+                                                             uint32_t cap) {
+  const uint32_t first = chunk_offsets[blockIdx.x];
+  if (first >= cap) return;  // the whole CTA: its ranks all lie past the cap
+  const size_t word = (size_t)blockIdx.x * kReqThreads + threadIdx.x;
+  const uint4 f = reinterpret_cast<const uint4 *>(flags)[word];
+  uint32_t total;
+  uint32_t rank = first + cta_exclusive(flag_count(f), total);
+  const uint32_t w4[4] = {f.x, f.y, f.z, f.w};
+#pragma unroll
+  for (int k = 0; k < 16; k++) {
+    if ((w4[k >> 2] >> (8 * (k & 3))) & 0xffu) {
+      if (rank < cap) queue[rank] = stage[word * 16 + k];
+      rank++;
+    }
+  }
+}
+
 }  // namespace
+
+svo_status launch_request_compaction(const TraceLaunch &a, uint32_t total_pixels, uint32_t *chunk_offsets,
+                                     void *stream) {
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const uint32_t chunks = (total_pixels + kRequestChunk - 1) / kRequestChunk;
+  if (!chunks) return SVO_OK;
+  k_req_count<<<chunks, kReqThreads, 0, s>>>(a.req_flag, chunk_offsets);
+  k_req_scan<<<1, 1024, 0, s>>>(chunk_offsets, chunks, a.request_count);
+  if (a.requests && a.request_cap)
+    k_req_scatter<<<chunks, kReqThreads, 0, s>>>(a.req_flag, chunk_offsets, a.req_stage, a.requests, a.request_cap);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return fail(SVO_ERR_CUDA, std::string("request compaction launch: ") + cudaGetErrorString(e));
+  return SVO_OK;
+}
 
 size_t trace_smem_bytes(const TraceLaunch &a, bool bases_in_smem) {
   size_t b = (size_t)a.n_views * sizeof(ViewParams);

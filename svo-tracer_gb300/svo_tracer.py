@@ -54,6 +54,7 @@ STATUS_NAMES = {
 }
 SCENE_SPHERE, SCENE_TERRAIN = 0, 1
 SCHEDULE_LANE, SCHEDULE_WARP = 1, 2
+REQUESTS_ARRIVAL, REQUESTS_PIXEL = 1, 2
 
 
 class SvoError(RuntimeError):
@@ -84,7 +85,8 @@ class TraceStatsC(C.Structure):
 
 class TraceConfigC(C.Structure):
     _fields_ = [(n, C.c_int32) for n in ("block_size", "ctas_per_sm", "ray_chunk", "cadence", "max_steps",
-                                          "collect_stats", "max_hits", "schedule", "mega_band_tiles", "l2_window")]
+                                          "collect_stats", "max_hits", "schedule", "mega_band_tiles", "l2_window",
+                                          "pass_limit", "request_order")]
 
 
 class SceneParamsC(C.Structure):
@@ -180,6 +182,8 @@ def load_library(path: str | None = None) -> C.CDLL:
         "svo_graft_payload_data": ([vp, C.POINTER(vp), C.POINTER(sz), C.POINTER(vp), C.POINTER(sz)], C.c_int32),
         "svo_graft_payload_free": ([vp], C.c_int32),
         "svo_scene_free": ([vp], C.c_int32),
+        "svo_trace_noalloc": ([C.c_int32, vp, C.c_uint8, vp, sz, vp, sz, vp, sz, C.c_int32, C.POINTER(TraceInputC),
+                               C.POINTER(TraceOutputC), vp, C.c_uint32, C.POINTER(C.c_uint32)], C.c_int32),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)

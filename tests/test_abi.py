@@ -68,3 +68,67 @@ def test_null_context_is_rejected():
     lib = st.load_library()
     assert lib.svo_trace(None, None, None) == 1
     assert lib.svo_upload_octree(None, 4, None, 0, None, 0, 0) == 1
+
+
+_SCALARS = {"int32_t": C.c_int32, "uint32_t": C.c_uint32, "uint16_t": C.c_uint16, "uint8_t": C.c_uint8,
+            "size_t": C.c_size_t, "float": C.c_float, "double": C.c_double, "char": C.c_char}
+_STRUCTS = {"svo_trace_input": "TraceInputC", "svo_trace_output": "TraceOutputC", "svo_trace_config": "TraceConfigC",
+            "svo_trace_stats": "TraceStatsC", "svo_mega_stats": "MegaStatsC", "svo_update_input": "UpdateInputC",
+            "svo_gc_report": "GcReportC", "svo_graft_report": "GraftReportC", "svo_prune_report": "PruneReportC",
+            "svo_scene_params": "SceneParamsC"}
+
+
+def declarations():
+    """(name, [parameter type strings]) of every SVO_API function in include/."""
+    out = []
+    for fn in os.listdir(os.path.join(ROOT, "include")):
+        if not fn.endswith(".h"):
+            continue
+        text = re.sub(r"/\*.*?\*/", " ", open(os.path.join(ROOT, "include", fn)).read(), flags=re.S)
+        for m in re.finditer(r"SVO_API\s+[\w\s\*]+?\b(svo_\w+)\s*\(([^)]*)\)\s*;", text):
+            params = [" ".join(p.split()) for p in m.group(2).split(",") if p.strip() and p.strip() != "void"]
+            out.append((m.group(1), [re.sub(r"\s*\b\w+$", "", p) for p in params]))
+    return out
+
+
+def _accepts(ctype_str, binding):
+    """Whether a ctypes argtype can carry the C parameter type `ctype_str`."""
+    t = ctype_str.replace("const ", "").strip()
+    stars = t.count("*")
+    base = t.replace("*", "").strip()
+    if stars == 0:
+        return binding is _SCALARS[base]
+    if stars == 2:
+        return binding is C.POINTER(C.c_void_p)
+    if base == "char":
+        return binding is C.c_char_p
+    if binding is C.c_void_p:  # arrays and opaque handles
+        return base not in _STRUCTS
+    if base in _STRUCTS:
+        return binding is C.POINTER(getattr(st, _STRUCTS[base]))
+    return binding is C.POINTER(_SCALARS[base])
+
+
+def test_binding_signatures_match_the_header():
+    """Every declared entry point, svo_trace_noalloc among them, is bound with its
+    header's parameter count and types in order (an argument reordered or
+    retyped in svo.h fails here, without a GPU)."""
+    lib = st.load_library()
+    decls = declarations()
+    assert {n for n, _ in decls} == set(declared_symbols())
+    for name, params in decls:
+        f = getattr(lib, name)
+        assert f.argtypes is not None, name + " has no bound signature"
+        assert len(f.argtypes) == len(params), name
+        for i, (cp, bt) in enumerate(zip(params, f.argtypes)):
+            assert _accepts(cp, bt), "%s argument %d: %s bound as %r" % (name, i, cp, bt)
+    assert ("svo_trace_noalloc", ["int32_t", "void *", "uint8_t", "const uint16_t *", "size_t", "const svo_block *",
+                                  "size_t", "svo_usage *", "size_t", "int32_t", "const svo_trace_input *",
+                                  "const svo_trace_output *", "svo_child_request *", "uint32_t",
+                                  "uint32_t *"]) in decls
+
+
+def test_trace_config_layout():
+    names = [n for n, _ in st.TraceConfigC._fields_]
+    assert names[-2:] == ["pass_limit", "request_order"]
+    assert C.sizeof(st.TraceConfigC) == 4 * len(names)

@@ -82,6 +82,69 @@ def test_stream_matches_oracle(tracer, base_depth, depth, initial, budget, thres
     assert grafted_total > 0 and pruned_total > 0
 
 
+def test_stream_past_the_request_cap_matches_oracle(tracer):
+    """The streaming workflow with frames that raise far more child requests than
+    the queue holds (the pixel-order rule decides which are kept), over enough frames
+    for a 30-frame staleness threshold to prune: per frame the trace outputs, the
+    request queue, the pruned, freed, free-list and claimed groups and the whole
+    block and usage arrays match the oracle; a second context that answers the
+    requests on the device (svo_graft_generate) reaches the same tree frame by
+    frame."""
+    cap, threshold, frames = 2048, 30, 40
+    scene = st.Scene(st.SCENE_TERRAIN, seed=5, base_depth=3, depth=10)
+    tree = scene.build_tree(8)
+    budget = (len(tree.Blocks) + 7) // 8 + (1 << 14)
+    dev = st.Tracer(0)
+    try:
+        for tr in (tracer, dev):
+            tr.set_config(block_size=256, ctas_per_sm=0, max_steps=1 << 16, collect_stats=0,
+                          request_order=st.REQUESTS_PIXEL)
+            tr.upload(tree, block_budget=budget * 8)
+            tr.init_usage_tree(1)
+        oracle = po.TreeState(tree, budget)
+        oracle.init_usage_tree(1)
+        cams = st.camera_path(seed=3, frames=frames, width=256, height=144, MaxChildRequestId=cap)
+        overflowed = pruned_total = grafted_total = 0
+        for f, cam in enumerate(cams):
+            tick = f + 1
+            got = tracer.trace(cam)
+            dev.trace(cam)
+            want = po.trace_view(oracle.as_octree(), cam, usage=oracle.usage)
+            for k in ("hit_index", "hit_depth", "t", "rgba"):
+                assert np.array_equal(getattr(got, k), want[k]), "frame %d: %s" % (f, k)
+            req, n = tracer.read_child_requests(cap=cap)
+            assert n == want["n_requests"], "frame %d: requests raised" % f
+            assert req.tobytes() == want["pixel_requests"][:cap].tobytes(), "frame %d: request queue" % f
+            overflowed += n > cap
+            rec, pay = scene.graft_payload(req)
+            rep = tracer.gc(tick, threshold)
+            assert dev.gc(tick, threshold) == rep, "frame %d: device-generation context's GC" % f
+            g_pruned, g_freed, g_free = tracer.gc_lists(rep["pruned"], rep["freed"], rep["free"])
+            o_pruned, o_freed, o_free = oracle.gc(tick, threshold)
+            assert np.array_equal(g_pruned, o_pruned), "frame %d: pruned sets differ" % f
+            assert np.array_equal(g_freed, o_freed), "frame %d: freed sets differ" % f
+            assert np.array_equal(g_free, o_free), "frame %d: free lists differ" % f
+            grep = tracer.graft(tick, rec, pay)
+            o_claims, applied = oracle.graft(tick, rec, pay)
+            claims = tracer.graft_claims(grep["claimed"])
+            assert np.array_equal(claims, o_claims), "frame %d: grafted groups differ" % f
+            assert grep["applied"] == int(applied.sum())
+            drep = dev.graft_generate(tick, scene)
+            assert drep == grep, "frame %d: %r vs %r" % (f, drep, grep)
+            assert_state(tracer, oracle, "frame %d" % f)
+            hb, hu = gpu_state(tracer, budget)
+            db, du = gpu_state(dev, budget)
+            assert hb.tobytes() == db.tobytes() and hu.tobytes() == du.tobytes(), "frame %d: generation paths" % f
+            pruned_total += len(g_pruned)
+            grafted_total += len(claims)
+        assert overflowed >= frames // 2, "the frames must overflow the queue"
+        assert pruned_total > 0 and grafted_total > 0
+    finally:
+        dev.close()
+        tracer.set_config(request_order=st.REQUESTS_ARRIVAL)
+        scene.close()
+
+
 def test_prune_matches_oracle(tracer):
     scene = st.Scene(st.SCENE_TERRAIN, seed=8, base_depth=3, depth=9)
     tree = scene.build_tree(8)

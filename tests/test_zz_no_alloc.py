@@ -5,9 +5,9 @@ real-time host loop that may not call cudaMalloc) keeps the octree and the outpu
 buffers in memory it already owns and calls svo_trace_noalloc, whose only scratch is
 a fixed static array inside libsvo. This test gives it buffers allocated here (the
 test may allocate; the entry point does not) and checks two calls in a row against
-the context-based svo_trace entry point on the same tree and view: hit indices, hit
-depths, usage ticks and child requests bit for bit, t and RGBA within the tolerance
-the other GPU tests use (they are in fact bit-exact)."""
+the context-based svo_trace entry point on the same tree and view, and against the
+oracle: hit indices, hit depths, usage ticks and child requests bit for bit, t and
+RGBA within the tolerance the other GPU tests use (they are in fact bit-exact)."""
 import ctypes as C
 
 import numpy as np
@@ -22,12 +22,7 @@ T_RTOL = 1e-5
 
 
 def _entry(lib):
-    f = lib.svo_trace_noalloc
-    f.argtypes = [C.c_int32, C.c_void_p, C.c_uint8, C.c_void_p, C.c_size_t, C.c_void_p, C.c_size_t, C.c_void_p,
-                  C.c_size_t, C.c_int32, C.POINTER(st.TraceInputC), C.POINTER(st.TraceOutputC), C.c_void_p,
-                  C.c_uint32, C.POINTER(C.c_uint32)]
-    f.restype = C.c_int32
-    return f
+    return lib.svo_trace_noalloc  # bound by svo_tracer with the header's signature (checked in test_abi)
 
 
 def test_noalloc_matches_trace_on_two_calls():
@@ -47,6 +42,8 @@ def test_noalloc_matches_trace_on_two_calls():
         usage_want = tr.read_usage(n_groups)
         req_want, n_want = tr.read_child_requests()
     assert n_want > 0 and (want.hit_index != st.MISS).any()
+    usage_oracle = usage0.copy()
+    oracle = po.trace_view(tree, cam, usage=usage_oracle)
 
     dev = torch.device("cuda", 0)
     d_bases = torch.from_numpy(tree.BaseBlocks.view(np.int16).copy()).to(dev)
@@ -71,16 +68,21 @@ def test_noalloc_matches_trace_on_two_calls():
         dep = d_dep.cpu().numpy()
         t = d_t.cpu().numpy()
         rgba = d_rgba.cpu().numpy().reshape(-1, 4)
-        assert np.array_equal(idx, want.hit_index), "call %d: hit_index" % call
-        assert np.array_equal(dep, want.hit_depth), "call %d: hit_depth" % call
-        np.testing.assert_allclose(t, want.t, rtol=T_RTOL, atol=0)
-        np.testing.assert_allclose(rgba, want.rgba, rtol=T_RTOL, atol=0)
         usage = d_usage.cpu().numpy().view(st.USAGE_DTYPE)
-        assert np.array_equal(usage["tick"], usage_want["tick"]), "call %d: usage ticks" % call
-        assert raised.value == n_want
         req = d_req.cpu().numpy().view(st.CHILD_REQUEST_DTYPE)[: min(raised.value, cap)]
-        same = po.sort_requests(req).tobytes() == po.sort_requests(req_want).tobytes()
-        assert same, "call %d: child requests differ" % call
+        # against the existing entry point, then against the oracle
+        for label, ref_idx, ref_dep, ref_t, ref_rgba, ref_ticks, ref_n, ref_req in (
+                ("svo_trace", want.hit_index, want.hit_depth, want.t, want.rgba, usage_want["tick"], n_want, req_want),
+                ("oracle", oracle["hit_index"], oracle["hit_depth"], oracle["t"], oracle["rgba"],
+                 usage_oracle["tick"], oracle["n_requests"], oracle["requests"])):
+            assert np.array_equal(idx, ref_idx), "call %d vs %s: hit_index" % (call, label)
+            assert np.array_equal(dep, ref_dep), "call %d vs %s: hit_depth" % (call, label)
+            np.testing.assert_allclose(t, ref_t, rtol=T_RTOL, atol=0)
+            np.testing.assert_allclose(rgba, ref_rgba, rtol=T_RTOL, atol=0)
+            assert np.array_equal(usage["tick"], ref_ticks), "call %d vs %s: usage ticks" % (call, label)
+            assert raised.value == ref_n, "call %d vs %s: requests raised" % (call, label)
+            same = po.sort_requests(req).tobytes() == po.sort_requests(ref_req).tobytes()
+            assert same, "call %d vs %s: child requests differ" % (call, label)
 
 
 def test_noalloc_rejects_oversized_views_and_host_outputs():
