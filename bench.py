@@ -118,6 +118,15 @@ def ncu_traffic():
         return None
 
 
+def roofline(alg_bytes, ms, what):
+    """HBM roofline of one timed launch (or sequence): the algorithmic bytes over the
+    CUDA-event time, against the measured copy bandwidth."""
+    peak, kind = measured_peak()
+    achieved = alg_bytes / (ms / 1000.0) / 1e9
+    return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "peak_kind": kind, "algorithmic_bytes": int(alg_bytes), "ms": ms, "bytes": what}
+
+
 def cpu_sample(tree, cam, kind, budget_s=12.0):
     """The CPU implementation over row bands of the same frame until ~budget_s."""
     import pyoracle as po
@@ -143,6 +152,21 @@ def cpu_sample(tree, cam, kind, budget_s=12.0):
             "sample": "%d rays in %d row bands of %d rows of the 1080p frame, %.1f s" % (rays, band, rows_per_band, el)}
 
 
+def reference_scene(st):
+    """The benchmarked tree read from the .oct file that __graft_entry__.build()
+    writes, with numpy alone: the reference arm's process never loads libsvo (a
+    missing file is written by a child process)."""
+    import __graft_entry__
+
+    path = __graft_entry__.REFERENCE_SCENE
+    if not os.path.exists(path):
+        subprocess.run([sys.executable, "-c", "import __graft_entry__ as g; g.write_reference_scene()"], cwd=ROOT,
+                       check=True)
+    tree = st.map_oct(path)
+    cam = st.look_at(CAM_ORIGIN, CAM_TARGET, WIDTH, HEIGHT, FOV, Tick=7, MaxChildRequestId=1 << 16)
+    return tree, cam
+
+
 def run_reference(args, rank, world):
     """The reference's own wavefront.cl kernels, built for the host CPU, on the same frame."""
     if rank != 0:
@@ -153,7 +177,7 @@ def run_reference(args, rank, world):
     if not po.ref_available():
         print(json.dumps({"impl": "reference", "unavailable": "reference kernels (oracle/_ref) not built on this host"}))
         return
-    tree, cam = workload(st)
+    tree, cam = reference_scene(st)
     threads = os.cpu_count() or 1
     # each step: 2 bands of 20 rows; the bands of all steps spread evenly over the
     # frame (its top rows are mostly sky, its bottom rows terrain)
@@ -198,6 +222,12 @@ def multiview(tr, torch, dev, stream, flush, args, windows=None):
     batched_t, batched_p = alloc()
     plain_t, plain_p = alloc()
     cfg0 = {n: getattr(tr.get_config(), n) for n in ("block_size", "ray_chunk", "cadence", "ctas_per_sm")}
+    # the reference walk's node and base reads of the 64 views (a counting launch, untimed)
+    tr.set_config(collect_stats=1)
+    tr.trace_device(views, batched_p)
+    vstats = tr.stats()
+    tr.set_config(collect_stats=0)
+    alg = 16 * vstats["block_node_reads"] + 2 * vstats["base_steps"] + OUT_BYTES * rays
     with torch.cuda.stream(stream):
         # plain: one launch per view with the default configuration
         for _ in range(2):
@@ -239,6 +269,9 @@ def multiview(tr, torch, dev, stream, flush, args, windows=None):
     return {"views": len(views), "rays": rays, "batched_ms": batched, "plain_ms": plain,
             "batched_mrays_s": rays / batched / 1e3, "plain_mrays_s": rays / plain / 1e3,
             "speedup": plain / batched, "identical_outputs": bool(same), "autotuned": tuned,
+            "roofline": roofline(alg, batched, "16 B per node read of the reference walk + 2 B per base chunk read "
+                                               "+ 25 B of output per pixel, summed over the 64 views"),
+            "roofline_plain": roofline(alg, plain, "the same bytes over the 64 plain launches"),
             "batched": "one persistent launch over all views, replayed from a CUDA graph",
             "plain": "64 sequential single-view launches, same stream, default configuration"}
 
@@ -309,6 +342,11 @@ def mega_workload(tr, torch, dev, stream, flush, args, tree, cam, windows=None):
     ptrs = [x.data_ptr() for x in o]
     steps = max(3, args.steps // 4)
     with torch.cuda.stream(stream):
+        # the primary and secondary cones' node and base reads (a counting launch, untimed)
+        tr.set_config(collect_stats=1)
+        tr.mega_trace_device(cam, *ptrs)
+        mstats = tr.stats()
+        tr.set_config(collect_stats=0)
         for _ in range(2):
             flush.zero_()
             tr.mega_trace_device(cam, *ptrs)
@@ -346,6 +384,9 @@ def mega_workload(tr, torch, dev, stream, flush, args, tree, cam, windows=None):
             "mrays_s": rays / frame_ms / 1e3, "primary_rays": stats["pixels"], "cones": stats["cones"],
             "cones_per_pixel": stats["cones"] / max(1, stats["pixels"]), "surfaces": stats["surfaces"],
             "cone_slots": stats["cone_slots"], "steps": steps,
+            "roofline": roofline(16 * mstats["block_node_reads"] + 2 * mstats["base_steps"] + n * OUT_BYTES, frame_ms,
+                                 "16 B per node read + 2 B per base chunk read of every primary and secondary cone "
+                                 "+ 25 B of output per pixel"),
             "e2e": {"frame_ms": 1000.0 * e2e_s, "mrays_s": rays / e2e_s / 1e6,
                     "d2h_bytes_per_step": n * OUT_BYTES},
             "workload": "kernel.cl trace over the 1080p terrain frame, reference default cone parameters"}
@@ -444,6 +485,8 @@ def _stream_run(st, scene, tree, cams, dev, device_generate):
         gpu["trace"] += m[0].elapsed_time(m[1])
         gpu["gc"] += m[1].elapsed_time(m[2])
         gpu["graft"] += m[2].elapsed_time(m[3])
+    upd_ms = gpu["gc"] + gpu["graft"]
+    upd_bytes = 8 * budget * len(cams) + 16 * 8 * totals["grafted_groups"]
     usage = tr.read_usage(budget)
     resident = int(((usage["tick"] >= 1) & (usage["tick"] <= 65533)).sum())
     digest = hashlib.sha256()
@@ -455,6 +498,9 @@ def _stream_run(st, scene, tree, cams, dev, device_generate):
             "mrays_s_with_updates": frames * n / loop_s / 1e6,
             "ms_per_frame_by_phase": {k: 1000 * v / frames for k, v in phase.items()},
             "gpu_ms_per_frame_by_phase": {k: v / frames for k, v in gpu.items()},
+            "roofline_updates": roofline(upd_bytes / frames, upd_ms / frames,
+                                         "per frame: 8 B per budget group of the GC's usage scan + 16 B per grafted "
+                                         "node, over the GC and graft GPU time"),
             "totals": totals, "resident_groups_end": resident}
 
 
@@ -544,6 +590,12 @@ def _diff_timed(tr, torch, dev, stream, flush, args, tree, views, rays, nodes, w
         return float(np.median(ms))
 
     steps = max(5, args.steps // 2)
+    # the forward walk's node and base reads and its composited hits (a counting launch, untimed)
+    tr.set_config(collect_stats=1)
+    tr.diff_forward_device(views, rgb.data_ptr())
+    dstats = tr.stats()
+    tr.set_config(collect_stats=0)
+    walk = 16 * dstats["block_node_reads"] + 2 * dstats["base_steps"]
     for _ in range(3):
         tr.diff_forward_device(views, rgb.data_ptr())
         tr.diff_backward_device(views, target.data_ptr())
@@ -574,6 +626,10 @@ def _diff_timed(tr, torch, dev, stream, flush, args, tree, views, rays, nodes, w
             "bwd_recompute_colour_ms": bwd_recompute_ms,
             "fwd_bwd_mrays_s": rays / step_ms / 1e3, "fwd_mrays_s": rays / fwd_ms / 1e3,
             "bwd_mrays_s": rays / bwd_ms / 1e3, "initial_loss": loss0,
+            "hits": int(dstats["hits"]),
+            "roofline": roofline(2 * (walk + 12 * rays) + 16 * dstats["hits"], step_ms,
+                                 "2 x (16 B per node read + 2 B per base chunk read of the walk + 12 B of colour or "
+                                 "target per ray) + 16 B of gradient per composited hit"),
             "e2e": {"value": rays / e2e_s / 1e6, "unit": "Mrays/s (fwd+bwd)",
                     "h2d_bytes_per_step": nodes * 16 + rays * 12, "d2h_bytes_per_step": rays * 12 + nodes * 16 + 8},
             "l2": "flushed between steps (256 MiB write)"}

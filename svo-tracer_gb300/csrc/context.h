@@ -83,7 +83,7 @@ struct Context {
   DevBuf<unsigned long long> stats;
   DevBuf<svo_child_request> requests;
   // pixel-order requests: the staged record and flag per pixel, chunk offsets
-  DevBuf<svo_child_request> req_stage;
+  DevBuf<StagedRequest> req_stage;
   DevBuf<uint8_t> req_flag;
   DevBuf<uint32_t> req_chunks;
   DevBuf<ViewParams> views;

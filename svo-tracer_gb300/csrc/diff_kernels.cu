@@ -122,13 +122,16 @@ __device__ __forceinline__ float3 sky_rgb(const Ray &r) {
 
 // Visits the hits of one ray in order: visit(node, is_background) with
 // is_background = true once for the sky contribution (node unused). Each pass
-// of the loop probes (and counts) a step, and a probe past max_steps ends the
-// ray in the sky, so a walk takes at most max_steps + 1 passes. A walk that
-// needs more than its bound (max_steps + 2, or the launch's pass_limit) records
-// the timeout in the error record and returns false without finishing.
-template <class Visit>
+// of the loop probes (and counts, in r.steps) a step, and a probe past
+// max_steps ends the ray in the sky, so a walk takes at most max_steps + 1
+// passes. A walk that has taken its bound of steps (max_steps + 2, or the
+// launch's pass_limit) without finishing records the timeout in the error
+// record and returns false.
+// kStats: the walk's reference-walk counters (V_block, V_base, hits) are
+// added to st, as the trace kernel's statistics count them.
+template <bool kStats, class Visit>
 __device__ __forceinline__ bool walk_hits(const DiffLaunch &d, const ViewParams *s_views, const uint16_t *s_bases,
-                                          uint32_t ray, Walk &w, Visit &&visit) {
+                                          uint32_t ray, Walk &w, Stats &st, Visit &&visit) {
   const TraceLaunch &a = d.t;
   const int B = a.base_depth;
   const uint4 *blocks = reinterpret_cast<const uint4 *>(a.blocks);
@@ -136,12 +139,22 @@ __device__ __forceinline__ bool walk_hits(const DiffLaunch &d, const ViewParams 
   setup_ray(a, s_views, ray, r);
   w.cur_addr = 0xffffffffu;
   w.last_group = 0xffffffffu;
-  Stats st;
+  w.v_block = 0;
+  w.v_base = 0;
+  auto counted = [&](bool ok) {
+    if (kStats) {
+      st.rays++;
+      st.block_reads += w.v_block;
+      st.base_steps += w.v_base;
+    }
+    return ok;
+  };
   const ViewParams &v = s_views[r.view];
   int hits = 0;
+  // every pass probes one step (r.steps counts them) or ends the walk
   const uint32_t limit = a.pass_limit ? a.pass_limit : (uint32_t)a.max_steps + 2u;
-  for (uint32_t pass = 1;; pass++) {
-    if (pass > limit) {
+  for (;;) {
+    if ((uint32_t)r.steps >= limit) {
       if (a.error && atomicCAS(a.error, 0u, (unsigned)SVO_ERR_TIMEOUT) == 0u) {
         a.error[1] = blockIdx.x;
         a.error[2] = threadIdx.x;
@@ -149,24 +162,25 @@ __device__ __forceinline__ bool walk_hits(const DiffLaunch &d, const ViewParams 
         a.error[4] = (uint32_t)r.depth;
         a.error[5] = (uint32_t)r.steps;
       }
-      return false;
+      return counted(false);
     }
-    int f = step<false, true>(a, v, s_bases, blocks, B, r, w, st);
+    int f = step<kStats, true>(a, v, s_bases, blocks, B, r, w, st);
     if (f == kStepOn) continue;
     if (f == kStepBackground) {
       visit(0u, true, r);
-      return true;
+      return counted(true);
     }
     visit(w.path[(r.depth - B - 2) * w.stride], false, r);
-    if (++hits >= d.max_hits) return true;
+    if (kStats) st.hits++;
+    if (++hits >= d.max_hits) return counted(true);
     if (step_past(a, blocks, B, r, w) == kStepBackground) {
       visit(0u, true, r);
-      return true;
+      return counted(true);
     }
   }
 }
 
-template <bool kBackward>
+template <bool kBackward, bool kStats>
 __global__ void __launch_bounds__(256, kBackward ? SVO_DIFF_BWD_MIN_CTAS : SVO_DIFF_FWD_MIN_CTAS) diff_kernel(const DiffLaunch d) {
   extern __shared__ __align__(16) uint8_t smem[];
   const TraceLaunch &a = d.t;
@@ -187,6 +201,7 @@ __global__ void __launch_bounds__(256, kBackward ? SVO_DIFF_BWD_MIN_CTAS : SVO_D
   w.path = s_path + threadIdx.x;
   w.stride = blockDim.x;
   double loss_part = 0.0;
+  Stats st = {0, 0, 0, 0, 0, 0, 0};
   // Warp-uniform loop over rays (lane i of a warp takes ray base + i) with a
   // warp vote (__any_sync, which also regroups the lanes) after each phase,
   // which every lane of the warp reaches on every iteration: the lanes regroup
@@ -208,7 +223,7 @@ __global__ void __launch_bounds__(256, kBackward ? SVO_DIFF_BWD_MIN_CTAS : SVO_D
     full.init();
     bool stopped = false;  // a walk ran past its pass bound: the warp leaves the loop
     if (live && (!kBackward || !d.use_saved)) {
-      stopped = !walk_hits(d, s_views, s_bases, ray, w, [&](uint32_t node, bool bg, const Ray &r) {
+      stopped = !walk_hits<kStats>(d, s_views, s_bases, ray, w, st, [&](uint32_t node, bool bg, const Ray &r) {
         if (bg)
           full.sky(sky_rgb(r));
         else
@@ -242,7 +257,7 @@ __global__ void __launch_bounds__(256, kBackward ? SVO_DIFF_BWD_MIN_CTAS : SVO_D
       // the gradient walk: replay the prefix sums, one contribution at a time
       Composite pre;
       pre.init();
-      stopped = !walk_hits(d, s_views, s_bases, ray, w, [&](uint32_t node, bool bg, const Ray &) {
+      stopped = !walk_hits<false>(d, s_views, s_bases, ray, w, st, [&](uint32_t node, bool bg, const Ray &) {
         if (bg) return;
         float4 p = __ldg(d.params + node);
         float T = pre.T, ta = __fmul_rn(T, p.w);
@@ -294,6 +309,15 @@ __global__ void __launch_bounds__(256, kBackward ? SVO_DIFF_BWD_MIN_CTAS : SVO_D
     double v = cooperative_groups::reduce(g, loss_part, cooperative_groups::plus<double>());
     if (g.thread_rank() == 0) atomicAdd(d.loss, v);
   }
+  if (kStats && a.stats) {
+    unsigned long long vals[7] = {st.rays, st.hits, st.base_steps, st.block_reads, st.block_steps, 0, st.limited};
+    cooperative_groups::coalesced_group g = cooperative_groups::coalesced_threads();
+#pragma unroll
+    for (int k = 0; k < 7; k++) {
+      unsigned long long x = cooperative_groups::reduce(g, vals[k], cooperative_groups::plus<unsigned long long>());
+      if (g.thread_rank() == 0 && x) atomicAdd(a.stats + k, x);
+    }
+  }
 }
 
 template <bool kBackward>
@@ -337,7 +361,13 @@ svo_status run_diff(Context &c, const svo_trace_input *views, int32_t n, const f
   d.t.block_size = 256;
   size_t smem = (size_t)n * sizeof(ViewParams) + ((c.n_bases * 2 + 15) & ~(size_t)15) +
                 (size_t)d.t.path_levels * 256 * 4;
-  auto kernel = diff_kernel<kBackward>;
+  // collect_stats: the forward counts its walk (V_block, V_base, hits) into the
+  // context's trace statistics (svo_last_trace_stats)
+  const bool stats = !kBackward && c.cfg.collect_stats > 0;
+  d.t.stats = stats ? c.stats.p : nullptr;
+  auto kernel = diff_kernel<kBackward, false>;
+  if constexpr (!kBackward)
+    if (stats) kernel = diff_kernel<false, true>;
   SVO_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem), "svo_diff: smem");
   int occ = 0;
   SVO_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kernel, 256, smem), "svo_diff: occupancy");
@@ -349,6 +379,7 @@ svo_status run_diff(Context &c, const svo_trace_input *views, int32_t n, const f
            "svo_diff: tables");
   SVO_CUDA(cudaEventRecord(c.staged, c.stream), "svo_diff: staging event");
   SVO_CUDA(cudaMemsetAsync(c.counters.p, 0, kErrorOffset * sizeof(uint32_t), c.stream), "svo_diff: counters");
+  if (stats) SVO_CUDA(cudaMemsetAsync(c.stats.p, 0, 8 * sizeof(unsigned long long), c.stream), "svo_diff: stats");
   if (kBackward) {
     SVO_CUDA(cudaMemsetAsync(c.grads.p, 0, c.grads.n * sizeof(float), c.stream), "svo_diff: grads");
     SVO_CUDA(cudaMemsetAsync(c.diff_loss.p, 0, sizeof(double), c.stream), "svo_diff: loss");
@@ -362,6 +393,7 @@ svo_status run_diff(Context &c, const svo_trace_input *views, int32_t n, const f
     if (es) return es;
   }
   if (!kBackward) {
+    c.last_stats_valid = stats;
     c.saved_views.assign(views, views + n);
     c.saved_params_gen = c.params_gen;
     c.saved_max_hits = c.cfg.max_hits;

@@ -162,7 +162,10 @@ svo_status run_mega(Context &c, const svo_trace_input *in, const svo_trace_outpu
     return fail(SVO_ERR_OUT_OF_MEMORY, "svo_mega_trace: allocation failed");
 
   MegaLaunch m{};
-  st = prepare_launch(c, 1, total_rays, m.t, false);
+  // collect_stats: the primary and cone kernels count their reference-walk reads
+  // (svo_last_trace_stats; rays = primary + secondary cones)
+  const bool stats = c.cfg.collect_stats > 0;
+  st = prepare_launch(c, 1, total_rays, m.t, stats);
   if (st) return st;
   m.pix = c.mega_pix.p;
   m.cone_dw = c.mega_cone_dw.p;
@@ -192,6 +195,7 @@ svo_status run_mega(Context &c, const svo_trace_input *in, const svo_trace_outpu
   SVO_CUDA(cudaEventRecord(c.staged, c.stream), fn);
   SVO_CUDA(cudaMemsetAsync(c.counters.p, 0, kErrorOffset * sizeof(uint32_t), c.stream), fn);
   SVO_CUDA(cudaMemsetAsync(c.mega_totals.p, 0, 2 * sizeof(unsigned long long), c.stream), fn);
+  if (stats) SVO_CUDA(cudaMemsetAsync(c.stats.p, 0, 8 * sizeof(unsigned long long), c.stream), fn);
   st = launch_mega_primary(m, c.stream);
   if (st) return st;
   uint64_t slots = 0;
@@ -218,7 +222,7 @@ svo_status run_mega(Context &c, const svo_trace_input *in, const svo_trace_outpu
   st = read_error(c, fn);  // one synchronisation: outputs, totals and the error record
   if (st) return st;
   c.last_rays = total_pixels;
-  c.last_stats_valid = false;
+  c.last_stats_valid = stats;
   c.last_mega.pixels = total_pixels;
   c.last_mega.cones = c.h_mega_totals.p[0];
   c.last_mega.surfaces = c.h_mega_totals.p[1];

@@ -26,6 +26,7 @@
 // order (no contraction). The trigonometry of the fan is per-launch constants
 // and a table over the 65536 int16 normal angles, (float)sin((double)x) on the
 // host like the ray-setup tables; normalize of a zero vector is that vector.
+#include <cooperative_groups/reduce.h>
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -185,26 +186,50 @@ __device__ __forceinline__ void record_timeout(const TraceLaunch &a, uint32_t it
 }
 
 // Runs a cone to its end: kStepHit at a surface, kStepBackground in the sky;
-// false when it needed more passes than max_steps allows (a fault).
-template <bool kSmemBases>
+// false when it needed more passes than max_steps allows (a fault). kStats: the
+// cone's reference-walk counters (V_block, V_base) and its hit go to st.
+template <bool kSmemBases, bool kStats>
 __device__ __forceinline__ bool run_cone(const TraceLaunch &a, const ViewParams &v, const uint16_t *s_bases,
-                                         const uint4 *blocks, int B, Ray &r, Walk &w, int &finish) {
-  Stats st;
+                                         const uint4 *blocks, int B, Ray &r, Walk &w, int &finish, Stats &st) {
   const uint32_t limit = a.pass_limit ? a.pass_limit : (uint32_t)a.max_steps + 2u;
   uint32_t n = 0;
   finish = kStepOn;
   while (finish == kStepOn) {
     if (++n > limit) return false;
-    finish = probe<false, kSmemBases, true>(a, v, s_bases, blocks, B, r, w, st);
+    finish = probe<kStats, kSmemBases, true>(a, v, s_bases, blocks, B, r, w, st);
+    if (SVO_TRACE_PROBE_RUNS)
+      while (finish == kStepOn) {
+        if (++n > limit) return false;
+        finish = probe<kStats, kSmemBases, true>(a, v, s_bases, blocks, B, r, w, st);
+      }
     if (finish == kStepEmpty) {
       finish = advance(a, blocks, B, r, w);
       r.fresh = false;
     }
   }
+  if (kStats) {
+    st.rays++;
+    st.block_reads += w.v_block;
+    st.base_steps += w.v_base;
+    if (finish == kStepHit) st.hits++;
+  }
   return true;
 }
 
-template <bool kSmemBases>
+// Adds a thread's counters to the launch's statistics (svo_trace_stats order).
+__device__ __forceinline__ void flush_stats(const TraceLaunch &a, const Stats &st) {
+  if (!a.stats) return;
+  unsigned long long vals[7] = {st.rays, st.hits, st.base_steps, st.block_reads, st.block_steps, st.requests,
+                                st.limited};
+  cg::coalesced_group g = cg::coalesced_threads();
+#pragma unroll
+  for (int k = 0; k < 7; k++) {
+    unsigned long long x = cg::reduce(g, vals[k], cg::plus<unsigned long long>());
+    if (g.thread_rank() == 0 && x) atomicAdd(a.stats + k, x);
+  }
+}
+
+template <bool kSmemBases, bool kStats>
 __global__ void __launch_bounds__(256, SVO_MEGA_MIN_CTAS) mega_primary_kernel(const MegaLaunch m) {
   extern __shared__ __align__(16) uint8_t smem[];
   const TraceLaunch &a = m.t;
@@ -222,6 +247,7 @@ __global__ void __launch_bounds__(256, SVO_MEGA_MIN_CTAS) mega_primary_kernel(co
   const uint32_t lane = threadIdx.x & 31u;
   bool timed_out = false;
   unsigned long long surfaces = 0;
+  Stats st = {0, 0, 0, 0, 0, 0, 0};
   for (;;) {
     uint32_t base = 0;
     if (lane == 0) base = atomicAdd(a.ray_counter, 32u);
@@ -242,7 +268,7 @@ __global__ void __launch_bounds__(256, SVO_MEGA_MIN_CTAS) mega_primary_kernel(co
         r.fresh = true;
         const bool entered = r.depth != 0;
         int finish;
-        if (!run_cone<kSmemBases>(a, v, s_bases, blocks, B, r, w, finish)) {
+        if (!run_cone<kSmemBases, kStats>(a, v, s_bases, blocks, B, r, w, finish, st)) {
           record_timeout(a, my, r);
           timed_out = true;
         }
@@ -285,6 +311,7 @@ __global__ void __launch_bounds__(256, SVO_MEGA_MIN_CTAS) mega_primary_kernel(co
   }
   surfaces = __reduce_add_sync(kFull, (unsigned)surfaces);
   if (lane == 0 && surfaces) atomicAdd(m.totals + 1, surfaces);
+  if (kStats) flush_stats(a, st);
 }
 
 // spawnRays for one slot of the band; one warp per tile.
@@ -457,7 +484,7 @@ __device__ __forceinline__ void start_cone(const MegaLaunch &m, uint32_t e, Ray 
 // accumulateRay's trace for every cone of the band's compacted list: warps
 // claim 32 consecutive entries (kLane false) or lanes refill from the list
 // every `cadence` steps (kLane true).
-template <bool kSmemBases, bool kLane>
+template <bool kSmemBases, bool kLane, bool kStats = false>
 __global__ void __launch_bounds__(256, SVO_MEGA_MIN_CTAS) mega_cone_kernel(const MegaLaunch m) {
   extern __shared__ __align__(16) uint8_t smem[];
   // a block that starts after some cone stopped takes no work (the whole block
@@ -484,6 +511,7 @@ __global__ void __launch_bounds__(256, SVO_MEGA_MIN_CTAS) mega_cone_kernel(const
   if (!kLane) {
     const uint32_t lane = threadIdx.x & 31u;
     bool timed_out = false;
+    Stats cs = {0, 0, 0, 0, 0, 0, 0};
     for (;;) {
       uint32_t base = 0;
       if (lane == 0) base = atomicAdd(m.queue, 32u);
@@ -494,7 +522,7 @@ __global__ void __launch_bounds__(256, SVO_MEGA_MIN_CTAS) mega_cone_kernel(const
         const uint32_t e = m.entries[i];
         start_cone(m, e, r, w);
         int finish;
-        if (!run_cone<kSmemBases>(a, v, s_bases, blocks, B, r, w, finish)) {
+        if (!run_cone<kSmemBases, kStats>(a, v, s_bases, blocks, B, r, w, finish, cs)) {
           record_timeout(a, e, r);
           timed_out = true;
         }
@@ -502,6 +530,7 @@ __global__ void __launch_bounds__(256, SVO_MEGA_MIN_CTAS) mega_cone_kernel(const
       }
       if (__any_sync(kFull, timed_out)) break;
     }
+    if (kStats) flush_stats(a, cs);
   } else {
     // every pass starts a cone or steps one, so a thread runs at most
     // n * (max_steps + 2) + 64 passes; past that it records its state and stops
@@ -611,8 +640,10 @@ int mega_occupancy(const MegaLaunch &m) {
 
 svo_status launch_mega_primary(const MegaLaunch &m, void *stream) {
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  cudaError_t e = bases_in_smem(m.t) ? launch_traversal(mega_primary_kernel<true>, m, m.t.grid, s)
-                                     : launch_traversal(mega_primary_kernel<false>, m, m.t.grid, s);
+  // statistics (m.t.stats) are counted by the shared-memory-bases warp-batch variants
+  cudaError_t e = !bases_in_smem(m.t) ? launch_traversal(mega_primary_kernel<false, false>, m, m.t.grid, s)
+                  : m.t.stats         ? launch_traversal(mega_primary_kernel<true, true>, m, m.t.grid, s)
+                                      : launch_traversal(mega_primary_kernel<true, false>, m, m.t.grid, s);
   if (e != cudaSuccess) return fail(SVO_ERR_CUDA, std::string("megakernel primary launch: ") + cudaGetErrorString(e));
   return SVO_OK;
 }
@@ -627,7 +658,8 @@ svo_status launch_mega_band(const MegaLaunch &m, void *stream) {
   if (e == cudaSuccess) {
     const bool sb = bases_in_smem(m.t), lane = m.cone_schedule == SVO_SCHEDULE_LANE;
     e = sb ? (lane ? launch_traversal(mega_cone_kernel<true, true>, m, m.grid_cones, s)
-                   : launch_traversal(mega_cone_kernel<true, false>, m, m.grid_cones, s))
+                   : (m.t.stats ? launch_traversal(mega_cone_kernel<true, false, true>, m, m.grid_cones, s)
+                                : launch_traversal(mega_cone_kernel<true, false>, m, m.grid_cones, s)))
            : (lane ? launch_traversal(mega_cone_kernel<false, true>, m, m.grid_cones, s)
                    : launch_traversal(mega_cone_kernel<false, false>, m, m.grid_cones, s));
   }

@@ -65,6 +65,18 @@ struct ViewParams {
 };
 static_assert(sizeof(ViewParams) % 8 == 0, "ViewParams alignment");
 
+// A child request staged by its pixel (the pixel-order rule): one aligned
+// 32-byte sector, written with a streaming store; the queue's 40-byte
+// svo_child_request is rebuilt from it (Tick 0, as the wavefront's requests).
+struct alignas(32) StagedRequest {
+  uint64_t location[3];
+  uint32_t address;
+  uint8_t depth;
+  uint8_t tree_size;
+  uint16_t _pad;
+};
+static_assert(sizeof(StagedRequest) == 32, "one sector per staged request");
+
 struct TraceLaunch {
   const uint16_t *bases;
   const void *blocks;  // svo_block[n_blocks]
@@ -100,7 +112,7 @@ struct TraceLaunch {
   // req_flag[pixel] = 1 (pixel in the batch's pixel space; the flags are
   // cleared before the launch), and launch_request_compaction builds the queue
   // afterwards. Null: requests are queued in arrival order.
-  svo_child_request *req_stage;
+  struct StagedRequest *req_stage;
   uint8_t *req_flag;
   // L2 persisting access-policy window of the launch (host side only; 0 bytes: none)
   const void *l2_base;

@@ -389,18 +389,23 @@ __device__ __forceinline__ int probe(const TraceLaunch &a, const ViewParams &v, 
     // ray's pixel slot and the queue is built after the trace. Arrival order:
     // one atomic per group of requesting lanes.
     if (kStats) st.requests++;
-    uint32_t slot = 0;
-    svo_child_request *dst = nullptr;
+    const uint8_t tree_size = kMega ? 1 : (c <= pow2_neg(r.depth + 1) ? 1 : 0);
     if (!kMega && a.req_stage) {
+      // streaming stores: ~one record per ray, read once by the compaction,
+      // and kept from evicting the tree's nodes from L2
       const uint32_t pixel = v.pixel_begin + r.id;
-      dst = a.req_stage + pixel;
-      a.req_flag[pixel] = 1;
-    } else {
-      cg::coalesced_group g = cg::coalesced_threads();
-      slot = claim(g, a.request_count, 1);
-      if (slot < a.request_cap && a.requests) dst = a.requests + slot;
+      uint4 *dst = reinterpret_cast<uint4 *>(a.req_stage + pixel);
+      const uint64_t lx = loc_x(r), ly = loc_y(r), lz = loc_z(r);
+      __stcs(dst, make_uint4((uint32_t)lx, (uint32_t)(lx >> 32), (uint32_t)ly, (uint32_t)(ly >> 32)));
+      __stcs(dst + 1, make_uint4((uint32_t)lz, (uint32_t)(lz >> 32), w.cur_addr,
+                                 (uint32_t)(uint8_t)r.depth | ((uint32_t)tree_size << 8)));
+      __stcs(a.req_flag + pixel, (uint8_t)1);
+      return kStepHit;
     }
-    if (dst) {
+    cg::coalesced_group g = cg::coalesced_threads();
+    const uint32_t slot = claim(g, a.request_count, 1);
+    if (slot < a.request_cap && a.requests) {
+      svo_child_request *dst = a.requests + slot;
       svo_child_request q;
       q.address = w.cur_addr;
       q.tick = kMega ? v.tick : 0;  // TraceData.Tick is never set by the wavefront's resolveTrace
@@ -409,7 +414,7 @@ __device__ __forceinline__ int probe(const TraceLaunch &a, const ViewParams &v, 
       q.location[0] = loc_x(r);
       q.location[1] = loc_y(r);
       q.location[2] = loc_z(r);
-      q.tree_size = kMega ? 1 : (c <= pow2_neg(r.depth + 1) ? 1 : 0);
+      q.tree_size = tree_size;
       for (int k = 0; k < 7; k++) q._pad1[k] = 0;
       *dst = q;
     }
@@ -521,6 +526,14 @@ __device__ __forceinline__ int advance(const TraceLaunch &a, const uint4 *blocks
   r.depth = nd == B + 1 ? B : nd;
   return kStepOn;
 }
+
+// Warp-batch walks: a ray's steps that keep its location (descents, LOD
+// ascents) run in an inner loop before its move (advance), so that the lanes
+// of a warp whose octants turned out empty move together. Every ray takes the
+// same steps in the same order either way.
+#ifndef SVO_TRACE_PROBE_RUNS
+#define SVO_TRACE_PROBE_RUNS 0
+#endif
 
 // One whole step.
 template <bool kStats, bool kSmemBases>

@@ -183,7 +183,18 @@ __global__ void __launch_bounds__(256, SVO_TRACE_MIN_CTAS) trace_kernel(const Tr
             timed_out = true;
             break;
           }
-          finish = step<kStats, kSmemBases>(a, v, s_bases, blocks, B, r, w, st);
+          int f = probe<kStats, kSmemBases>(a, v, s_bases, blocks, B, r, w, st);
+          if (SVO_TRACE_PROBE_RUNS) {
+            // steps that keep the location (descents, LOD ascents) run back to
+            // back, so the move below runs with every lane whose octant is empty
+            while (f == kStepOn && ++ray_iters <= ray_limit) f = probe<kStats, kSmemBases>(a, v, s_bases, blocks, B, r, w, st);
+            if (f == kStepOn) {
+              record_timeout();
+              timed_out = true;
+              break;
+            }
+          }
+          finish = f == kStepEmpty ? advance(a, blocks, B, r, w) : f;
         }
         if (!timed_out) finish_ray(v, finish);
       }
@@ -313,7 +324,7 @@ __global__ void __launch_bounds__(1024) k_req_scan(uint32_t *chunk, uint32_t n, 
 // Each flagged pixel's staged record goes to queue slot (its rank in pixel
 // order) while that rank is below the cap.
 __global__ void __launch_bounds__(kReqThreads) k_req_scatter(const uint8_t *flags, const uint32_t *chunk_offsets,
-                                                             const svo_child_request *stage, svo_child_request *queue,
+                                                             const StagedRequest *stage, svo_child_request *queue,
                                                              uint32_t cap) {
   const uint32_t first = chunk_offsets[blockIdx.x];
   if (first >= cap) return;  // the whole CTA: its ranks all lie past the cap
@@ -325,7 +336,20 @@ __global__ void __launch_bounds__(kReqThreads) k_req_scatter(const uint8_t *flag
 #pragma unroll
   for (int k = 0; k < 16; k++) {
     if ((w4[k >> 2] >> (8 * (k & 3))) & 0xffu) {
-      if (rank < cap) queue[rank] = stage[word * 16 + k];
+      if (rank < cap) {
+        const StagedRequest sr = stage[word * 16 + k];
+        svo_child_request q;
+        q.address = sr.address;
+        q.tick = 0;  // TraceData.Tick is never set by the wavefront's resolveTrace
+        q.depth = sr.depth;
+        q._pad0 = 0;
+        q.location[0] = sr.location[0];
+        q.location[1] = sr.location[1];
+        q.location[2] = sr.location[2];
+        q.tree_size = sr.tree_size;
+        for (int j = 0; j < 7; j++) q._pad1[j] = 0;
+        queue[rank] = q;
+      }
       rank++;
     }
   }

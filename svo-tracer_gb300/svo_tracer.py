@@ -258,6 +258,23 @@ def read_oct(path: str) -> Octree:
     return _tree_from_handle(lib, h)
 
 
+def map_oct(path: str) -> Octree:
+    """The same file as read_oct, mapped with numpy alone (libsvo is not loaded): the
+    header, the base chunks and BlockCount blocks as read-only memory maps."""
+    head = np.fromfile(path, dtype=np.uint8, count=5)
+    if len(head) < 5:
+        raise SvoError("LoadTree", 11, "truncated header: " + path)
+    base_depth = int(head[0])
+    block_count = int(head[1]) | int(head[2]) << 8 | int(head[3]) << 16 | int(head[4]) << 24
+    n_bases = pow_sum(base_depth)
+    need = 5 + 2 * n_bases + BLOCK_DTYPE.itemsize * block_count
+    if os.path.getsize(path) < need:
+        raise SvoError("LoadTree", 11, "%s holds %d bytes, the header needs %d" % (path, os.path.getsize(path), need))
+    bases = np.memmap(path, dtype="<u2", mode="r", offset=5, shape=(n_bases,))
+    blocks = np.memmap(path, dtype=BLOCK_DTYPE, mode="r", offset=5 + 2 * n_bases, shape=(block_count,))
+    return Octree(base_depth, block_count, bases, blocks)
+
+
 class TreeManager:
     """ITreeManager over `{path}/{fileName}.oct` (SvoTracer.Domain/TreeManager.cs)."""
 

@@ -193,3 +193,41 @@ def test_pinned_host_buffers_equal_pageable(tracer, fitting):
         got_grad = tracer.diff_grads(len(tree.Blocks))
         assert abs(got_loss - want_loss) <= 1e-12 * want_loss
         assert np.abs(got_grad - want_grad).max() <= 1e-6 * np.abs(want_grad).max()  # atomic order only
+
+
+def test_full_size_colour_fitting_matches_fp64(tracer):
+    """The benchmarked colour-fitting workload at its stated size: the depth-9 SDF
+    sphere, 16 views of 512x512 at world distance 1.5, FP32 parameters uniform in
+    [0, 1], targets from the sinusoid ground truth (opacity 0.9). Every ray's
+    forward colour is within 1e-5 of the FP64 oracle; the fwd+bwd step (backward
+    fed with the forward's saved colour, as the bench runs it) gives the FP64 loss
+    and, on 256 random hit nodes, gradients within 1e-3 relative of FP64 central
+    differences (h = 1e-4), with the same absolute floor as the test-size check."""
+    tree = st.TreeBuilder(st.SCENE_SPHERE, seed=1).BuildTree(4, 9)
+    views = st.orbit_views(seed=7, n=16, width=512, height=512, distance=0.75)
+    hl = po.HitLists(tree, views, max_hits=16)
+    assert hl.n_rays == 16 * 512 * 512
+    params = np.random.default_rng(3).uniform(0.0, 1.0, (len(tree.Blocks), 4)).astype(np.float32)
+    _, target64, _ = hl.eval(st.sinusoid_field(tree, seed=9).astype(np.float64), want_rgb=True)
+    target = target64.astype(np.float32)
+    tracer.upload(tree)
+    tracer.diff_set_params(params)
+    rgb = tracer.diff_forward(views)
+    want_loss, want_rgb, want_grad = hl.eval(params.astype(np.float64), target.astype(np.float64), want_rgb=True,
+                                             want_grad=True)
+    err = np.abs(rgb - want_rgb)
+    assert err.max() <= 1e-5, "max |C - C64| = %g" % err.max()
+    loss = tracer.diff_backward(views, target, use_saved=True)
+    assert abs(loss - want_loss) <= 1e-9 * want_loss, (loss, want_loss)
+    grad = tracer.diff_grads(len(tree.Blocks))
+    scale = np.abs(want_grad).max()
+    ok = np.abs(grad - want_grad) <= 1e-4 * np.abs(want_grad) + 1e-6 * scale
+    assert ok.all(), "%d of %d gradient entries off the FP64 gradient" % ((~ok).sum(), ok.size)
+    touched = np.unique(hl.hits[np.arange(hl.max_hits)[None] < hl.n_hits[:, None]])
+    nodes = np.random.default_rng(11).choice(touched, 256, replace=False)
+    fd = hl.finite_differences(params.astype(np.float64), target.astype(np.float64), nodes, h=1e-4)
+    g = grad[nodes].astype(np.float64)
+    floor = 1e-5 * np.abs(fd).max()
+    rel = np.abs(g - fd) / np.maximum(np.abs(fd), floor)
+    assert rel.max() <= 1e-3, "max relative error %g" % rel.max()
+    assert (np.abs(fd) > floor).mean() > 0.6

@@ -230,10 +230,35 @@ def test_mixed_views_batched_graph_equals_plain_launches(tracer):
         assert np.array_equal(batched[i][3].numpy().reshape(-1, 4), want["rgba"])
 
 
-def test_full_size_terrain_1080p(tracer):
+@pytest.fixture(scope="module")
+def terrain11():
+    """The benchmarked tree: the depth-11 fBm terrain (seed 5, base depth 4, ~48M nodes)."""
+    return st.TreeBuilder(st.SCENE_TERRAIN, seed=5).BuildTree(4, 11)
+
+
+def test_full_size_mixed_views_against_oracle(tracer, terrain11):
+    """The 64 mixed-resolution views at their stated size (30.9M rays, 128x128 to
+    1920x1080 in pixel count) over the benchmarked depth-11 terrain, traced in one
+    graph-replayed batch: every ray of every view equals the oracle, the hit
+    outputs and t and RGBA bit for bit."""
+    tree = terrain11
+    views = st.mixed_views(seed=4, Tick=7, MaxChildRequestId=1 << 16)
+    assert sum(v.ScreenSize[0] * v.ScreenSize[1] for v in views) == 30908596
+    tracer.set_config(collect_stats=0, schedule=st.SCHEDULE_WARP, block_size=128)
+    tracer.upload(tree)
+    tracer.trace_batch(views, graph=True)
+    got = tracer.trace_batch(views, graph=True)  # a replay of the captured graph
+    tracer.set_config(block_size=256)
+    for i, (v, g) in enumerate(zip(views, got)):
+        want = po.trace_view(tree, v)
+        for k in ("hit_index", "hit_depth", "t", "rgba"):
+            assert np.array_equal(getattr(g, k), want[k]), "view %d (%dx%d): %s" % (i, *v.ScreenSize, k)
+
+
+def test_full_size_terrain_1080p(tracer, terrain11):
     """The headline workload: 1920x1080 over the depth-11 terrain (~48M nodes),
     compared pixel for pixel with the oracle (OpenMP over all host cores)."""
-    tree = st.TreeBuilder(st.SCENE_TERRAIN, seed=5).BuildTree(4, 11)
+    tree = terrain11
     cam = st.look_at((0.08, 0.12, 0.62), (0.75, 0.8, 0.88), 1920, 1080, 60.0, Tick=21, MaxChildRequestId=1 << 16)
     tracer.set_config(collect_stats=0)
     tracer.upload(tree)

@@ -99,3 +99,19 @@ def test_tree_manager(tmp_path):
     assert back.Blocks.tobytes() == tree.Blocks[:back.BlockCount].tobytes()
     tm.DeleteTree("sphere")
     assert not tm.TreeExists("sphere")
+
+
+def test_numpy_mapping_equals_the_library_reader(tmp_path):
+    """map_oct (numpy alone, as the benchmark's reference arm reads its scene) gives
+    the same tree as the library's svo_oct_read."""
+    tree = st.TreeBuilder(st.SCENE_TERRAIN, seed=5).BuildTree(3, 7)
+    path = str(tmp_path / "t.oct")
+    st.write_oct(path, tree)
+    a, b = st.read_oct(path), st.map_oct(path)
+    assert (a.BaseDepth, a.BlockCount) == (b.BaseDepth, b.BlockCount)
+    assert np.array_equal(a.BaseBlocks, b.BaseBlocks)
+    assert a.Blocks.tobytes() == np.asarray(b.Blocks).tobytes()
+    with open(path, "r+b") as f:
+        f.truncate(100)
+    with pytest.raises(st.SvoError):
+        st.map_oct(path)
