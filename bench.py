@@ -392,6 +392,35 @@ def mega_workload(tr, torch, dev, stream, flush, args, tree, cam, windows=None):
             "workload": "kernel.cl trace over the 1080p terrain frame, reference default cone parameters"}
 
 
+def gi_workload(tr, torch, dev, stream, flush, args, cam, outs, windows=None):
+    """The 1080p frame with the wavefront's secondary-cone stage as the reference
+    wires it (svo_trace_config.gi_stage): the trace, then per hit the cone fan of
+    evaluateMaterial, each cone lit by evaluateBackground (default cone
+    parameters, AmbientLightLevel 100)."""
+    steps = max(5, args.steps // 2)
+    tr.set_config(gi_stage=1)
+    with torch.cuda.stream(stream):
+        for _ in range(2):
+            tr.trace_device([cam], outs)
+        ev = []
+        t_win = time.perf_counter()
+        for _ in range(steps):
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            tr.trace_device([cam], outs)
+            e1.record(stream)
+            ev.append((e0, e1))
+        torch.cuda.synchronize(dev)
+        if windows is not None:
+            windows.append((t_win, time.perf_counter()))
+    tr.set_config(gi_stage=-1)
+    ms = float(np.median([a.elapsed_time(b) for a, b in ev]))
+    return {"frame_ms": ms, "mrays_s": WIDTH * HEIGHT / ms / 1e3, "steps": steps,
+            "workload": "1080p terrain frame with the material stage (evaluateMaterial + saveAccumulator + "
+                        "evaluateBackground of every hit's cone fan)"}
+
+
 def mega_cpu_sample(tree, cam, budget_s=8.0):
     """The reference's megakernel (kernel.cl built for the host CPU) over row bands
     of the same frame until ~budget_s; rays = primary + secondary cones, the cone
@@ -755,6 +784,8 @@ def run_ours(args, rank, world):
         line["megakernel"] = mega_workload(tr, torch, dev, stream, flush, args, tree, cam, windows)
     if not args.no_sphere:
         line["sphere_640x480"] = sphere_workload(torch, dev, flush, args, windows)
+    if not args.no_gi:
+        line["gi_stage"] = gi_workload(tr, torch, dev, stream, flush, args, cam, outs, windows)
     clk.__exit__(None, None, None)
     line["clocks"] = clk.summary(windows)
     if args.stream_frames > 0:
@@ -784,6 +815,7 @@ def main():
     ap.add_argument("--no-diff", action="store_true")
     ap.add_argument("--no-mega", action="store_true")
     ap.add_argument("--no-sphere", action="store_true")
+    ap.add_argument("--no-gi", action="store_true")
     ap.add_argument("--schedule", choices=["lane", "warp"], default=None)
     ap.add_argument("--diff-views", type=int, default=16)
     ap.add_argument("--diff-size", type=int, default=512)

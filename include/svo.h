@@ -192,6 +192,12 @@ typedef struct svo_trace_config {
                            test of that path. A stopped kernel is reported by the next call that synchronises
                            with the device (svo_synchronize included) and then cleared. */
   int32_t request_order; /* SVO_REQUESTS_ARRIVAL (default) or SVO_REQUESTS_PIXEL, see below */
+  int32_t gi_stage;     /* 1: svo_trace / svo_trace_batch also run the wavefront's secondary-cone stage as the
+                           reference wires it (MainWindow.cs:390-402, disabled there): evaluateMaterial's cone fan
+                           of every primary hit (wavefront.cl:1568-1739), each cone of weighting > 5 put straight
+                           on the background queue by saveAccumulator (:338-355) and lit by evaluateBackground
+                           (:1741-1797), the hit's own colour never added. The views of a call must share their
+                           cone parameters and AmbientLightLevel. -1 or 0: off */
 } svo_trace_config;
 
 /* Child requests of svo_trace / svo_trace_batch past the queue's cap

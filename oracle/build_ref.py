@@ -13,6 +13,10 @@ oracle/_ref/wavefront_ref.c (and oracle/_ref/kernel_ref.c):
   ``ref_float_to_ulong(fabs(x) * ULONG_MAX)``: C leaves the conversion of NaN and
   of values >= 2^64 undefined (x86 gives 2^63, GPUs and Arm saturate), and the
   shim's function saturates (NaN -> 0), as the parity contract defines it;
+* the material stage's float-to-uchar conversions (evaluateMaterial's
+  ``(uchar)(ringWeighting * baseWeighting)`` and evaluateBackground's ambient
+  blend) become ``ref_float_to_uchar(...)``: out-of-range values are undefined in
+  C, and the shim's function saturates, as the parity contract defines it;
 * the kernels' ``local uint localQueue[5];`` gets a zero initialiser. ``increment``
   (wavefront.cl:254-258) relies on work-items 0..4 of a group to clear the five
   entries; the harness runs one work-item per group, which would clear only entry 0.
@@ -85,6 +89,12 @@ def rewrite(src: str) -> str:
     src = _rewrite_literals(src)
     src = src.replace("local uint localQueue[5];", "local uint localQueue[5] = {0, 0, 0, 0, 0};")
     src = src.replace("return (ulong)(fabs(x) * ULONG_MAX);", "return ref_float_to_ulong(fabs(x) * ULONG_MAX);")
+    # the material stage's float-to-uchar conversions can leave uchar's range (a
+    # negative or > 1 weighting; evaluateBackground's blend when the luminosity is
+    # at most the ambient level wraps colourBoundary - baseColour to ~2^32)
+    src = src.replace("(uchar)(ringWeighting * baseWeighting)", "ref_float_to_uchar(ringWeighting * baseWeighting)")
+    src = re.sub(r"colour([RGB]) = \((baseColour\1 \+ lightQuotient \* colour\1 \* \(colourBoundary - baseColour\1\))\);",
+                 r"colour\1 = ref_float_to_uchar(\2);", src)
     src = re.sub(r"\.([xyzw])\b", lambda m: "[%d]" % "xyzw".index(m.group(1)), src)
     return src
 

@@ -47,6 +47,8 @@ def oracle_lib() -> C.CDLL:
         lib.oracle_trace_view.restype = C.c_int64
         lib.oracle_trace_rows.argtypes = lib.oracle_trace_view.argtypes + [C.c_uint32, C.c_uint32]
         lib.oracle_trace_rows.restype = C.c_int64
+        lib.oracle_trace_rows_gi.argtypes = lib.oracle_trace_rows.argtypes + [C.c_int32]
+        lib.oracle_trace_rows_gi.restype = C.c_int64
         lib.oracle_mega_trace_rows.argtypes = [_vp, C.c_uint8, _vp, C.c_size_t, _vp, C.c_size_t, C.c_char_p,
                                                C.c_int32, C.c_int32, C.POINTER(_ViewOut), _vp, _vp, C.c_uint32,
                                                C.POINTER(C.c_uint32), C.c_int32, C.c_uint32, C.c_uint32]
@@ -102,6 +104,8 @@ def ref_lib() -> C.CDLL:
         lib.ref_trace_view.restype = C.c_long
         lib.ref_trace_rows.argtypes = lib.ref_trace_view.argtypes + [C.c_uint, C.c_uint]
         lib.ref_trace_rows.restype = C.c_long
+        lib.ref_trace_rows_gi.argtypes = lib.ref_trace_rows.argtypes + [C.c_int]
+        lib.ref_trace_rows_gi.restype = C.c_long
         lib.ref_prune.argtypes = [_vp, C.c_uint8, _vp, C.c_size_t, _vp, C.c_size_t, _vp, C.c_uint, _vp, C.c_size_t,
                                   _vp, C.c_size_t, C.c_uint16]
         lib.ref_prune.restype = C.c_long
@@ -187,11 +191,13 @@ def _result(n, counts=True):
     return r
 
 
-def trace_view(tree, inp: TraceInput, usage=None, max_steps: int = 1 << 16, threads: int = 0, req_cap: int = 1 << 20):
+def trace_view(tree, inp: TraceInput, usage=None, max_steps: int = 1 << 16, threads: int = 0, req_cap: int = 1 << 20,
+               gi: bool = False):
     """Runs the oracle on one view. usage (USAGE_DTYPE array) is stamped in place.
     ``requests`` holds the queue in arrival order (capped at req_cap);
     ``pixel_requests`` every raised request in pixel order, whose first
-    MaxChildRequestId entries are the queue of the pixel-order rule."""
+    MaxChildRequestId entries are the queue of the pixel-order rule. gi: also the
+    wavefront's secondary-cone stage as the reference wires it."""
     lib = oracle_lib()
     w, h = inp.ScreenSize
     n = w * h
@@ -205,8 +211,11 @@ def trace_view(tree, inp: TraceInput, usage=None, max_steps: int = 1 << 16, thre
     req = np.zeros(min(req_cap, n), CHILD_REQUEST_DTYPE)
     nreq = C.c_uint32(0)
     ng = 0 if usage is None else len(usage)
-    limited = lib.oracle_trace_view(_p(bases), tree.BaseDepth, _p(blocks), len(blocks), _p(usage), ng,
-                                    inp.to_bytes(), max_steps, C.byref(vo), _p(req), len(req), C.byref(nreq), threads)
+    limited = lib.oracle_trace_rows_gi(_p(bases), tree.BaseDepth, _p(blocks), len(blocks), _p(usage), ng,
+                                       inp.to_bytes(), max_steps, C.byref(vo), _p(req), len(req), C.byref(nreq),
+                                       threads, 0, h, int(gi))
+    if limited == -2:
+        raise ValueError("cone schedule does not end")
     r["step_limited"] = int(limited)
     r["requests"] = req[: min(nreq.value, len(req))]
     r["n_requests"] = nreq.value
@@ -222,8 +231,9 @@ def pixel_order_queue(per_view_requests, cap: int) -> np.ndarray:
     return allq[:cap]
 
 
-def ref_trace_view(tree, inp: TraceInput, usage=None, threads: int = 0, max_passes: int = 1 << 20):
-    """Runs the reference's own kernels (CPU build) on one view."""
+def ref_trace_view(tree, inp: TraceInput, usage=None, threads: int = 0, max_passes: int = 1 << 20, gi: bool = False):
+    """Runs the reference's own kernels (CPU build) on one view; gi: with the
+    secondary-cone stage that MainWindow.RunWavefront has commented out."""
     lib = ref_lib()
     w, h = inp.ScreenSize
     n = w * h
@@ -233,9 +243,11 @@ def ref_trace_view(tree, inp: TraceInput, usage=None, threads: int = 0, max_pass
     req = np.zeros(n, CHILD_REQUEST_DTYPE)
     nreq = C.c_uint32(0)
     ng = 0 if usage is None else len(usage)
-    passes = lib.ref_trace_view(_p(bases), tree.BaseDepth, _p(blocks), len(blocks), _p(usage), ng, inp.to_bytes(),
-                                _p(r["hit_index"]), _p(r["hit_depth"]), _p(r["t"]), _p(r["rgba"]), _p(r["acc"]),
-                                _p(req), len(req), C.byref(nreq), threads, max_passes)
+    passes = lib.ref_trace_rows_gi(_p(bases), tree.BaseDepth, _p(blocks), len(blocks), _p(usage), ng, inp.to_bytes(),
+                                   _p(r["hit_index"]), _p(r["hit_depth"]), _p(r["t"]), _p(r["rgba"]), _p(r["acc"]),
+                                   _p(req), len(req), C.byref(nreq), threads, max_passes, 0, h, int(gi))
+    if passes == -2:
+        raise ValueError("cone schedule does not end")
     r["passes"] = int(passes)
     r["requests"] = req[: min(nreq.value, len(req))]
     r["n_requests"] = nreq.value

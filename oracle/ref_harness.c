@@ -30,13 +30,43 @@ uint ref_image_width;
 
 static void *zalloc(size_t n) { return calloc(n ? n : 1, 1); }
 
-/* Returns the number of traversal passes, or -1 if max_passes ran out.
- * Only rows [row_begin, row_end) get an init work-item (a bounded sample of the
- * view); per-pixel outputs still cover the whole W x H image. */
-long ref_trace_rows(const ushort *bases, uchar base_depth, const Block *blocks_in, size_t n_blocks, Usage *usage,
-                    size_t n_groups, const TraceInput *in, uint *hit_index, uchar *hit_depth, float *t, float *rgba,
-                    uint *acc, ChildRequest *req_out, uint req_cap, uint *n_req, int threads, long max_passes,
-                    uint row_begin, uint row_end) {
+/* Cones per pixel of a fan that takes no `break` (evaluateMaterial's spine
+ * and ring loops, wavefront.cl:1655-1739, which depend only on the input): 0
+ * when the kernel returns at once, -1 past 4096 (the loops would not end). */
+static long gi_max_cones(const TraceInput *in) {
+  if (in->FovConstant <= 0 || in->FovMultiplier >= 1 || in->FovMultiplier <= -1) return 0;
+  float fov = in->FovConstant, oldfov = fov, spineAngle = 0;
+  long cones = 1;
+  while (spineAngle < M_PI_F) {
+    fov = (in->FovMultiplier * (spineAngle + fov) + in->FovConstant) / (1 - in->FovMultiplier);
+    spineAngle = (1 + in->FovMultiplier) * (spineAngle + oldfov) / (1 - in->FovMultiplier);
+    oldfov = fov;
+    cones += 1;
+    for (int j = 1; j * fov < M_PI_2_F; j++)
+      if ((cones += 2) > 4096) return -1;
+    if (cones > 4096) return -1;
+  }
+  return cones;
+}
+
+static void *grow(void *p, size_t old_bytes, size_t new_bytes) {
+  if (new_bytes <= old_bytes) return p;
+  void *q = realloc(p, new_bytes);
+  memset((char *)q + old_bytes, 0, new_bytes - old_bytes);
+  return q;
+}
+
+/* Returns the number of traversal passes, or -1 if max_passes ran out (-2: the
+ * material stage's cone loops would not end). Only rows [row_begin, row_end) get
+ * an init work-item (a bounded sample of the view); per-pixel outputs still
+ * cover the whole W x H image. gi = 1 also runs the secondary-cone stage that
+ * MainWindow.RunWavefront has commented out (MainWindow.cs:390-402), as written
+ * there: EvaulateMaterial (swap the Root buffers, reset the material queue,
+ * evaluateMaterial), RunTraces, EvaulateBackground. */
+long ref_trace_rows_gi(const ushort *bases, uchar base_depth, const Block *blocks_in, size_t n_blocks, Usage *usage,
+                       size_t n_groups, const TraceInput *in, uint *hit_index, uchar *hit_depth, float *t, float *rgba,
+                       uint *acc, ChildRequest *req_out, uint req_cap, uint *n_req, int threads, long max_passes,
+                       uint row_begin, uint row_end, int gi) {
   (void)n_groups;
   TraceInput input = *in;
   input.BaseDepth = base_depth;
@@ -81,54 +111,52 @@ long ref_trace_rows(const ushort *bases, uchar base_depth, const Block *blocks_i
          FinalColourBs, FinalWeightings, input);
   }
 
-  for (;;) { /* MainWindow.RunTraces, MainWindow.cs:452-481 */
-    uint nb = BaseTraceQueueID;
-    BaseTraceQueueID = 0;
-    if (nb) {
-      uint *tmp = BaseTraces;
-      BaseTraces = BaseTraceQueue;
-      BaseTraceQueue = tmp;
-      ref_gsize[0] = nb;
-#ifdef _OPENMP
-#pragma omp parallel for schedule(dynamic, 1024) num_threads(nt)
-#endif
-      for (size_t i = 0; i < nb; i++) {
-        ref_gid[0] = i;
-        ref_gid[1] = 0;
-        runBaseTrace(Bases, Origins, Directions, FoVs, Locations, Weightings, Depths, BaseTraces, BlockTraceQueue,
-                     &BlockTraceQueueID, BaseTraceQueue, &BaseTraceQueueID, BackgroundQueue, &BackgroundQueueID, input);
-      }
-    }
-    uint nk = BlockTraceQueueID;
-    BlockTraceQueueID = 0;
-    if (nk) {
-      uint *tmp = BlockTraces;
-      BlockTraces = BlockTraceQueue;
-      BlockTraceQueue = tmp;
-      ref_gsize[0] = nk;
-#ifdef _OPENMP
-#pragma omp parallel for schedule(dynamic, 1024) num_threads(nt)
-#endif
-      for (size_t i = 0; i < nk; i++) {
-        ref_gid[0] = i;
-        ref_gid[1] = 0;
-        runBlockTrace(Blocks, Usages, &ChildRequestID, ChildRequests, Origins, Directions, FoVs, Locations,
-                      Weightings, Depths, BlockTraces, BlockTraceQueue, &BlockTraceQueueID, BaseTraceQueue,
-                      &BaseTraceQueueID, BackgroundQueue, &BackgroundQueueID, MaterialQueue, &MaterialQueueID,
-                      ParentTraces, input);
-      }
-    }
-    if (!nb && !nk) break;
-    if (++passes > max_passes) {
-      passes = -1;
-      break;
-    }
+#define RUN_TRACES(INPUT)\
+  for (;;) { /* MainWindow.RunTraces, MainWindow.cs:452-481 */ \
+    uint nb = BaseTraceQueueID; \
+    BaseTraceQueueID = 0; \
+    if (nb) { \
+      uint *tmp = BaseTraces; \
+      BaseTraces = BaseTraceQueue; \
+      BaseTraceQueue = tmp; \
+      ref_gsize[0] = nb; \
+      _Pragma("omp parallel for schedule(dynamic, 1024) num_threads(nt)") \
+      for (size_t i = 0; i < nb; i++) { \
+        ref_gid[0] = i; \
+        ref_gid[1] = 0; \
+        runBaseTrace(Bases, Origins, Directions, FoVs, Locations, Weightings, Depths, BaseTraces, BlockTraceQueue, \
+                     &BlockTraceQueueID, BaseTraceQueue, &BaseTraceQueueID, BackgroundQueue, &BackgroundQueueID, INPUT); \
+      } \
+    } \
+    uint nk = BlockTraceQueueID; \
+    BlockTraceQueueID = 0; \
+    if (nk) { \
+      uint *tmp = BlockTraces; \
+      BlockTraces = BlockTraceQueue; \
+      BlockTraceQueue = tmp; \
+      ref_gsize[0] = nk; \
+      _Pragma("omp parallel for schedule(dynamic, 1024) num_threads(nt)") \
+      for (size_t i = 0; i < nk; i++) { \
+        ref_gid[0] = i; \
+        ref_gid[1] = 0; \
+        runBlockTrace(Blocks, Usages, &ChildRequestID, ChildRequests, Origins, Directions, FoVs, Locations, \
+                      Weightings, Depths, BlockTraces, BlockTraceQueue, &BlockTraceQueueID, BaseTraceQueue, \
+                      &BaseTraceQueueID, BackgroundQueue, &BackgroundQueueID, MaterialQueue, &MaterialQueueID, \
+                      ParentTraces, INPUT); \
+      } \
+    } \
+    if (!nb && !nk) break; \
+    if (++passes > max_passes) { \
+      passes = -1; \
+      break; \
+    } \
   }
-
+  RUN_TRACES(input);
   TraceInput flat = input; /* MainWindow.cs:384-385: DoF zeroed after the traces */
   flat.DoF[0] = 0;
   flat.DoF[1] = 0;
   uint nbg = BackgroundQueueID;
+  BackgroundQueueID = 0; /* EvaulateBackground's ResetIDBuffer */
   ref_gsize[0] = nbg;
 #ifdef _OPENMP
 #pragma omp parallel for schedule(dynamic, 1024) num_threads(nt)
@@ -137,6 +165,76 @@ long ref_trace_rows(const ushort *bases, uchar base_depth, const Block *blocks_i
     ref_gid[0] = i;
     evaluateBackground(BackgroundQueue, Directions, ParentTraces, ColourRs, ColourGs, ColourBs, Weightings,
                        FinalColourRs, FinalColourGs, FinalColourBs, FinalWeightings, flat);
+  }
+  /* the primary states of the material queue (hit outputs below) */
+  uint n_hits = MaterialQueueID;
+  ulong3 *HitLocations = Locations;
+  uchar *HitDepths = Depths;
+  uint *HitParents = ParentTraces;
+  ulong3 *RootLocations = NULL;
+  float3 *RootDirections = NULL;
+  uchar *RootDepths = NULL, *RootWeightings = NULL, *Luminosities = NULL;
+  uint *RootParentTraces = NULL;
+  float *RayLengths = NULL;
+  if (gi && passes >= 0) {
+    long K = gi_max_cones(&flat);
+    if (K < 0) {
+      passes = -2;
+    } else {
+      /* EvaulateMaterial (MainWindow.cs:529-560): the Root buffers swap with the
+       * traces' state buffers, then the material queue count is read and reset */
+      size_t cap = (size_t)n_hits * (size_t)(K > 0 ? K : 1) + 1;
+      if (cap < N) cap = N;
+      RootDirections = zalloc(sizeof(float3) * cap);
+      RootLocations = zalloc(sizeof(ulong3) * cap);
+      RootDepths = zalloc(cap);
+      RootWeightings = zalloc(cap);
+      RootParentTraces = zalloc(4 * cap);
+      float3 *t3 = Directions; Directions = RootDirections; RootDirections = t3;
+      ulong3 *tl = Locations; Locations = RootLocations; RootLocations = tl;
+      uchar *tc = Depths; Depths = RootDepths; RootDepths = tc;
+      tc = Weightings; Weightings = RootWeightings; RootWeightings = tc;
+      uint *tu = ParentTraces; ParentTraces = RootParentTraces; RootParentTraces = tu;
+      HitLocations = RootLocations;
+      HitDepths = RootDepths;
+      HitParents = RootParentTraces;
+      /* saveAccumulator writes these at the cone ids too */
+      Origins = grow(Origins, sizeof(float3) * N, sizeof(float3) * cap);
+      FoVs = grow(FoVs, sizeof(float) * N, sizeof(float) * cap);
+      ColourRs = grow(ColourRs, N, cap);
+      ColourGs = grow(ColourGs, N, cap);
+      ColourBs = grow(ColourBs, N, cap);
+      BackgroundQueue = grow(BackgroundQueue, 4 * N, 4 * cap);
+      Luminosities = zalloc(cap);
+      RayLengths = zalloc(sizeof(float) * cap);
+      uint AccumulatorID = 0;
+      uint nmat = MaterialQueueID;
+      MaterialQueueID = 0;
+      ref_gsize[0] = nmat;
+#ifdef _OPENMP
+#pragma omp parallel for schedule(dynamic, 256) num_threads(nt)
+#endif
+      for (size_t i = 0; i < nmat; i++) {
+        ref_gid[0] = i;
+        evaluateMaterial(Blocks, Usages, Origins, Directions, FoVs, Locations, Depths, Weightings, ColourRs, ColourGs,
+                         ColourBs, RayLengths, Luminosities, MaterialQueue, ParentTraces, RootDirections,
+                         RootLocations, RootDepths, RootWeightings, RootParentTraces, BaseTraceQueue,
+                         &BaseTraceQueueID, FinalWeightings, &AccumulatorID, BackgroundQueue, &BackgroundQueueID,
+                         flat);
+      }
+      RUN_TRACES(flat); /* the material rays' traces: every queue is empty */
+      uint nbg2 = BackgroundQueueID;
+      BackgroundQueueID = 0;
+      ref_gsize[0] = nbg2;
+#ifdef _OPENMP
+#pragma omp parallel for schedule(dynamic, 1024) num_threads(nt)
+#endif
+      for (size_t i = 0; i < nbg2; i++) {
+        ref_gid[0] = i;
+        evaluateBackground(BackgroundQueue, Directions, ParentTraces, ColourRs, ColourGs, ColourBs, Weightings,
+                           FinalColourRs, FinalColourGs, FinalColourBs, FinalWeightings, flat);
+      }
+    }
   }
   uint nm = MaterialQueueID;
   ref_gsize[0] = nm;
@@ -165,15 +263,15 @@ long ref_trace_rows(const ushort *bases, uchar base_depth, const Block *blocks_i
     if (t) t[id] = INFINITY;
   }
   Buffers walk = {.Blocks = Blocks, .BaseDepth = base_depth};
-  for (size_t i = 0; i < nm; i++) {
+  for (size_t i = 0; i < n_hits; i++) {
     uint id = MaterialQueue[i];
-    uint px = ParentTraces[id];
-    if (hit_index) hit_index[px] = getBlockAddress(walk, Depths[id], Locations[id]);
-    if (hit_depth) hit_depth[px] = Depths[id];
-    if (t) {
-      float x = ulongToFloat(Locations[id][0]) - Origins[id][0];
-      float y = ulongToFloat(Locations[id][1]) - Origins[id][1];
-      float z = ulongToFloat(Locations[id][2]) - Origins[id][2];
+    uint px = HitParents[id];
+    if (hit_index) hit_index[px] = getBlockAddress(walk, HitDepths[id], HitLocations[id]);
+    if (hit_depth) hit_depth[px] = HitDepths[id];
+    if (t) { /* a primary ray's Origin is the camera's */
+      float x = ulongToFloat(HitLocations[id][0]) - input.Origin[0];
+      float y = ulongToFloat(HitLocations[id][1]) - input.Origin[1];
+      float z = ulongToFloat(HitLocations[id][2]) - input.Origin[2];
       t[px] = sqrtf(x * x + y * y + z * z);
     }
   }
@@ -193,7 +291,18 @@ long ref_trace_rows(const ushort *bases, uchar base_depth, const Block *blocks_i
   free(ColourRs); free(ColourGs); free(ColourBs); free(ParentTraces); free(BaseTraces); free(BaseTraceQueue);
   free(BlockTraces); free(BlockTraceQueue); free(BackgroundQueue); free(MaterialQueue); free(FinalColourRs);
   free(FinalColourGs); free(FinalColourBs); free(FinalWeightings); free(ChildRequests);
+  free(RootDirections); free(RootLocations); free(RootDepths); free(RootWeightings); free(RootParentTraces);
+  free(Luminosities); free(RayLengths);
   return passes;
+}
+#undef RUN_TRACES
+
+long ref_trace_rows(const ushort *bases, uchar base_depth, const Block *blocks_in, size_t n_blocks, Usage *usage,
+                    size_t n_groups, const TraceInput *in, uint *hit_index, uchar *hit_depth, float *t, float *rgba,
+                    uint *acc, ChildRequest *req_out, uint req_cap, uint *n_req, int threads, long max_passes,
+                    uint row_begin, uint row_end) {
+  return ref_trace_rows_gi(bases, base_depth, blocks_in, n_blocks, usage, n_groups, in, hit_index, hit_depth, t, rgba,
+                           acc, req_out, req_cap, n_req, threads, max_passes, row_begin, row_end, 0);
 }
 
 long ref_trace_view(const ushort *bases, uchar base_depth, const Block *blocks_in, size_t n_blocks, Usage *usage,

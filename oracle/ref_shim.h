@@ -95,6 +95,14 @@ static inline ulong ref_float_to_ulong(double v) {
   return (ulong)v;
 }
 
+/* (uchar)x of the material stage (rewritten by build_ref.py): truncation inside
+ * [0, 255], saturating outside, NaN -> 0. */
+static inline uchar ref_float_to_uchar(float v) {
+  if (!(v > 0.0f)) return 0;
+  if (v >= 255.0f) return 255;
+  return (uchar)v;
+}
+
 static inline float native_sin(float x) { return (float)sin((double)x); }
 static inline float native_cos(float x) { return (float)cos((double)x); }
 

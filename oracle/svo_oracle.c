@@ -282,6 +282,7 @@ typedef struct ray_result {
   int step_limited;
   int requested; /* the ray stopped with a child request (at most one per ray) */
   svo_child_request request;
+  float dir[3];  /* setupInitialTrace's direction */
 } ray_result;
 
 static void trace_ray(const uint16_t *bases, uint8_t B, const svo_block *blocks, size_t n_blocks, svo_usage *usage,
@@ -302,6 +303,7 @@ static void trace_ray(const uint16_t *bases, uint8_t B, const svo_block *blocks,
   dir[1] = F[1] * m0 + F[4] * m1 + F[7] * m2;
   dir[2] = F[2] * m0 + F[5] * m1 + F[8] * m2;
   for (int k = 0; k < 3; k++) {
+    r->dir[k] = dir[k];
     inv[k] = 1.0f / dir[k];
     sign[k] = dir[k] >= 0;
     o[k] = in->origin[k];
@@ -442,15 +444,35 @@ int64_t oracle_trace_view(const uint16_t *bases, uint8_t base_depth, const svo_b
                           svo_usage *usage, size_t n_groups, const svo_trace_input *in, int32_t max_steps,
                           const oracle_view_out *out, svo_child_request *req, uint32_t req_cap, uint32_t *n_req,
                           int32_t threads) {
-  return oracle_trace_rows(bases, base_depth, blocks, n_blocks, usage, n_groups, in, max_steps, out, req, req_cap, n_req,
-                           threads, 0, in->screen_size[1]);
+  return oracle_trace_rows_gi(bases, base_depth, blocks, n_blocks, usage, n_groups, in, max_steps, out, req, req_cap,
+                              n_req, threads, 0, in->screen_size[1], 0);
 }
 
 int64_t oracle_trace_rows(const uint16_t *bases, uint8_t base_depth, const svo_block *blocks, size_t n_blocks,
                           svo_usage *usage, size_t n_groups, const svo_trace_input *in, int32_t max_steps,
                           const oracle_view_out *out, svo_child_request *req, uint32_t req_cap, uint32_t *n_req,
                           int32_t threads, uint32_t row_begin, uint32_t row_end) {
+  return oracle_trace_rows_gi(bases, base_depth, blocks, n_blocks, usage, n_groups, in, max_steps, out, req, req_cap,
+                              n_req, threads, row_begin, row_end, 0);
+}
+
+typedef struct mega_schedule mega_schedule;
+static int gi_schedule(const svo_trace_input *in, mega_schedule **S);
+static void gi_free_schedule(mega_schedule *S);
+static void gi_pixel(const svo_block *blk, const float dir[3], const svo_trace_input *in, const mega_schedule *S,
+                     uint32_t acc[4]);
+
+int64_t oracle_trace_rows_gi(const uint16_t *bases, uint8_t base_depth, const svo_block *blocks, size_t n_blocks,
+                             svo_usage *usage, size_t n_groups, const svo_trace_input *in, int32_t max_steps,
+                             const oracle_view_out *out, svo_child_request *req, uint32_t req_cap, uint32_t *n_req,
+                             int32_t threads, uint32_t row_begin, uint32_t row_end, int32_t gi) {
   uint32_t W = in->screen_size[0], H = in->screen_size[1];
+  /* the material stage: evaluateMaterial returns at once for unusable cone
+   * parameters (wavefront.cl:1575-1576); a schedule whose loops would not end is
+   * refused (-2) */
+  const int gi_valid = gi && !(in->fov_constant <= 0 || in->fov_multiplier >= 1 || in->fov_multiplier <= -1);
+  mega_schedule *S = NULL;
+  if (gi_valid && !gi_schedule(in, &S)) return -2;
   if (row_end > H) row_end = H;
   if (row_begin > row_end) row_begin = row_end;
   float *su = (float *)malloc(sizeof(float) * (W + 1));
@@ -479,6 +501,19 @@ int64_t oracle_trace_rows(const uint16_t *bases, uint8_t base_depth, const svo_b
     if (out->steps) out->steps[id] = r.steps;
     if (out->requested) out->requested[id] = (uint8_t)r.requested;
     if (out->pixel_request && r.requested) out->pixel_request[id] = r.request;
+    if (gi && r.hit_index != SVO_MISS) {
+      /* the secondary-cone stage replaces a hit's accumulators (resolveRemainders
+       * then finds the material queue empty) and stamps the hit block's usage */
+      if (gi_valid) {
+        uint32_t g = r.hit_index >> 3;
+        if (usage && g < n_groups && usage[g].tick < 65534 && usage[g].tick != in->tick) usage[g].tick = in->tick;
+        gi_pixel(node_at(blocks, n_blocks, r.hit_index), r.dir, in, S, r.acc);
+      } else {
+        r.acc[0] = r.acc[1] = r.acc[2] = r.acc[3] = 0;
+      }
+      if (out->acc)
+        for (int k = 0; k < 4; k++) out->acc[4 * id + k] = r.acc[k];
+    }
     if (out->rgba) {
       /* drawTrace, wavefront.cl:1835-1850 */
       float *px = &out->rgba[4 * id];
@@ -500,6 +535,7 @@ int64_t oracle_trace_rows(const uint16_t *bases, uint8_t base_depth, const svo_b
   free(cu);
   free(sv);
   free(cv);
+  if (S) gi_free_schedule(S);
   return limited;
 }
 
@@ -759,11 +795,11 @@ typedef struct {
 typedef struct {
   float c, s, one_minus_c; /* cos/sin(-ringAngle), 1 - cos */
 } mega_ring;
-typedef struct {
+struct mega_schedule {
   int n_spines, n_rings;
   mega_spine *spine;
   mega_ring *ring;
-} mega_schedule;
+};
 
 /* Returns 0 when the loops would not end within `limit` cones per pixel. */
 static int mega_build_schedule(const svo_trace_input *in, int limit, mega_schedule *S) {
@@ -1177,4 +1213,109 @@ int64_t oracle_mega_trace_rows(const uint16_t *bases, uint8_t base_depth, const 
   free(S.spine);
   free(S.ring);
   return 0;
+}
+
+
+/* ---- the wavefront's secondary-cone stage, as the reference wires it --------
+ *
+ * MainWindow.RunWavefront (MainWindow.cs:390-402) has it commented out; enabled
+ * as written, per primary hit: evaluateMaterial (wavefront.cl:1568-1739) builds
+ * the hit's cone fan (the same fan as kernel.cl's spawnRays), saveAccumulator
+ * (:338-355) puts every cone of weighting > 5 on the background queue without
+ * tracing it, evaluateBackground (:1741-1797) adds its sky light (blended with
+ * the hit block's colour by the ambient light level) to the pixel, and
+ * resolveRemainders finds the material queue already reset, so the hit's own
+ * colour is never added. Float-to-uchar conversions saturate. */
+
+static int gi_schedule(const svo_trace_input *in, mega_schedule **S) {
+  *S = (mega_schedule *)calloc(1, sizeof(mega_schedule));
+  if (!mega_build_schedule(in, SVO_MEGA_MAX_CONES, *S)) {
+    gi_free_schedule(*S);
+    *S = NULL;
+    return 0;
+  }
+  return 1;
+}
+
+static void gi_free_schedule(mega_schedule *S) {
+  free(S->spine);
+  free(S->ring);
+  free(S);
+}
+
+/* saveAccumulator + evaluateBackground of one cone with weighting w. */
+static void gi_cone(const float d[3], uint8_t w, const svo_block *blk, uint8_t ambient, uint32_t acc[4]) {
+  if (w <= 5) return;
+  float dotp = d[0] * 0.0f + d[1] * 0.0f + d[2] * -1.0f;
+  uint8_t c[3], lum;
+  if (dotp > 0.8f) {
+    c[0] = c[1] = c[2] = 255;
+    lum = sat_u8(dotp * 200.0f);
+  } else {
+    c[0] = 135;
+    c[1] = 206;
+    c[2] = 235;
+    lum = 1;
+  }
+  if (w < 255) {
+    uint32_t boundary = lum > ambient ? 255u : 0u;
+    float q = (float)(lum > ambient ? lum - ambient : ambient - lum) / ((float)(lum + ambient) * 255.0f);
+    const uint8_t base[3] = {blk->colour_r, blk->colour_g, blk->colour_b};
+    for (int k = 0; k < 3; k++) c[k] = sat_u8((float)base[k] + q * (float)c[k] * (float)(uint32_t)(boundary - base[k]));
+  }
+  acc[0] += w;
+  if (lum > 0)
+    for (int k = 0; k < 3; k++) acc[1 + k] += (uint32_t)c[k] * w;
+}
+
+static void gi_pixel(const svo_block *blk, const float dir[3], const svo_trace_input *in, const mega_schedule *S,
+                     uint32_t acc[4]) {
+  acc[0] = acc[1] = acc[2] = acc[3] = 0;
+  const float base_w = 255.0f; /* the primary's Weighting */
+  float nrm[3];
+  mega_normal(blk->normal_pitch, blk->normal_yaw, nrm);
+  if (in->weighting_constant * base_w < 6) {
+    acc[0] = 255; /* FinalWeightings[traceID] = baseWeighting */
+    return;
+  }
+  if (dot3(dir, nrm) >= 0) { /* seen edge-on: one cone along the primary direction */
+    gi_cone(dir, 255, blk, in->ambient_light_level, acc);
+    return;
+  }
+  const float *D = dir;
+  float axis[3] = {D[1] * nrm[2] - D[2] * nrm[1], D[2] * nrm[0] - D[0] * nrm[2], D[0] * nrm[1] - D[1] * nrm[0]};
+  normalize3(axis);
+  float d2 = 2.0f * dot3(D, nrm);
+  float refl[3] = {D[0] - d2 * nrm[0], D[1] - d2 * nrm[1], D[2] - d2 * nrm[2]};
+  float fov = in->fov_constant, weighting = in->weighting_constant, rw = weighting;
+  float dp = dot3(refl, nrm);
+  if (dp < fov) rw = weighting * dp / fov;
+  gi_cone(refl, sat_u8(rw * base_w), blk, in->ambient_light_level, acc);
+  for (int s = 0; s < S->n_spines; s++) {
+    const mega_spine *sp = &S->spine[s];
+    fov = sp->fov;
+    weighting = sp->weighting;
+    rw = weighting;
+    float seed[3];
+    rotate3(axis, sp->c, sp->s, sp->one_minus_c, refl, 0, seed);
+    normalize3(seed);
+    dp = dot3(seed, nrm);
+    if (dp < 0) break;
+    if (dp < fov) rw = weighting * dp / fov;
+    gi_cone(seed, sat_u8(rw * base_w), blk, in->ambient_light_level, acc);
+    for (int j = 0; j < sp->n_rings; j++) {
+      const mega_ring *rg = &S->ring[sp->ring_begin + j];
+      rw = weighting;
+      float v[3];
+      rotate3(refl, rg->c, rg->s, rg->one_minus_c, seed, 0, v);
+      normalize3(v);
+      dp = dot3(v, nrm);
+      if (dp < 0) break;
+      if (dp < fov) rw = weighting * dp / fov;
+      gi_cone(v, sat_u8(rw * base_w), blk, in->ambient_light_level, acc);
+      rotate3(refl, rg->c, rg->s, rg->one_minus_c, seed, 1, v);
+      normalize3(v);
+      gi_cone(v, sat_u8(rw * base_w), blk, in->ambient_light_level, acc);
+    }
+  }
 }

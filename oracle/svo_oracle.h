@@ -51,6 +51,14 @@ int64_t oracle_trace_rows(const uint16_t *bases, uint8_t base_depth, const svo_b
                           const oracle_view_out *out, svo_child_request *req, uint32_t req_cap, uint32_t *n_req,
                           int32_t threads, uint32_t row_begin, uint32_t row_end);
 
+/* Same, with gi = 1 also running the wavefront's secondary-cone stage as the
+ * reference wires it (the hits' accumulators and colour, their usage stamps);
+ * returns -2 when the cone schedule's loops would not end. */
+int64_t oracle_trace_rows_gi(const uint16_t *bases, uint8_t base_depth, const svo_block *blocks, size_t n_blocks,
+                             svo_usage *usage, size_t n_groups, const svo_trace_input *in, int32_t max_steps,
+                             const oracle_view_out *out, svo_child_request *req, uint32_t req_cap, uint32_t *n_req,
+                             int32_t threads, uint32_t row_begin, uint32_t row_end, int32_t gi);
+
 /* Ray-setup tables of the parity contract: sinU/cosU per column, sinV/cosV
  * per row, each (float)sin((double)angle). */
 void oracle_view_tables(const svo_trace_input *in, float *sin_u, float *cos_u, float *sin_v, float *cos_v);

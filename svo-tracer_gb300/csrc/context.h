@@ -86,6 +86,8 @@ struct Context {
   DevBuf<StagedRequest> req_stage;
   DevBuf<uint8_t> req_flag;
   DevBuf<uint32_t> req_chunks;
+  // the material stage (gi_stage): hit indices of views whose caller asked for none
+  DevBuf<uint32_t> gi_hit;
   DevBuf<ViewParams> views;
   DevBuf<float> tables;
   DevBuf<uint32_t> ray_v_block, ray_v_base;
@@ -175,6 +177,7 @@ struct Context {
     bases.release();
     blocks.release();
     usage.release();
+    gi_hit.release();
     req_stage.release();
     req_flag.release();
     req_chunks.release();
@@ -256,7 +259,7 @@ inline void *pinned_device_ptr(const void *p) {
 // tiles (total_rays then exceeds total_pixels by the padding slots); 0 = rows.
 svo_status stage_views(Context &c, const svo_trace_input *in, int32_t n, const svo_trace_output *out,
                        bool outputs_on_device, uint32_t tile_w, uint32_t &total_rays, uint32_t &total_pixels,
-                       size_t &table_floats);
+                       size_t &table_floats, uint32_t *hit_fallback = nullptr);
 svo_status prepare_launch(Context &c, int32_t n_views, uint32_t total_rays, TraceLaunch &a, bool stats);
 // Synchronises the context's stream and returns the error a kernel recorded
 // since the last report (SVO_ERR_TIMEOUT with the stopped thread's ray, depth

@@ -18,12 +18,14 @@ constexpr float kPi2F = 1.57079637050628662109f;  // M_PI_2_F
 // Cone slots of one band (16 + 2 + 1 bytes each).
 constexpr uint64_t kBandSlots = 1ull << 26;
 
+}  // namespace
+
 // spawnRays's spine and ring loops (kernel.cl:1115-1253) evaluated once per
 // input: they depend only on FovMultiplier/Constant and
 // WeightingMultiplier/Constant. native_sin/cos are (float)sin((double)x).
 // Returns the cones of a fan that takes no `break` (the slot stride), or 0 when
 // that exceeds SVO_MEGA_MAX_CONES.
-int32_t build_schedule(const svo_trace_input &in, std::vector<MegaSpine> &spines, std::vector<MegaRing> &rings) {
+static int32_t build_schedule(const svo_trace_input &in, std::vector<MegaSpine> &spines, std::vector<MegaRing> &rings) {
   spines.clear();
   rings.clear();
   const float FM = in.fov_multiplier, FC = in.fov_constant;
@@ -58,6 +60,40 @@ int32_t build_schedule(const svo_trace_input &in, std::vector<MegaSpine> &spines
   return (int32_t)cones;
 }
 
+int32_t ensure_cone_schedule(Context &c, const svo_trace_input &in, svo_status &st) {
+  st = SVO_OK;
+  uint32_t key[4];
+  std::memcpy(&key[0], &in.fov_multiplier, 4);
+  std::memcpy(&key[1], &in.fov_constant, 4);
+  std::memcpy(&key[2], &in.weighting_multiplier, 4);
+  std::memcpy(&key[3], &in.weighting_constant, 4);
+  const std::array<uint32_t, 4> k4{key[0], key[1], key[2], key[3]};
+  if (c.mega_sched_valid && c.mega_sched_key == k4) return c.mega_k_max;
+  std::vector<MegaSpine> spines;
+  std::vector<MegaRing> rings;
+  const int32_t k_max = build_schedule(in, spines, rings);
+  if (k_max <= 0) return 0;
+  if (c.mega_spine.reserve(std::max<size_t>(1, spines.size())) || c.mega_ring.reserve(std::max<size_t>(1, rings.size()))) {
+    st = fail(SVO_ERR_OUT_OF_MEMORY, "cone schedule allocation");
+    return 0;
+  }
+  // a running kernel may still read the old schedule
+  cudaError_t e = cudaStreamSynchronize(c.stream);
+  if (e == cudaSuccess && !spines.empty())
+    e = cudaMemcpy(c.mega_spine.p, spines.data(), sizeof(MegaSpine) * spines.size(), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess && !rings.empty())
+    e = cudaMemcpy(c.mega_ring.p, rings.data(), sizeof(MegaRing) * rings.size(), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    st = fail(SVO_ERR_CUDA, std::string("cone schedule upload: ") + cudaGetErrorString(e));
+    return 0;
+  }
+  c.mega_sched_key = k4;
+  c.mega_sched_valid = true;
+  c.mega_n_spines = (int32_t)spines.size();
+  c.mega_k_max = k_max;
+  return k_max;
+}
+
 svo_status ensure_normal_table(Context &c) {
   if (c.mega_normal_sc.n == 65536) return SVO_OK;
   // normalVector (kernel.cl:264-275): angle = a * M_PI_F / 32767.0f
@@ -72,6 +108,8 @@ svo_status ensure_normal_table(Context &c) {
   return SVO_OK;
 }
 
+namespace {
+
 svo_status read_error(Context &c, const char *fn) { return report_kernel_error(c, fn); }
 
 svo_status run_mega(Context &c, const svo_trace_input *in, const svo_trace_output *out_in) {
@@ -84,32 +122,12 @@ svo_status run_mega(Context &c, const svo_trace_input *in, const svo_trace_outpu
     return fail(SVO_ERR_INVALID_ARGUMENT, "svo_mega_trace: block size must be a multiple of 32 up to 256");
 
   // the cone schedule, uploaded when the input's cone parameters change
-  uint32_t key[4];
-  std::memcpy(&key[0], &in->fov_multiplier, 4);
-  std::memcpy(&key[1], &in->fov_constant, 4);
-  std::memcpy(&key[2], &in->weighting_multiplier, 4);
-  std::memcpy(&key[3], &in->weighting_constant, 4);
-  const std::array<uint32_t, 4> k4{key[0], key[1], key[2], key[3]};
-  if (!c.mega_sched_valid || c.mega_sched_key != k4) {
-    std::vector<MegaSpine> spines;
-    std::vector<MegaRing> rings;
-    const int32_t k_max = build_schedule(*in, spines, rings);
-    if (k_max <= 0)
-      return fail(SVO_ERR_INVALID_ARGUMENT,
-                  "svo_mega_trace: the cone schedule exceeds SVO_MEGA_MAX_CONES cones per pixel (its loops would not end)");
-    if (c.mega_spine.reserve(std::max<size_t>(1, spines.size())) || c.mega_ring.reserve(std::max<size_t>(1, rings.size())))
-      return fail(SVO_ERR_OUT_OF_MEMORY, "svo_mega_trace: schedule allocation");
-    SVO_CUDA(cudaStreamSynchronize(c.stream), fn);  // a running band may still read the old schedule
-    if (!spines.empty())
-      SVO_CUDA(cudaMemcpy(c.mega_spine.p, spines.data(), sizeof(MegaSpine) * spines.size(), cudaMemcpyHostToDevice), fn);
-    if (!rings.empty())
-      SVO_CUDA(cudaMemcpy(c.mega_ring.p, rings.data(), sizeof(MegaRing) * rings.size(), cudaMemcpyHostToDevice), fn);
-    c.mega_sched_key = k4;
-    c.mega_sched_valid = true;
-    c.mega_n_spines = (int32_t)spines.size();
-    c.mega_k_max = k_max;
-  }
-  svo_status st = ensure_normal_table(c);
+  svo_status st = SVO_OK;
+  if (ensure_cone_schedule(c, *in, st) <= 0)
+    return st ? st
+              : fail(SVO_ERR_INVALID_ARGUMENT,
+                     "svo_mega_trace: the cone schedule exceeds SVO_MEGA_MAX_CONES cones per pixel (its loops would not end)");
+  st = ensure_normal_table(c);
   if (st) return st;
 
   // outputs: device pointers, pinned host memory the kernels write directly, or

@@ -56,6 +56,30 @@ struct MegaLaunch {
   int32_t cone_schedule;        // SVO_SCHEDULE_WARP: 32 entries per warp claim; LANE: lanes refill
 };
 
+// The wavefront's secondary-cone stage as the reference wires it (see
+// gi_kernels.cu), over every pixel of a traced batch.
+struct GiLaunch {
+  const ViewParams *views;  // device view table of the trace (hit_index set for every view)
+  const float *tables;      // the trace's ray-setup tables
+  const uint4 *blocks;
+  svo_usage *usage;
+  const float2 *normal_sc;
+  const MegaSpine *spine;
+  const MegaRing *ring;
+  uint32_t n_blocks, n_groups, total_pixels;
+  int32_t n_views, n_spines;
+  float fov_c, weighting_c;   // FovConstant, WeightingConstant of every view
+  uint32_t ambient;           // AmbientLightLevel of every view
+  int32_t valid;              // 0: evaluateMaterial returns at once (FovConstant <= 0 or |FovMultiplier| >= 1)
+};
+svo_status launch_gi(const GiLaunch &g, void *stream);
+// spawnRays's spine and ring constants for an input (cached in the context by
+// its cone parameters); returns the cones per pixel of a fan without a break
+// (0 when that exceeds SVO_MEGA_MAX_CONES: the reference's loops would not end).
+struct Context;
+int32_t ensure_cone_schedule(Context &c, const svo_trace_input &in, svo_status &st);
+svo_status ensure_normal_table(Context &c);
+
 svo_status launch_mega_primary(const MegaLaunch &m, void *stream);
 svo_status launch_mega_band(const MegaLaunch &m, void *stream);
 int mega_occupancy(const MegaLaunch &m);

@@ -36,6 +36,7 @@
 #define SVO_CVT_INTEGER 1  // integer ulong_to_float: faster in this kernel mix
 #endif
 #include "trace_core.cuh"
+#include "fan.cuh"
 
 namespace svo {
 namespace {
@@ -46,38 +47,6 @@ namespace {
 
 __device__ __forceinline__ size_t cone_slot(const MegaLaunch &m, uint32_t tile_in_band, uint32_t k, uint32_t lane) {
   return ((size_t)tile_in_band * (uint32_t)m.k_max + k) * 32u + lane;
-}
-
-__device__ __forceinline__ float dot3(float ax, float ay, float az, float bx, float by, float bz) {
-  return __fadd_rn(__fadd_rn(__fmul_rn(ax, bx), __fmul_rn(ay, by)), __fmul_rn(az, bz));
-}
-
-// normalize (OpenCL C): v / sqrt(x*x + y*y + z*z); a zero vector stays zero.
-__device__ __forceinline__ void normalize3(float &x, float &y, float &z) {
-  if (x == 0.0f && y == 0.0f && z == 0.0f) return;
-  const float l = __fsqrt_rn(dot3(x, y, z, x, y, z));
-  x = __fdiv_rn(x, l);
-  y = __fdiv_rn(y, l);
-  z = __fdiv_rn(z, l);
-}
-
-// Rotation of v about the unit axis a (cos c, sin s, k = 1 - c) in kernel.cl's
-// product order (spineRotation / ringRotation); `transpose` rotates by the
-// opposite angle (the second vector of a ring pair).
-__device__ __forceinline__ void rotate3(float ax, float ay, float az, float c, float s, float k, float vx, float vy,
-                                        float vz, bool transpose, float &ox, float &oy, float &oz) {
-  const float r3 = __fmul_rn(__fmul_rn(k, ax), ax), r4 = __fmul_rn(__fmul_rn(k, ax), ay);
-  const float r5 = __fmul_rn(__fmul_rn(k, ax), az), r6 = __fmul_rn(__fmul_rn(k, ay), ay);
-  const float r7 = __fmul_rn(__fmul_rn(k, ay), az), r8 = __fmul_rn(__fmul_rn(k, az), az);
-  const float r9 = __fmul_rn(s, ax), r10 = __fmul_rn(s, ay), r11 = __fmul_rn(s, az);
-  const float sg = transpose ? -1.0f : 1.0f;  // exact: flips the sign of the sine terms
-  const float q9 = __fmul_rn(sg, r9), q10 = __fmul_rn(sg, r10), q11 = __fmul_rn(sg, r11);
-  ox = __fadd_rn(__fadd_rn(__fmul_rn(__fadd_rn(r3, c), vx), __fmul_rn(__fsub_rn(r4, q11), vy)),
-                 __fmul_rn(__fadd_rn(r5, q10), vz));
-  oy = __fadd_rn(__fadd_rn(__fmul_rn(__fadd_rn(r4, q11), vx), __fmul_rn(__fadd_rn(r6, c), vy)),
-                 __fmul_rn(__fsub_rn(r7, q9), vz));
-  oz = __fadd_rn(__fadd_rn(__fmul_rn(__fsub_rn(r5, q10), vx), __fmul_rn(__fadd_rn(r7, q9), vy)),
-                 __fmul_rn(__fadd_rn(r8, c), vz));
 }
 
 // roundUlong (kernel.cl:240-251) in real coordinates.
@@ -325,61 +294,15 @@ __global__ void __launch_bounds__(256) mega_fan_kernel(const MegaLaunch m) {
     MegaPixel P = m.pix[slot];
     if (P.kind == kMegaSky || P.kind == kMegaSurface) {
       float n[3] = {0.0f, 0.0f, 0.0f};
-      if (P.kind == kMegaSurface) {
-        // normalVector (kernel.cl:264-275) of the block's NormalPitch/NormalYaw
-        const uint4 nd = load_node(reinterpret_cast<const uint4 *>(m.t.blocks), m.t.n_blocks, P.node);
-        const int16_t pitch = (int16_t)(nd.y >> 16), yaw = (int16_t)(nd.z & 0xffffu);
-        const float2 sp = __ldg(m.normal_sc + (pitch + 32768)), sy = __ldg(m.normal_sc + (yaw + 32768));
-        n[0] = __fmul_rn(sy.y, sp.y);
-        n[1] = __fmul_rn(sy.x, sp.y);
-        n[2] = sp.x;
-      }
-      const float Dx = P.dir[0], Dy = P.dir[1], Dz = P.dir[2];
-      float axx = __fsub_rn(__fmul_rn(Dy, n[2]), __fmul_rn(Dz, n[1]));
-      float axy = __fsub_rn(__fmul_rn(Dz, n[0]), __fmul_rn(Dx, n[2]));
-      float axz = __fsub_rn(__fmul_rn(Dx, n[1]), __fmul_rn(Dy, n[0]));
-      normalize3(axx, axy, axz);
-      const float d2 = __fmul_rn(2.0f, dot3(Dx, Dy, Dz, n[0], n[1], n[2]));
-      const float rx = __fsub_rn(Dx, __fmul_rn(d2, n[0]));
-      const float ry = __fsub_rn(Dy, __fmul_rn(d2, n[1]));
-      const float rz = __fsub_rn(Dz, __fmul_rn(d2, n[2]));
-      auto emit = [&](float x, float y, float z, float wgt, uint32_t s) {
-        const size_t i = cone_slot(m, tile, count, lane);
-        m.cone_dw[i] = make_float4(x, y, z, __fmul_rn(wgt, 1.0f));  // ringWeighting * baseWeighting
-        m.cone_s[i] = (uint16_t)s;
-        count++;
-      };
-      float fov = m.fov_c, weighting = m.weighting_c, rw = weighting;
-      float dp = dot3(rx, ry, rz, n[0], n[1], n[2]);
-      if (dp < fov) rw = __fdiv_rn(__fmul_rn(weighting, dp), fov);
-      emit(rx, ry, rz, rw, 0);
-      for (int s = 0; s < m.n_spines; s++) {
-        const MegaSpine sp = m.spine[s];
-        fov = sp.fov;
-        weighting = sp.weighting;
-        rw = weighting;
-        float sx, sy, sz;
-        rotate3(axx, axy, axz, sp.c, sp.s, sp.k, rx, ry, rz, false, sx, sy, sz);
-        normalize3(sx, sy, sz);
-        dp = dot3(sx, sy, sz, n[0], n[1], n[2]);
-        if (dp < 0.0f) break;
-        if (dp < fov) rw = __fdiv_rn(__fmul_rn(weighting, dp), fov);
-        emit(sx, sy, sz, rw, s + 1);
-        for (uint32_t j = 0; j < sp.n_rings; j++) {
-          const MegaRing rg = m.ring[sp.ring_begin + j];
-          rw = weighting;
-          float vx, vy, vz;
-          rotate3(rx, ry, rz, rg.c, rg.s, rg.k, sx, sy, sz, false, vx, vy, vz);
-          normalize3(vx, vy, vz);
-          dp = dot3(vx, vy, vz, n[0], n[1], n[2]);
-          if (dp < 0.0f) break;
-          if (dp < fov) rw = __fdiv_rn(__fmul_rn(weighting, dp), fov);
-          emit(vx, vy, vz, rw, s + 1);
-          rotate3(rx, ry, rz, rg.c, rg.s, rg.k, sx, sy, sz, true, vx, vy, vz);
-          normalize3(vx, vy, vz);
-          emit(vx, vy, vz, rw, s + 1);
-        }
-      }
+      if (P.kind == kMegaSurface)
+        block_normal(m.normal_sc, load_node(reinterpret_cast<const uint4 *>(m.t.blocks), m.t.n_blocks, P.node), n);
+      spawn_fan(n, P.dir[0], P.dir[1], P.dir[2], m.fov_c, m.weighting_c, m.spine, m.n_spines, m.ring,
+                [&](float x, float y, float z, float wgt, int s) {
+                  const size_t i = cone_slot(m, tile, count, lane);
+                  m.cone_dw[i] = make_float4(x, y, z, __fmul_rn(wgt, 1.0f));  // ringWeighting * baseWeighting
+                  m.cone_s[i] = (uint16_t)s;
+                  count++;
+                });
       // setupTrace (kernel.cl:524-544): Origin from the end location, then one
       // cell along the normal
 #pragma unroll

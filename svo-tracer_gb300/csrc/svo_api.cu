@@ -41,6 +41,7 @@ static svo_trace_config default_config() {
   c.l2_window = -1;
   c.pass_limit = 0;
   c.request_order = SVO_REQUESTS_ARRIVAL;
+  c.gi_stage = -1;
   return c;
 }
 
@@ -87,7 +88,7 @@ static int scan_tree_depth(const svo_block *blocks, size_t n_blocks, int B) {
 // Builds the view table and trig tables for `n` views in pinned staging.
 svo_status stage_views(Context &c, const svo_trace_input *in, int32_t n, const svo_trace_output *out,
                        bool outputs_on_device, uint32_t tile_w, uint32_t &total_rays, uint32_t &total_pixels,
-                       size_t &table_floats) {
+                       size_t &table_floats, uint32_t *hit_fallback) {
   const uint32_t tile_h = tile_w ? 32 / tile_w : 0;
   total_rays = 0;
   total_pixels = 0;
@@ -138,6 +139,7 @@ svo_status stage_views(Context &c, const svo_trace_input *in, int32_t n, const s
       v.t = out[i].t ? c.o_t.p + out_off : nullptr;
       v.rgba = out[i].rgba ? c.o_rgba.p + 4 * out_off : nullptr;
     }
+    if (!v.hit_index && hit_fallback) v.hit_index = hit_fallback + out_off;
     // Ray-setup angles (wavefront.cl:566-572); sin/cos are (float)sin((double)a).
     // Views of the same field of view and size share their tables.
     float *tb = c.h_tables.p + toff;
@@ -305,6 +307,29 @@ static svo_status run_trace(Context &c, const svo_trace_input *in, int32_t n, co
   }
   if (c.requests.reserve(cap) != cudaSuccess) return fail(SVO_ERR_OUT_OF_MEMORY, "svo_trace: request queue allocation");
   c.request_cap = cap;
+  // the wavefront's secondary-cone stage: one cone schedule for the call, and
+  // every view's hit indices (in a library buffer where the caller wants none)
+  const bool gi = c.cfg.gi_stage == 1;
+  bool gi_valid = false;
+  if (gi) {
+    for (int i = 1; i < n; i++)
+      if (in[i].fov_multiplier != in[0].fov_multiplier || in[i].fov_constant != in[0].fov_constant ||
+          in[i].weighting_multiplier != in[0].weighting_multiplier ||
+          in[i].weighting_constant != in[0].weighting_constant ||
+          in[i].ambient_light_level != in[0].ambient_light_level)
+        return fail(SVO_ERR_INVALID_ARGUMENT,
+                    "svo_trace: with gi_stage the views of a call must share their cone parameters and AmbientLightLevel");
+    // evaluateMaterial returns at once for these (wavefront.cl:1575-1576)
+    gi_valid = !(in[0].fov_constant <= 0 || in[0].fov_multiplier >= 1 || in[0].fov_multiplier <= -1);
+    svo_status sst = SVO_OK;
+    if (gi_valid && ensure_cone_schedule(c, in[0], sst) <= 0)
+      return sst ? sst
+                 : fail(SVO_ERR_INVALID_ARGUMENT,
+                        "svo_trace: the cone schedule exceeds SVO_MEGA_MAX_CONES cones per pixel (its loops would not end)");
+    sst = ensure_normal_table(c);
+    if (sst) return sst;
+    if (c.gi_hit.reserve(pixels)) return fail(SVO_ERR_OUT_OF_MEMORY, "svo_trace: hit index buffer allocation failed");
+  }
   uint32_t total_rays, total_pixels;
   size_t table_floats;
   // the previous call's uploads must have read the pinned staging before it is rewritten
@@ -312,8 +337,8 @@ static svo_status run_trace(Context &c, const svo_trace_input *in, int32_t n, co
   // warp batches take pixel tiles: wider ones when the kernel writes host memory
   const uint32_t tile_w =
       c.cfg.schedule != SVO_SCHEDULE_WARP ? 0 : (host_outputs && on_device ? kTraceHostTileW : kTraceTileW);
-  svo_status st = stage_views(c, in, n, out, on_device, tile_w, total_rays,
-                              total_pixels, table_floats);
+  svo_status st = stage_views(c, in, n, out, on_device, tile_w, total_rays, total_pixels, table_floats,
+                              gi ? c.gi_hit.p : nullptr);
   if (st) return st;
   bool stats = c.cfg.collect_stats > 0;
   if (c.views.reserve(n) || c.tables.reserve(table_floats))
@@ -323,6 +348,25 @@ static svo_status run_trace(Context &c, const svo_trace_input *in, int32_t n, co
   TraceLaunch a;
   st = prepare_launch(c, n, total_rays, a, stats);
   if (st) return st;
+  GiLaunch g{};
+  if (gi) {
+    g.views = c.views.p;
+    g.tables = c.tables.p;
+    g.blocks = reinterpret_cast<const uint4 *>(c.blocks.p);
+    g.usage = c.usage.p;
+    g.normal_sc = c.mega_normal_sc.p;
+    g.spine = c.mega_spine.p;
+    g.ring = c.mega_ring.p;
+    g.n_blocks = (uint32_t)c.budget;
+    g.n_groups = (uint32_t)c.n_groups;
+    g.total_pixels = total_pixels;
+    g.n_views = n;
+    g.n_spines = gi_valid ? c.mega_n_spines : 0;
+    g.fov_c = in[0].fov_constant;
+    g.weighting_c = in[0].weighting_constant;
+    g.ambient = in[0].ambient_light_level;
+    g.valid = gi_valid ? 1 : 0;
+  }
   // pixel-order child requests: staged per pixel, the queue built after the trace
   const bool pixel_order = c.cfg.request_order == SVO_REQUESTS_PIXEL;
   const size_t flag_bytes = ((size_t)total_pixels + kRequestChunk - 1) / kRequestChunk * kRequestChunk;
@@ -345,8 +389,9 @@ static svo_status run_trace(Context &c, const svo_trace_input *in, int32_t n, co
     if (stats) SVO_CUDA(cudaMemsetAsync(c.stats.p, 0, 8 * sizeof(unsigned long long), c.stream), "svo_trace: stats reset");
     if (pixel_order) SVO_CUDA(cudaMemsetAsync(a.req_flag, 0, flag_bytes, c.stream), "svo_trace: request flags");
     svo_status lst = launch_trace(a, stats, c.stream);
-    if (lst || !pixel_order) return lst;
-    return launch_request_compaction(a, total_pixels, c.req_chunks.p, c.stream);
+    if (!lst && pixel_order) lst = launch_request_compaction(a, total_pixels, c.req_chunks.p, c.stream);
+    if (!lst && gi) lst = launch_gi(g, c.stream);
+    return lst;
   };
 
   if (use_graph && !stats) {
@@ -367,6 +412,19 @@ static svo_status run_trace(Context &c, const svo_trace_input *in, int32_t n, co
     key.push_back((uint32_t)(uintptr_t)c.req_stage.p);
     key.push_back((uint32_t)(uintptr_t)c.requests.p);
     key.push_back(c.request_cap);
+    key.push_back(gi ? 1u + (uint32_t)g.valid : 0u);
+    if (gi) {
+      uint32_t bits[3];
+      std::memcpy(&bits[0], &g.fov_c, 4);
+      std::memcpy(&bits[1], &g.weighting_c, 4);
+      bits[2] = g.ambient;
+      key.insert(key.end(), bits, bits + 3);
+      key.push_back((uint32_t)g.n_spines);
+      key.push_back((uint32_t)(uintptr_t)g.spine);
+      key.push_back((uint32_t)(uintptr_t)g.ring);
+      key.push_back((uint32_t)(uintptr_t)g.normal_sc);
+      key.push_back((uint32_t)(uintptr_t)c.gi_hit.p);
+    }
     if (!c.graph_exec || key != c.graph_key) {
       if (c.graph_exec) cudaGraphExecDestroy(c.graph_exec);
       c.graph_exec = nullptr;
@@ -498,6 +556,9 @@ SVO_API svo_status svo_set_trace_config(void *ctx, const svo_trace_config *cfg) 
   if (n.schedule == 0) n.schedule = d.schedule;
   if (n.l2_window == 0) n.l2_window = d.l2_window;
   if (n.request_order == 0) n.request_order = d.request_order;
+  if (n.gi_stage == 0) n.gi_stage = -1;
+  if (n.gi_stage != 1 && n.gi_stage != -1)
+    return fail(SVO_ERR_INVALID_ARGUMENT, "svo_set_trace_config: gi_stage must be 1 (on) or -1 / 0 (off)");
   if (n.request_order != SVO_REQUESTS_ARRIVAL && n.request_order != SVO_REQUESTS_PIXEL)
     return fail(SVO_ERR_INVALID_ARGUMENT, "svo_set_trace_config: request_order must be SVO_REQUESTS_ARRIVAL or _PIXEL");
   if (n.pass_limit < 0) return fail(SVO_ERR_INVALID_ARGUMENT, "svo_set_trace_config: pass_limit must be >= 0");

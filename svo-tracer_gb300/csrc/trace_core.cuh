@@ -459,6 +459,23 @@ __device__ __forceinline__ bool ray_slot(const TraceLaunch &a, const ViewParams 
   return true;
 }
 
+// setupInitialTrace's direction (wavefront.cl:566-578) of pixel (px, py):
+// Facing * (cosU cosV, -sinU cosV, sinV), not normalised, from the view's
+// sine/cosine tables.
+__device__ __forceinline__ void ray_direction(const ViewParams &v, const float *tables, uint32_t px, uint32_t py,
+                                              float &dx, float &dy, float &dz) {
+  const float *tb = tables + v.table_off;
+  float su = __ldg(tb + px), cu = __ldg(tb + v.width + px);
+  float sv = __ldg(tb + 2 * v.width + py), cv = __ldg(tb + 2 * v.width + v.height + py);
+  float m0 = __fmul_rn(cu, cv);
+  float m1 = __fmul_rn(__fsub_rn(0.0f, su), cv);
+  float m2 = sv;
+  const float *F = v.facing;
+  dx = __fadd_rn(__fadd_rn(__fmul_rn(F[0], m0), __fmul_rn(F[3], m1)), __fmul_rn(F[6], m2));
+  dy = __fadd_rn(__fadd_rn(__fmul_rn(F[1], m0), __fmul_rn(F[4], m1)), __fmul_rn(F[7], m2));
+  dz = __fadd_rn(__fadd_rn(__fmul_rn(F[2], m0), __fmul_rn(F[5], m1)), __fmul_rn(F[8], m2));
+}
+
 // setupInitialTrace (wavefront.cl:563-595) for ray slot `my` of the batch,
 // then traceIntoVolume; a ray that misses the cube gets depth 0 (background).
 // Returns false (and sets nothing else) for a padding slot. kernel.cl's
@@ -471,16 +488,7 @@ __device__ __forceinline__ bool setup_ray(const TraceLaunch &a, const ViewParams
   const ViewParams &v = s_views[view];
   r.view = view;
   r.id = py * v.width + px;
-  const float *tb = a.tables + v.table_off;
-  float su = __ldg(tb + px), cu = __ldg(tb + v.width + px);
-  float sv = __ldg(tb + 2 * v.width + py), cv = __ldg(tb + 2 * v.width + v.height + py);
-  float m0 = __fmul_rn(cu, cv);
-  float m1 = __fmul_rn(__fsub_rn(0.0f, su), cv);
-  float m2 = sv;
-  const float *F = v.facing;
-  r.dx = __fadd_rn(__fadd_rn(__fmul_rn(F[0], m0), __fmul_rn(F[3], m1)), __fmul_rn(F[6], m2));
-  r.dy = __fadd_rn(__fadd_rn(__fmul_rn(F[1], m0), __fmul_rn(F[4], m1)), __fmul_rn(F[7], m2));
-  r.dz = __fadd_rn(__fadd_rn(__fmul_rn(F[2], m0), __fmul_rn(F[5], m1)), __fmul_rn(F[8], m2));
+  ray_direction(v, a.tables, px, py, r.dx, r.dy, r.dz);
   r.ix = __frcp_rn(r.dx);
   r.iy = __frcp_rn(r.dy);
   r.iz = __frcp_rn(r.dz);

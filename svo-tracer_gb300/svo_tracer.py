@@ -86,7 +86,7 @@ class TraceStatsC(C.Structure):
 class TraceConfigC(C.Structure):
     _fields_ = [(n, C.c_int32) for n in ("block_size", "ctas_per_sm", "ray_chunk", "cadence", "max_steps",
                                           "collect_stats", "max_hits", "schedule", "mega_band_tiles", "l2_window",
-                                          "pass_limit", "request_order")]
+                                          "pass_limit", "request_order", "gi_stage")]
 
 
 class SceneParamsC(C.Structure):

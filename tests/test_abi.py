@@ -130,5 +130,5 @@ def test_binding_signatures_match_the_header():
 
 def test_trace_config_layout():
     names = [n for n, _ in st.TraceConfigC._fields_]
-    assert names[-2:] == ["pass_limit", "request_order"]
+    assert names[-3:] == ["pass_limit", "request_order", "gi_stage"]
     assert C.sizeof(st.TraceConfigC) == 4 * len(names)
