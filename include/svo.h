@@ -183,7 +183,7 @@ typedef struct svo_trace_config {
   int32_t max_steps;    /* per-ray step limit */
   int32_t collect_stats; /* 0 none, 1 totals (svo_last_trace_stats), 2 totals and per-ray counts */
   int32_t max_hits;     /* differentiable forward: LOD hits composited per ray (1..1024) */
-  int32_t schedule;     /* SVO_SCHEDULE_LANE or SVO_SCHEDULE_WARP */
+  int32_t schedule;     /* SVO_SCHEDULE_LANE, SVO_SCHEDULE_WARP or SVO_SCHEDULE_WAVEFRONT */
   int32_t mega_band_tiles; /* megakernel: pixel tiles of 32 per cone band (0: as many as 2^26 cone slots hold) */
   int32_t l2_window;    /* 1: the trace kernel reads the dense level-(B+2) nodes through an L2 persisting
                            access-policy window, -1: no window */
@@ -214,8 +214,12 @@ enum { SVO_REQUESTS_ARRIVAL = 1, SVO_REQUESTS_PIXEL = 2 };
 /* Ray scheduling of the persistent trace kernel. LANE: each thread claims rays
  * on its own and finished rays are replaced every `cadence` steps. WARP: each
  * warp claims 32 consecutive rays, runs them to the end and regroups before the
- * next claim (ray_chunk and cadence unused). Results are identical. */
-enum { SVO_SCHEDULE_LANE = 1, SVO_SCHEDULE_WARP = 2 };
+ * next claim (ray_chunk and cadence unused). WAVEFRONT: the reference's queue
+ * compaction between passes (wavefront.cl:249-336, MainWindow.cs:452-481) inside
+ * each CTA: every pass, each thread takes one step of its ray, and the rays
+ * whose octant was empty are compacted into a shared-memory queue whose moves
+ * the CTA's first threads run in full warps. Results are identical. */
+enum { SVO_SCHEDULE_LANE = 1, SVO_SCHEDULE_WARP = 2, SVO_SCHEDULE_WAVEFRONT = 3 };
 
 /* Counters of the last svo_mega_trace. */
 typedef struct svo_mega_stats {
@@ -274,7 +278,8 @@ SVO_API svo_status svo_trace_batch_graph(void *ctx, const svo_trace_input *input
                                          const svo_trace_output *out);
 SVO_API svo_status svo_last_trace_stats(void *ctx, svo_trace_stats *stats);
 /* Autotuner for a view set (no reference counterpart): times svo_trace_batch
- * over block sizes {64,128,256} x ray chunks {1,2,4,8} x cadences {4,8,16,32}
+ * with warp batches and the CTA wavefront at block sizes {64,128,256}, and lane
+ * refills at those sizes x ray chunks {1,2,4,8} x cadences {4,8,16,32}
  * (best of `repeats` runs each; outputs must be device pointers), keeps the
  * fastest configuration in the context and returns it. Results are identical
  * for every configuration. */

@@ -185,6 +185,7 @@ svo_status run_mega(Context &c, const svo_trace_input *in, const svo_trace_outpu
   const bool stats = c.cfg.collect_stats > 0;
   st = prepare_launch(c, 1, total_rays, m.t, stats);
   if (st) return st;
+  m.t.schedule = c.cfg.schedule == SVO_SCHEDULE_LANE ? SVO_SCHEDULE_LANE : SVO_SCHEDULE_WARP;  // the cone kernel's two
   m.pix = c.mega_pix.p;
   m.cone_dw = c.mega_cone_dw.p;
   m.cone_s = c.mega_cone_s.p;

@@ -336,7 +336,7 @@ static svo_status run_trace(Context &c, const svo_trace_input *in, int32_t n, co
   SVO_CUDA(cudaEventSynchronize(c.staged), "svo_trace: staging");
   // warp batches take pixel tiles: wider ones when the kernel writes host memory
   const uint32_t tile_w =
-      c.cfg.schedule != SVO_SCHEDULE_WARP ? 0 : (host_outputs && on_device ? kTraceHostTileW : kTraceTileW);
+      c.cfg.schedule == SVO_SCHEDULE_LANE ? 0 : (host_outputs && on_device ? kTraceHostTileW : kTraceTileW);
   svo_status st = stage_views(c, in, n, out, on_device, tile_w, total_rays, total_pixels, table_floats,
                               gi ? c.gi_hit.p : nullptr);
   if (st) return st;
@@ -566,7 +566,8 @@ SVO_API svo_status svo_set_trace_config(void *ctx, const svo_trace_config *cfg) 
     return fail(SVO_ERR_INVALID_ARGUMENT, "svo_set_trace_config: block_size must be a multiple of 32 in 32..256");
   if (n.ray_chunk < 1 || n.ray_chunk > 64 || n.cadence < 1 || n.cadence > 1024 || n.max_steps < 1 || n.ctas_per_sm < 0 ||
       n.collect_stats < 0 || n.collect_stats > 2 || n.max_hits < 1 || n.max_hits > 1024 || n.mega_band_tiles < 0 ||
-      (n.schedule != SVO_SCHEDULE_LANE && n.schedule != SVO_SCHEDULE_WARP) || (n.l2_window != 1 && n.l2_window != -1))
+      (n.schedule != SVO_SCHEDULE_LANE && n.schedule != SVO_SCHEDULE_WARP && n.schedule != SVO_SCHEDULE_WAVEFRONT) ||
+      (n.l2_window != 1 && n.l2_window != -1))
     return fail(SVO_ERR_INVALID_ARGUMENT, "svo_set_trace_config: value out of range");
   if (n.l2_window < 0) c.release_l2_set_aside();
   c.cfg = n;
@@ -750,6 +751,8 @@ SVO_API svo_status svo_autotune(void *ctx, const svo_trace_input *inputs, int32_
     svo_trace_config cfg = base;
     cfg.block_size = bs;
     cfg.schedule = SVO_SCHEDULE_WARP;
+    cands.push_back(cfg);
+    cfg.schedule = SVO_SCHEDULE_WAVEFRONT;
     cands.push_back(cfg);
     for (int ch : chunks)
       for (int cd : cadences) {

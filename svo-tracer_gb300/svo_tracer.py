@@ -53,7 +53,7 @@ STATUS_NAMES = {
     6: "NoTree", 7: "StepLimit", 8: "Budget", 9: "NoDevice", 10: "Internal",
 }
 SCENE_SPHERE, SCENE_TERRAIN = 0, 1
-SCHEDULE_LANE, SCHEDULE_WARP = 1, 2
+SCHEDULE_LANE, SCHEDULE_WARP, SCHEDULE_WAVEFRONT = 1, 2, 3
 REQUESTS_ARRIVAL, REQUESTS_PIXEL = 1, 2
 
 

@@ -52,7 +52,8 @@ def compare(tracer, tree, view):
     return got, want
 
 
-@pytest.mark.parametrize("schedule", [st.SCHEDULE_WARP, st.SCHEDULE_LANE], ids=["warp", "lane"])
+@pytest.mark.parametrize("schedule", [st.SCHEDULE_WARP, st.SCHEDULE_LANE, st.SCHEDULE_WAVEFRONT],
+                         ids=["warp", "lane", "wavefront"])
 @pytest.mark.parametrize("scene", ["sphere", "terrain_random_normals"])
 def test_gi_stage_matches_oracle(tracer, trees, scene, schedule):
     tracer.set_config(schedule=schedule)

@@ -33,7 +33,8 @@ def _queue(tracer, cap):
     return req.copy(), n
 
 
-@pytest.mark.parametrize("schedule", [st.SCHEDULE_WARP, st.SCHEDULE_LANE], ids=["warp", "lane"])
+@pytest.mark.parametrize("schedule", [st.SCHEDULE_WARP, st.SCHEDULE_LANE, st.SCHEDULE_WAVEFRONT],
+                         ids=["warp", "lane", "wavefront"])
 def test_queue_past_the_cap_is_the_lowest_pixels_in_order(tracer, terrain, schedule):
     cap = 700
     cam = st.look_at((0.1, 0.15, 0.55), (0.7, 0.7, 0.9), 160, 90, 60.0, Tick=3, MaxChildRequestId=cap)

@@ -39,7 +39,7 @@ def _stopped(call):
 
 def test_trace_reports_a_stopped_kernel_under_both_schedules(tracer, sphere):
     tree, cam = sphere
-    for schedule in (st.SCHEDULE_WARP, st.SCHEDULE_LANE):
+    for schedule in (st.SCHEDULE_WARP, st.SCHEDULE_LANE, st.SCHEDULE_WAVEFRONT):
         tracer.set_config(pass_limit=1, schedule=schedule)
         _stopped(lambda: tracer.trace(cam))  # host outputs: the call synchronises and reports
     tracer.set_config(pass_limit=0, schedule=st.SCHEDULE_WARP)

@@ -83,7 +83,8 @@ SCENES = [
 ]
 
 
-@pytest.mark.parametrize("schedule", [st.SCHEDULE_LANE, st.SCHEDULE_WARP], ids=["lane", "warp"])
+@pytest.mark.parametrize("schedule", [st.SCHEDULE_LANE, st.SCHEDULE_WARP, st.SCHEDULE_WAVEFRONT],
+                         ids=["lane", "warp", "wavefront"])
 @pytest.mark.parametrize("scene", SCENES, ids=[s[0] for s in SCENES])
 def test_trace_matches_oracle(tracer, scene, schedule):
     _, kind, seed, b, d, o, t, w, h, fov, dof = scene
@@ -106,7 +107,8 @@ def test_trace_matches_oracle(tracer, scene, schedule):
     assert stats["step_limited"] == 0
 
 
-@pytest.mark.parametrize("schedule", [st.SCHEDULE_LANE, st.SCHEDULE_WARP], ids=["lane", "warp"])
+@pytest.mark.parametrize("schedule", [st.SCHEDULE_LANE, st.SCHEDULE_WARP, st.SCHEDULE_WAVEFRONT],
+                         ids=["lane", "warp", "wavefront"])
 def test_step_limit_matches_oracle(tracer, schedule):
     tracer.set_config(schedule=schedule)
     tree = st.TreeBuilder(st.SCENE_TERRAIN, seed=5).BuildTree(3, 8)
@@ -179,7 +181,9 @@ def test_l2_window_in_graph_replay(tracer):
                                  dict(block_size=64, ray_chunk=3, cadence=5, ctas_per_sm=1),
                                  dict(block_size=128, schedule=st.SCHEDULE_WARP),
                                  dict(block_size=64, schedule=st.SCHEDULE_WARP, ctas_per_sm=1),
-                                 dict(schedule=st.SCHEDULE_WARP, l2_window=1)])
+                                 dict(schedule=st.SCHEDULE_WARP, l2_window=1),
+                                 dict(block_size=96, schedule=st.SCHEDULE_WAVEFRONT),
+                                 dict(block_size=256, schedule=st.SCHEDULE_WAVEFRONT, ctas_per_sm=1)])
 def test_launch_shapes_do_not_change_results(tracer, cfg):
     tree = st.TreeBuilder(st.SCENE_SPHERE, seed=6).BuildTree(4, 8)
     cam = st.look_at((1.1, 0.2, 0.9), (0.5, 0.5, 0.5), 120, 90, 60.0)
@@ -295,7 +299,7 @@ def test_errors(tracer):
     with pytest.raises(st.SvoError):
         tracer.set_config(block_size=100)
     with pytest.raises(st.SvoError):
-        tracer.set_config(schedule=3)
+        tracer.set_config(schedule=4)
     with pytest.raises(st.SvoError):
         tracer.set_config(l2_window=2)
     assert lib is not None
