@@ -179,19 +179,53 @@ __device__ __forceinline__ uint4 load_node(const uint4 *blocks, uint32_t n_block
 // returning leaving (:433-437) of the new location. A sum that the reference
 // clamps (0 to kAll) always leaves, so the clamp is left to the caller's
 // leaving branch.
+// SVO_TRACE_AXIS_BOUNDS (off): traverseChunk's axis chosen from bounds on the
+// three boundary distances, one exact 64-bit conversion instead of three when
+// the choice is clear. Identical results; measured on GB300 (1080p frame / 64
+// views / megakernel frame): 1.536 vs 1.522 ms, 8.54 vs 8.66 ms, 16.96 vs 15.07
+// ms, so the FP64-pipe conversions it saves do not bound these kernels.
+#ifndef SVO_TRACE_AXIS_BOUNDS
+#define SVO_TRACE_AXIS_BOUNDS 0
+#endif
 __device__ __forceinline__ bool traverse(Ray &r, int depth) {
   const uint32_t low_hi = 0xffffffffu >> (depth + 1);  // kAll >> (depth + 1), depth < 31
   uint64_t d0 = boundary_distance(r.wx, low_hi, r.sx);
   uint64_t d1 = boundary_distance(r.wy, low_hi, r.sy);
   uint64_t d2 = boundary_distance(r.wz, low_hi, r.sz);
-  const float f0 = ulong_to_float(d0), f1 = ulong_to_float(d1), f2 = ulong_to_float(d2);
-  float a0 = fabsf(__fmul_rn(f0, r.ix));
-  float a1 = fabsf(__fmul_rn(f1, r.iy));
-  float a2 = fabsf(__fmul_rn(f2, r.iz));
-  int ax = (a0 <= a1 && a0 <= a2) ? 0 : ((a1 <= a0 && a1 <= a2) ? 1 : 2);
+  int ax = -1;
+  float fa = 0.0f;
+  if (SVO_TRACE_AXIS_BOUNDS) {
+    // The axis from bounds. A distance d with high word h >= 1 lies in
+    // [h, h + 1) * 2^32, so fl(d) lies in [RZ(h), RU(h + 1)] * 2^32 (floats
+    // below and above d), and a = fl(fl(d) * |inv|) lies between the rounded
+    // products of those bounds (the rounded product is monotone). An axis whose
+    // upper bound is below both other lower bounds is the strict minimum, the
+    // reference's choice whatever its tie rule; only its distance is then
+    // converted exactly. Otherwise all three are (below).
+    const uint32_t h0 = hi32(d0), h1 = hi32(d1), h2 = hi32(d2);
+    if (h0 && h1 && h2) {
+      const float i0 = fabsf(r.ix), i1 = fabsf(r.iy), i2 = fabsf(r.iz);
+      const float l0 = __fmul_rn(__fmul_rn(__uint2float_rz(h0), 0x1p32f), i0);
+      const float l1 = __fmul_rn(__fmul_rn(__uint2float_rz(h1), 0x1p32f), i1);
+      const float l2 = __fmul_rn(__fmul_rn(__uint2float_rz(h2), 0x1p32f), i2);
+      const float u0 = __fmul_rn(__fmul_rn(__uint2float_ru(h0 + (h0 != 0xffffffffu)), 0x1p32f), i0);
+      const float u1 = __fmul_rn(__fmul_rn(__uint2float_ru(h1 + (h1 != 0xffffffffu)), 0x1p32f), i1);
+      const float u2 = __fmul_rn(__fmul_rn(__uint2float_ru(h2 + (h2 != 0xffffffffu)), 0x1p32f), i2);
+      ax = (u0 < l1 && u0 < l2) ? 0 : ((u1 < l0 && u1 < l2) ? 1 : ((u2 < l0 && u2 < l1) ? 2 : -1));
+      if (ax >= 0) fa = ulong_to_float(ax == 0 ? d0 : (ax == 1 ? d1 : d2));
+    }
+  }
+  if (ax < 0) {
+    const float f0 = ulong_to_float(d0), f1 = ulong_to_float(d1), f2 = ulong_to_float(d2);
+    float a0 = fabsf(__fmul_rn(f0, r.ix));
+    float a1 = fabsf(__fmul_rn(f1, r.iy));
+    float a2 = fabsf(__fmul_rn(f2, r.iz));
+    ax = (a0 <= a1 && a0 <= a2) ? 0 : ((a1 <= a0 && a1 <= a2) ? 1 : 2);
+    fa = ax == 0 ? f0 : (ax == 1 ? f1 : f2);
+  }
   float inv = ax == 0 ? r.ix : (ax == 1 ? r.iy : r.iz);
   // ulongToFloat of the chosen distance: its float conversion times 2^-64 (exact)
-  float u = __fmul_rn(ax == 0 ? f0 : (ax == 1 ? f1 : f2), 0x1p-64f);
+  float u = __fmul_rn(fa, 0x1p-64f);
   // the two other axes' moves, exactly two conversions per lane: A is x unless x
   // was chosen (then y), B is z unless z was chosen (then y)
   const bool c0 = ax == 0, c2 = ax == 2;
