@@ -168,10 +168,20 @@ struct Context {
   // graph cache for svo_trace_batch_graph
   cudaGraphExec_t graph_exec = nullptr;
   std::vector<uint32_t> graph_key;
+  // the GC's launch sequence as a graph (svo_gc), its key, the tick/threshold
+  // word it copies in and the counts it copies out (pinned)
+  cudaGraphExec_t gc_exec = nullptr;
+  std::vector<uint64_t> gc_key;
+  DevBuf<uint32_t> gc_params;
+  PinBuf<uint32_t> h_gc_params, h_gc_out;
 
   ~Context() {
     if (device >= 0) cudaSetDevice(device);
     if (graph_exec) cudaGraphExecDestroy(graph_exec);
+    if (gc_exec) cudaGraphExecDestroy(gc_exec);
+    gc_params.release();
+    h_gc_params.release();
+    h_gc_out.release();
     release_l2_set_aside();
     if (staged) cudaEventDestroy(staged);
     bases.release();

@@ -133,7 +133,11 @@ __global__ void k_init_usage_tree(TreeView t, const uint32_t *reach, const uint3
 }
 
 // Stale groups: flag and detach from the parent node that still points at them.
-__global__ void k_stale_detach(TreeView t, uint16_t now, uint32_t threshold, uint8_t *flags) {
+// params: [0] the frame's tick, [1] the staleness threshold (device memory, so
+// that a captured GC graph replays with the current frame's values).
+__global__ void k_stale_detach(TreeView t, const uint32_t *params, uint8_t *flags) {
+  const uint16_t now = (uint16_t)params[0];
+  const uint32_t threshold = params[1];
   for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < t.n_groups; g += gridDim.x * blockDim.x) {
     uint8_t f = 0;
     uint32_t tk = t.usage[g].tick;
@@ -411,7 +415,7 @@ svo_status ensure_tree_buffers(Context &c) {
   size_t nb = (g + kScanBlock - 1) / kScanBlock + 1;
   if (c.reach.reserve(g) || c.parent_min.reserve(g) || c.frontier_a.reserve(g) || c.frontier_b.reserve(g) ||
       c.flags.reserve(g) || c.scan_tmp.reserve(nb + 12) || c.free_list.reserve(g) || c.pruned_list.reserve(g) ||
-      c.freed_list.reserve(g))
+      c.freed_list.reserve(g) || c.gc_params.reserve(2) || c.h_gc_params.reserve(2) || c.h_gc_out.reserve(4))
     return fail(SVO_ERR_OUT_OF_MEMORY, "tree update: device allocation failed");
   return SVO_OK;
 }
@@ -468,10 +472,10 @@ void compact_async(Context &c, const uint8_t *flags, uint32_t n, uint32_t *out, 
 
 
 // Reachability, the sweep of unreachable allocated groups and the free list,
-// then one read-back of the counts: the freed count, the free-list length and
-// (with `pruned_total`, a device slot already written) the pruned count.
-svo_status sweep_and_free_list(Context &c, const TreeView &t, uint64_t *n_freed, uint64_t *n_pruned = nullptr,
-                               const uint32_t *pruned_total = nullptr) {
+// enqueued without a synchronisation (a GC graph captures it): the freed count,
+// the free-list length, the frontier left and (with `pruned_total`, a device
+// slot already written) the pruned count go to the pinned h_out[0..3].
+svo_status enqueue_sweep(Context &c, const TreeView &t, const uint32_t *pruned_total, uint32_t *h_out) {
   uint32_t *left = reachability_async(c, t, false);
   uint32_t *totals = c.scan_tmp.p + (c.scan_tmp.n - 4);  // [0] freed, [1] free, [2] frontier left
   k_sweep<<<grid_for(t.n_groups), 256, 0, c.stream>>>(t, c.reach.p, c.flags.p, left);
@@ -480,11 +484,14 @@ svo_status sweep_and_free_list(Context &c, const TreeView &t, uint64_t *n_freed,
   compact_async(c, c.flags.p, t.n_groups, c.free_list.p, totals + 1);
   SVO_CUDA(cudaMemcpyAsync(totals + 2, left, 4, cudaMemcpyDeviceToDevice, c.stream), "tree update: frontier");
   SVO_CUDA(cudaGetLastError(), "tree update: kernels");
-  uint32_t h[4] = {0, 0, 0, 0};
-  SVO_CUDA(cudaMemcpyAsync(h, totals, 3 * sizeof(uint32_t), cudaMemcpyDeviceToHost, c.stream), "tree update: counts");
+  SVO_CUDA(cudaMemcpyAsync(h_out, totals, 3 * sizeof(uint32_t), cudaMemcpyDeviceToHost, c.stream), "tree update: counts");
   if (pruned_total)
-    SVO_CUDA(cudaMemcpyAsync(h + 3, pruned_total, 4, cudaMemcpyDeviceToHost, c.stream), "tree update: counts");
-  SVO_CUDA(cudaStreamSynchronize(c.stream), "tree update: synchronize");
+    SVO_CUDA(cudaMemcpyAsync(h_out + 3, pruned_total, 4, cudaMemcpyDeviceToHost, c.stream), "tree update: counts");
+  return SVO_OK;
+}
+
+// The host side of a completed sweep: the counts read back into h[0..3].
+svo_status finish_sweep(Context &c, const uint32_t *h, uint64_t *n_freed, uint64_t *n_pruned) {
   if (h[2]) {
     c.free_valid = false;
     return fail(SVO_ERR_INTERNAL, "tree update: tree deeper than its recorded depth; nothing was freed");
@@ -495,6 +502,16 @@ svo_status sweep_and_free_list(Context &c, const TreeView &t, uint64_t *n_freed,
   c.free_used = 0;
   c.free_valid = true;
   return SVO_OK;
+}
+
+svo_status sweep_and_free_list(Context &c, const TreeView &t, uint64_t *n_freed, uint64_t *n_pruned = nullptr,
+                               const uint32_t *pruned_total = nullptr) {
+  uint32_t *h = c.h_gc_out.p;
+  h[0] = h[1] = h[2] = h[3] = 0;
+  svo_status st = enqueue_sweep(c, t, pruned_total, h);
+  if (st) return st;
+  SVO_CUDA(cudaStreamSynchronize(c.stream), "tree update: synchronize");
+  return finish_sweep(c, h, n_freed, n_pruned);
 }
 
 // ---- graft payloads generated on the device (terrain scenes) -------------------
@@ -823,10 +840,44 @@ SVO_API svo_status svo_gc(void *ctx, const svo_update_input *in, svo_gc_report *
   svo_status st = svo::ensure_tree_buffers(c);
   if (st) return st;
   svo::TreeView t = svo::view_of(c);
-  svo::k_stale_detach<<<svo::grid_for(t.n_groups), 256, 0, c.stream>>>(t, in->tick, in->offset, c.flags.p);
+  // The GC's ~30 launches (stale detach, one reachability level per tree level,
+  // sweep, three compactions) and count read-backs replay from a CUDA graph,
+  // captured for the tree's shape and buffers; the frame's tick and threshold
+  // reach it through a pinned word its first node copies.
+  c.h_gc_params.p[0] = in->tick;
+  c.h_gc_params.p[1] = in->offset;
   uint32_t *pruned_total = c.scan_tmp.p + (c.scan_tmp.n - 5 + 4);  // the slot after the GC totals
-  svo::compact_async(c, c.flags.p, t.n_groups, c.pruned_list.p, pruned_total);
-  st = svo::sweep_and_free_list(c, t, &c.n_freed, &c.n_pruned, pruned_total);
+  const std::vector<uint64_t> key = {c.n_groups, (uint64_t)c.tree_depth, c.base_depth, (uintptr_t)c.blocks.p,
+                                     (uintptr_t)c.usage.p, (uintptr_t)c.bases.p, (uintptr_t)c.reach.p,
+                                     (uintptr_t)c.flags.p, (uintptr_t)c.scan_tmp.p, c.scan_tmp.n,
+                                     (uintptr_t)c.free_list.p, (uintptr_t)c.pruned_list.p, (uintptr_t)c.freed_list.p,
+                                     (uintptr_t)c.frontier_a.p, (uintptr_t)c.frontier_b.p, (uintptr_t)c.stream};
+  if (!c.gc_exec || c.gc_key != key) {
+    if (c.gc_exec) cudaGraphExecDestroy(c.gc_exec);
+    c.gc_exec = nullptr;
+    SVO_CUDA(cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal), "svo_gc: capture");
+    cudaMemcpyAsync(c.gc_params.p, c.h_gc_params.p, 2 * sizeof(uint32_t), cudaMemcpyHostToDevice, c.stream);
+    svo::k_stale_detach<<<svo::grid_for(t.n_groups), 256, 0, c.stream>>>(t, c.gc_params.p, c.flags.p);
+    svo::compact_async(c, c.flags.p, t.n_groups, c.pruned_list.p, pruned_total);
+    svo_status est = svo::enqueue_sweep(c, t, pruned_total, c.h_gc_out.p);
+    cudaGraph_t g = nullptr;
+    cudaError_t ce = cudaStreamEndCapture(c.stream, &g);
+    if (est) {
+      if (g) cudaGraphDestroy(g);
+      return est;
+    }
+    if (ce != cudaSuccess) return fail(SVO_ERR_CUDA, std::string("svo_gc: end capture: ") + cudaGetErrorString(ce));
+    ce = cudaGraphInstantiate(&c.gc_exec, g, 0);
+    cudaGraphDestroy(g);
+    if (ce != cudaSuccess) {
+      c.gc_exec = nullptr;
+      return fail(SVO_ERR_CUDA, std::string("svo_gc: instantiate: ") + cudaGetErrorString(ce));
+    }
+    c.gc_key = key;
+  }
+  SVO_CUDA(cudaGraphLaunch(c.gc_exec, c.stream), "svo_gc: launch");
+  SVO_CUDA(cudaStreamSynchronize(c.stream), "svo_gc: synchronize");
+  st = svo::finish_sweep(c, c.h_gc_out.p, &c.n_freed, &c.n_pruned);
   if (st) return st;
   if (report) {
     report->pruned = c.n_pruned;
