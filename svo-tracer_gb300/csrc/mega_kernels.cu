@@ -401,6 +401,7 @@ __device__ __forceinline__ void start_cone(const MegaLaunch &m, uint32_t e, Ray 
   r.id = P->id;
   r.depth = 1;
   r.steps = 0;
+  if (SVO_TRACE_CELL_CACHE) r.cell = cell_index(1, r.wx, r.wy, r.wz, r.flip);
   reset_walk(w);
 }
 

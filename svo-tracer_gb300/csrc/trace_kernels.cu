@@ -317,6 +317,7 @@ __global__ void __launch_bounds__(256, SVO_TRACE_MIN_CTAS) trace_kernel(const Tr
         const uint32_t sw = s_st[slot];
         r.depth = (int)(sw & 0xffu);
         r.cone = -1.0f;
+        if (SVO_TRACE_CELL_CACHE && r.depth >= 1 && r.depth <= B) r.cell = cell_index(r.depth, r.wx, r.wy, r.wz, r.flip);
         if ((int)(sw >> 8) == kStepBackground) {
           finish_ray(s_views[r.view], kStepBackground);
           have = false;
