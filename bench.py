@@ -803,6 +803,33 @@ def run_ours(args, rank, world):
         dist.destroy_process_group()
 
 
+def run_ncu_case(args):
+    """One launch of a profiled case, for an ncu capture, then exit: `batch64` is
+    the 64 mixed views over the depth-11 terrain in one batched launch (the
+    multiview section's kernel, warp batches of 128 threads)."""
+    import torch
+
+    import svo_tracer as st
+
+    tree, _ = reference_scene(st)
+    views = st.mixed_views(seed=4, Tick=7, MaxChildRequestId=1 << 16)
+    tr = st.Tracer(0)
+    tr.upload(tree)
+    tr.init_usage()
+    keep, outs = [], []
+    for v in views:
+        n = v.ScreenSize[0] * v.ScreenSize[1]
+        o = (torch.empty(n, dtype=torch.int32, device="cuda"), torch.empty(n, dtype=torch.uint8, device="cuda"),
+             torch.empty(n, dtype=torch.float32, device="cuda"), torch.empty(4 * n, dtype=torch.float32, device="cuda"))
+        keep.append(o)
+        outs.append(tuple(x.data_ptr() for x in o))
+    tr.set_config(block_size=128)
+    tr.trace_device(views, outs)
+    torch.cuda.synchronize()
+    tr.close()
+    print("%s: one batched launch of %d views" % (args.ncu_case, len(views)))
+
+
 def main():
     global WIDTH, HEIGHT
     ap = argparse.ArgumentParser()
@@ -816,6 +843,8 @@ def main():
     ap.add_argument("--no-mega", action="store_true")
     ap.add_argument("--no-sphere", action="store_true")
     ap.add_argument("--no-gi", action="store_true")
+    ap.add_argument("--ncu-case", choices=["batch64"], default=None,
+                    help="run one launch of a profiled case and exit (for an ncu capture)")
     ap.add_argument("--schedule", choices=["lane", "warp"], default=None)
     ap.add_argument("--diff-views", type=int, default=16)
     ap.add_argument("--diff-size", type=int, default=512)
@@ -827,7 +856,13 @@ def main():
     args.warmup = max(3, args.warmup)
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", str(args.gpus if args.impl == "reference" else 1)))
-    if args.impl == "reference":
+    if args.ncu_case:
+        import __graft_entry__
+
+        if not os.path.exists(os.path.join(ROOT, "svo-tracer_gb300", "lib", "libsvo.so")):
+            __graft_entry__.build()
+        run_ncu_case(args)
+    elif args.impl == "reference":
         run_reference(args, rank, world)
     else:
         import __graft_entry__
