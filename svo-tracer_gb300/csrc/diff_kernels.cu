@@ -50,8 +50,12 @@
 #include <vector>
 
 #include "context.h"
-#ifndef SVO_CVT_INTEGER
-#define SVO_CVT_INTEGER 1  // integer ulong_to_float: faster in this kernel mix
+// The base cell kept in a register across descents (the trace kernel's default)
+// costs these kernels registers: measured on GB300 (16 x 512^2 sphere views),
+// forward 1.93 -> 1.92 ms, saved-colour backward 2.22 -> 2.12 ms, recomputing
+// backward 6.99 -> 6.19 ms without it (the backward's spill 280 -> 160 bytes).
+#ifndef SVO_TRACE_CELL_CACHE
+#define SVO_TRACE_CELL_CACHE 0
 #endif
 #include "trace_core.cuh"
 

@@ -28,16 +28,19 @@ __device__ __forceinline__ uint32_t pow_sum(int depth) {
 
 // The fixed-point conversions exist in two exact forms: the 64-bit conversion
 // instructions, which run on this GPU's FP64 pipe at 1/64 of the FP32 rate, and
-// an integer form around the 32-bit conversion (more instructions, no FP64
-// pipe). Which is faster depends on the kernel's instruction mix: a
-// translation unit defines SVO_CVT_INTEGER to 1 before including this header
-// to take the integer form of ulong_to_float (the colour-fitting backward:
-// 1.15 -> 1.04 ms; the megakernel's cones: 19.03 -> 18.91 ms per frame; the
-// primary trace: 1.80 -> 1.83 ms, and 1.574 -> 1.754 ms at the current step
-// code, so it keeps the instruction). unit_to_ulong keeps the instruction
-// everywhere.
+// integer forms (more instructions, no FP64 pipe). Which is faster depends on
+// the kernel's instruction mix, measured on GB300 with identical outputs:
+//  * ulong_to_float (SVO_CVT_INTEGER): the integer form everywhere. Primary
+//    trace 1.519 -> 1.458 ms per 1080p frame, 64 views 8.50 -> 8.42 ms (at an
+//    earlier step code the instruction was faster: 1.574 vs 1.754 ms), the
+//    colour-fitting backward 1.15 -> 1.04 ms, the megakernel's cones 19.03 ->
+//    18.91 ms per frame.
+//  * unit_to_ulong (SVO_CVT_INTEGER_F2U): the instruction unless set.
 #ifndef SVO_CVT_INTEGER
-#define SVO_CVT_INTEGER 0
+#define SVO_CVT_INTEGER 1
+#endif
+#ifndef SVO_CVT_INTEGER_F2U
+#define SVO_CVT_INTEGER_F2U 0
 #endif
 
 // (float)x of a 64-bit fixed-point value, rounded to nearest even
@@ -58,8 +61,21 @@ __device__ __forceinline__ float ulong_to_float(uint64_t x) {
 __device__ __forceinline__ float ulong_to_unit(uint64_t x) { return __fmul_rn(ulong_to_float(x), 0x1p-64f); }
 
 // floatToUlong (wavefront.cl:200-207); out-of-range products saturate, NaN -> 0.
+// Integer form: |x| * 2^64 is exact (a power-of-two scale of a float below the
+// overflow range), so its truncation is the 24-bit significand m shifted by
+// e = exponent(|x|) + 64 - 150: m << e for e >= 0, m >> -e for e in (-24, 0),
+// 0 below; |x| >= 1 saturates to 2^64 - 1 as the instruction does.
 __device__ __forceinline__ uint64_t unit_to_ulong(float x) {
   if (x >= 0.999999911f) return kAll;
+  if (SVO_CVT_INTEGER_F2U) {
+    const uint32_t u = __float_as_uint(x) & 0x7fffffffu;
+    if (u > 0x7f800000u) return 0;       // NaN
+    if (u >= 0x3f800000u) return kAll;   // |x| >= 1 (and infinity)
+    const int e = (int)(u >> 23) - 86;   // exponent + 64 - 150, at most 40
+    const uint32_t m = (u & 0x7fffffu) | 0x800000u;
+    if (e >= 0) return (uint64_t)m << e;
+    return e > -24 ? (uint64_t)(m >> -e) : 0ull;
+  }
   const float v = __fmul_rn(fabsf(x), 0x1p64f);
   // the conversion clamps v >= 2^64 to kAll, but turns NaN into 2^63
   return v != v ? 0 : __float2ull_rz(v);

@@ -50,7 +50,17 @@ namespace svo {
 namespace {
 
 #ifndef SVO_TRACE_MIN_CTAS
-#define SVO_TRACE_MIN_CTAS 4  // 57 registers, no spills (5: 48 registers with a spill, 1.4% slower on the 1080p frame)
+#define SVO_TRACE_MIN_CTAS 4  // 59 registers, no spills (5: 48 registers with a spill, 1.62 vs 1.455 ms on the 1080p frame)
+#endif
+// SVO_TRACE_WARP_REFILL = T > 0: warp batches whose idle lanes take the next
+// ray slots (tile order, one atomic per warp) once at most T lanes of the warp
+// still hold a ray, instead of waiting for the whole batch. 0: plain batches.
+// Identical results; measured on GB300 (1080p frame / 64 views, medians), T = 4,
+// 8, 16: 1.72, 1.83, 1.93 ms and 9.48, 9.77, 10.28 ms against 1.52 and 8.50 ms. The
+// refilled lanes start far from the stragglers they join, so the steps of the
+// warp diverge more than the idle lanes cost.
+#ifndef SVO_TRACE_WARP_REFILL
+#define SVO_TRACE_WARP_REFILL 0
 #endif
 // Dynamic shared memory before the wavefront schedule's area: the view table,
 // the base chunks (when staged) and the path cache, rounded to 16 bytes.
@@ -172,7 +182,57 @@ __global__ void __launch_bounds__(256, SVO_TRACE_MIN_CTAS) trace_kernel(const Tr
     }
   };
 
-  if (kSched == 1) {
+  if (kSched == 1 && SVO_TRACE_WARP_REFILL > 0) {
+    // ---- warp batches with refills: every control decision below is taken
+    // from warp votes, so all 32 lanes run every iteration of the loop
+    const uint32_t lane = threadIdx.x & 31u, below = (1u << lane) - 1u;
+    const uint32_t ray_limit = a.pass_limit ? a.pass_limit : (uint32_t)a.max_steps + 2u;
+    bool have = false, timed_out = false, drained = false;
+    uint32_t ray_iters = 0;
+    for (;;) {
+      if (++iters > iter_limit) {  // the same count in every lane
+        record_timeout();
+        break;
+      }
+      unsigned act = __ballot_sync(kFull, have);
+      if (__popc(act) <= SVO_TRACE_WARP_REFILL && !drained) {
+        if (__any_sync(kFull, timed_out)) break;
+        const unsigned idle = ~act;
+        const uint32_t n = (uint32_t)__popc(idle);
+        uint32_t first = 0;
+        if (lane == 0) first = atomicAdd(a.ray_counter, n);
+        first = __shfl_sync(kFull, first, 0);
+        drained = (uint64_t)first + n >= (uint64_t)a.total_rays;
+        if (!have) {
+          const uint32_t my = first + (uint32_t)__popc(idle & below);
+          if (my < a.total_rays && start_ray(my)) {
+            have = true;
+            ray_iters = 0;
+          }
+        }
+        act = __ballot_sync(kFull, have);
+      }
+      if (act == 0) {
+        if (drained) break;
+        continue;
+      }
+      if (have) {
+        if (++ray_iters > ray_limit) {
+          record_timeout();
+          timed_out = true;
+          have = false;
+        } else {
+          const ViewParams &v = s_views[r.view];
+          const int f = probe<kStats, kSmemBases>(a, v, s_bases, blocks, B, r, w, st);
+          const int finish = f == kStepEmpty ? advance(a, blocks, B, r, w) : f;
+          if (finish != kStepOn) {
+            finish_ray(v, finish);
+            have = false;
+          }
+        }
+      }
+    }
+  } else if (kSched == 1) {
     // ---- warp batches: 32 consecutive ray slots (one pixel tile of a tiled
     // view) per warp, regrouped between batches
     const uint32_t lane = threadIdx.x & 31u;
