@@ -150,10 +150,12 @@ typedef struct svo_child_request {
 /* Per-pixel results of a trace. Pointers are host memory unless on_device is
  * non-zero, then they are device pointers the caller owns. Any pointer may be
  * NULL to skip that output. When every host output of a call is pinned
- * (cudaMallocHost / cudaHostRegister), the kernel writes them directly and the
- * transfer overlaps the trace; other host memory goes through device buffers
- * and a copy after the trace. Either way the call returns with the outputs
- * written. */
+ * (cudaMallocHost / cudaHostRegister), the kernel writes hit_index, t and rgba
+ * directly, so their transfer overlaps the trace, and hit_depth (one byte per
+ * pixel, too small a store to cross to host memory efficiently) goes through a
+ * device buffer and one copy per view; other host memory goes through device
+ * buffers and a copy after the trace. Either way the call returns with the
+ * outputs written. */
 typedef struct svo_trace_output {
   uint32_t *hit_index; /* node index of the hit, SVO_MISS for background */
   uint8_t *hit_depth;  /* level of the hit node, 0 for background */

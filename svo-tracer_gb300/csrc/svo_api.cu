@@ -270,18 +270,36 @@ static svo_status run_trace(Context &c, const svo_trace_input *in, int32_t n, co
   for (int i = 1; i < n; i++)
     if ((out[i].on_device == 0) != host_outputs)
       return fail(SVO_ERR_INVALID_ARGUMENT, "svo_trace: outputs of one call must all be host or all device");
+  size_t pixels = 0;
+  uint32_t cap = 0;
+  for (int i = 0; i < n; i++) {
+    pixels += (size_t)in[i].screen_size[0] * in[i].screen_size[1];
+    cap = std::max(cap, in[i].max_child_request_id);
+  }
   // Host outputs in pinned memory are written by the kernel itself (the GPU
-  // addresses pinned memory directly), so their transfer overlaps the trace;
-  // any other host output goes through device buffers and copies afterwards.
+  // addresses pinned memory directly), so their transfer overlaps the trace.
+  // The outputs in kStagedHostOutputs are the exception: a warp's stores of
+  // them are too small to cross to host memory efficiently (one byte of hit
+  // depth per pixel), so they go to a device buffer and one copy per view
+  // after the trace. Any other host output goes through device buffers and
+  // copies afterwards.
   std::vector<svo_trace_output> mapped;
+  const svo_trace_output *caller_out = out;
+  bool staged_copies = false;
   if (host_outputs) {
     bool all_pinned = true;
     mapped.assign(out, out + n);
     for (int i = 0; i < n && all_pinned; i++) {
       void **ptrs[4] = {reinterpret_cast<void **>(&mapped[i].hit_index), reinterpret_cast<void **>(&mapped[i].hit_depth),
                         reinterpret_cast<void **>(&mapped[i].t), reinterpret_cast<void **>(&mapped[i].rgba)};
-      for (void **pp : ptrs) {
+      for (int k = 0; k < 4 && all_pinned; k++) {
+        void **pp = ptrs[k];
         if (!*pp) continue;
+        if (kStagedHostOutputs & (1u << k)) {
+          staged_copies = true;  // checked below; the pointer is replaced once the buffers exist
+          if (!pinned_device_ptr(*pp)) all_pinned = false;
+          continue;
+        }
         void *d = pinned_device_ptr(*pp);
         if (!d) {
           all_pinned = false;
@@ -291,15 +309,26 @@ static svo_status run_trace(Context &c, const svo_trace_input *in, int32_t n, co
       }
       mapped[i].on_device = 1;
     }
-    if (all_pinned) out = mapped.data();
+    if (all_pinned) {
+      if (staged_copies) {
+        if (((kStagedHostOutputs & 1u) && c.o_index.reserve(pixels)) || ((kStagedHostOutputs & 2u) && c.o_depth.reserve(pixels)) ||
+            ((kStagedHostOutputs & 4u) && c.o_t.reserve(pixels)) || ((kStagedHostOutputs & 8u) && c.o_rgba.reserve(4 * pixels)))
+          return fail(SVO_ERR_OUT_OF_MEMORY, "svo_trace: output buffer allocation failed");
+        size_t off = 0;
+        for (int i = 0; i < n; i++) {
+          if ((kStagedHostOutputs & 1u) && mapped[i].hit_index) mapped[i].hit_index = c.o_index.p + off;
+          if ((kStagedHostOutputs & 2u) && mapped[i].hit_depth) mapped[i].hit_depth = c.o_depth.p + off;
+          if ((kStagedHostOutputs & 4u) && mapped[i].t) mapped[i].t = c.o_t.p + off;
+          if ((kStagedHostOutputs & 8u) && mapped[i].rgba) mapped[i].rgba = c.o_rgba.p + 4 * off;
+          off += (size_t)in[i].screen_size[0] * in[i].screen_size[1];
+        }
+      }
+      out = mapped.data();
+    } else {
+      staged_copies = false;
+    }
   }
   const bool on_device = out[0].on_device != 0;  // device buffers, or pinned host memory the kernel writes
-  size_t pixels = 0;
-  uint32_t cap = 0;
-  for (int i = 0; i < n; i++) {
-    pixels += (size_t)in[i].screen_size[0] * in[i].screen_size[1];
-    cap = std::max(cap, in[i].max_child_request_id);
-  }
   if (!on_device) {
     if (c.o_index.reserve(pixels) || c.o_depth.reserve(pixels) || c.o_t.reserve(pixels) ||
         c.o_rgba.reserve(4 * pixels))
@@ -469,6 +498,24 @@ static svo_status run_trace(Context &c, const svo_trace_input *in, int32_t n, co
       off += np;
     }
     return check_kernel_error(c);  // synchronises after the copies
+  }
+  if (staged_copies) {
+    // the staged outputs of pinned host buffers: from the device buffers to the
+    // caller's host memory
+    size_t off = 0;
+    for (int i = 0; i < n; i++) {
+      const size_t np = (size_t)in[i].screen_size[0] * in[i].screen_size[1];
+      const svo_trace_output &h = caller_out[i];
+      if ((kStagedHostOutputs & 1u) && h.hit_index)
+        SVO_CUDA(cudaMemcpyAsync(h.hit_index, c.o_index.p + off, np * 4, cudaMemcpyDeviceToHost, c.stream), "svo_trace: read hit_index");
+      if ((kStagedHostOutputs & 2u) && h.hit_depth)
+        SVO_CUDA(cudaMemcpyAsync(h.hit_depth, c.o_depth.p + off, np, cudaMemcpyDeviceToHost, c.stream), "svo_trace: read hit_depth");
+      if ((kStagedHostOutputs & 4u) && h.t)
+        SVO_CUDA(cudaMemcpyAsync(h.t, c.o_t.p + off, np * 4, cudaMemcpyDeviceToHost, c.stream), "svo_trace: read t");
+      if ((kStagedHostOutputs & 8u) && h.rgba)
+        SVO_CUDA(cudaMemcpyAsync(h.rgba, c.o_rgba.p + 4 * off, np * 16, cudaMemcpyDeviceToHost, c.stream), "svo_trace: read rgba");
+      off += np;
+    }
   }
   if (host_outputs) return check_kernel_error(c);  // the kernel wrote pinned host memory: wait for it
   return SVO_OK;

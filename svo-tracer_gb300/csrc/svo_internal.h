@@ -29,8 +29,14 @@ struct TreeHost;
 #ifndef SVO_DIFF_TILE_W
 #define SVO_DIFF_TILE_W 8
 #endif
+// The outputs of pinned host buffers that a trace stages in device memory and
+// copies after the kernel instead of writing them from the kernel (bit 0 hit
+// index, 1 hit depth, 2 t, 3 RGBA).
+#ifndef SVO_STAGED_HOST_OUTPUTS
+#define SVO_STAGED_HOST_OUTPUTS 2
+#endif
 constexpr uint32_t kTraceTileW = SVO_TRACE_TILE_W, kTraceHostTileW = SVO_TRACE_HOST_TILE_W,
-                   kDiffTileW = SVO_DIFF_TILE_W;
+                   kDiffTileW = SVO_DIFF_TILE_W, kStagedHostOutputs = SVO_STAGED_HOST_OUTPUTS;
 static_assert((kTraceTileW & (kTraceTileW - 1)) == 0 && kTraceTileW <= 32, "tile width: a power of two up to 32");
 static_assert((kDiffTileW & (kDiffTileW - 1)) == 0 && kDiffTileW <= 32, "tile width: a power of two up to 32");
 static_assert((kTraceHostTileW & (kTraceHostTileW - 1)) == 0 && kTraceHostTileW <= 32, "tile width");

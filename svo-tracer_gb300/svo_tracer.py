@@ -693,8 +693,10 @@ class Tracer:
         _check("MegaStats", self._lib.svo_last_mega_stats(self._ctx, C.byref(s)))
         return {n: getattr(s, n) for n, _ in MegaStatsC._fields_}
 
-    def trace_batch(self, inputs, graph: bool = False):
-        res = [self._alloc(*i.ScreenSize) for i in inputs]
+    def trace_batch(self, inputs, graph: bool = False, out=None):
+        """Many views in one launch; `out`, when given, holds one TraceResult per
+        view (arrays may be None to skip an output)."""
+        res = list(out) if out is not None else [self._alloc(*i.ScreenSize) for i in inputs]
         c_in = (TraceInputC * len(inputs))(*[i.to_c() for i in inputs])
         c_out = (TraceOutputC * len(inputs))(*[self._out(r) for r in res])
         fn = self._lib.svo_trace_batch_graph if graph else self._lib.svo_trace_batch

@@ -330,3 +330,18 @@ def test_pinned_host_outputs_equal_staged_outputs(tracer):
             for k in ("hit_index", "hit_depth", "t", "rgba"):
                 assert np.array_equal(getattr(got, k).reshape(-1), getattr(want, k).reshape(-1)), k
     assert (want.hit_index != st.MISS).any()
+    # a batch (plain and graph-replayed) of pinned outputs, one view without its
+    # hit depth (the output staged in device memory) and one without t, against
+    # the oracle
+    wants = [po.trace_view(tree, cam) for cam in cams]
+    for graph in (False, True):
+        for _ in range(2):
+            outs = [pinned(*cam.ScreenSize) for cam in cams]
+            outs[0].hit_depth = None
+            outs[1].t = None
+            got = tracer.trace_batch(cams, graph=graph, out=outs)
+            for g, w in zip(got, wants):
+                assert np.array_equal(g.hit_index, w["hit_index"])
+                assert np.array_equal(g.rgba.view(np.uint32), w["rgba"].view(np.uint32))
+            assert np.array_equal(got[0].t.view(np.uint32), wants[0]["t"].view(np.uint32))
+            assert np.array_equal(got[1].hit_depth, wants[1]["hit_depth"])
