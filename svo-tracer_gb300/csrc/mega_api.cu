@@ -130,32 +130,51 @@ svo_status run_mega(Context &c, const svo_trace_input *in, const svo_trace_outpu
   st = ensure_normal_table(c);
   if (st) return st;
 
-  // outputs: device pointers, pinned host memory the kernels write directly, or
-  // library buffers copied back to pageable host memory
+  // outputs: device pointers, pinned host memory the kernels write directly
+  // (but for the outputs in kStagedHostOutputs, which go to library buffers and
+  // one copy each, as in svo_trace), or library buffers copied back to pageable
+  // host memory
   svo_trace_output out = *out_in;
+  const svo_trace_output caller = *out_in;
   const bool host_outputs = out.on_device == 0;
   bool direct = !host_outputs;
+  uint32_t staged = 0;  // outputs of pinned buffers staged in library buffers
   if (host_outputs) {
     svo_trace_output mapped = out;
     bool all_pinned = true;
     void **ptrs[4] = {reinterpret_cast<void **>(&mapped.hit_index), reinterpret_cast<void **>(&mapped.hit_depth),
                       reinterpret_cast<void **>(&mapped.t), reinterpret_cast<void **>(&mapped.rgba)};
-    for (void **pp : ptrs) {
+    for (int k = 0; k < 4; k++) {
+      void **pp = ptrs[k];
       if (!*pp) continue;
       void *d = pinned_device_ptr(*pp);
       if (!d) {
         all_pinned = false;
         break;
       }
-      *pp = d;
+      if (kStagedHostOutputs & (1u << k))
+        staged |= 1u << k;
+      else
+        *pp = d;
     }
     if (all_pinned) {
       mapped.on_device = 1;
       out = mapped;
       direct = true;
+    } else {
+      staged = 0;
     }
   }
   const size_t pixels = (size_t)in->screen_size[0] * in->screen_size[1];
+  if (staged) {
+    if (((staged & 1u) && c.o_index.reserve(pixels)) || ((staged & 2u) && c.o_depth.reserve(pixels)) ||
+        ((staged & 4u) && c.o_t.reserve(pixels)) || ((staged & 8u) && c.o_rgba.reserve(4 * pixels)))
+      return fail(SVO_ERR_OUT_OF_MEMORY, "svo_mega_trace: output buffer allocation failed");
+    if (staged & 1u) out.hit_index = c.o_index.p;
+    if (staged & 2u) out.hit_depth = c.o_depth.p;
+    if (staged & 4u) out.t = c.o_t.p;
+    if (staged & 8u) out.rgba = c.o_rgba.p;
+  }
   if (!direct && (c.o_index.reserve(pixels) || c.o_depth.reserve(pixels) || c.o_t.reserve(pixels) ||
                   c.o_rgba.reserve(4 * pixels)))
     return fail(SVO_ERR_OUT_OF_MEMORY, "svo_mega_trace: output buffer allocation failed");
@@ -230,6 +249,10 @@ svo_status run_mega(Context &c, const svo_trace_input *in, const svo_trace_outpu
   SVO_CUDA(cudaMemcpyAsync(c.h_mega_totals.p, c.mega_totals.p, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
                            c.stream),
            fn);
+  if (staged & 1u) SVO_CUDA(cudaMemcpyAsync(caller.hit_index, c.o_index.p, pixels * 4, cudaMemcpyDeviceToHost, c.stream), fn);
+  if (staged & 2u) SVO_CUDA(cudaMemcpyAsync(caller.hit_depth, c.o_depth.p, pixels, cudaMemcpyDeviceToHost, c.stream), fn);
+  if (staged & 4u) SVO_CUDA(cudaMemcpyAsync(caller.t, c.o_t.p, pixels * 4, cudaMemcpyDeviceToHost, c.stream), fn);
+  if (staged & 8u) SVO_CUDA(cudaMemcpyAsync(caller.rgba, c.o_rgba.p, pixels * 16, cudaMemcpyDeviceToHost, c.stream), fn);
   if (!direct) {
     if (out.hit_index)
       SVO_CUDA(cudaMemcpyAsync(out.hit_index, c.o_index.p, pixels * 4, cudaMemcpyDeviceToHost, c.stream), fn);
