@@ -182,6 +182,17 @@ struct Ray {
 #ifndef SVO_TRACE_CELL_CACHE
 #define SVO_TRACE_CELL_CACHE 1
 #endif
+// SVO_TRACE_BASE_RUN: a base-level step that descends runs the ray's following
+// base-level steps in the same call while they descend (with the cell cache
+// only). Identical results; measured on GB300 (1080p frame / 64 views /
+// megakernel frame): 1.453 vs 1.464 ms, 8.12 vs 8.43 ms, 14.69 vs 14.91 ms, and
+// 56 instead of 59 registers in the trace kernel.
+#ifndef SVO_TRACE_BASE_RUN
+#define SVO_TRACE_BASE_RUN 1
+#endif
+// (The same for block-level descents, where the next step loads the child node,
+// measured much slower: 1.82 vs 1.46 ms, 10.5 vs 8.1 ms, 18.7 vs 14.7 ms.)
+
 
 __device__ __forceinline__ uint64_t loc_x(const Ray &r) { return r.wx ^ dir_mask(r.sx); }
 __device__ __forceinline__ uint64_t loc_y(const Ray &r) { return r.wy ^ dir_mask(r.sy); }
@@ -418,10 +429,27 @@ __device__ __forceinline__ int probe(const TraceLaunch &a, const ViewParams &v, 
       w.last_group = group;
     }
   }
-  const uint32_t oct = octant(r.depth, r.wx, r.wy, r.wz, r.flip);
+  uint32_t oct = octant(r.depth, r.wx, r.wy, r.wz, r.flip);
   if (((chunk >> (oct * 2)) & 2) == 0) return kStepEmpty;
   if (!block) {
     // geometry below a base cell: descend, jumping from level B to B+2
+#if SVO_TRACE_BASE_RUN && SVO_TRACE_CELL_CACHE
+    // the following base-level steps of the ray run here while they descend:
+    // each is the step the next call would take (same step count, limit and
+    // order), without the call's dispatch
+    while (r.depth < B) {
+      r.depth++;
+      r.cell = r.cell * 8u + oct;
+      if (a.max_steps > 0 && r.steps >= a.max_steps) return kStepOn;  // the next call ends the ray
+      r.steps++;
+      const uint32_t c2 = kSmemBases ? s_bases[pow_sum(r.depth - 1) + r.cell] : __ldg(a.bases + pow_sum(r.depth - 1) + r.cell);
+      if (kStats) w.v_base++;
+      oct = octant(r.depth, r.wx, r.wy, r.wz, r.flip);
+      if (((c2 >> (oct * 2)) & 2) == 0) return kStepEmpty;
+    }
+    r.depth = B + 2;
+    w.path[0] = (r.cell * 8u + oct) * 8u + octant(B + 1, r.wx, r.wy, r.wz, r.flip);
+#else
     if (r.depth < B) {
       r.depth++;
       if (SVO_TRACE_CELL_CACHE) r.cell = r.cell * 8u + oct;
@@ -430,6 +458,7 @@ __device__ __forceinline__ int probe(const TraceLaunch &a, const ViewParams &v, 
       w.path[0] = SVO_TRACE_CELL_CACHE ? (r.cell * 8u + oct) * 8u + octant(B + 1, r.wx, r.wy, r.wz, r.flip)
                                        : cell_index(B + 2, r.wx, r.wy, r.wz, r.flip);
     }
+#endif
     return kStepOn;
   }
   // geometry below a node: the cone LOD decision (ConeDepth = -half_log2(c));
