@@ -152,20 +152,20 @@ __device__ __forceinline__ void record_timeout(const TraceLaunch &a, uint32_t it
 }
 
 // Runs a cone to its end: kStepHit at a surface, kStepBackground in the sky;
-// false when it needed more passes than max_steps allows (a fault). kStats: the
+// false when its step count reached the pass bound (max_steps + 2, which only a
+// fault reaches, or the launch's pass_limit) before it ended. kStats: the
 // cone's reference-walk counters (V_block, V_base) and its hit go to st.
 template <bool kSmemBases, bool kStats>
 __device__ __forceinline__ bool run_cone(const TraceLaunch &a, const ViewParams &v, const uint16_t *s_bases,
                                          const uint4 *blocks, int B, Ray &r, Walk &w, int &finish, Stats &st) {
   const uint32_t limit = a.pass_limit ? a.pass_limit : (uint32_t)a.max_steps + 2u;
-  uint32_t n = 0;
   finish = kStepOn;
   while (finish == kStepOn) {
-    if (++n > limit) return false;
+    if ((uint32_t)r.steps >= limit) return false;  // every pass takes a step or ends the cone
     finish = probe<kStats, kSmemBases, true>(a, v, s_bases, blocks, B, r, w, st);
     if (SVO_TRACE_PROBE_RUNS)
       while (finish == kStepOn) {
-        if (++n > limit) return false;
+        if ((uint32_t)r.steps >= limit) return false;
         finish = probe<kStats, kSmemBases, true>(a, v, s_bases, blocks, B, r, w, st);
       }
     if (finish == kStepEmpty) {

@@ -50,7 +50,7 @@ namespace svo {
 namespace {
 
 #ifndef SVO_TRACE_MIN_CTAS
-#define SVO_TRACE_MIN_CTAS 4  // 59 registers, no spills (5: 48 registers with a spill, 1.62 vs 1.455 ms on the 1080p frame)
+#define SVO_TRACE_MIN_CTAS 4  // 53 registers, no spills (5: 48 registers, no spill, 1.56 vs 1.45 ms on the 1080p frame)
 #endif
 // SVO_TRACE_WARP_REFILL = T > 0: warp batches whose idle lanes take the next
 // ray slots (tile order, one atomic per warp) once at most T lanes of the warp
@@ -246,12 +246,12 @@ __global__ void __launch_bounds__(256, SVO_TRACE_MIN_CTAS) trace_kernel(const Tr
       if (my < a.total_rays && !timed_out && start_ray(my)) {
         const ViewParams &v = s_views[r.view];
         int finish = kStepOn;
-        // a step ends a ray after max_steps steps, so a ray needing more
-        // passes than that is a fault: record it and stop the warp
+        // a probe ends a ray once it has taken max_steps steps, so a ray whose
+        // step count reaches max_steps + 2 is a fault: record it and stop the warp
         const uint32_t ray_limit = a.pass_limit ? a.pass_limit : (uint32_t)a.max_steps + 2u;
-        uint32_t ray_iters = 0;
         while (finish == kStepOn) {
-          if (++ray_iters > ray_limit) {
+          // every pass takes a step (counted in r.steps) or ends the ray
+          if ((uint32_t)r.steps >= ray_limit) {
             record_timeout();
             timed_out = true;
             break;
@@ -260,7 +260,7 @@ __global__ void __launch_bounds__(256, SVO_TRACE_MIN_CTAS) trace_kernel(const Tr
           if (SVO_TRACE_PROBE_RUNS) {
             // steps that keep the location (descents, LOD ascents) run back to
             // back, so the move below runs with every lane whose octant is empty
-            while (f == kStepOn && ++ray_iters <= ray_limit) f = probe<kStats, kSmemBases>(a, v, s_bases, blocks, B, r, w, st);
+            while (f == kStepOn && (uint32_t)r.steps < ray_limit) f = probe<kStats, kSmemBases>(a, v, s_bases, blocks, B, r, w, st);
             if (f == kStepOn) {
               record_timeout();
               timed_out = true;
