@@ -120,6 +120,26 @@ def test_step_limit_matches_oracle(tracer, schedule):
     assert np.array_equal(usage["tick"], u_ref["tick"])
 
 
+@pytest.mark.parametrize("schedule", [st.SCHEDULE_LANE, st.SCHEDULE_WARP, st.SCHEDULE_WAVEFRONT],
+                         ids=["lane", "warp", "wavefront"])
+def test_small_step_limits_inside_base_level_runs(tracer, schedule):
+    """Step limits of 1 to 8 stop rays in the middle of their first descents, which
+    the kernel runs as base-level runs within one step call (B = 4, so a ray's
+    first four steps are base levels): each limit must stop every ray at the same
+    step as the oracle, with the same stamps, per-ray counts and outputs."""
+    tracer.set_config(schedule=schedule)
+    tree = st.TreeBuilder(st.SCENE_TERRAIN, seed=5).BuildTree(4, 9)
+    cam = st.look_at((0.1, 0.15, 0.55), (0.7, 0.7, 0.9), 48, 32, 60.0)
+    for limit in range(1, 9):
+        got, usage, req, n, stats, (vb, vs), want, u_ref = run_both(tracer, tree, cam, max_steps=limit)
+        assert want["step_limited"] > 0
+        assert stats["step_limited"] == want["step_limited"], limit
+        assert_same(got, want, "max_steps %d" % limit)
+        assert np.array_equal(usage["tick"], u_ref["tick"]), limit
+        assert np.array_equal(vs, want["v_base"]), limit
+        assert np.array_equal(vb, want["v_block"]), limit
+
+
 def test_request_cap(tracer):
     tree = st.TreeBuilder(st.SCENE_TERRAIN, seed=5).BuildTree(2, 7)
     cam = st.look_at((0.1, 0.15, 0.55), (0.7, 0.7, 0.9), 128, 72, 60.0, MaxChildRequestId=50)
