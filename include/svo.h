@@ -453,6 +453,19 @@ SVO_API svo_status svo_oct_write(const char *path, uint8_t base_depth, uint32_t 
                                  size_t n_bases, const svo_block *blocks, size_t n_blocks);
 SVO_API svo_status svo_oct_read(const char *path, void **tree);
 
+/* Streaming-state snapshot (checkpoint / resume). svo_state_save writes, after
+ * the context's pending work, everything later frames depend on: the base
+ * chunks, every block of the budget (grafted groups included), the usage
+ * array, the depth the tree has grown to, and the free list of the last GC with
+ * the part grafts have claimed. svo_state_load replaces the context's resident
+ * tree with a saved state (its own budget); the frames that follow (the caller
+ * keeps the tick) give what they would have given in the saved context.
+ * SVO_ERR_IO for a file that cannot be read or written or is truncated,
+ * SVO_ERR_INVALID_ARGUMENT for one that is not a consistent state file. The
+ * reference persists only the octree (.oct). */
+SVO_API svo_status svo_state_save(void *ctx, const char *path);
+SVO_API svo_status svo_state_load(void *ctx, const char *path);
+
 /* A persistent scene: the tree builder and the graft payload source of the
  * streaming workflow (the host-side procedural generator behind
  * WorldManager.UpdateGrafting, SvoTracer.Window/WorldManager.cs:84-103).

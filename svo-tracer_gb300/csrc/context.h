@@ -275,5 +275,7 @@ svo_status prepare_launch(Context &c, int32_t n_views, uint32_t total_rays, Trac
 // since the last report (SVO_ERR_TIMEOUT with the stopped thread's ray, depth
 // and steps), clearing the record; SVO_OK when none did.
 svo_status report_kernel_error(Context &c, const char *fn);
+// Reserves the tree updates' scratch for the context's budget (tree_ops.cu).
+svo_status ensure_tree_buffers(Context &c);
 
 }  // namespace svo

@@ -174,6 +174,8 @@ __device__ __forceinline__ bool walk_hits(const DiffLaunch &d, const ViewParams 
       visit(0u, true, r);
       return counted(true);
     }
+    if (!SVO_CHECK(a.error, r.depth - B - 2 >= 0 && r.depth - B - 2 < a.path_levels, 9, (uint32_t)(r.depth - B - 2)))
+      return counted(false);
     visit(w.path[(r.depth - B - 2) * w.stride], false, r);
     if (kStats) st.hits++;
     if (++hits >= d.max_hits) return counted(true);

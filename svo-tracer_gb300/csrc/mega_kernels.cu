@@ -255,7 +255,10 @@ __global__ void __launch_bounds__(256, SVO_MEGA_MIN_CTAS) mega_primary_kernel(co
           // resolveRayData: the block, RayLength = length(Location - Origin)
           P.kind = kMegaSurface;
           P.depth = (uint8_t)r.depth;
-          P.node = w.path[(r.depth - B - 2) * w.stride];
+          P.node = SVO_CHECK(a.error, r.depth - B - 2 >= 0 && r.depth - B - 2 < a.path_levels, 8,
+                             (uint32_t)(r.depth - B - 2))
+                       ? w.path[(r.depth - B - 2) * w.stride]
+                       : SVO_MISS;
           hit_index = P.node;
           hit_depth = (uint8_t)r.depth;
           const float x = __fsub_rn(ulong_to_unit(P.loc[0]), r.ox);

@@ -255,6 +255,10 @@ svo_status report_kernel_error(Context &c, const char *fn) {
     return fail(SVO_ERR_TIMEOUT, std::string(fn) + ": thread " + std::to_string(e[2]) + " of block " +
                                      std::to_string(e[1]) + " exceeded its pass bound on ray " + std::to_string(e[3]) +
                                      " (depth " + std::to_string(e[4]) + ", steps " + std::to_string(e[5]) + ")");
+  if (e[0] == SVO_ERR_INTERNAL)
+    return fail(SVO_ERR_INTERNAL, std::string(fn) + ": index check " + std::to_string(e[3]) + " failed (index " +
+                                      std::to_string(e[4]) + ") in thread " + std::to_string(e[2]) + " of block " +
+                                      std::to_string(e[1]));
   return fail((svo_status)e[0], std::string(fn) + ": kernel reported error " + std::to_string(e[0]));
 }
 

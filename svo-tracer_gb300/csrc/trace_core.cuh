@@ -371,6 +371,31 @@ __device__ __forceinline__ uint32_t claim(cg::coalesced_group &g, uint32_t *coun
   return g.shfl(base, 0) + g.thread_rank();
 }
 
+// SVO_CHECKED (a debugging build, off by default): every index of the step code
+// into the path cache, the base chunks and the per-pixel outputs is checked
+// before the access. A failed check records SVO_ERR_INTERNAL with the check's
+// number and the index in the kernel error record (the next synchronising call
+// reports it) and the access is skipped: the ray ends as background. Nothing
+// traps. With the option off the checks compile to nothing.
+#ifndef SVO_CHECKED
+#define SVO_CHECKED 0
+#endif
+#if SVO_CHECKED
+__device__ __noinline__ inline void checked_fail(uint32_t *error, uint32_t check, uint32_t index) {
+  if (error && atomicCAS(error, 0u, (unsigned)SVO_ERR_INTERNAL) == 0u) {
+    error[1] = blockIdx.x;
+    error[2] = threadIdx.x;
+    error[3] = check;
+    error[4] = index;
+    error[5] = 0;
+  }
+}
+// True when `cond` holds; false after recording the failed check.
+#define SVO_CHECK(err, cond, check, index) ((cond) || (checked_fail((err), (check), (index)), false))
+#else
+#define SVO_CHECK(err, cond, check, index) true
+#endif
+
 // Per-thread traversal state besides the ray itself.
 struct Walk {
   uint32_t *path;  // path[level * stride]: node address of each level below B+2
@@ -405,9 +430,11 @@ __device__ __forceinline__ int probe(const TraceLaunch &a, const ViewParams &v, 
   uint32_t chunk;
   if (!block) {
     uint32_t idx = pow_sum(r.depth - 1) + (SVO_TRACE_CELL_CACHE ? r.cell : cell_index(r.depth, r.wx, r.wy, r.wz, r.flip));
+    if (!SVO_CHECK(a.error, idx < a.n_bases, 1, idx)) return kStepBackground;
     chunk = kSmemBases ? s_bases[idx] : __ldg(a.bases + idx);
     if (kStats) w.v_base++;
   } else {
+    if (!SVO_CHECK(a.error, lvl >= 0 && lvl < a.path_levels, 3, (uint32_t)lvl)) return kStepBackground;
     uint32_t addr = w.path[lvl * w.stride];
     if (addr != w.cur_addr) {
       uint4 nd = load_node(blocks, a.n_blocks, addr);
@@ -442,6 +469,8 @@ __device__ __forceinline__ int probe(const TraceLaunch &a, const ViewParams &v, 
       r.cell = r.cell * 8u + oct;
       if (a.max_steps > 0 && r.steps >= a.max_steps) return kStepOn;  // the next call ends the ray
       r.steps++;
+      if (!SVO_CHECK(a.error, pow_sum(r.depth - 1) + r.cell < a.n_bases, 2, pow_sum(r.depth - 1) + r.cell))
+        return kStepBackground;
       const uint32_t c2 = kSmemBases ? s_bases[pow_sum(r.depth - 1) + r.cell] : __ldg(a.bases + pow_sum(r.depth - 1) + r.cell);
       if (kStats) w.v_base++;
       oct = octant(r.depth, r.wx, r.wy, r.wz, r.flip);
@@ -628,6 +657,7 @@ __device__ __forceinline__ int advance(const TraceLaunch &a, const uint4 *blocks
     for (int d = B + 2; d < nd; d++) {
       uint4 n2 = load_node(blocks, a.n_blocks, n);
       n = n2.x + octant(d, r.wx, r.wy, r.wz, r.flip);
+      if (!SVO_CHECK(a.error, d - B - 1 < a.path_levels, 5, (uint32_t)(d - B - 1))) return kStepBackground;
       w.path[(d - B - 1) * w.stride] = n;
     }
   }

@@ -143,7 +143,8 @@ __global__ void __launch_bounds__(256, SVO_TRACE_MIN_CTAS) trace_kernel(const Tr
     uint32_t hit_index = SVO_MISS, cr, cg_, cb;
     uint8_t hit_depth = 0;
     float t = __int_as_float(0x7f800000);
-    if (finish == kStepHit) {
+    if (finish == kStepHit &&
+        SVO_CHECK(a.error, r.depth - B - 2 >= 0 && r.depth - B - 2 < a.path_levels, 6, (uint32_t)(r.depth - B - 2))) {
       uint32_t addr = w.path[(r.depth - B - 2) * w.stride];
       uint4 nd = load_node(blocks, a.n_blocks, addr);
       hit_index = addr;
@@ -168,6 +169,7 @@ __global__ void __launch_bounds__(256, SVO_TRACE_MIN_CTAS) trace_kernel(const Tr
     px.y = fminf(__fdiv_rn(__uint2float_rn(cg_ * 255u), fw), 1.0f);
     px.z = fminf(__fdiv_rn(__uint2float_rn(cb * 255u), fw), 1.0f);
     px.w = 1.0f;
+    if (!SVO_CHECK(a.error, r.id < v.width * v.height, 7, r.id)) return;
     if (v.hit_index) v.hit_index[r.id] = hit_index;
     if (v.hit_depth) v.hit_depth[r.id] = hit_depth;
     if (v.t) v.t[r.id] = t;

@@ -410,15 +410,6 @@ TreeView view_of(Context &c) {
   return t;
 }
 
-svo_status ensure_tree_buffers(Context &c) {
-  size_t g = c.n_groups;
-  size_t nb = (g + kScanBlock - 1) / kScanBlock + 1;
-  if (c.reach.reserve(g) || c.parent_min.reserve(g) || c.frontier_a.reserve(g) || c.frontier_b.reserve(g) ||
-      c.flags.reserve(g) || c.scan_tmp.reserve(nb + 12) || c.free_list.reserve(g) || c.pruned_list.reserve(g) ||
-      c.freed_list.reserve(g) || c.gc_params.reserve(2) || c.h_gc_params.reserve(2) || c.h_gc_out.reserve(4))
-    return fail(SVO_ERR_OUT_OF_MEMORY, "tree update: device allocation failed");
-  return SVO_OK;
-}
 
 // Breadth-first reachability from the dense-real groups, one launch per tree
 // level below B+2 without reading the frontier sizes back: each launch reads
@@ -805,6 +796,17 @@ __global__ void k_gen_write(const DevTerrain T, TreeView t, const GenJob *jobs, 
 }
 
 }  // namespace
+
+// The tree updates' scratch (reachability, flags, lists) for the context's budget.
+svo_status ensure_tree_buffers(Context &c) {
+  size_t g = c.n_groups;
+  size_t nb = (g + kScanBlock - 1) / kScanBlock + 1;
+  if (c.reach.reserve(g) || c.parent_min.reserve(g) || c.frontier_a.reserve(g) || c.frontier_b.reserve(g) ||
+      c.flags.reserve(g) || c.scan_tmp.reserve(nb + 12) || c.free_list.reserve(g) || c.pruned_list.reserve(g) ||
+      c.freed_list.reserve(g) || c.gc_params.reserve(2) || c.h_gc_params.reserve(2) || c.h_gc_out.reserve(4))
+    return fail(SVO_ERR_OUT_OF_MEMORY, "tree update: device allocation failed");
+  return SVO_OK;
+}
 }  // namespace svo
 
 using svo::Context;

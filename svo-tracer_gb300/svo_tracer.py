@@ -165,6 +165,8 @@ def load_library(path: str | None = None) -> C.CDLL:
         "svo_graft_generate": ([vp, vp, C.POINTER(UpdateInputC), C.POINTER(GraftReportC)], C.c_int32),
         "svo_oct_write": ([C.c_char_p, C.c_uint8, C.c_uint32, vp, sz, vp, sz], C.c_int32),
         "svo_oct_read": ([C.c_char_p, C.POINTER(C.c_void_p)], C.c_int32),
+        "svo_state_save": ([vp, C.c_char_p], C.c_int32),
+        "svo_state_load": ([vp, C.c_char_p], C.c_int32),
         "svo_diff_set_params": ([vp, vp, sz, C.c_int32], C.c_int32),
         "svo_diff_get_grads": ([vp, vp, sz, C.c_int32], C.c_int32),
         "svo_diff_forward": ([vp, C.POINTER(TraceInputC), C.c_int32, vp, C.c_int32], C.c_int32),
@@ -647,6 +649,14 @@ class Tracer:
     def write_usage(self, usage: np.ndarray) -> None:
         u = np.ascontiguousarray(usage, dtype=USAGE_DTYPE)
         _check("WriteBuffer:Usages", self._lib.svo_write_usage(self._ctx, _ptr(u), len(u)))
+
+    def save_state(self, path: str) -> None:
+        """Checkpoint of the streaming state (tree, usage, tree depth, free list)."""
+        _check("SaveState", self._lib.svo_state_save(self._ctx, os.fsencode(path)))
+
+    def load_state(self, path: str) -> None:
+        """Resume from a checkpoint: replaces the resident tree and its state."""
+        _check("LoadState", self._lib.svo_state_load(self._ctx, os.fsencode(path)))
 
     def read_blocks(self, first: int = 0, n: int | None = None) -> np.ndarray:
         if n is None:

@@ -132,3 +132,12 @@ def test_trace_config_layout():
     names = [n for n, _ in st.TraceConfigC._fields_]
     assert names[-3:] == ["pass_limit", "request_order", "gi_stage"]
     assert C.sizeof(st.TraceConfigC) == 4 * len(names)
+
+
+def test_state_io_rejects_null_arguments():
+    """svo_state_save / svo_state_load refuse a null context or path (no GPU work)."""
+    lib = st.load_library()
+    assert lib.svo_state_save(None, b"x.svostate") == 1
+    assert b"svo_state_save" in lib.svo_last_error_string()
+    assert lib.svo_state_load(None, b"x.svostate") == 1
+    assert b"svo_state_load" in lib.svo_last_error_string()

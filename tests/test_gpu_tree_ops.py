@@ -145,6 +145,70 @@ def test_stream_past_the_request_cap_matches_oracle(tracer):
         scene.close()
 
 
+def test_state_checkpoint_resumes_the_stream(tracer, tmp_path):
+    """Checkpoint / resume: a stream (pixel-order requests past the cap, grafts
+    generated on the device, GC with a staleness threshold that prunes) saved with
+    svo_state_save after frame k (its free list partly claimed by that frame's
+    grafts) and loaded into a fresh context with svo_state_load goes on exactly as
+    the uninterrupted stream: the same trace outputs, GC reports and graft reports
+    every frame, and the same blocks and usage at the end. Missing, malformed and
+    truncated state files are refused."""
+    cap, threshold, frames = 2048, 6, 16
+    scene = st.Scene(st.SCENE_TERRAIN, seed=5, base_depth=3, depth=10)
+    tree = scene.build_tree(8)
+    budget = (len(tree.Blocks) + 7) // 8 + (1 << 14)
+    cams = st.camera_path(seed=3, frames=frames, width=160, height=90, MaxChildRequestId=cap)
+    cfg = dict(block_size=256, ctas_per_sm=0, max_steps=1 << 16, collect_stats=0, request_order=st.REQUESTS_PIXEL)
+    saves = {3: str(tmp_path / "frame3.svostate"), 9: str(tmp_path / "frame9.svostate")}
+    resumed = []
+    try:
+        tracer.set_config(**cfg)
+        tracer.upload(tree, block_budget=budget * 8)
+        tracer.init_usage_tree(1)
+        log = []
+        for f, cam in enumerate(cams):
+            tick = f + 1
+            got = tracer.trace(cam)
+            rep = tracer.gc(tick, threshold)
+            grep = tracer.graft_generate(tick, scene)
+            log.append((got, rep, grep))
+            if f in saves:
+                assert grep["claimed"] > 0  # the saved free list is partly claimed
+                tracer.save_state(saves[f])
+        assert sum(r[1]["pruned"] for r in log) > 0, "the stream must prune"
+        want_b, want_u = gpu_state(tracer, budget)
+        for f0, path in saves.items():
+            tr = st.Tracer(0)
+            resumed.append(tr)
+            tr.set_config(**cfg)
+            tr.load_state(path)
+            for f in range(f0 + 1, frames):
+                tick = f + 1
+                got = tr.trace(cams[f])
+                for k in ("hit_index", "hit_depth", "t", "rgba"):
+                    assert np.array_equal(getattr(got, k), getattr(log[f][0], k)), "resume %d, frame %d: %s" % (f0, f, k)
+                assert tr.gc(tick, threshold) == log[f][1], "resume %d, frame %d: GC" % (f0, f)
+                assert tr.graft_generate(tick, scene) == log[f][2], "resume %d, frame %d: grafts" % (f0, f)
+            got_b, got_u = gpu_state(tr, budget)
+            assert got_b.tobytes() == want_b.tobytes(), "resume %d: blocks" % f0
+            assert got_u.tobytes() == want_u.tobytes(), "resume %d: usage" % f0
+        with pytest.raises(st.SvoError):
+            resumed[0].load_state(str(tmp_path / "missing.svostate"))
+        bad = tmp_path / "bad.svostate"
+        bad.write_bytes(b"SVOSTAT1" + bytes(56))
+        with pytest.raises(st.SvoError):
+            resumed[0].load_state(str(bad))
+        data = open(saves[3], "rb").read()
+        (tmp_path / "short.svostate").write_bytes(data[: len(data) // 2])
+        with pytest.raises(st.SvoError):
+            resumed[0].load_state(str(tmp_path / "short.svostate"))
+    finally:
+        for tr in resumed:
+            tr.close()
+        tracer.set_config(request_order=st.REQUESTS_ARRIVAL)
+        scene.close()
+
+
 def test_prune_matches_oracle(tracer):
     scene = st.Scene(st.SCENE_TERRAIN, seed=8, base_depth=3, depth=9)
     tree = scene.build_tree(8)
