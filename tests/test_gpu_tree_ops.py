@@ -249,6 +249,80 @@ def test_prune_matches_oracle(tracer):
     assert rep["requests"] == len(o_req)
 
 
+def test_malformed_records_and_no_free_groups(tracer):
+    """Records a host could get wrong are skipped, never applied in part and never
+    read or written out of range, as the specification says: graft records with no
+    groups, a misaligned or overflowing payload range, a target past the budget or
+    a Location index past the locations; payload child links outside their record
+    (nulled); prune records addressing past the blocks, the base chunks or the
+    locations. The tree and the reports equal the oracle's. A budget with no free
+    group lets a GC free nothing new and every graft be skipped."""
+    scene = st.Scene(st.SCENE_TERRAIN, seed=5, base_depth=3, depth=9)
+    tree = scene.build_tree(7)
+    budget = (len(tree.Blocks) + 7) // 8 + 64
+    tracer.upload(tree, block_budget=budget * 8)
+    tracer.init_usage_tree(1)
+    oracle = po.TreeState(tree, budget)
+    oracle.init_usage_tree(1)
+    cam = st.look_at((0.1, 0.15, 0.55), (0.7, 0.7, 0.9), 64, 36, 60.0, Tick=1)
+    tracer.trace(cam)
+    req, n = tracer.read_child_requests()
+    assert n > 4
+    rec, pay = scene.graft_payload(req)
+    rec = rec[:6].copy()
+    pay = pay.copy()
+    rep = tracer.gc(2, 100)
+    o_pruned, o_freed, o_free = oracle.gc(2, 100)
+    assert (rep["pruned"], rep["freed"], rep["free"]) == (len(o_pruned), len(o_freed), len(o_free))
+    n_pay = len(pay)
+    rec[0]["graft_total_size"] = 0                           # no groups
+    rec[1]["graft_data_address"] += 3                         # misaligned payload range
+    rec[2]["graft_data_address"] = (n_pay // 8) * 8           # the range runs past the payload
+    rec[2]["graft_total_size"] = 2
+    rec[3]["graft_address"] = budget * 8 + 5                  # target past the budget
+    rec[4]["depth"] = 6                                       # Location walk ...
+    rec[4]["graft_address"] = 1000                            # ... with an index past the locations
+    first5 = int(rec[5]["graft_data_address"])
+    pay[first5]["child"] = 0x7FFFFFF0                         # a payload child link outside its record
+    locs = np.zeros(6, np.uint64)
+    grep = tracer.graft(2, rec, pay, locs)
+    o_claims, applied = oracle.graft(2, rec, pay, locs)
+    assert grep["applied"] == int(applied.sum()) and grep["skipped"] >= 5
+    assert np.array_equal(tracer.graft_claims(grep["claimed"]), o_claims)
+    assert_state(tracer, oracle, "malformed grafts")
+    prec = np.zeros(4, st.PRUNING_DTYPE)
+    prec["child_address"] = NONE
+    prec[0]["properties"], prec[0]["depth"], prec[0]["address"] = 0b1000, 255, budget * 8 + 1    # node past the blocks
+    prec[1]["properties"], prec[1]["depth"], prec[1]["address"] = 0b10000, 255, st.pow_sum(3) + 9  # base chunk past the bases
+    prec[2]["properties"], prec[2]["depth"], prec[2]["address"] = 0b0110, 6, 50                   # Location index past the locations
+    prec[3]["properties"], prec[3]["depth"], prec[3]["address"] = 1, 255, budget * 8 + 64          # cull past the blocks
+    surface = np.zeros(1, st.BLOCK_DTYPE)
+    surface["child"] = NONE
+    rep = tracer.prune(3, prec, surface, locs)
+    o_freed, o_req = oracle.prune(3, prec, surface, locs)
+    assert rep["freed"] == len(o_freed) == 0 and rep["requests"] == len(o_req)
+    assert_state(tracer, oracle, "malformed prunes")
+    assert np.array_equal(tracer.read_bases(), oracle.bases)
+    # no free group at all: a budget that is the tree itself
+    full = (len(tree.Blocks) + 7) // 8
+    with st.Tracer(0) as tight:
+        tight.upload(tree, block_budget=full * 8)
+        tight.init_usage_tree(1)
+        o2 = po.TreeState(tree, full)
+        o2.init_usage_tree(1)
+        tight.trace(cam)
+        req2, _ = tight.read_child_requests()
+        rec2, pay2 = scene.graft_payload(req2)
+        rep2 = tight.gc(2, 100)
+        o_pruned, o_freed2, o_free = o2.gc(2, 100)
+        assert rep2["pruned"] == len(o_pruned) and rep2["freed"] == len(o_freed2) and rep2["free"] == len(o_free)
+        g2 = tight.graft(2, rec2, pay2)
+        o_claims2, applied2 = o2.graft(2, rec2, pay2)
+        assert g2["applied"] == int(applied2.sum()) and g2["claimed"] == len(o_claims2)
+        assert g2["skipped"] + g2["applied"] == len(rec2)
+        assert_state(tight, o2, "no free groups")
+
+
 def test_graft_location_targets_and_budget(tracer):
     scene = st.Scene(st.SCENE_TERRAIN, seed=5, base_depth=3, depth=9)
     tree = scene.build_tree(7)
