@@ -243,13 +243,16 @@ svo_status prepare_launch(Context &c, int32_t n_views, uint32_t total_rays, Trac
 constexpr int kMaxViews = 512;
 
 svo_status report_kernel_error(Context &c, const char *fn) {
-  uint32_t e[kErrorWords] = {0};
-  SVO_CUDA(cudaMemcpyAsync(e, c.counters.p + kErrorOffset, sizeof(e), cudaMemcpyDeviceToHost, c.stream),
+  // through pinned memory: one asynchronous copy behind the stream's work, one wait
+  uint32_t *e = c.h_counters.p;
+  SVO_CUDA(cudaMemcpyAsync(e, c.counters.p + kErrorOffset, kErrorWords * sizeof(uint32_t), cudaMemcpyDeviceToHost,
+                           c.stream),
            std::string(fn) + ": error record");
   SVO_CUDA(cudaStreamSynchronize(c.stream), std::string(fn) + ": synchronize");
   if (!e[0]) return SVO_OK;
   // reported once: the next launches start with a clear record
-  SVO_CUDA(cudaMemsetAsync(c.counters.p + kErrorOffset, 0, sizeof(e), c.stream), std::string(fn) + ": error record");
+  SVO_CUDA(cudaMemsetAsync(c.counters.p + kErrorOffset, 0, kErrorWords * sizeof(uint32_t), c.stream),
+           std::string(fn) + ": error record");
   SVO_CUDA(cudaStreamSynchronize(c.stream), std::string(fn) + ": synchronize");
   if (e[0] == SVO_ERR_TIMEOUT)
     return fail(SVO_ERR_TIMEOUT, std::string(fn) + ": thread " + std::to_string(e[2]) + " of block " +
@@ -569,7 +572,7 @@ SVO_API svo_status svo_create(int32_t device, void **ctx) {
   SVO_CUDA(c->counters.reserve(svo::kCounterWords), "svo_create: counters");
   SVO_CUDA(cudaMemset(c->counters.p, 0, svo::kCounterWords * sizeof(uint32_t)), "svo_create: counters");
   SVO_CUDA(c->stats.reserve(8), "svo_create: stats");
-  SVO_CUDA(c->h_counters.reserve(4), "svo_create: pinned counters");
+  SVO_CUDA(c->h_counters.reserve(svo::kErrorWords), "svo_create: pinned counters");
   *ctx = c.release();
   return SVO_OK;
   GUARD_END("svo_create")
