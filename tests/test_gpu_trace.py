@@ -24,6 +24,9 @@ def default_config(tracer):
 T_RTOL = 1e-5  # the required tolerance for t and RGBA (relative); the checks below are tighter (exact)
 
 
+NONE_BLOCK = 0xFFFFFFFF
+
+
 def assert_same(got, want, label=""):
     for k in ("hit_index", "hit_depth", "t", "rgba"):
         a = getattr(got, k)
@@ -138,6 +141,61 @@ def test_small_step_limits_inside_base_level_runs(tracer, schedule):
         assert np.array_equal(usage["tick"], u_ref["tick"]), limit
         assert np.array_equal(vs, want["v_base"]), limit
         assert np.array_equal(vb, want["v_block"]), limit
+
+
+def deep_needle_tree(p, depth=24):
+    """A tree at the deepest level the library takes (SVO_MAX_TREE_DEPTH = 24) and the
+    smallest base depth (1): air everywhere except a one-cell needle of geometry
+    around the point p, one node per level from the base down to level 24."""
+    P = [int(np.float64(v) * 2.0 ** 64) for v in p]
+
+    def oc(d):  # p's octant below level d
+        s = 63 - d
+        return ((P[0] >> s) & 1) | (((P[1] >> s) & 1) << 1) | (((P[2] >> s) & 1) << 2)
+
+    B = 1
+    bases = np.full(st.pow_sum(B), 0x5555, np.uint16)
+    bases[oc(0)] = 0x5555 | (2 << (2 * oc(1)))
+    chain = depth - (B + 2)
+    blocks = np.zeros(512 + 8 * chain, st.BLOCK_DTYPE)
+    blocks["child"] = NONE_BLOCK
+    blocks["chunk"] = 0x5555
+    blocks["colour_r"], blocks["colour_g"], blocks["colour_b"] = 180, 90, 40
+    dense = oc(0) * 64 + oc(1) * 8 + oc(2)
+    blocks[dense]["chunk"] = 0x5555 | (2 << (2 * oc(3)))
+    blocks[dense]["child"] = 512
+    for k in range(chain):
+        level = B + 3 + k
+        node = 512 + 8 * k + oc(level - 1)
+        blocks[node]["chunk"] = 0x5555 | (2 << (2 * oc(level)))
+        if k + 1 < chain:
+            blocks[node]["child"] = 512 + 8 * (k + 1)
+    return st.Octree(B, len(blocks), bases, blocks)
+
+
+@pytest.mark.parametrize("schedule", [st.SCHEDULE_LANE, st.SCHEDULE_WARP, st.SCHEDULE_WAVEFRONT],
+                         ids=["lane", "warp", "wavefront"])
+def test_deepest_tree(tracer, schedule):
+    """Maximum sizes: a needle of geometry down to level 24 in a tree of base depth
+    1, seen with cones narrow enough to reach it. The LOD stops rays at levels 20 and
+    22 for wider views and lets the narrowest reach the level-24 leaf, which has no
+    children and raises requests; every output, stamp and request equals the
+    oracle's."""
+    tracer.set_config(schedule=schedule)
+    p = (0.3127, 0.4271, 0.5833)
+    tree = deep_needle_tree(p)
+    o = (p[0] + 0.2, p[1] + 0.15, p[2] - 0.1)
+    deepest = 0
+    for fov in (1e-4, 2e-5, 4e-6, 1e-6):
+        cam = st.look_at(o, p, 32, 32, np.degrees(fov), Tick=2, MaxChildRequestId=4096)
+        got, usage, req, n, stats, (vb, vs), want, u_ref = run_both(tracer, tree, cam)
+        assert_same(got, want, "FoV %g: " % fov)
+        assert np.array_equal(usage["tick"], u_ref["tick"])
+        ok, msg = same_requests(req[:n], want["requests"])
+        assert ok, msg
+        assert np.array_equal(vb, want["v_block"]) and np.array_equal(vs, want["v_base"])
+        deepest = max(deepest, int(got.hit_depth.max()))
+    assert deepest == 24
 
 
 def test_request_cap(tracer):
