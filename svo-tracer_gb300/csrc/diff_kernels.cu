@@ -133,7 +133,9 @@ __device__ __forceinline__ float3 sky_rgb(const Ray &r) {
 // record and returns false.
 // kStats: the walk's reference-walk counters (V_block, V_base, hits) are
 // added to st, as the trace kernel's statistics count them.
-template <bool kStats, class Visit>
+// kSmemBases: the base chunks are read from shared memory (staged by the
+// kernel) rather than from global memory.
+template <bool kStats, bool kSmemBases, class Visit>
 __device__ __forceinline__ bool walk_hits(const DiffLaunch &d, const ViewParams *s_views, const uint16_t *s_bases,
                                           uint32_t ray, Walk &w, Stats &st, Visit &&visit) {
   const TraceLaunch &a = d.t;
@@ -168,7 +170,7 @@ __device__ __forceinline__ bool walk_hits(const DiffLaunch &d, const ViewParams 
       }
       return counted(false);
     }
-    int f = step<kStats, true>(a, v, s_bases, blocks, B, r, w, st);
+    int f = step<kStats, kSmemBases>(a, v, s_bases, blocks, B, r, w, st);
     if (f == kStepOn) continue;
     if (f == kStepBackground) {
       visit(0u, true, r);
@@ -186,19 +188,20 @@ __device__ __forceinline__ bool walk_hits(const DiffLaunch &d, const ViewParams 
   }
 }
 
-template <bool kBackward, bool kStats>
+template <bool kBackward, bool kStats, bool kSmemBases>
 __global__ void __launch_bounds__(256, kBackward ? SVO_DIFF_BWD_MIN_CTAS : SVO_DIFF_FWD_MIN_CTAS) diff_kernel(const DiffLaunch d) {
   extern __shared__ __align__(16) uint8_t smem[];
   const TraceLaunch &a = d.t;
   ViewParams *s_views = reinterpret_cast<ViewParams *>(smem);
   uint16_t *s_bases = reinterpret_cast<uint16_t *>(smem + a.n_views * sizeof(ViewParams));
-  size_t bases_bytes = (a.n_bases * 2 + 15) & ~15u;
+  size_t bases_bytes = kSmemBases ? ((a.n_bases * 2 + 15) & ~15u) : 0;
   uint32_t *s_path = reinterpret_cast<uint32_t *>(smem + a.n_views * sizeof(ViewParams) + bases_bytes);
   {
     const uint32_t *src = reinterpret_cast<const uint32_t *>(a.views);
     uint32_t *dst = reinterpret_cast<uint32_t *>(s_views);
     for (uint32_t i = threadIdx.x; i < a.n_views * sizeof(ViewParams) / 4; i += blockDim.x) dst[i] = src[i];
-    for (uint32_t i = threadIdx.x; i < a.n_bases; i += blockDim.x) s_bases[i] = __ldg(a.bases + i);
+    if (kSmemBases)
+      for (uint32_t i = threadIdx.x; i < a.n_bases; i += blockDim.x) s_bases[i] = __ldg(a.bases + i);
     fill_spread_table();
   }
   __syncthreads();
@@ -229,7 +232,7 @@ __global__ void __launch_bounds__(256, kBackward ? SVO_DIFF_BWD_MIN_CTAS : SVO_D
     full.init();
     bool stopped = false;  // a walk ran past its pass bound: the warp leaves the loop
     if (live && (!kBackward || !d.use_saved)) {
-      stopped = !walk_hits<kStats>(d, s_views, s_bases, ray, w, st, [&](uint32_t node, bool bg, const Ray &r) {
+      stopped = !walk_hits<kStats, kSmemBases>(d, s_views, s_bases, ray, w, st, [&](uint32_t node, bool bg, const Ray &r) {
         if (bg)
           full.sky(sky_rgb(r));
         else
@@ -263,7 +266,7 @@ __global__ void __launch_bounds__(256, kBackward ? SVO_DIFF_BWD_MIN_CTAS : SVO_D
       // the gradient walk: replay the prefix sums, one contribution at a time
       Composite pre;
       pre.init();
-      stopped = !walk_hits<false>(d, s_views, s_bases, ray, w, st, [&](uint32_t node, bool bg, const Ray &) {
+      stopped = !walk_hits<false, kSmemBases>(d, s_views, s_bases, ray, w, st, [&](uint32_t node, bool bg, const Ray &) {
         if (bg) return;
         float4 p = __ldg(d.params + node);
         float T = pre.T, ta = __fmul_rn(T, p.w);
@@ -332,7 +335,6 @@ svo_status run_diff(Context &c, const svo_trace_input *views, int32_t n, const f
   if (!c.has_tree) return fail(SVO_ERR_NO_TREE, "svo_diff: no octree uploaded");
   if (!c.has_params) return fail(SVO_ERR_INVALID_ARGUMENT, "svo_diff: no parameters set");
   if (n <= 0 || n > 512 || !views) return fail(SVO_ERR_INVALID_ARGUMENT, "svo_diff: bad view list");
-  if (c.n_bases * 2 > 96 * 1024) return fail(SVO_ERR_INVALID_ARGUMENT, "svo_diff: base chunks exceed shared memory");
   std::vector<svo_trace_output> outs(n);
   std::memset(outs.data(), 0, sizeof(svo_trace_output) * n);
   for (auto &o : outs) o.on_device = 1;
@@ -365,15 +367,18 @@ svo_status run_diff(Context &c, const svo_trace_input *views, int32_t n, const f
   d.inv_pixels = 1.0 / (double)pixels;
   d.max_hits = c.cfg.max_hits;
   d.t.block_size = 256;
-  size_t smem = (size_t)n * sizeof(ViewParams) + ((c.n_bases * 2 + 15) & ~(size_t)15) +
+  // base chunks of up to 96 KB (base depth 5 and less) are staged in shared
+  // memory, larger ones read from global memory, as the trace kernels do
+  const bool smem_bases = c.n_bases * 2 <= 96 * 1024;
+  size_t smem = (size_t)n * sizeof(ViewParams) + (smem_bases ? ((c.n_bases * 2 + 15) & ~(size_t)15) : 0) +
                 (size_t)d.t.path_levels * 256 * 4;
   // collect_stats: the forward counts its walk (V_block, V_base, hits) into the
   // context's trace statistics (svo_last_trace_stats)
   const bool stats = !kBackward && c.cfg.collect_stats > 0;
   d.t.stats = stats ? c.stats.p : nullptr;
-  auto kernel = diff_kernel<kBackward, false>;
+  auto kernel = smem_bases ? diff_kernel<kBackward, false, true> : diff_kernel<kBackward, false, false>;
   if constexpr (!kBackward)
-    if (stats) kernel = diff_kernel<false, true>;
+    if (stats) kernel = smem_bases ? diff_kernel<false, true, true> : diff_kernel<false, true, false>;
   SVO_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem), "svo_diff: smem");
   int occ = 0;
   SVO_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kernel, 256, smem), "svo_diff: occupancy");

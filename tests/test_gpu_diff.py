@@ -80,6 +80,32 @@ def test_backward_matches_fp64_gradient(tracer, fitting):
     assert not grad[np.abs(want).sum(1) == 0].any()
 
 
+def test_base_chunks_in_global_memory(tracer):
+    """Base depth 6: the 299,592 base chunks (585 KB) do not fit shared memory and
+    the colour-fitting kernels read them from global memory; forward colour,
+    loss and gradient hold the FP64 bounds of the shared-memory case."""
+    tree = st.TreeBuilder(st.SCENE_SPHERE, seed=1).BuildTree(6, 9)
+    views = st.orbit_views(seed=7, n=2, width=96, height=64, distance=0.75)
+    hl = po.HitLists(tree, views, max_hits=16)
+    params = np.random.default_rng(3).uniform(0.0, 1.0, (len(tree.Blocks), 4)).astype(np.float32)
+    _, target64, _ = hl.eval(st.sinusoid_field(tree).astype(np.float64), want_rgb=True)
+    target = target64.astype(np.float32)
+    tracer.upload(tree)
+    tracer.diff_set_params(params)
+    rgb = tracer.diff_forward(views)
+    want_loss, want_rgb, want = hl.eval(params.astype(np.float64), target.astype(np.float64), want_rgb=True,
+                                        want_grad=True)
+    err = np.abs(rgb - want_rgb)
+    assert err.max() <= 1e-5, "max |C - C64| = %g" % err.max()
+    assert (hl.n_hits > 1).sum() > 1000
+    loss = tracer.diff_backward(views, target)
+    assert abs(loss - want_loss) <= 1e-9 * want_loss, (loss, want_loss)
+    grad = tracer.diff_grads(len(tree.Blocks))
+    scale = np.abs(want).max()
+    ok = np.abs(grad - want) <= 1e-4 * np.abs(want) + 1e-6 * scale
+    assert ok.all(), "%d of %d gradient entries off the FP64 gradient" % ((~ok).sum(), ok.size)
+
+
 def test_backward_matches_fp64_finite_differences(tracer, fitting):
     """The acceptance check of the adjoint: within 1e-3 relative of FP64 central
     differences (h = 1e-4) on 256 random nodes that rays hit. Entries below

@@ -31,6 +31,12 @@ def terrain():
 
 
 @pytest.fixture(scope="module")
+def terrain_global_bases():
+    """Base depth 6: the base chunks (585 KB) are read from global memory, not staged in shared memory."""
+    return st.TreeBuilder(st.SCENE_TERRAIN, seed=5).BuildTree(6, 10)
+
+
+@pytest.fixture(scope="module")
 def tracer():
     t = st.Tracer(0)
     yield t
@@ -95,6 +101,15 @@ def test_cone_schedules(tracer, terrain, schedule):
     v = st.orbit_views(seed=11, n=1, width=56, height=40, distance=1.25)[0]
     sched = {"lane": st.SCHEDULE_LANE, "warp": st.SCHEDULE_WARP}[schedule]
     check(tracer, terrain, v, schedule=sched, cadence=5)
+
+
+@pytest.mark.parametrize("schedule", ["lane", "warp"])
+def test_base_chunks_in_global_memory(tracer, terrain_global_bases, schedule):
+    sched = {"lane": st.SCHEDULE_LANE, "warp": st.SCHEDULE_WARP}[schedule]
+    for v in (st.look_at((0.1, 0.15, 0.55), (0.7, 0.7, 0.9), 96, 54, 60.0, Tick=3),
+              st.orbit_views(seed=11, n=1, width=56, height=40, distance=1.25)[0]):
+        got, stats, ref = check(tracer, terrain_global_bases, v, schedule=sched, cadence=5)
+        assert ref["n_requests"] > 0 and stats["surfaces"] > 0
 
 
 def test_inside_cube_with_dof(tracer, sphere):

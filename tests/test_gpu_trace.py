@@ -83,6 +83,11 @@ SCENES = [
     ("sphere_dof", st.SCENE_SPHERE, 3, 3, 8, (0.1, 1.3, 0.3), (0.5, 0.5, 0.5), 96, 64, 60.0, (0.01, 0.7)),
     ("terrain_b4_d9", st.SCENE_TERRAIN, 5, 4, 9, (0.1, 0.15, 0.55), (0.7, 0.7, 0.9), 320, 180, 60.0, (0.0, 0.0)),
     ("terrain_b2_d8_odd", st.SCENE_TERRAIN, 7, 2, 8, (0.93, 0.81, 0.4), (0.2, 0.3, 0.95), 77, 53, 90.0, (0.0, 0.0)),
+    # base depth 6: 299,592 base chunks (585 KB) do not fit shared memory, the kernels read them from global memory
+    ("terrain_b6_d10_global_bases", st.SCENE_TERRAIN, 5, 6, 10, (0.1, 0.15, 0.55), (0.7, 0.7, 0.9), 320, 180, 60.0,
+     (0.0, 0.0)),
+    ("sphere_inside_b6_d9_global_bases", st.SCENE_SPHERE, 2, 6, 9, (0.9, 0.1, 0.15), (0.4, 0.6, 0.5), 256, 192, 60.0,
+     (0.0, 0.0)),
 ]
 
 
@@ -196,6 +201,33 @@ def test_deepest_tree(tracer, schedule):
         assert np.array_equal(vb, want["v_block"]) and np.array_equal(vs, want["v_base"])
         deepest = max(deepest, int(got.hit_depth.max()))
     assert deepest == 24
+
+
+@pytest.mark.parametrize("kind", ["all_air", "solid_without_blocks"])
+def test_degenerate_trees(tracer, kind):
+    """Empty and degenerate inputs: a tree of air only (every ray reaches the sky
+    and stamps nothing), and one that is geometry everywhere with no block level
+    below the dense one (every ray that enters stops at level B+2 and asks for
+    children). Equal to the oracle, from outside and from inside the cube."""
+    B = 2
+    bases = np.full(st.pow_sum(B), 0x5555 if kind == "all_air" else 0xAAAA, np.uint16)
+    blocks = np.zeros(8 ** (B + 2), st.BLOCK_DTYPE)
+    blocks["child"] = NONE_BLOCK
+    blocks["chunk"] = 0x5555 if kind == "all_air" else 0xAAAA
+    blocks["colour_g"] = 120
+    tree = st.Octree(B, len(blocks), bases, blocks)
+    for cam in (st.look_at((1.6, 1.3, -0.4), (0.5, 0.5, 0.5), 40, 24, 60.0, Tick=3, MaxChildRequestId=1 << 12),
+                st.look_at((0.4, 0.5, 0.6), (0.9, 0.1, 0.3), 24, 40, 80.0, Tick=3, MaxChildRequestId=1 << 12)):
+        got, usage, req, n, stats, (vb, vs), want, u_ref = run_both(tracer, tree, cam)
+        assert_same(got, want, kind + ": ")
+        assert np.array_equal(usage["tick"], u_ref["tick"])
+        ok, msg = same_requests(req[:n], want["requests"])
+        assert ok, msg
+        if kind == "all_air":
+            assert (got.hit_index == st.MISS).all() and n == 0
+        else:
+            hit = got.hit_index != st.MISS
+            assert hit.any() and (got.hit_depth[hit] == B + 2).all() and n == int(hit.sum())
 
 
 def test_request_cap(tracer):
