@@ -41,11 +41,14 @@ def test_init_usage_tree_matches_oracle(tracer):
     assert_state(tracer, oracle, "init")
 
 
-@pytest.mark.parametrize("base_depth,depth,initial,budget,threshold", [(3, 9, 7, 1 << 15, 3), (2, 8, 6, 1 << 13, 2)])
+@pytest.mark.parametrize("base_depth,depth,initial,budget,threshold",
+                         [(3, 9, 7, 1 << 15, 3), (2, 8, 6, 1 << 13, 2), (6, 10, 9, (1 << 21) + (1 << 16), 2)],
+                         ids=["b3", "b2", "b6_global_bases"])
 def test_stream_matches_oracle(tracer, base_depth, depth, initial, budget, threshold):
     """Frames of the streaming workflow: trace (usage stamps + child requests), graft
     payloads from the procedural scene, GC of groups unused for `threshold` frames,
-    grafting into freed groups; GPU and oracle evolve their own copies of the tree."""
+    grafting into freed groups; GPU and oracle evolve their own copies of the tree.
+    Base depth 6: 2.1M dense groups at level 8, base chunks in global memory."""
     scene = st.Scene(st.SCENE_TERRAIN, seed=5, base_depth=base_depth, depth=depth)
     tree = scene.build_tree(initial)
     tracer.upload(tree, block_budget=budget * 8)
