@@ -28,14 +28,22 @@ __device__ __forceinline__ uint32_t pow_sum(int depth) {
 
 // The fixed-point conversions exist in two exact forms: the 64-bit conversion
 // instructions, which run on this GPU's FP64 pipe at 1/64 of the FP32 rate, and
-// integer forms (more instructions, no FP64 pipe). Which is faster depends on
-// the kernel's instruction mix, measured on GB300 with identical outputs:
-//  * ulong_to_float (SVO_CVT_INTEGER): the integer form everywhere. Primary
-//    trace 1.519 -> 1.458 ms per 1080p frame, 64 views 8.50 -> 8.42 ms (at an
-//    earlier step code the instruction was faster: 1.574 vs 1.754 ms), the
-//    colour-fitting backward 1.15 -> 1.04 ms, the megakernel's cones 19.03 ->
-//    18.91 ms per frame.
-//  * unit_to_ulong (SVO_CVT_INTEGER_F2U): the instruction unless set.
+// integer forms (more instructions, no FP64 pipe). The step code is bound by
+// instruction issue, and by the FP64 pipe once it carries most conversions, so
+// the fastest mix splits them between the two; measured on GB300 with
+// identical outputs (1080p frame / 64 views / megakernel frame):
+//  * ulong_to_float (SVO_CVT_INTEGER): the integer form, except where
+//    SVO_CVT_HW_TRAVERSE and SVO_CVT_HW_CONE give the number of traverseChunk's
+//    three boundary distances and coneSize's three coordinates converted by the
+//    instruction. Counts (traverse, cone) 0,0: 1.451 / 8.12 / 14.60 ms;
+//    2,2: 1.371 / 7.61 / 13.85 ms; 2,1: 1.384 / 7.72 / 13.95; 2,3: 1.386 / 7.65
+//    / 13.92; 1,2: 1.398 / 7.80 / 14.04; 3,0: 1.409 / 7.77 / 14.08; 3,3 (the
+//    instruction everywhere): 1.445 / 7.91 / 14.29. An integer form without
+//    the 32-bit conversion (normalise, round by guard and sticky bits) at 2,2:
+//    1.470 / 8.16 / 14.55 ms.
+//  * unit_to_ulong (SVO_CVT_INTEGER_F2U): the instruction unless set. The
+//    integer form for one of traverseChunk's two moves at 2,2: 1.415 / 7.90 /
+//    14.26 ms; for both: 1.467 / 8.17 / 14.71 ms.
 #ifndef SVO_CVT_INTEGER
 #define SVO_CVT_INTEGER 1
 #endif
@@ -59,6 +67,15 @@ __device__ __forceinline__ float ulong_to_float(uint64_t x) {
 }
 // ulongToFloat (wavefront.cl:209): (float)x * 2^-64, the scaling exact.
 __device__ __forceinline__ float ulong_to_unit(uint64_t x) { return __fmul_rn(ulong_to_float(x), 0x1p-64f); }
+// The same conversion by the 64-bit instruction (kHw) or the integer form.
+template <bool kHw>
+__device__ __forceinline__ float ulong_to_float_by(uint64_t x) { return kHw ? __ull2float_rn(x) : ulong_to_float(x); }
+#ifndef SVO_CVT_HW_CONE
+#define SVO_CVT_HW_CONE 2
+#endif
+#ifndef SVO_CVT_HW_TRAVERSE
+#define SVO_CVT_HW_TRAVERSE 2
+#endif
 
 // floatToUlong (wavefront.cl:200-207); out-of-range products saturate, NaN -> 0.
 // Integer form: |x| * 2^64 is exact (a power-of-two scale of a float below the
@@ -255,7 +272,9 @@ __device__ __forceinline__ bool traverse(Ray &r, int depth) {
     }
   }
   if (ax < 0) {
-    const float f0 = ulong_to_float(d0), f1 = ulong_to_float(d1), f2 = ulong_to_float(d2);
+    const float f0 = ulong_to_float_by<(SVO_CVT_HW_TRAVERSE >= 1)>(d0);
+    const float f1 = ulong_to_float_by<(SVO_CVT_HW_TRAVERSE >= 2)>(d1);
+    const float f2 = ulong_to_float_by<(SVO_CVT_HW_TRAVERSE >= 3)>(d2);
     float a0 = fabsf(__fmul_rn(f0, r.ix));
     float a1 = fabsf(__fmul_rn(f1, r.iy));
     float a2 = fabsf(__fmul_rn(f2, r.iz));
@@ -292,9 +311,9 @@ __device__ __forceinline__ int pop_depth(const Ray &r, int depth, uint64_t px, u
 
 // coneSize (wavefront.cl:387-391) at the distance setConeDepth uses (:394-399).
 __device__ __forceinline__ float cone_at(const Ray &r, float dof0, float dof1) {
-  float x = __fsub_rn(r.ox, ulong_to_unit(loc_x(r)));
-  float y = __fsub_rn(r.oy, ulong_to_unit(loc_y(r)));
-  float z = __fsub_rn(r.oz, ulong_to_unit(loc_z(r)));
+  float x = __fsub_rn(r.ox, __fmul_rn(ulong_to_float_by<(SVO_CVT_HW_CONE >= 1)>(loc_x(r)), 0x1p-64f));
+  float y = __fsub_rn(r.oy, __fmul_rn(ulong_to_float_by<(SVO_CVT_HW_CONE >= 2)>(loc_y(r)), 0x1p-64f));
+  float z = __fsub_rn(r.oz, __fmul_rn(ulong_to_float_by<(SVO_CVT_HW_CONE >= 3)>(loc_z(r)), 0x1p-64f));
   float m = fabsf(__fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(x, x), __fmul_rn(y, y)), __fmul_rn(z, z))));
   float eye = __fmul_rn(r.fov, m);
   float f = fabsf(__fmul_rn(dof0, __fsub_rn(dof1, m)));
