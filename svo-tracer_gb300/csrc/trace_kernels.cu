@@ -50,7 +50,7 @@ namespace svo {
 namespace {
 
 #ifndef SVO_TRACE_MIN_CTAS
-#define SVO_TRACE_MIN_CTAS 4  // 53 registers, no spills (5: 48 registers, no spill, 1.56 vs 1.45 ms on the 1080p frame)
+#define SVO_TRACE_MIN_CTAS 4  // 55 registers, no spills (5: 48 registers, no spill, 1.56 vs 1.45 ms on the 1080p frame at 53)
 #endif
 // SVO_TRACE_WARP_REFILL = T > 0: warp batches whose idle lanes take the next
 // ray slots (tile order, one atomic per warp) once at most T lanes of the warp
