@@ -112,6 +112,24 @@ def test_base_chunks_in_global_memory(tracer, terrain_global_bases, schedule):
         assert ref["n_requests"] > 0 and stats["surfaces"] > 0
 
 
+@pytest.mark.parametrize("schedule", ["lane", "warp"])
+def test_axis_aligned_views(tracer, sphere, schedule):
+    """Direction components exactly zero and an origin on the cell boundaries of
+    every level; the CPU tests pin the oracle to kernel.cl on the same views."""
+    from test_mega_oracle import mega_axis_aligned_cases
+    sched = {"lane": st.SCHEDULE_LANE, "warp": st.SCHEDULE_WARP}[schedule]
+    for name, tree, v in mega_axis_aligned_cases(sphere):
+        check(tracer, tree, v, schedule=sched, cadence=5)
+
+
+def test_extreme_views(tracer, sphere):
+    """A field of view past 180 degrees and origins on a face and an edge of the
+    cube (with a depth of field); the CPU tests pin the oracle to kernel.cl."""
+    from test_mega_oracle import mega_extreme_cases
+    for name, tree, v in mega_extreme_cases(sphere):
+        check(tracer, tree, v)
+
+
 def test_inside_cube_with_dof(tracer, sphere):
     v = st.look_at((0.5, 0.5, 0.12), (0.5, 0.55, 0.6), 48, 40, 70.0, DoF=(0.02, 0.3), Tick=9)
     check(tracer, with_random_normals(sphere, 3), v)

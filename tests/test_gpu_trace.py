@@ -11,6 +11,7 @@ import pytest
 import pyoracle as po
 import svo_tracer as st
 from test_golden_cpu import GOLDEN, load_case
+from test_oracle_vs_reference import axis_aligned_cases, extreme_camera_cases
 
 pytestmark = pytest.mark.gpu
 
@@ -201,6 +202,39 @@ def test_deepest_tree(tracer, schedule):
         assert np.array_equal(vb, want["v_block"]) and np.array_equal(vs, want["v_base"])
         deepest = max(deepest, int(got.hit_depth.max()))
     assert deepest == 24
+
+
+@pytest.mark.parametrize("schedule", [st.SCHEDULE_LANE, st.SCHEDULE_WARP, st.SCHEDULE_WAVEFRONT],
+                         ids=["lane", "warp", "wavefront"])
+def test_axis_aligned_rays(tracer, schedule):
+    """Rays with direction components that are exactly zero (infinite inverse
+    direction), origins on the cell boundaries of every level and on the cube's
+    corner, and child requests raised along an axis: equal to the oracle, which
+    the CPU tests pin to the reference's kernels on the same cameras."""
+    tracer.set_config(schedule=schedule)
+    for name, tree, cam in axis_aligned_cases():
+        got, usage, req, n, stats, (vb, vs), want, u_ref = run_both(tracer, tree, cam)
+        assert_same(got, want, name + ": ")
+        assert np.array_equal(usage["tick"], u_ref["tick"]), name
+        assert n == want["n_requests"], name
+        ok, msg = same_requests(req, want["requests"])
+        assert ok, name + ": " + msg
+        assert np.array_equal(vb, want["v_block"]) and np.array_equal(vs, want["v_base"]), name
+
+
+@pytest.mark.parametrize("schedule", [st.SCHEDULE_LANE, st.SCHEDULE_WARP, st.SCHEDULE_WAVEFRONT],
+                         ids=["lane", "warp", "wavefront"])
+def test_extreme_cameras(tracer, schedule):
+    """Fields of view past 180 degrees and origins on a face and an edge of the
+    cube: equal to the oracle (pinned to the reference's kernels on the CPU)."""
+    tracer.set_config(schedule=schedule)
+    for name, tree, cam in extreme_camera_cases():
+        got, usage, req, n, stats, _, want, u_ref = run_both(tracer, tree, cam)
+        assert_same(got, want, name + ": ")
+        assert np.array_equal(usage["tick"], u_ref["tick"]), name
+        assert n == want["n_requests"], name
+        ok, msg = same_requests(req, want["requests"])
+        assert ok, name + ": " + msg
 
 
 @pytest.mark.parametrize("kind", ["all_air", "solid_without_blocks"])

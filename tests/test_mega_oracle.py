@@ -77,6 +77,40 @@ def test_inside_cube_with_dof(sphere):
     check(tree, v)
 
 
+def mega_axis_aligned_cases(sphere):
+    """Cameras whose Facing columns are exact unit axes (direction components
+    exactly zero in the centre row and column), the second with its origin on the
+    cell boundaries of every level and seeded normals (child requests, every
+    spawnRays branch)."""
+    kw = dict(Tick=3, MaxChildRequestId=1 << 20)
+    return [("down_z", sphere, st.look_at((0.5, 0.5, 1.6), (0.5, 0.5, 0.5), 64, 48, 60.0, **kw)),
+            ("origin_on_boundaries", with_random_normals(sphere, 4),
+             st.look_at((0.5, 0.25, 0.5), (0.5, 0.9, 0.5), 48, 32, 70.0, **kw))]
+
+
+def mega_extreme_cases(sphere):
+    """A field of view past 180 degrees, an origin on a face of the cube and one on
+    an edge with a depth of field, two of them with seeded normals."""
+    kw = dict(Tick=3, MaxChildRequestId=1 << 20)
+    return [("fov_200", with_random_normals(sphere, 5), st.look_at((0.5, 0.5, 0.1), (0.5, 0.5, 0.9), 48, 32, 200.0, **kw)),
+            ("on_face", sphere, st.look_at((1.0, 0.5, 0.5), (0.0, 0.5, 0.5), 48, 32, 60.0, **kw)),
+            ("on_edge_dof", with_random_normals(sphere, 6),
+             st.look_at((1.0, 1.0, 0.5), (0.3, 0.3, 0.5), 48, 32, 60.0, DoF=(0.05, 0.5), **kw))]
+
+
+def test_extreme_views(sphere):
+    for name, tree, v in mega_extreme_cases(sphere):
+        ref, got = check(tree, v)
+        assert got["n_requests"] > 0 and got["cones"].sum() > 1000, name
+
+
+def test_axis_aligned_views(sphere):
+    for name, tree, v in mega_axis_aligned_cases(sphere):
+        ref, got = check(tree, v)
+        assert got["cones"].sum() > 1000, name
+    assert got["n_requests"] > 0
+
+
 def test_cone_schedule_parameters(terrain):
     tree = with_random_normals(terrain, 4)
     v = st.look_at((0.2, 0.1, 0.05), (0.5, 0.5, 0.8), 40, 32, 75.0, FovMultiplier=0.1, FovConstant=0.08,

@@ -48,6 +48,60 @@ def test_terrain_matches_reference(b, d):
     assert (out["hit_index"] != st.MISS).mean() > 0.3
 
 
+def axis_aligned_cases():
+    """Cameras whose Facing columns are exact unit axes: the centre row and column
+    of an even-sized view have direction components that are exactly zero (an
+    infinite inverse direction), and two origins lie exactly on cell boundaries of
+    every level (0.5) or on the cube's corner. The short terrain (built three
+    levels above its scene) makes the rays raise child requests."""
+    sphere = st.TreeBuilder(st.SCENE_SPHERE, seed=1).BuildTree(4, 8)
+    scene = st.Scene(st.SCENE_TERRAIN, seed=5, base_depth=3, depth=10)
+    try:
+        short = scene.build_tree(7)
+    finally:
+        scene.close()
+    kw = dict(Tick=3, MaxChildRequestId=1 << 20)
+    return [
+        ("sphere_down_z", sphere, st.look_at((0.5, 0.5, 1.6), (0.5, 0.5, 0.5), 64, 48, 60.0, **kw)),
+        ("sphere_origin_on_boundaries", sphere, st.look_at((0.5, 0.25, 0.5), (0.5, 0.9, 0.5), 64, 48, 70.0, **kw)),
+        ("sphere_from_corner", sphere, st.look_at((0.0, 0.0, 0.0), (0.5, 0.5, 0.5), 40, 30, 60.0, **kw)),
+        ("terrain_down_z_requests", short, st.look_at((0.5, 0.5, 0.6), (0.5, 0.5, 0.95), 64, 48, 60.0, **kw)),
+        ("terrain_along_x_requests", short, st.look_at((0.0, 0.5, 0.75), (1.0, 0.5, 0.75), 64, 48, 60.0, **kw)),
+    ]
+
+
+def extreme_camera_cases():
+    """Horizontal fields of view past 180 degrees (rays pointing backwards, the
+    equi-angular model wrapping around), origins on a face and on an edge of the
+    cube (a coordinate of exactly 0 or 1), one of them looking out of the cube."""
+    sphere = st.TreeBuilder(st.SCENE_SPHERE, seed=1).BuildTree(4, 8)
+    terrain = st.TreeBuilder(st.SCENE_TERRAIN, seed=5).BuildTree(3, 8)
+    kw = dict(Tick=3, MaxChildRequestId=1 << 20)
+    return [
+        ("fov_200", sphere, st.look_at((0.5, 0.5, 0.1), (0.5, 0.5, 0.9), 64, 48, 200.0, **kw)),
+        ("fov_330", terrain, st.look_at((0.4, 0.45, 0.6), (0.6, 0.5, 0.9), 64, 48, 330.0, **kw)),
+        ("on_face_x1", sphere, st.look_at((1.0, 0.5, 0.5), (0.0, 0.5, 0.5), 48, 32, 60.0, **kw)),
+        ("on_face_x0_looking_out", sphere, st.look_at((0.0, 0.3, 0.7), (-1.0, 0.3, 0.7), 48, 32, 100.0, **kw)),
+        ("on_edge", terrain, st.look_at((1.0, 1.0, 0.5), (0.3, 0.3, 0.8), 48, 32, 60.0, **kw)),
+    ]
+
+
+def test_extreme_cameras_match_reference():
+    hits = {}
+    for name, tree, cam in extreme_camera_cases():
+        out = _compare(tree, cam)
+        hits[name] = int((out["hit_index"] != st.MISS).sum())
+    assert hits["on_face_x0_looking_out"] == 0
+    assert min(v for k, v in hits.items() if k != "on_face_x0_looking_out") > 100
+
+
+def test_axis_aligned_rays_match_reference():
+    for name, tree, cam in axis_aligned_cases():
+        out = _compare(tree, cam)
+        assert (out["hit_index"] != st.MISS).any(), name
+    assert out["n_requests"] > 0
+
+
 def test_empty_scene_matches_reference():
     tree = st.TreeBuilder(st.SCENE_SPHERE, seed=1).BuildTree(2, 4)
     tree.BaseBlocks[:] = 0x5555  # every octant air only
