@@ -96,3 +96,22 @@ def test_endless_schedule_is_refused(sphere):
         po.trace_view(sphere, view, gi=True)
     with pytest.raises(ValueError):
         po.ref_trace_view(sphere, view, gi=True)
+
+
+def edge_camera_cases():
+    """The trace's edge cameras (exact axes, origins on cell boundaries, the cube's
+    faces, edges and corner, fields of view past 180 degrees), every second one
+    with seeded normals."""
+    from test_oracle_vs_reference import axis_aligned_cases, extreme_camera_cases
+    out = []
+    for i, (name, tree, cam) in enumerate(axis_aligned_cases() + extreme_camera_cases()):
+        out.append((name, with_random_normals(tree, 20 + i) if i % 2 else tree, cam))
+    return out
+
+
+def test_edge_cameras(sphere):
+    lit = 0
+    for name, tree, cam in edge_camera_cases():
+        _, got = check(tree, cam)
+        lit += int((got["hit_index"] != st.MISS).sum())
+    assert lit > 5000

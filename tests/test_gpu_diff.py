@@ -106,6 +106,36 @@ def test_base_chunks_in_global_memory(tracer):
     assert ok.all(), "%d of %d gradient entries off the FP64 gradient" % ((~ok).sum(), ok.size)
 
 
+def test_edge_cameras(tracer):
+    """Cameras along exact axes, on cell boundaries, on the cube's faces, edges and
+    corner, and with fields of view past 180 degrees: forward colour, loss and
+    gradient within the FP64 bounds of the other cases."""
+    from test_oracle_vs_reference import axis_aligned_cases, extreme_camera_cases
+    rng = np.random.default_rng(12)
+    for name, tree, cam in axis_aligned_cases() + extreme_camera_cases():
+        hl = po.HitLists(tree, [cam], max_hits=16)
+        params = rng.uniform(0.0, 1.0, (len(tree.Blocks), 4)).astype(np.float32)
+        target = rng.uniform(0.0, 1.0, (cam.ScreenSize[0] * cam.ScreenSize[1], 3)).astype(np.float32)
+        tracer.upload(tree)
+        tracer.diff_set_params(params)
+        rgb = tracer.diff_forward([cam])
+        want_loss, want_rgb, want = hl.eval(params.astype(np.float64), target.astype(np.float64), want_rgb=True,
+                                            want_grad=True)
+        err = np.abs(rgb - want_rgb)
+        assert err.max() <= 1e-5, "%s: max |C - C64| = %g" % (name, err.max())
+        loss = tracer.diff_backward([cam], target)
+        # the loss is (1/P) sum over pixels and channels of e^2, e = C - target:
+        # a colour error of at most d per channel moves it by at most
+        # 2 sqrt(3 L) d + 3 d^2 (Cauchy-Schwarz), d the forward's bound above
+        d = float(err.max())
+        bound = 2.0 * np.sqrt(3.0 * want_loss) * d + 3.0 * d * d + 1e-12
+        assert abs(loss - want_loss) <= bound, (name, loss, want_loss, bound)
+        grad = tracer.diff_grads(len(tree.Blocks))
+        scale = max(np.abs(want).max(), 1e-30)
+        ok = np.abs(grad - want) <= 1e-4 * np.abs(want) + 1e-6 * scale
+        assert ok.all(), "%s: %d gradient entries off the FP64 gradient" % (name, (~ok).sum())
+
+
 def test_backward_matches_fp64_finite_differences(tracer, fitting):
     """The acceptance check of the adjoint: within 1e-3 relative of FP64 central
     differences (h = 1e-4) on 256 random nodes that rays hit. Entries below

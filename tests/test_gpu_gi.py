@@ -63,6 +63,18 @@ def test_gi_stage_matches_oracle(tracer, trees, scene, schedule):
     assert (got.hit_index != st.MISS).any()
 
 
+@pytest.mark.parametrize("schedule", [st.SCHEDULE_WARP, st.SCHEDULE_LANE, st.SCHEDULE_WAVEFRONT],
+                         ids=["warp", "lane", "wavefront"])
+def test_gi_edge_cameras(tracer, schedule):
+    """Cameras along exact axes, on cell boundaries, on the cube's faces, edges and
+    corner, and with fields of view past 180 degrees (the CPU tests pin the oracle
+    to the reference on the same cameras)."""
+    from test_gi_oracle import edge_camera_cases
+    tracer.set_config(schedule=schedule)
+    for name, tree, cam in edge_camera_cases():
+        compare(tracer, tree, cam)
+
+
 @pytest.mark.parametrize("kw", [
     {"FovMultiplier": 0.1, "FovConstant": 0.08, "WeightingMultiplier": -0.2, "WeightingConstant": 1.5},
     {"AmbientLightLevel": 0},
