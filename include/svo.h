@@ -178,7 +178,7 @@ typedef struct svo_trace_stats {
 
 /* Tuning of the persistent trace kernel (0 = library default). */
 typedef struct svo_trace_config {
-  int32_t block_size;   /* threads per CTA, multiple of 32 up to 256 */
+  int32_t block_size;   /* threads per CTA, multiple of 32 up to 256 (default 192) */
   int32_t ctas_per_sm;  /* resident CTAs per SM for the persistent grid */
   int32_t ray_chunk;    /* rays a thread claims per ray-queue fetch (1..64) */
   int32_t cadence;      /* steps a thread runs between ray retire/refill points (1..1024) */

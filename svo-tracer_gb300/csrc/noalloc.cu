@@ -194,7 +194,7 @@ extern "C" SVO_API svo_status svo_trace_noalloc(int32_t device, void *stream, ui
   a.max_steps = 1 << 16;
   a.ray_chunk = 1;
   a.cadence = 16;
-  a.block_size = 256;
+  a.block_size = 192;  // svo_trace's default block size
   a.schedule = SVO_SCHEDULE_WARP;
   a.path_levels = depth - base_depth - 1;
   int occ = trace_occupancy(a, false);

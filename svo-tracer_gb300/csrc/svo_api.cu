@@ -30,7 +30,12 @@ svo_status fail(svo_status status, const std::string &message) {
 
 static svo_trace_config default_config() {
   svo_trace_config c{};
-  c.block_size = 256;
+  // 192 threads: with the trace kernel's 55 registers, 6 CTAs (36 warps) fit an
+  // SM against 4 of 256 threads (32 warps). Measured on GB300, 256 / 128 / 192 /
+  // 224 threads: 1080p frame 1.373 / 1.350 / 1.340 / 1.351 ms, megakernel frame
+  // 13.85 / 13.44 / 13.41 / 13.52 ms, the frame with the secondary-cone stage
+  // 1.526 / 1.505 / 1.500 / 1.515 ms, identical outputs.
+  c.block_size = 192;
   c.ctas_per_sm = 0;  // occupancy-derived
   c.ray_chunk = 1;
   c.cadence = 16;
@@ -797,7 +802,7 @@ SVO_API svo_status svo_autotune(void *ctx, const svo_trace_input *inputs, int32_
   // Scheduling, block size, rays claimed per queue fetch and steps between
   // retire points (the last two for lane scheduling only); results do not
   // depend on any of them, only the time does.
-  const int sizes[] = {64, 128, 256};
+  const int sizes[] = {64, 128, 192, 256};
   const int chunks[] = {1, 2, 4, 8};
   const int cadences[] = {4, 8, 16, 32};
   std::vector<svo_trace_config> cands;

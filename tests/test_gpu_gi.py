@@ -31,7 +31,7 @@ def trees():
 
 @pytest.fixture(autouse=True)
 def gi_on(tracer):
-    tracer.set_config(gi_stage=1, schedule=st.SCHEDULE_WARP, block_size=256, ctas_per_sm=0, collect_stats=0)
+    tracer.set_config(gi_stage=1, schedule=st.SCHEDULE_WARP, block_size=192, ctas_per_sm=0, collect_stats=0)
     yield
     tracer.set_config(gi_stage=-1, schedule=st.SCHEDULE_WARP)
 

@@ -130,6 +130,13 @@ def test_extreme_views(tracer, sphere):
         check(tracer, tree, v)
 
 
+@pytest.mark.parametrize("block_size", [64, 128, 256])
+def test_block_sizes(tracer, terrain, block_size):
+    """Launch shapes other than the default (192 threads) give the same frame."""
+    v = st.orbit_views(seed=11, n=1, width=56, height=40, distance=1.25)[0]
+    check(tracer, terrain, v, block_size=block_size)
+
+
 def test_inside_cube_with_dof(tracer, sphere):
     v = st.look_at((0.5, 0.5, 0.12), (0.5, 0.55, 0.6), 48, 40, 70.0, DoF=(0.02, 0.3), Tick=9)
     check(tracer, with_random_normals(sphere, 3), v)

@@ -11,7 +11,7 @@ pytestmark = pytest.mark.gpu
 
 @pytest.fixture(autouse=True)
 def default_config(tracer):
-    tracer.set_config(block_size=256, ctas_per_sm=0, ray_chunk=1, cadence=16, max_steps=1 << 16, collect_stats=0)
+    tracer.set_config(block_size=192, ctas_per_sm=0, ray_chunk=1, cadence=16, max_steps=1 << 16, collect_stats=0)
     yield
 
 

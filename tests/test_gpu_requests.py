@@ -23,7 +23,7 @@ def terrain(tracer):
     tracer.upload(tree)
     tracer.init_usage()
     yield tree
-    tracer.set_config(request_order=st.REQUESTS_ARRIVAL, schedule=st.SCHEDULE_WARP, block_size=256, ctas_per_sm=0,
+    tracer.set_config(request_order=st.REQUESTS_ARRIVAL, schedule=st.SCHEDULE_WARP, block_size=192, ctas_per_sm=0,
                       collect_stats=0)
     scene.close()
 

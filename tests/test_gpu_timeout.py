@@ -26,7 +26,7 @@ def sphere(tracer):
     tracer.upload(tree)
     tracer.init_usage()
     yield tree, cam
-    tracer.set_config(pass_limit=0, schedule=st.SCHEDULE_WARP, block_size=256, ctas_per_sm=0, collect_stats=0)
+    tracer.set_config(pass_limit=0, schedule=st.SCHEDULE_WARP, block_size=192, ctas_per_sm=0, collect_stats=0)
 
 
 def _stopped(call):

@@ -15,7 +15,7 @@ NONE = 0xFFFFFFFF
 
 @pytest.fixture(autouse=True)
 def default_config(tracer):
-    tracer.set_config(block_size=256, ctas_per_sm=0, ray_chunk=1, cadence=16, max_steps=1 << 16, collect_stats=0)
+    tracer.set_config(block_size=192, ctas_per_sm=0, ray_chunk=1, cadence=16, max_steps=1 << 16, collect_stats=0)
     yield
 
 
@@ -100,7 +100,7 @@ def test_stream_past_the_request_cap_matches_oracle(tracer):
     dev = st.Tracer(0)
     try:
         for tr in (tracer, dev):
-            tr.set_config(block_size=256, ctas_per_sm=0, max_steps=1 << 16, collect_stats=0,
+            tr.set_config(block_size=192, ctas_per_sm=0, max_steps=1 << 16, collect_stats=0,
                           request_order=st.REQUESTS_PIXEL)
             tr.upload(tree, block_budget=budget * 8)
             tr.init_usage_tree(1)
@@ -161,7 +161,7 @@ def test_state_checkpoint_resumes_the_stream(tracer, tmp_path):
     tree = scene.build_tree(8)
     budget = (len(tree.Blocks) + 7) // 8 + (1 << 14)
     cams = st.camera_path(seed=3, frames=frames, width=160, height=90, MaxChildRequestId=cap)
-    cfg = dict(block_size=256, ctas_per_sm=0, max_steps=1 << 16, collect_stats=0, request_order=st.REQUESTS_PIXEL)
+    cfg = dict(block_size=192, ctas_per_sm=0, max_steps=1 << 16, collect_stats=0, request_order=st.REQUESTS_PIXEL)
     saves = {3: str(tmp_path / "frame3.svostate"), 9: str(tmp_path / "frame9.svostate")}
     resumed = []
     try:
@@ -420,7 +420,7 @@ def test_graft_generate_matches_host_path(tracer, initial, extra_groups):
     dev = st.Tracer(0)
     try:
         for tr in (tracer, dev):
-            tr.set_config(block_size=256, ctas_per_sm=0, ray_chunk=1, cadence=16, max_steps=1 << 16, collect_stats=0)
+            tr.set_config(block_size=192, ctas_per_sm=0, ray_chunk=1, cadence=16, max_steps=1 << 16, collect_stats=0)
             tr.upload(tree, block_budget=budget * 8)
             tr.init_usage_tree(1)
         cams = st.camera_path(seed=3, frames=8, width=160, height=90, MaxChildRequestId=1 << 16)
