@@ -41,10 +41,14 @@ enum {
   SVO_ERR_INVALID_ARGUMENT = 1,
   SVO_ERR_CUDA = 2,
   SVO_ERR_OUT_OF_MEMORY = 3,
-  SVO_ERR_QUEUE_FULL = 4,  /* a capped device queue overflowed (child requests) */
+  SVO_ERR_QUEUE_FULL = 4,  /* reserved: no call returns it. A child-request queue past its cap is not an
+                              error (the reference drops the requests past MaxChildRequestId); the raised
+                              count that svo_read_child_requests returns then exceeds the cap */
   SVO_ERR_TIMEOUT = 5,     /* a bounded device wait ran out */
   SVO_ERR_NO_TREE = 6,     /* trace/prune/graft before svo_upload_octree */
-  SVO_ERR_STEP_LIMIT = 7,  /* a ray exceeded the per-ray step limit */
+  SVO_ERR_STEP_LIMIT = 7,  /* reserved: no call returns it. A ray that reaches max_steps ends in the sky,
+                              as a ray the reference stops does, and is counted in
+                              svo_trace_stats.step_limited */
   SVO_ERR_BUDGET = 8,      /* block budget exhausted (builder, graft) */
   SVO_ERR_NO_DEVICE = 9,   /* no usable CUDA device / kernel image */
   SVO_ERR_INTERNAL = 10,
