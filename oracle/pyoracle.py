@@ -162,6 +162,24 @@ def ref_mega_lib() -> C.CDLL:
     return _ref_mega
 
 
+def _ref_usage(usage, n_blocks):
+    """The usage array handed to the reference's kernels: the caller's entries plus
+    room for the last, partial block group. The reference sizes its Usages buffer
+    BlockCount >> 3 (MainWindow.cs:130), so when BlockCount is not a multiple of 8
+    its updateUsage (wavefront.cl:377-381, kernel.cl's twin) stamps one entry past
+    the buffer; here that entry exists and is dropped (_ref_usage_back)."""
+    if usage is None:
+        return None
+    padded = np.zeros(max(len(usage), (n_blocks + 7) // 8 + 1), USAGE_DTYPE)
+    padded[: len(usage)] = usage
+    return padded
+
+
+def _ref_usage_back(usage, padded):
+    if usage is not None:
+        usage[:] = padded[: len(usage)]
+
+
 def ref_mega_trace_view(tree, inp: TraceInput, usage=None, threads: int = 0, rows=None, req_cap: int = 1 << 22,
                         cone_limit: int = 1 << 16):
     """Runs the reference's megakernel (CPU build of kernel.cl's `trace`) on one view,
@@ -174,8 +192,10 @@ def ref_mega_trace_view(tree, inp: TraceInput, usage=None, threads: int = 0, row
     bases = np.ascontiguousarray(tree.BaseBlocks, np.uint16)
     blocks = np.ascontiguousarray(tree.Blocks)
     req = np.zeros(req_cap, CHILD_REQUEST_DTYPE)
-    n = lib.ref_mega_trace_rows(_p(bases), tree.BaseDepth, _p(blocks), len(blocks), _p(usage), inp.to_bytes()[:96],
+    u = _ref_usage(usage, len(blocks))
+    n = lib.ref_mega_trace_rows(_p(bases), tree.BaseDepth, _p(blocks), len(blocks), _p(u), inp.to_bytes()[:96],
                                 _p(rgba), _p(req), req_cap, threads, r0, r1, cone_limit)
+    _ref_usage_back(usage, u)
     if n < 0:
         raise ValueError("cone schedule does not end")
     return {"rgba": rgba, "requests": req[: min(n, req_cap)], "n_requests": int(n)}
@@ -242,10 +262,12 @@ def ref_trace_view(tree, inp: TraceInput, usage=None, threads: int = 0, max_pass
     blocks = np.ascontiguousarray(tree.Blocks)
     req = np.zeros(n, CHILD_REQUEST_DTYPE)
     nreq = C.c_uint32(0)
-    ng = 0 if usage is None else len(usage)
-    passes = lib.ref_trace_rows_gi(_p(bases), tree.BaseDepth, _p(blocks), len(blocks), _p(usage), ng, inp.to_bytes(),
+    u = _ref_usage(usage, len(blocks))
+    ng = 0 if u is None else len(u)
+    passes = lib.ref_trace_rows_gi(_p(bases), tree.BaseDepth, _p(blocks), len(blocks), _p(u), ng, inp.to_bytes(),
                                    _p(r["hit_index"]), _p(r["hit_depth"]), _p(r["t"]), _p(r["rgba"]), _p(r["acc"]),
                                    _p(req), len(req), C.byref(nreq), threads, max_passes, 0, h, int(gi))
+    _ref_usage_back(usage, u)
     if passes == -2:
         raise ValueError("cone schedule does not end")
     r["passes"] = int(passes)

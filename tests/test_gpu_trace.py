@@ -11,7 +11,7 @@ import pytest
 import pyoracle as po
 import svo_tracer as st
 from test_golden_cpu import GOLDEN, load_case
-from test_oracle_vs_reference import axis_aligned_cases, extreme_camera_cases
+from test_oracle_vs_reference import axis_aligned_cases, extreme_camera_cases, random_cameras
 
 pytestmark = pytest.mark.gpu
 
@@ -235,6 +235,24 @@ def test_extreme_cameras(tracer, schedule):
         assert n == want["n_requests"], name
         ok, msg = same_requests(req, want["requests"])
         assert ok, name + ": " + msg
+
+
+@pytest.mark.parametrize("schedule", [st.SCHEDULE_LANE, st.SCHEDULE_WARP, st.SCHEDULE_WAVEFRONT],
+                         ids=["lane", "warp", "wavefront"])
+def test_random_cameras(tracer, schedule):
+    """60 seeded random cameras (origins in and around the cube, 1-96 pixels each
+    way, fields of view 5-350 degrees, depth of field on a third): every output,
+    the usage ticks, the child requests and the per-ray walk counts equal the
+    oracle's; the CPU tests pin the oracle to the reference on the same cameras."""
+    tracer.set_config(schedule=schedule)
+    for name, tree, cam in random_cameras(cap=1 << 20):
+        got, usage, req, n, stats, (vb, vs), want, u_ref = run_both(tracer, tree, cam)
+        assert_same(got, want, name + ": ")
+        assert np.array_equal(usage["tick"], u_ref["tick"]), name
+        assert n == want["n_requests"], name
+        ok, msg = same_requests(req, want["requests"])
+        assert ok, name + ": " + msg
+        assert np.array_equal(vb, want["v_block"]) and np.array_equal(vs, want["v_base"]), name
 
 
 @pytest.mark.parametrize("kind", ["all_air", "solid_without_blocks"])

@@ -95,6 +95,37 @@ def test_extreme_cameras_match_reference():
     assert min(v for k, v in hits.items() if k != "on_face_x0_looking_out") > 100
 
 
+def random_cameras(seed=2026, n=60, cap=None):
+    """Seeded random cameras over two trees: origins inside and around the cube,
+    sizes 1-96 in each direction, horizontal fields of view 5-350 degrees, depth
+    of field on a third of them, random ticks; child-request caps random (or
+    `cap`)."""
+    rng = np.random.default_rng(seed)
+    trees = [st.TreeBuilder(st.SCENE_SPHERE, seed=3).BuildTree(3, 8),
+             st.TreeBuilder(st.SCENE_TERRAIN, seed=9).BuildTree(2, 8)]
+    out = []
+    for i in range(n):
+        o = rng.uniform(-0.6, 1.6, 3)
+        t = rng.uniform(0.2, 0.8, 3)
+        w, h = int(rng.integers(1, 97)), int(rng.integers(1, 97))
+        fov = float(rng.uniform(5.0, 350.0))
+        dof = (float(rng.uniform(0.0, 0.05)) if i % 3 == 0 else 0.0, float(rng.uniform(0.0, 1.5)))
+        tick = int(rng.integers(1, 60000))
+        req_cap = int(rng.integers(0, 5000)) if cap is None else cap
+        cam = st.look_at(tuple(o), tuple(t), w, h, fov, DoF=dof, Tick=tick, MaxChildRequestId=req_cap)
+        out.append(("camera%d" % i, trees[i % 2], cam))
+    return out
+
+
+def test_random_cameras_match_reference():
+    hits = requests = 0
+    for name, tree, cam in random_cameras():
+        out = _compare(tree, cam)
+        hits += int((out["hit_index"] != st.MISS).sum())
+        requests += out["n_requests"]
+    assert hits > 5000 and requests > 1000
+
+
 def test_axis_aligned_rays_match_reference():
     for name, tree, cam in axis_aligned_cases():
         out = _compare(tree, cam)
