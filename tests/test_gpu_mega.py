@@ -122,6 +122,15 @@ def test_axis_aligned_views(tracer, sphere, schedule):
         check(tracer, tree, v, schedule=sched, cadence=5)
 
 
+@pytest.mark.parametrize("schedule", ["lane", "warp"])
+def test_random_views(tracer, schedule):
+    """30 seeded random cameras; the CPU tests pin the oracle to kernel.cl on them."""
+    from test_mega_oracle import mega_random_cases
+    sched = {"lane": st.SCHEDULE_LANE, "warp": st.SCHEDULE_WARP}[schedule]
+    for name, tree, v in mega_random_cases():
+        check(tracer, tree, v, schedule=sched, cadence=7)
+
+
 def test_extreme_views(tracer, sphere):
     """A field of view past 180 degrees and origins on a face and an edge of the
     cube (with a depth of field); the CPU tests pin the oracle to kernel.cl."""

@@ -104,6 +104,22 @@ def test_extreme_views(sphere):
         assert got["n_requests"] > 0 and got["cones"].sum() > 1000, name
 
 
+def mega_random_cases():
+    """30 seeded random cameras (the trace's random-camera generator), every second
+    tree with seeded normals."""
+    from test_oracle_vs_reference import random_cameras
+    return [(name, with_random_normals(tree, 40 + i) if i % 2 else tree, cam)
+            for i, (name, tree, cam) in enumerate(random_cameras(seed=77, n=30, cap=1 << 20))]
+
+
+def test_random_views():
+    cones = 0
+    for name, tree, v in mega_random_cases():
+        ref, got = check(tree, v)
+        cones += int(got["cones"].sum())
+    assert cones > 100000
+
+
 def test_axis_aligned_views(sphere):
     for name, tree, v in mega_axis_aligned_cases(sphere):
         ref, got = check(tree, v)
