@@ -115,3 +115,19 @@ def test_edge_cameras(sphere):
         _, got = check(tree, cam)
         lit += int((got["hit_index"] != st.MISS).sum())
     assert lit > 5000
+
+
+def random_cases():
+    """30 seeded random cameras (the trace's random-camera generator), every second
+    tree with seeded normals."""
+    from test_oracle_vs_reference import random_cameras
+    return [(name, with_random_normals(tree, 60 + i) if i % 2 else tree, cam)
+            for i, (name, tree, cam) in enumerate(random_cameras(seed=91, n=30, cap=1 << 20))]
+
+
+def test_random_cameras():
+    lit = 0
+    for name, tree, cam in random_cases():
+        _, got = check(tree, cam)
+        lit += int((got["hit_index"] != st.MISS).sum())
+    assert lit > 3000

@@ -106,13 +106,9 @@ def test_base_chunks_in_global_memory(tracer):
     assert ok.all(), "%d of %d gradient entries off the FP64 gradient" % ((~ok).sum(), ok.size)
 
 
-def test_edge_cameras(tracer):
-    """Cameras along exact axes, on cell boundaries, on the cube's faces, edges and
-    corner, and with fields of view past 180 degrees: forward colour, loss and
-    gradient within the FP64 bounds of the other cases."""
-    from test_oracle_vs_reference import axis_aligned_cases, extreme_camera_cases
-    rng = np.random.default_rng(12)
-    for name, tree, cam in axis_aligned_cases() + extreme_camera_cases():
+def check_cameras(tracer, cases, seed):
+    rng = np.random.default_rng(seed)
+    for name, tree, cam in cases:
         hl = po.HitLists(tree, [cam], max_hits=16)
         params = rng.uniform(0.0, 1.0, (len(tree.Blocks), 4)).astype(np.float32)
         target = rng.uniform(0.0, 1.0, (cam.ScreenSize[0] * cam.ScreenSize[1], 3)).astype(np.float32)
@@ -134,6 +130,22 @@ def test_edge_cameras(tracer):
         scale = max(np.abs(want).max(), 1e-30)
         ok = np.abs(grad - want) <= 1e-4 * np.abs(want) + 1e-6 * scale
         assert ok.all(), "%s: %d gradient entries off the FP64 gradient" % (name, (~ok).sum())
+
+
+def test_random_cameras(tracer):
+    """30 seeded random cameras (origins in and around the cube, 1-96 pixels each
+    way, fields of view 5-350 degrees, depth of field on a third): forward
+    colour, loss and gradient within the FP64 bounds."""
+    from test_oracle_vs_reference import random_cameras
+    check_cameras(tracer, random_cameras(seed=55, n=30, cap=1 << 20), 13)
+
+
+def test_edge_cameras(tracer):
+    """Cameras along exact axes, on cell boundaries, on the cube's faces, edges and
+    corner, and with fields of view past 180 degrees: forward colour, loss and
+    gradient within the FP64 bounds of the other cases."""
+    from test_oracle_vs_reference import axis_aligned_cases, extreme_camera_cases
+    check_cameras(tracer, axis_aligned_cases() + extreme_camera_cases(), 12)
 
 
 def test_backward_matches_fp64_finite_differences(tracer, fitting):

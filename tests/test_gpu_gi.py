@@ -75,6 +75,17 @@ def test_gi_edge_cameras(tracer, schedule):
         compare(tracer, tree, cam)
 
 
+@pytest.mark.parametrize("schedule", [st.SCHEDULE_WARP, st.SCHEDULE_LANE, st.SCHEDULE_WAVEFRONT],
+                         ids=["warp", "lane", "wavefront"])
+def test_gi_random_cameras(tracer, schedule):
+    """30 seeded random cameras (the CPU tests pin the oracle to the reference on
+    them)."""
+    from test_gi_oracle import random_cases
+    tracer.set_config(schedule=schedule)
+    for name, tree, cam in random_cases():
+        compare(tracer, tree, cam)
+
+
 @pytest.mark.parametrize("kw", [
     {"FovMultiplier": 0.1, "FovConstant": 0.08, "WeightingMultiplier": -0.2, "WeightingConstant": 1.5},
     {"AmbientLightLevel": 0},
