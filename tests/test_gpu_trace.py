@@ -320,6 +320,37 @@ def test_batch_equals_single_views_and_graph(tracer):
         assert_same(s, want)
 
 
+@pytest.mark.parametrize("schedule", [st.SCHEDULE_LANE, st.SCHEDULE_WARP, st.SCHEDULE_WAVEFRONT],
+                         ids=["lane", "warp", "wavefront"])
+def test_random_views_in_one_batch(tracer, schedule):
+    """30 seeded random views of one tree (1-96 pixels each way, ragged tiles) in
+    one batched launch and its graph replay: every view's outputs, the usage
+    ticks stamped by all views and the union of their child requests equal the
+    oracle's view by view."""
+    import dataclasses
+    cases = [c for i, c in enumerate(random_cameras(seed=33, n=60, cap=1 << 20)) if i % 2 == 0]
+    tree = cases[0][1]
+    views = [dataclasses.replace(cam, Tick=9) for _, _, cam in cases]
+    tracer.set_config(schedule=schedule, collect_stats=0)
+    tracer.upload(tree)
+    tracer.init_usage()
+    batch = tracer.trace_batch(views, graph=True)
+    req, n = tracer.read_child_requests()
+    tracer.init_usage()
+    replay = tracer.trace_batch(views, graph=True)
+    usage = tracer.read_usage(len(tree.Blocks) // 8)
+    u_ref = po.init_usage(tree)
+    wants = [po.trace_view(tree, v, usage=u_ref) for v in views]
+    for (name, _, _), b, r, want in zip(cases, batch, replay, wants):
+        assert_same(b, want, name + ": ")
+        assert_same(r, want, name + " (replay): ")
+    assert np.array_equal(usage["tick"], u_ref["tick"])
+    want_req = np.concatenate([w["requests"] for w in wants])
+    assert n == len(want_req)
+    ok, msg = same_requests(req, want_req)
+    assert ok, msg
+
+
 def test_l2_window_in_graph_replay(tracer):
     """A graph captured with the L2 persisting window on replays the same frames."""
     tree = st.TreeBuilder(st.SCENE_TERRAIN, seed=3).BuildTree(3, 8)
