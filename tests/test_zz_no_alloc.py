@@ -85,6 +85,54 @@ def test_noalloc_matches_trace_on_two_calls():
             assert same, "call %d vs %s: child requests differ" % (call, label)
 
 
+def test_noalloc_random_cameras():
+    """30 seeded random cameras over two trees (origins in and around the cube,
+    1-96 pixels each way, fields of view 5-350 degrees, depth of field on a third)
+    through svo_trace_noalloc: every output, the usage ticks and the child
+    requests equal the oracle's (the CPU tests pin the oracle to the reference on
+    the same cameras)."""
+    torch = pytest.importorskip("torch")
+    from test_oracle_vs_reference import random_cameras
+    lib = st.load_library()
+    trace_noalloc = _entry(lib)
+    dev = torch.device("cuda", 0)
+    cap = 1 << 16
+    resident = {}
+    for name, tree, cam in random_cameras(seed=21, n=30, cap=cap):
+        if id(tree) not in resident:
+            resident[id(tree)] = (torch.from_numpy(tree.BaseBlocks.view(np.int16).copy()).to(dev),
+                                  torch.from_numpy(tree.Blocks.view(np.uint8).copy()).to(dev))
+        d_bases, d_blocks = resident[id(tree)]
+        W, H = cam.ScreenSize
+        n_groups = len(tree.Blocks) // 8
+        usage0 = po.init_usage(tree)
+        want_usage = usage0.copy()
+        want = po.trace_view(tree, cam, usage=want_usage)
+        d_usage = torch.from_numpy(usage0.view(np.uint8).copy()).to(dev)
+        d_idx = torch.full((W * H,), -7, dtype=torch.int32, device=dev)
+        d_dep = torch.full((W * H,), 99, dtype=torch.uint8, device=dev)
+        d_t = torch.full((W * H,), -1.0, dtype=torch.float32, device=dev)
+        d_rgba = torch.full((W * H * 4,), -1.0, dtype=torch.float32, device=dev)
+        d_req = torch.zeros((cap * 40,), dtype=torch.uint8, device=dev)
+        out = st.TraceOutputC(d_idx.data_ptr(), d_dep.data_ptr(), d_t.data_ptr(), d_rgba.data_ptr(), 1, 0)
+        raised = C.c_uint32(0)
+        c_in = cam.to_c()
+        torch.cuda.synchronize()
+        status = trace_noalloc(0, None, tree.BaseDepth, d_bases.data_ptr(), len(tree.BaseBlocks), d_blocks.data_ptr(),
+                               len(tree.Blocks), d_usage.data_ptr(), n_groups, 0, C.byref(c_in), C.byref(out),
+                               d_req.data_ptr(), cap, C.byref(raised))
+        assert status == 0, (name, lib.svo_last_error_string())
+        torch.cuda.synchronize()
+        assert np.array_equal(d_idx.cpu().numpy().view(np.uint32), want["hit_index"]), name
+        assert np.array_equal(d_dep.cpu().numpy(), want["hit_depth"]), name
+        assert np.array_equal(d_t.cpu().numpy().view(np.uint32), want["t"].view(np.uint32)), name
+        assert np.array_equal(d_rgba.cpu().numpy().reshape(-1, 4).view(np.uint32), want["rgba"].view(np.uint32)), name
+        assert np.array_equal(d_usage.cpu().numpy().view(st.USAGE_DTYPE)["tick"], want_usage["tick"]), name
+        assert raised.value == want["n_requests"], name
+        req = d_req.cpu().numpy().view(st.CHILD_REQUEST_DTYPE)[: raised.value]
+        assert po.sort_requests(req).tobytes() == po.sort_requests(want["requests"]).tobytes(), name
+
+
 def test_noalloc_rejects_oversized_views_and_host_outputs():
     lib = st.load_library()
     trace_noalloc = _entry(lib)
