@@ -41,21 +41,25 @@ def test_init_usage_tree_matches_oracle(tracer):
     assert_state(tracer, oracle, "init")
 
 
-@pytest.mark.parametrize("base_depth,depth,initial,budget,threshold",
-                         [(3, 9, 7, 1 << 15, 3), (2, 8, 6, 1 << 13, 2), (6, 10, 9, (1 << 21) + (1 << 16), 2)],
-                         ids=["b3", "b2", "b6_global_bases"])
-def test_stream_matches_oracle(tracer, base_depth, depth, initial, budget, threshold):
+@pytest.mark.parametrize("base_depth,depth,initial,budget,threshold,scene_seed,path_seed",
+                         [(3, 9, 7, 1 << 15, 3, 5, 3), (2, 8, 6, 1 << 13, 2, 5, 3),
+                          (6, 10, 9, (1 << 21) + (1 << 16), 2, 5, 3),
+                          (3, 9, 7, 1 << 15, 1, 11, 17), (2, 9, 6, 1 << 14, 4, 23, 29), (3, 10, 8, 1 << 17, 2, 31, 41)],
+                         ids=["b3", "b2", "b6_global_bases", "seeded_a", "seeded_b", "seeded_c"])
+def test_stream_matches_oracle(tracer, base_depth, depth, initial, budget, threshold, scene_seed, path_seed):
     """Frames of the streaming workflow: trace (usage stamps + child requests), graft
     payloads from the procedural scene, GC of groups unused for `threshold` frames,
     grafting into freed groups; GPU and oracle evolve their own copies of the tree.
-    Base depth 6: 2.1M dense groups at level 8, base chunks in global memory."""
-    scene = st.Scene(st.SCENE_TERRAIN, seed=5, base_depth=base_depth, depth=depth)
+    Base depth 6: 2.1M dense groups at level 8, base chunks in global memory. The
+    seeded cases vary the scene, the camera path, the tree's initial depth and
+    the staleness threshold (1 to 4 frames)."""
+    scene = st.Scene(st.SCENE_TERRAIN, seed=scene_seed, base_depth=base_depth, depth=depth)
     tree = scene.build_tree(initial)
     tracer.upload(tree, block_budget=budget * 8)
     tracer.init_usage_tree(1)
     oracle = po.TreeState(tree, budget)
     oracle.init_usage_tree(1)
-    cams = st.camera_path(seed=3, frames=10, width=160, height=90, MaxChildRequestId=1 << 16)
+    cams = st.camera_path(seed=path_seed, frames=10, width=160, height=90, MaxChildRequestId=1 << 16)
     grafted_total = pruned_total = 0
     for f, cam in enumerate(cams):
         tick = f + 1
