@@ -499,6 +499,33 @@ def test_errors(tracer):
     assert lib is not None
 
 
+def test_random_cameras_pinned_host_outputs(tracer):
+    """30 seeded random cameras traced into pinned host outputs (written by the
+    kernel over 8x4 tiles, hit depth staged in device memory) and, as a graph-
+    replayed batch, into pinned host outputs: equal to the oracle."""
+    torch = pytest.importorskip("torch")
+    import dataclasses
+    cases = [c for i, c in enumerate(random_cameras(seed=44, n=60, cap=1 << 20)) if i % 2 == 1]
+    tree = cases[0][1]
+
+    def pinned(w, h):
+        n = w * h
+        return st.TraceResult(torch.empty(n, dtype=torch.int32, pin_memory=True).numpy().view(np.uint32),
+                              torch.empty(n, dtype=torch.uint8, pin_memory=True).numpy(),
+                              torch.empty(n, dtype=torch.float32, pin_memory=True).numpy(),
+                              torch.empty(n * 4, dtype=torch.float32, pin_memory=True).numpy().reshape(n, 4))
+
+    tracer.upload(tree)
+    tracer.init_usage()
+    views = [dataclasses.replace(cam, Tick=5) for _, _, cam in cases]
+    wants = [po.trace_view(tree, v) for v in views]
+    for (name, _, _), v, want in zip(cases, views, wants):
+        assert_same(tracer.trace(v, out=pinned(*v.ScreenSize)), want, name + ": ")
+    outs = tracer.trace_batch(views, graph=True, out=[pinned(*v.ScreenSize) for v in views])
+    for (name, _, _), got, want in zip(cases, outs, wants):
+        assert_same(got, want, name + " (batch): ")
+
+
 def test_pinned_host_outputs_equal_staged_outputs(tracer):
     """Host outputs in pinned memory are written by the kernel directly; pageable
     host outputs go through device buffers. Both give the same results, on two
